@@ -1,0 +1,166 @@
+"""Generate the golden fixtures by running the reference's own numpy path.
+
+Run in a container that has the EasyDistillation sources (read-only is fine):
+
+    python tests/golden/make_golden.py [path/to/EasyDistillation]
+
+The reference package imports ``mpi4py`` through its work-queue module
+(``lattice/dispatch.py:6``); that module is off the hot path, so a stub is
+placed in ``sys.modules`` before the import.  The reference numpy backend is
+selected (``lattice/backend.py:14-33``) and the public generator classes are
+driven through small in-memory ``GaugeField``/``Eigenvector`` adaptors that
+expose the ``load(key)[...]`` protocol of ``lattice.preset``.
+
+Every fixture stores its inputs next to the reference outputs, so the tests
+need neither the reference sources nor this script at run time.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+
+from oracle.restatement import synthetic_gauge, random_colour_vectors  # noqa: E402
+
+
+def import_reference(ref_root: str):
+    stub = types.ModuleType("mpi4py")
+    stub.MPI = types.SimpleNamespace(COMM_WORLD=None)
+    sys.modules.setdefault("mpi4py", stub)
+    sys.path.insert(0, ref_root)
+    import lattice  # noqa: F401
+
+    lattice.set_backend("numpy")
+    return lattice
+
+
+class _Data:
+    def __init__(self, arr, name):
+        self.arr = arr
+        self.file = name
+        self.sizeInByte = arr.nbytes
+        self.timeInSec = 1e-3
+
+    def __getitem__(self, key):
+        return np.asarray(self.arr[key]).copy()
+
+
+class MemGauge:
+    """In-memory stand-in for a ``lattice.preset.GaugeField``."""
+
+    def __init__(self, arr):
+        self.data = _Data(arr, "memory-gauge")
+
+    def load(self, key):
+        return self.data
+
+
+class MemEigen:
+    """In-memory stand-in for a ``lattice.preset.Eigenvector``."""
+
+    def __init__(self, arr, Ne):
+        self.Ne = Ne
+        self.data = _Data(arr, "memory-eigenvector")
+
+    def load(self, key):
+        return self.data
+
+
+def main(ref_root: str):
+    lattice = import_reference(ref_root)
+    from lattice.generator.eigenvector import _Laplacian
+    from lattice.insertion.derivative import derivative
+    from lattice.insertion.mom_dict import mom_dict_to_list
+    from lattice.insertion.phase import MomentumPhase
+
+    out = {}
+
+    # --- metadata -------------------------------------------------------
+    np.savez_compressed(
+        os.path.join(HERE, "metadata.npz"),
+        derivative=np.array([list(derivative(n)) + [-1] * (2 - len(derivative(n))) for n in range(13)]),
+        mom3=np.array(mom_dict_to_list(3)),
+    )
+
+    # --- Laplacian on random vectors (two lattices, incl. an L=2 axis) --
+    for tag, latt, eps, seed in (("443", [4, 4, 4, 2], 0.3, 11), ("642", [6, 4, 2, 1], 0.1, 12)):
+        Lx, Ly, Lz, Lt = latt
+        g = synthetic_gauge(latt, eps, seed)
+        U = g.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0].copy()
+        U_dag = U.transpose(0, 1, 2, 3, 5, 4).conj()
+        rng = np.random.default_rng(seed + 100)
+        n = Lz * Ly * Lx * 3
+        F = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+        LF = _Laplacian(F, U, U_dag, latt)
+        np.savez_compressed(os.path.join(HERE, f"laplacian_{tag}.npz"), latt=latt, gauge=g, F=F, LF=LF)
+
+    # --- momentum phases -------------------------------------------------
+    latt = [4, 6, 2, 1]
+    mp = MomentumPhase(latt)
+    moms = mom_dict_to_list(3)[:7] + [(0, 1, 2), (1, 1, 2)]
+    np.savez_compressed(
+        os.path.join(HERE, "phase_462.npz"),
+        latt=latt,
+        moms=np.array(moms),
+        phase=np.stack([mp.get(tuple(p)) for p in moms]),
+    )
+
+    # --- elementals through the public generator -------------------------
+    cases = [
+        # tag, latt, eps, seed, Ne, num_nabla, momenta, t, dilution
+        ("n2_test7", [4, 4, 4, 2], 0.3, 21, 6, 2,
+         [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (0, 0, 2), (0, 1, 2), (1, 1, 2)], 1, None),
+        ("n1_mom27", [4, 4, 4, 1], 0.3, 22, 4, 1, mom_dict_to_list(3), 0, None),
+        ("n0_mom7", [4, 4, 2, 1], 0.1, 23, 5, 0, mom_dict_to_list(3)[:7], 0, None),
+        ("n2_blend", [4, 4, 4, 1], 0.3, 24, 6, 2, mom_dict_to_list(3)[:3], 0, ([4, 5], 3)),
+    ]
+    for tag, latt, eps, seed, Ne, nn, moms, t, dil in cases:
+        Lx, Ly, Lz, Lt = latt
+        g = synthetic_gauge(latt, eps, seed)
+        evec = np.stack([random_colour_vectors(Ne, latt, seed + 1000 + tt) for tt in range(Lt)])
+        gen = lattice.ElementalGenerator(
+            latt, MemGauge(g), MemEigen(evec, Ne), nn, moms, dilution=dil, is_blending=dil is not None
+        )
+        gen.load("mem")
+        E = gen.calc(t).copy()
+        np.savez_compressed(
+            os.path.join(HERE, f"elemental_{tag}.npz"),
+            latt=latt, gauge=g, evec=evec, num_nabla=nn, moms=np.array(moms), t=t, E=E,
+            dil_tot=np.array(dil[0] if dil else []), dil_used=np.array(dil[1] if dil else 0),
+        )
+
+    # --- displacement elemental -------------------------------------------
+    latt = [4, 4, 4, 1]
+    g = synthetic_gauge(latt, 0.3, 31)
+    evec = random_colour_vectors(4, latt, 1031)[None]
+    moms = mom_dict_to_list(3)[:3]
+    gen = lattice.DisplacementElementalGenerator(latt, MemGauge(g), MemEigen(evec, 4), 2, moms)
+    gen.load("mem")
+    E = gen.calc(0).copy()
+    np.savez_compressed(os.path.join(HERE, "displacement_d2.npz"), latt=latt, gauge=g, evec=evec, moms=np.array(moms), E=E)
+
+    # --- eigensolve + stout smearing through EigenvectorGenerator --------
+    latt = [4, 4, 4, 2]
+    g = synthetic_gauge(latt, 0.3, 41)
+    gen = lattice.EigenvectorGenerator(latt, MemGauge(g), 8, 1e-10)
+    gen.load("mem")
+    evecs0, evals0 = gen.calc(0)
+    gen.stout_smear(2, 0.12)
+    smeared = gen._U[:3].copy()
+    evecs1, evals1 = gen.calc(1)
+    np.savez_compressed(
+        os.path.join(HERE, "eigen_443.npz"),
+        latt=latt, gauge=g, Ne=8, tol=1e-10,
+        evecs0=evecs0, evals0=np.asarray(evals0), smeared=smeared, evecs1=evecs1, evals1=np.asarray(evals1),
+    )
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
