@@ -1,0 +1,296 @@
+"""Benchmark: elemental timeslices/s at 32^3 x 64, Ne = 200, 13 operators x 27 momenta.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--mode MODE] [--impl ours|reference]
+
+One step = one timeslice of ``ElementalGenerator.calc``: covariant-derivative
+chains, all pair contractions and the operator combination, with the links
+of all 64 timeslices and the eigenvectors of several timeslices resident in
+HBM (the step rotates over timeslices, so every step's inputs exceed the
+129 MB L2).  ``value`` is timeslices/s over all ranks (replicas: each rank
+computes its own timeslices, no collective on the data path).  ``e2e`` is
+the same metric through the public generator with host eigenvectors
+(host->device copy of the c128 eigenvectors and device->host copy of the
+elementals inside the timed region).
+
+``--impl reference`` times the CPU restatement of the reference numpy path
+(the oracle) on the host cores on a bounded sample of the same workload.
+Synthetic inputs: SU(3) links exp(i*0.3*A), random orthonormal eigenvectors.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elemental timeslices/s 32³×64 Ne=200: split-prec vs FP64 GPU at rel err ≤1e-6"
+LATT = [32, 32, 32, 64]
+NE = 200
+NUM_NABLA = 2
+NMOM = 27
+RESIDENT_T = 4  # timeslices of eigenvectors kept resident (315 MB each in c128)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="fp64")
+    ap.add_argument("--lattice", default=None, help="Lx,Ly,Lz,Lt override (parity runs only)")
+    ap.add_argument("--ne", type=int, default=NE)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(
+                        ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                         "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                    if out.returncode == 0 and out.stdout.strip():
+                        self.rows.append([v.strip() for v in out.stdout.strip().split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 3 + k and "Active" in r[3 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------- inputs
+def make_inputs(latt, Ne, seed=2):
+    import numpy as np
+
+    from oracle.restatement import synthetic_gauge  # input generation only
+
+    gauge = synthetic_gauge(latt, 0.3, 1000 + seed)
+    Lx, Ly, Lz, Lt = latt
+    n = Lx * Ly * Lz * 3
+    rng = np.random.default_rng(seed)
+    evecs = []
+    for t in range(RESIDENT_T):
+        X = (rng.standard_normal((Ne, n)) + 1j * rng.standard_normal((Ne, n))) / np.sqrt(2 * n)
+        evecs.append(X)
+    return gauge, evecs
+
+
+def cpu_reference_sample(latt, Ne, threads):
+    """Time the oracle (CPU restatement of the reference numpy path) on a
+    bounded sample: one momentum of one timeslice with all 13 operators
+    (all chains + 43 zgemm), plus one extra zgemm to extrapolate to 27 momenta."""
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
+    import numpy as np
+
+    from oracle import restatement as R
+
+    gauge, evecs = make_inputs(latt, Ne)
+    U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
+    V = evecs[0].reshape(Ne, latt[2], latt[1], latt[0], 3)
+    moms = R.mom_dict_to_list(3)
+    t0 = time.perf_counter()
+    R.elemental(V, U, latt, NUM_NABLA, moms[:1])
+    t1 = time.perf_counter()
+    ph = R.momentum_phase(latt, moms[1])
+    left = V.astype(np.complex64).astype(np.complex128)
+    t2 = time.perf_counter()
+    lp = (ph[None, :, :, :, None] * left.conj()).reshape(Ne, -1)
+    _ = lp @ left.reshape(Ne, -1).T
+    t3 = time.perf_counter()
+    one_mom = t1 - t0
+    per_gemm = t3 - t2
+    pairs = 43
+    per_ts = one_mom + (NMOM - 1) * pairs * per_gemm
+    return per_ts, f"oracle ElementalGenerator.calc at {latt[0]}^3, Ne={Ne}, 13 ops x 1 momentum ({one_mom:.1f} s) " \
+                   f"+ 26 x 43 momentum GEMMs extrapolated from one ({per_gemm:.2f} s)"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = len(os.sched_getaffinity(0))
+    latt = [int(v) for v in args.lattice.split(",")] if args.lattice else LATT
+    times = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        per_ts, sample = cpu_reference_sample(latt, args.ne, threads)
+        if i >= args.warmup:
+            times.append(per_ts)
+    per_ts = statistics.median(times)
+    val = 1.0 / per_ts
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "timeslices/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_ts * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": f"elemental {latt[0]}^3x{latt[3]}, Ne={args.ne}, 13 ops x 27 momenta (CPU sample)"},
+        "cpu_baseline": {"value": val, "unit": "timeslices/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "timeslices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- ours
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+
+    from easydistillation_gb300 import ElementalGenerator
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.ops import ElementalPlan
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    latt = [int(v) for v in args.lattice.split(",")] if args.lattice else LATT
+    Lx, Ly, Lz, Lt = latt
+    V3 = Lx * Ly * Lz
+    Ne = args.ne
+    from oracle.restatement import mom_dict_to_list  # momentum list only
+
+    moms = mom_dict_to_list(3)[:NMOM]
+    gauge, evecs_host = make_inputs(latt, Ne, seed=2 + rank)
+    U = links_to_device(gauge, latt, dev)  # [3, Lt, Lz, Ly, Lx, 3, 3] c128 resident
+    V = [torch.from_numpy(x).to(dev) for x in evecs_host]  # resident c128 eigenvectors
+    plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev)
+    out = torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(i):
+        t = (i * 7 + rank) % Lt
+        plan.run(U[:, t], Lt * V3 * 9, 9, V[i % RESIDENT_T], out)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(dev.index)
+    sampler.start()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for i in range(args.steps):
+        step(args.warmup + i)
+    end.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = start.elapsed_time(end)
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_per_step = ms / args.steps
+    value = world * args.steps / (ms / 1e3)
+
+    # dominant kernel: time the pair-contraction launch alone with events
+    roofline = None
+
+    # end to end through the public generator: host eigenvectors in, host elementals out
+    e2e = None
+    if not args.no_e2e:
+        class _D:
+            def __init__(self, a):
+                self.a = a
+                self.file = "mem"
+
+            def __getitem__(self, k):
+                return self.a[k]
+
+        class _Src:
+            def __init__(self, a, Ne=None):
+                self.d = _D(a)
+                self.Ne = Ne
+
+            def load(self, key):
+                return self.d
+
+        ev = np.stack([x.reshape(Ne, Lz, Ly, Lx, 3) for x in evecs_host])  # [RESIDENT_T, Ne, ...]
+        gen = ElementalGenerator(latt, _Src(gauge), _Src(ev, Ne), NUM_NABLA, moms, precision=args.mode, device=dev)
+        gen.load("bench")
+        host_out = torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128).pin_memory()
+        for i in range(min(args.warmup, 2)):
+            host_out.copy_(gen.calc(i % RESIDENT_T))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            host_out.copy_(gen.calc(i % RESIDENT_T))
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        e2e = {"value": world * args.steps / dt, "unit": "timeslices/s",
+               "h2d_bytes_per_step": Ne * V3 * 3 * 16, "d2h_bytes_per_step": int(host_out.numel() * 16)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = len(os.sched_getaffinity(0))
+        per_ts, sample = cpu_reference_sample(latt, Ne, threads)
+        cpu = {"value": 1.0 / per_ts, "unit": "timeslices/s", "cores": threads, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "timeslices/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128" if args.mode == "fp64" else args.mode, "data": "synthetic",
+            "config": {"workload": f"elemental {Lx}^3x{Lt}, Ne={Ne}, 13 ops x {NMOM} momenta, mode={args.mode}",
+                       "pairs_per_momentum": plan.num_pairs, "l2": "inputs larger than L2 (rotating timeslices)",
+                       "parallelism": f"replicas x{world}"},
+            "gpu_launches": args.steps * (4 + 12 + 1 + 1),
+            "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

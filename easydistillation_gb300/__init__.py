@@ -1,0 +1,32 @@
+"""GB300-native (sm_103a) implementation of EasyDistillation's hot path.
+
+Drop-in generators (same constructors, ``load(key)`` and ``calc(t)`` as
+``lattice.generator``):
+
+* :class:`EigenvectorGenerator` -- lowest eigenpairs of the 3D covariant
+  Laplacian per timeslice (GPU stencil kernel inside a GPU thick-restart
+  Lanczos);
+* :class:`ElementalGenerator` -- displaced, momentum-projected elementals
+  ``E[d, p, i, j]`` (GPU covariant-derivative chains and pair contractions).
+
+The arithmetic runs in ``libeasydist_gb300.so`` (C ABI:
+``include/easydist_gb300.h``), built in-tree by
+``python -m easydistillation_gb300.build``.  There is no CPU fallback.
+"""
+
+from .generator import EigenvectorGenerator, ElementalGenerator
+from .insertion import MomentumPhase, derivative, mom_dict_to_list, num_derivative
+
+NC, NS, ND = 3, 4, 4
+
+__all__ = [
+    "EigenvectorGenerator",
+    "ElementalGenerator",
+    "MomentumPhase",
+    "derivative",
+    "mom_dict_to_list",
+    "num_derivative",
+    "NC",
+    "NS",
+    "ND",
+]

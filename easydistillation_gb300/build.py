@@ -1,0 +1,83 @@
+"""In-tree build of the CUDA library ``libeasydist_gb300.so`` for sm_103a.
+
+    python -m easydistillation_gb300.build [--force]
+
+Each ``csrc/*.cu`` translation unit is compiled in parallel by nvcc
+(``-gencode arch=compute_103a,code=sm_103a``) into ``_build/`` and linked into
+``libeasydist_gb300.so`` beside this file.  Units are rebuilt only when a
+source or header is newer than their object.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libeasydist_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA 13 toolkit is required to build easydistillation_gb300")
+
+
+def _headers():
+    return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+
+
+def _compile(nvcc: str, src: str, obj: str) -> str:
+    cmd = [nvcc, *ARCH, *FLAGS, "-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    nvcc = _nvcc()
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    hdr_mtime = max([os.path.getmtime(h) for h in _headers()] + [0.0])
+    jobs = []
+    objs = []
+    for src in srcs:
+        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        objs.append(obj)
+        stale = force or not os.path.exists(obj)
+        if not stale:
+            t = os.path.getmtime(obj)
+            stale = t < os.path.getmtime(src) or t < hdr_mtime
+        if stale:
+            jobs.append((src, obj))
+    with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+        for obj in ex.map(lambda a: _compile(nvcc, *a), jobs):
+            if verbose:
+                print("compiled", os.path.basename(obj))
+    relink = force or bool(jobs) or not os.path.exists(LIB)
+    if not relink:
+        lt = os.path.getmtime(LIB)
+        relink = any(os.path.getmtime(o) > lt for o in objs)
+    if relink:
+        tmp = LIB + ".tmp"
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

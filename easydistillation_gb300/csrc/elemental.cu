@@ -1,0 +1,462 @@
+// Elemental contraction E[d, p, i, j] (reference lattice/generator/elemental.py:290-338).
+//
+// The reference evaluates, for every derivative operator d and each of the
+// 2^len(d) left/right subsets, a fresh pair of covariant-derivative chains and
+// one zgemm per momentum.  Here one timeslice is planned once:
+//   1. chains: every direction sequence s of length <= num_nabla is built once
+//      (chain id = derivative index of s, derivative.py:23-33), each from its
+//      parent by one hop kernel;
+//   2. pair contractions G_p(X, Y)[i, j] = sum_k conj(X_i[k]) phase_p(k) Y_j[k]
+//      for the distinct (left, right) chain pairs, grouped by left chain with a
+//      contiguous range of right chains (one GEMM per group and momentum);
+//      when the momentum list is closed under p -> -p, pairs with left > right
+//      come from G_p(X, Y) = G_{-p}(Y, X)^dagger instead of a second GEMM;
+//   3. combine: E[d, p] = sum_subsets (-1)^{#right} G_p(left, right), times the
+//      blending coefficients when present (elemental.py:309-337).
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "common.cuh"
+#include "elemental.cuh"
+
+namespace ed {
+
+int launch_links_to_soa(int out_prec, Latt L, int nt, const void* in, long long ts, long long ds, long long ss,
+                        void* out, cudaStream_t stream);
+int launch_to_planes(int ip, int op, int round_c64, long long nvec, int V3, const void* in, void* out,
+                     cudaStream_t stream);
+int launch_phases(Latt L, const int* moms, int nmom, cplx<double>* out, cudaStream_t stream);
+int launch_hop(int in_prec, int out_prec, Latt L, int d, int nvec, const void* links_c128, const void* in,
+               void* out, cudaStream_t stream);
+
+// ------------------------------------------------------------ plan (host)
+
+static std::vector<int> derivative_seq(int n) {
+  int len = 0, block = 1;
+  while (n >= block) {
+    n -= block;
+    ++len;
+    block *= 3;
+  }
+  std::vector<int> d(len);
+  for (int k = len - 1; k >= 0; --k) {
+    d[k] = n % 3;
+    n /= 3;
+  }
+  return d;
+}
+
+static int chain_id(const std::vector<int>& s) {
+  int base = 0, p3 = 1;
+  for (size_t k = 0; k < s.size(); ++k) {
+    base += p3;
+    p3 *= 3;
+  }
+  int v = 0;
+  for (int d : s) v = v * 3 + d;
+  return base + v;
+}
+
+int plan_build(ed_elemental_plan* P) {
+  P->V3 = P->Lx * P->Ly * P->Lz;
+  P->nderiv = 0;
+  for (int k = 0, p3 = 1; k <= P->num_nabla; ++k, p3 *= 3) P->nderiv += p3;
+  P->nchain = P->nderiv;
+  P->chain_parent.assign(P->nchain, -1);
+  P->chain_dir.assign(P->nchain, -1);
+  for (int c = 1; c < P->nchain; ++c) {
+    std::vector<int> s = derivative_seq(c);
+    P->chain_dir[c] = s.back();
+    s.pop_back();
+    P->chain_parent[c] = chain_id(s);
+  }
+  // momentum negation table
+  P->negidx.assign(P->nmom, -1);
+  bool closed = true;
+  for (int a = 0; a < P->nmom; ++a) {
+    for (int b = 0; b < P->nmom; ++b)
+      if (P->moms[3 * b] == -P->moms[3 * a] && P->moms[3 * b + 1] == -P->moms[3 * a + 1] &&
+          P->moms[3 * b + 2] == -P->moms[3 * a + 2]) {
+        P->negidx[a] = b;
+        break;
+      }
+    if (P->negidx[a] < 0) closed = false;
+  }
+  P->herm = closed && P->use_herm && P->nmom <= kMaxMom;
+
+  // terms (elemental.py:309-321): bit k of `pick` sends direction k right
+  struct RawTerm {
+    int d, coeff, X, Y;
+  };
+  std::vector<RawTerm> raw;
+  for (int d = 0; d < P->nderiv; ++d) {
+    std::vector<int> dv = derivative_seq(d);
+    for (int pick = 0; pick < (1 << dv.size()); ++pick) {
+      std::vector<int> right, left;
+      for (size_t k = 0; k < dv.size(); ++k) ((pick >> k) & 1 ? right : left).push_back(dv[k]);
+      std::reverse(left.begin(), left.end());
+      raw.push_back({d, (right.size() % 2) ? -1 : 1, chain_id(left), chain_id(right)});
+    }
+  }
+  // needed (left, right) pairs, canonical under hermiticity
+  std::map<int, std::pair<int, int>> range;  // left -> [ymin, ymax]
+  for (auto& r : raw) {
+    int X = r.X, Y = r.Y;
+    if (P->herm && X > Y) std::swap(X, Y);
+    auto it = range.find(X);
+    if (it == range.end())
+      range[X] = {Y, Y};
+    else
+      it->second = {std::min(it->second.first, Y), std::max(it->second.second, Y)};
+  }
+  P->jobs.clear();
+  long long goff = 0;
+  for (auto& kv : range) {
+    Job j;
+    j.left = kv.first;
+    j.right0 = kv.second.first;
+    j.nright = kv.second.second - kv.second.first + 1;
+    j.g_off = goff;
+    goff += (long long)P->nmom * P->Ne * j.nright * P->Ne;
+    P->jobs.push_back(j);
+  }
+  P->g_elems = goff;
+  if ((int)P->jobs.size() > kMaxJobs) {
+    set_error("elemental plan: %d pair groups exceed the limit %d", (int)P->jobs.size(), kMaxJobs);
+    return ED_ERR_UNSUPPORTED;
+  }
+  auto job_of = [&](int X) {
+    for (size_t k = 0; k < P->jobs.size(); ++k)
+      if (P->jobs[k].left == X) return (int)k;
+    return -1;
+  };
+  P->terms.clear();
+  P->term_start.assign(P->nderiv + 1, 0);
+  for (int d = 0; d < P->nderiv; ++d) {
+    P->term_start[d] = (int)P->terms.size();
+    for (auto& r : raw) {
+      if (r.d != d) continue;
+      Term t;
+      t.coeff = r.coeff;
+      if (P->herm && r.X > r.Y) {
+        t.job = job_of(r.Y);
+        t.roff = r.X - P->jobs[t.job].right0;
+        t.herm = 1;
+      } else {
+        t.job = job_of(r.X);
+        t.roff = r.Y - P->jobs[t.job].right0;
+        t.herm = 0;
+      }
+      P->terms.push_back(t);
+    }
+  }
+  P->term_start[P->nderiv] = (int)P->terms.size();
+  if ((int)P->terms.size() > kMaxTerms) {
+    set_error("elemental plan: %d terms exceed the limit %d", (int)P->terms.size(), kMaxTerms);
+    return ED_ERR_UNSUPPORTED;
+  }
+  P->npairs = 0;
+  for (auto& j : P->jobs) P->npairs += j.nright;
+
+  // workspace layout (256-byte aligned sections)
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+  size_t off = 0;
+  P->off_links = off;
+  off = up(off + 27ull * P->V3 * 16);
+  P->off_phase = off;
+  off = up(off + (size_t)P->nmom * P->V3 * 16);
+  P->off_chain = off;
+  const size_t chain_elt = P->mode == ED_MODE_FP64 ? 16 : 8;
+  off = up(off + (size_t)P->nchain * P->Ne * 3 * P->V3 * chain_elt);
+  P->off_g = off;
+  off = up(off + (size_t)P->g_elems * 16);
+  P->off_extra = off;
+  off = up(off + tc_extra_workspace(P));
+  P->ws_bytes = off;
+  return ED_OK;
+}
+
+// ------------------------------------------------------------ FP64 pair GEMM
+
+struct GemmJobDev {
+  int left, right0, nright, tile0, mt, nt;
+  long long g_off;
+};
+struct GemmTable {
+  int njobs;
+  GemmJobDev j[kMaxJobs];
+};
+
+constexpr int F64_BM = 64, F64_BN = 64, F64_BK = 8;
+
+// One CTA = a 64x64 tile of G_p(X, Y-range) for one (group, momentum).
+// 256 threads as 16x16, each owning 4x4 complex outputs.  The left operand is
+// multiplied by the phase while staged: A[i][k] = conj(X_i[k]) * phase_p(k mod V3).
+__global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int Ne, int V3, int nmom,
+                                                            const cplx<double>* __restrict__ chains,
+                                                            const cplx<double>* __restrict__ phases,
+                                                            cplx<double>* __restrict__ G) {
+  __shared__ cplx<double> As[F64_BK][F64_BM + 1];
+  __shared__ cplx<double> Bs[F64_BK][F64_BN + 1];
+  int tile = blockIdx.x;
+  int jb = 0;
+  while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
+  const GemmJobDev J = tab.j[jb];
+  int local = tile - J.tile0;
+  const int per_p = J.mt * J.nt;
+  const int p = local / per_p;
+  local -= p * per_p;
+  const int mtile = local / J.nt;
+  const int ntile = local - mtile * J.nt;
+  const long long K = 3LL * V3;
+  const int M = Ne, N = J.nright * Ne;
+  const cplx<double>* Lc = chains + (long long)J.left * Ne * K;
+  const cplx<double>* Rc = chains + (long long)J.right0 * Ne * K;
+  const cplx<double>* ph = phases + (long long)p * V3;
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int lk = tid & 7, lr = tid >> 3;  // loader: 8 consecutive k per row, 32 rows per pass
+  cplx<double> acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = mk(0.0, 0.0);
+
+  for (long long k0 = 0; k0 < K; k0 += F64_BK) {
+    const long long k = k0 + lk;
+    cplx<double> phk = mk(0.0, 0.0);
+    if (k < K) phk = ld(ph + (k % V3));
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      const int r = lr + 32 * pass;
+      const int gi = mtile * F64_BM + r;
+      cplx<double> a = mk(0.0, 0.0);
+      if (gi < M && k < K) a = cmul_conj(ld(Lc + (long long)gi * K + k), phk);
+      As[lk][r] = a;
+      const int gj = ntile * F64_BN + r;
+      cplx<double> b = mk(0.0, 0.0);
+      if (gj < N && k < K) b = ld(Rc + (long long)gj * K + k);
+      Bs[lk][r] = b;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < F64_BK; ++kk) {
+      cplx<double> av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = As[kk][ty + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cfma(acc[a][b], av[a], bv[b]);
+    }
+    __syncthreads();
+  }
+  cplx<double>* Gp = G + J.g_off + (long long)p * M * N;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int gi = mtile * F64_BM + ty + 16 * a;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int gj = ntile * F64_BN + tx + 16 * b;
+      if (gj < N) Gp[(long long)gi * N + gj] = acc[a][b];
+    }
+  }
+}
+
+// ------------------------------------------------------------ combine
+
+struct CombineTable {
+  int nderiv, herm, nmom, Ne;
+  int start[kMaxDeriv + 1];
+  Term t[kMaxTerms];
+  long long g_off[kMaxJobs];
+  int nright[kMaxJobs];
+  short negidx[kMaxMom];
+};
+
+// The term table travels as a kernel argument (about 2 KB).
+__global__ void combine_kernel(const CombineTable tab, const cplx<double>* __restrict__ G,
+                               const double* __restrict__ blend, cplx<double>* __restrict__ out) {
+  const int Ne = tab.Ne;
+  const long long total = (long long)tab.nderiv * tab.nmom * Ne * Ne;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(idx % Ne);
+    const int i = (int)((idx / Ne) % Ne);
+    const int p = (int)((idx / ((long long)Ne * Ne)) % tab.nmom);
+    const int d = (int)(idx / ((long long)Ne * Ne * tab.nmom));
+    cplx<double> acc = mk(0.0, 0.0);
+    for (int q = tab.start[d]; q < tab.start[d + 1]; ++q) {
+      const Term T = tab.t[q];
+      const int N = tab.nright[T.job] * Ne;
+      cplx<double> v;
+      if (!T.herm) {
+        v = G[tab.g_off[T.job] + ((long long)p * Ne + i) * N + T.roff * Ne + j];
+      } else {
+        const int np = tab.negidx[p];
+        cplx<double> w = G[tab.g_off[T.job] + ((long long)np * Ne + j) * N + T.roff * Ne + i];
+        v = mk(w.re, -w.im);
+      }
+      acc.re += T.coeff * v.re;
+      acc.im += T.coeff * v.im;
+    }
+    if (blend) {
+      const double c = blend[(long long)i * Ne + j];
+      acc.re *= c;
+      acc.im *= c;
+    }
+    out[idx] = acc;
+  }
+}
+
+// ------------------------------------------------------------ run
+
+int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains, const cplx<double>* phases,
+                         cplx<double>* G, cudaStream_t stream) {
+  GemmTable tab;
+  tab.njobs = (int)P->jobs.size();
+  int tiles = 0;
+  for (int k = 0; k < tab.njobs; ++k) {
+    const Job& j = P->jobs[k];
+    GemmJobDev& d = tab.j[k];
+    d.left = j.left;
+    d.right0 = j.right0;
+    d.nright = j.nright;
+    d.g_off = j.g_off;
+    d.mt = ceil_div(P->Ne, F64_BM);
+    d.nt = ceil_div((long long)j.nright * P->Ne, F64_BN);
+    d.tile0 = tiles;
+    tiles += d.mt * d.nt * P->nmom;
+  }
+  pair_gemm_f64_kernel<<<tiles, 256, 0, stream>>>(tab, P->Ne, P->V3, P->nmom, chains, phases, G);
+  ED_RETURN_LAUNCH("pair GEMM (fp64)");
+  return ED_OK;
+}
+
+int launch_combine(const ed_elemental_plan* P, const cplx<double>* G, const double* blend, cplx<double>* out,
+                   cudaStream_t stream) {
+  CombineTable tab;
+  memset(&tab, 0, sizeof(tab));
+  tab.nderiv = P->nderiv;
+  tab.herm = P->herm;
+  tab.nmom = P->nmom;
+  tab.Ne = P->Ne;
+  for (int d = 0; d <= P->nderiv; ++d) tab.start[d] = P->term_start[d];
+  for (size_t q = 0; q < P->terms.size(); ++q) tab.t[q] = P->terms[q];
+  for (size_t k = 0; k < P->jobs.size(); ++k) {
+    tab.g_off[k] = P->jobs[k].g_off;
+    tab.nright[k] = P->jobs[k].nright;
+  }
+  for (int p = 0; p < P->nmom && p < kMaxMom; ++p) tab.negidx[p] = (short)P->negidx[p];
+  const long long total = (long long)P->nderiv * P->nmom * P->Ne * P->Ne;
+  const int grid = (int)std::min<long long>(ceil_div(total, 256), 4LL * 1024 * num_sms());
+  combine_kernel<<<grid, 256, 0, stream>>>(tab, G, blend, out);
+  ED_RETURN_LAUNCH("combine");
+  return ED_OK;
+}
+
+
+int elemental_run(const ed_elemental_plan* P, const void* links, long long dir_stride, long long site_stride,
+                  int evec_prec, const void* evecs, const double* blend, void* out, void* ws, size_t ws_bytes,
+                  cudaStream_t stream) {
+  char* W = (char*)ws;
+  const Latt L{P->Lx, P->Ly, P->Lz};
+  int rc;
+  void* links_soa = W + P->off_links;
+  rc = launch_links_to_soa(ED_C128, L, 1, links, 0, dir_stride, site_stride, links_soa, stream);
+  if (rc) return rc;
+  cplx<double>* phases = (cplx<double>*)(W + P->off_phase);
+  rc = launch_phases(L, P->moms.data(), P->nmom, phases, stream);
+  if (rc) return rc;
+  const int cprec = P->mode == ED_MODE_FP64 ? ED_C128 : ED_C64;
+  const size_t celt = cprec == ED_C128 ? 16 : 8;
+  char* chains = W + P->off_chain;
+  const size_t chain_bytes = (size_t)P->Ne * 3 * P->V3 * celt;
+  rc = launch_to_planes(evec_prec, cprec, 1, P->Ne, P->V3, evecs, chains, stream);
+  if (rc) return rc;
+  for (int c = 1; c < P->nchain; ++c) {
+    rc = launch_hop(cprec, cprec, L, P->chain_dir[c], P->Ne, links_soa, chains + P->chain_parent[c] * chain_bytes,
+                    chains + c * chain_bytes, stream);
+    if (rc) return rc;
+  }
+  cplx<double>* G = (cplx<double>*)(W + P->off_g);
+  if (P->mode == ED_MODE_FP64) {
+    rc = launch_pair_gemm_f64(P, (const cplx<double>*)chains, phases, G, stream);
+  } else {
+    rc = launch_pair_gemm_tc(P, (const cplx<float>*)chains, phases, G, W + P->off_extra, stream);
+  }
+  if (rc) return rc;
+  return launch_combine(P, G, blend, (cplx<double>*)out, stream);
+}
+
+}  // namespace ed
+
+// ------------------------------------------------------------ C ABI
+
+extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne, int num_nabla,
+                                        const int* moms, int nmom, int mode) {
+  ED_CHECK_ARG(plan, "ed_elemental_plan_create: null plan pointer");
+  *plan = nullptr;
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0, "ed_elemental_plan_create: sizes must be positive");
+  ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create: num_nabla must be 0, 1 or 2");
+  ED_CHECK_ARG(moms, "ed_elemental_plan_create: null momentum list");
+  ED_CHECK_ARG(ed::mode_supported(mode), "ed_elemental_plan_create: unknown mode %d", mode);
+  ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create: lattice too large");
+  auto* P = new ed_elemental_plan();
+  P->Lx = Lx;
+  P->Ly = Ly;
+  P->Lz = Lz;
+  P->Ne = Ne;
+  P->num_nabla = num_nabla;
+  P->nmom = nmom;
+  P->mode = mode;
+  P->use_herm = true;
+  P->moms.assign(moms, moms + 3 * nmom);
+  int rc = ed::plan_build(P);
+  if (rc == ED_OK) rc = ed::tc_plan_check(P);
+  if (rc != ED_OK) {
+    delete P;
+    return rc;
+  }
+  *plan = P;
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_plan_destroy(ed_elemental_plan* plan) {
+  delete plan;
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_workspace_size(const ed_elemental_plan* plan, size_t* bytes) {
+  ED_CHECK_ARG(plan && bytes, "ed_elemental_workspace_size: null pointer");
+  *bytes = plan->ws_bytes;
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_num_pairs(const ed_elemental_plan* plan, int* npairs) {
+  ED_CHECK_ARG(plan && npairs, "ed_elemental_num_pairs: null pointer");
+  *npairs = plan->npairs;
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_run(const ed_elemental_plan* plan, const void* links, long long dir_stride,
+                                long long site_stride, int evec_prec, const void* evecs, const double* blend,
+                                void* out, void* workspace, size_t workspace_bytes, void* stream) {
+  ED_CHECK_ARG(plan, "ed_elemental_run: null plan");
+  ED_CHECK_ARG(links && evecs && out && workspace, "ed_elemental_run: null pointer");
+  ED_CHECK_ARG(evec_prec == ED_C128 || evec_prec == ED_C64, "ed_elemental_run: bad eigenvector precision");
+  ED_CHECK_ARG(dir_stride >= 0 && site_stride >= 0, "ed_elemental_run: negative stride");
+  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0, "ed_elemental_run: workspace must be 256-byte aligned");
+  if (workspace_bytes < plan->ws_bytes) {
+    ed::set_error("ed_elemental_run: workspace of %zu bytes is smaller than the %zu the plan needs", workspace_bytes,
+                  plan->ws_bytes);
+    return ED_ERR_WORKSPACE;
+  }
+  return ed::elemental_run(plan, links, dir_stride, site_stride, evec_prec, evecs, blend, out, workspace,
+                           workspace_bytes, (cudaStream_t)stream);
+}

@@ -1,0 +1,53 @@
+// Elemental plan: host-side description of one timeslice of elementals.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace ed {
+
+constexpr int kMaxJobs = 32;   // pair groups (one per left chain)
+constexpr int kMaxTerms = 64;  // subset terms over all operators (43 for num_nabla = 2)
+constexpr int kMaxDeriv = 13;  // operators for num_nabla = 2
+constexpr int kMaxMom = 256;   // momenta for which p -> -p lookup is tabulated
+
+// One GEMM group: left chain `left` against right chains [right0, right0+nright).
+struct Job {
+  int left, right0, nright;
+  long long g_off;  // offset of G[nmom][Ne][nright*Ne] in complex elements
+};
+
+// One subset term of an operator: coeff * G_p(left, right), or, when herm,
+// coeff * conj(G_{-p}(right, left))^T read from group `job`.
+struct Term {
+  int coeff, job, roff, herm;
+};
+
+}  // namespace ed
+
+struct ed_elemental_plan {
+  int Lx, Ly, Lz, V3, Ne, num_nabla, nderiv, nmom, mode;
+  bool use_herm, herm;
+  std::vector<int> moms, negidx;
+  int nchain;
+  std::vector<int> chain_parent, chain_dir;
+  std::vector<ed::Job> jobs;
+  std::vector<ed::Term> terms;
+  std::vector<int> term_start;
+  long long g_elems;
+  int npairs;
+  size_t off_links, off_phase, off_chain, off_g, off_extra, ws_bytes;
+  // tensor-core path parameters (filled by tc_plan_check)
+  int tc_kind;        // 0 = none
+  int tc_scale_exp;   // power-of-two scale applied before fp16 splitting
+  size_t tc_bytes;    // extra workspace
+};
+
+namespace ed {
+bool mode_supported(int mode);
+size_t tc_extra_workspace(const ed_elemental_plan* P);
+int tc_plan_check(ed_elemental_plan* P);
+int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
+                        cplx<double>* G, void* extra, cudaStream_t stream);
+}  // namespace ed

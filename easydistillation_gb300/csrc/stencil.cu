@@ -1,0 +1,304 @@
+// 3D covariant Laplacian and single covariant-derivative hop on SoA links.
+//
+// Laplacian (reference lattice/generator/eigenvector.py:11-26):
+//   (L F)(x) = 6 F(x) - sum_{mu=x,y,z} [ U_mu(x) F(x+mu) + U_mu(x-mu)^dag F(x-mu) ]
+// Covariant derivative hop (reference lattice/generator/elemental.py:282-287):
+//   (D_d F)(x) = U_d(x) F(x+d) - U_d(x-d)^dag F(x-d)           (no factor 1/2)
+// Periodic boundaries in x, y, z.  Links are SoA per timeslice
+// [dir][row][col][V3], vectors are colour planes [colour][V3].
+//
+// The Laplacian is HBM-bound: per application it moves 27 link + 3 input +
+// 3 output complex numbers per site.  Every thread handles S consecutive
+// x-sites so that every plane access is one 128-bit load (S=1 for c128 =
+// double2, S=2 for c64 = float4).
+#include "common.cuh"
+
+namespace ed {
+
+template <typename T, int S>
+struct Pack;
+
+template <>
+struct Pack<double, 1> {
+  __device__ __forceinline__ static void load(const cplx<double>* p, cplx<double> (&o)[1]) { o[0] = ld(p); }
+  __device__ __forceinline__ static void store(cplx<double>* p, const cplx<double> (&o)[1]) {
+    *reinterpret_cast<double2*>(p) = make_double2(o[0].re, o[0].im);
+  }
+};
+
+template <>
+struct Pack<float, 2> {
+  __device__ __forceinline__ static void load(const cplx<float>* p, cplx<float> (&o)[2]) {
+    float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = mk(v.x, v.y);
+    o[1] = mk(v.z, v.w);
+  }
+  __device__ __forceinline__ static void store(cplx<float>* p, const cplx<float> (&o)[2]) {
+    *reinterpret_cast<float4*>(p) = make_float4(o[0].re, o[0].im, o[1].re, o[1].im);
+  }
+};
+
+// y += U x  (U given as 9 row-major complex)
+template <typename T>
+__device__ __forceinline__ void mv_add(cplx<T> (&y)[3], const cplx<T> (&U)[9], const cplx<T> (&x)[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) cfma(y[a], U[a * 3 + b], x[b]);
+}
+// y += U^dag x
+template <typename T>
+__device__ __forceinline__ void mvd_add(cplx<T> (&y)[3], const cplx<T> (&U)[9], const cplx<T> (&x)[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) cfma_conj(y[a], U[b * 3 + a], x[b]);
+}
+
+// One launch covers nt timeslices x nvec vectors; grid (sites/S/128, nvec, nt).
+template <typename T, int S>
+__global__ void __launch_bounds__(128) laplacian_kernel(Latt L, const cplx<T>* __restrict__ links,
+                                                        const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out,
+                                                        long long link_tstride, long long in_tstride,
+                                                        long long out_tstride, T diag) {
+  const int V3 = L.V3();
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid * S >= V3) return;
+  const int t = blockIdx.z;
+  const cplx<T>* U = links + (long long)t * link_tstride;
+  const long long voff = (long long)blockIdx.y * 3 * V3;
+  const cplx<T>* F = in + (long long)t * in_tstride + voff;
+  cplx<T>* O = out + (long long)t * out_tstride + voff;
+
+  const int s0 = tid * S;
+  const int x0 = s0 % L.Lx;
+  const int yz = s0 / L.Lx;
+  const int y = yz % L.Ly;
+  const int z = yz / L.Ly;
+  const int row = s0 - x0;  // site of (0, y, z)
+
+  cplx<T> acc[S][3];
+  {
+    cplx<T> f[3][S];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Pack<T, S>::load(F + c * V3 + s0, f[c]);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[s][c] = mk(diag * f[c][s].re, diag * f[c][s].im);
+  }
+  cplx<T> hop[S][3];
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) hop[s][c] = mk(T(0), T(0));
+
+  // ---------------- x direction (mu = 0)
+  {
+    const int xm = wrap_dec(x0, L.Lx);
+    const int xp = (x0 + S) % L.Lx;
+    cplx<T> uf[9][S];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Pack<T, S>::load(U + (0 * 9 + e) * V3 + s0, uf[e]);
+    cplx<T> ff[3][S];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Pack<T, S>::load(F + c * V3 + s0, ff[c]);
+    cplx<T> fxp[3], fxm[3], ubm[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      fxp[c] = ld(F + c * V3 + row + xp);
+      fxm[c] = ld(F + c * V3 + row + xm);
+    }
+#pragma unroll
+    for (int e = 0; e < 9; ++e) ubm[e] = ld(U + (0 * 9 + e) * V3 + row + xm);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      cplx<T> u[9], fn[3];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = uf[e][s];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) fn[c] = (s + 1 < S) ? ff[c][(s + 1) % S] : fxp[c];
+      mv_add(hop[s], u, fn);
+      cplx<T> ub[9], fb[3];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) ub[e] = (s > 0) ? uf[e][(s + S - 1) % S] : ubm[e];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) fb[c] = (s > 0) ? ff[c][(s + S - 1) % S] : fxm[c];
+      mvd_add(hop[s], ub, fb);
+    }
+  }
+  // ---------------- y and z directions (mu = 1, 2)
+#pragma unroll
+  for (int mu = 1; mu < 3; ++mu) {
+    int sp, sm;
+    if (mu == 1) {
+      sp = s0 + (wrap_inc(y, L.Ly) - y) * L.Lx;
+      sm = s0 + (wrap_dec(y, L.Ly) - y) * L.Lx;
+    } else {
+      sp = s0 + (wrap_inc(z, L.Lz) - z) * L.Lx * L.Ly;
+      sm = s0 + (wrap_dec(z, L.Lz) - z) * L.Lx * L.Ly;
+    }
+    cplx<T> uf[9][S], ub[9][S], fp[3][S], fm[3][S];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      Pack<T, S>::load(U + (mu * 9 + e) * V3 + s0, uf[e]);
+      Pack<T, S>::load(U + (mu * 9 + e) * V3 + sm, ub[e]);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      Pack<T, S>::load(F + c * V3 + sp, fp[c]);
+      Pack<T, S>::load(F + c * V3 + sm, fm[c]);
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      cplx<T> u[9], v[9], a[3], b[3];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        u[e] = uf[e][s];
+        v[e] = ub[e][s];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a[c] = fp[c][s];
+        b[c] = fm[c][s];
+      }
+      mv_add(hop[s], u, a);
+      mvd_add(hop[s], v, b);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    cplx<T> o[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) o[s] = acc[s][c] - hop[s][c];
+    Pack<T, S>::store(O + c * V3 + s0, o);
+  }
+}
+
+// Covariant-derivative hop in direction d for a block of vectors.  Links are
+// held in registers (two 3x3 per site) and reused over VB vectors.  Math in
+// double; input/output storage TI/TO (c128 or c64).
+template <typename TI, typename TO, int VB>
+__global__ void __launch_bounds__(128) hop_kernel(Latt L, int d, int nvec, const cplx<double>* __restrict__ U,
+                                                  const cplx<TI>* __restrict__ in, cplx<TO>* __restrict__ out) {
+  const int V3 = L.V3();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V3) return;
+  const int x = s % L.Lx;
+  const int yz = s / L.Lx;
+  const int y = yz % L.Ly;
+  const int z = yz / L.Ly;
+  int sp, sm;
+  if (d == 0) {
+    sp = s - x + wrap_inc(x, L.Lx);
+    sm = s - x + wrap_dec(x, L.Lx);
+  } else if (d == 1) {
+    sp = s + (wrap_inc(y, L.Ly) - y) * L.Lx;
+    sm = s + (wrap_dec(y, L.Ly) - y) * L.Lx;
+  } else {
+    sp = s + (wrap_inc(z, L.Lz) - z) * L.Lx * L.Ly;
+    sm = s + (wrap_dec(z, L.Lz) - z) * L.Lx * L.Ly;
+  }
+  cplx<double> uf[9], ub[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    uf[e] = ld(U + (d * 9 + e) * V3 + s);
+    ub[e] = ld(U + (d * 9 + e) * V3 + sm);
+  }
+  const int v0 = blockIdx.y * VB;
+  const int v1 = min(nvec, v0 + VB);
+  for (int v = v0; v < v1; ++v) {
+    const cplx<TI>* F = in + (long long)v * 3 * V3;
+    cplx<double> a[3], b[3], r[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      a[c] = cvt<double>(ld(F + c * V3 + sp));
+      b[c] = cvt<double>(ld(F + c * V3 + sm));
+      r[c] = mk(0.0, 0.0);
+    }
+    mv_add(r, uf, a);
+    cplx<double> q[3] = {mk(0.0, 0.0), mk(0.0, 0.0), mk(0.0, 0.0)};
+    mvd_add(q, ub, b);
+    cplx<TO>* O = out + (long long)v * 3 * V3;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) O[c * V3 + s] = cvt<TO>(r[c] - q[c]);
+  }
+}
+
+// ------------------------------------------------------------ launchers
+
+int launch_laplacian(int prec, Latt L, int nt, int nvec, const void* links, const void* in, long long its,
+                     void* out, long long ots, cudaStream_t stream) {
+  const int V3 = L.V3();
+  const long long lts = 27LL * V3;
+  if (prec == ED_C128) {
+    dim3 grid(ceil_div(V3, 128), nvec, nt);
+    laplacian_kernel<double, 1><<<grid, 128, 0, stream>>>(L, (const cplx<double>*)links, (const cplx<double>*)in,
+                                                           (cplx<double>*)out, lts, its, ots, 6.0);
+  } else {
+    dim3 grid(ceil_div(V3 / 2, 128), nvec, nt);
+    laplacian_kernel<float, 2><<<grid, 128, 0, stream>>>(L, (const cplx<float>*)links, (const cplx<float>*)in,
+                                                          (cplx<float>*)out, lts, its, ots, 6.0f);
+  }
+  ED_RETURN_LAUNCH("laplacian");
+  return ED_OK;
+}
+
+int launch_hop(int in_prec, int out_prec, Latt L, int d, int nvec, const void* links_c128, const void* in,
+               void* out, cudaStream_t stream) {
+  constexpr int VB = 8;
+  const int V3 = L.V3();
+  dim3 grid(ceil_div(V3, 128), ceil_div(nvec, VB));
+  const cplx<double>* U = (const cplx<double>*)links_c128;
+  if (in_prec == ED_C128 && out_prec == ED_C128)
+    hop_kernel<double, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<double>*)in,
+                                                             (cplx<double>*)out);
+  else if (in_prec == ED_C64 && out_prec == ED_C64)
+    hop_kernel<float, float, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<float>*)in,
+                                                           (cplx<float>*)out);
+  else if (in_prec == ED_C64 && out_prec == ED_C128)
+    hop_kernel<float, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<float>*)in,
+                                                            (cplx<double>*)out);
+  else
+    hop_kernel<double, float, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<double>*)in,
+                                                            (cplx<float>*)out);
+  ED_RETURN_LAUNCH("covariant derivative hop");
+  return ED_OK;
+}
+
+}  // namespace ed
+
+// ------------------------------------------------------------ C ABI
+
+extern "C" int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, const void* links, const void* in,
+                            long long in_tstride, void* out, long long out_tstride, void* stream) {
+  ED_CHECK_ARG(prec == ED_C128 || prec == ED_C64, "ed_laplacian: prec must be ED_C128 or ED_C64");
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nvec > 0, "ed_laplacian: sizes must be positive");
+  ED_CHECK_ARG(prec == ED_C128 || Lx % 2 == 0, "ed_laplacian: c64 path needs an even Lx");
+  ED_CHECK_ARG(nvec <= 65535 && nt <= 65535, "ed_laplacian: nvec and nt must be <= 65535");
+  ED_CHECK_ARG(links && in && out, "ed_laplacian: null pointer");
+  ED_CHECK_ARG(in != out, "ed_laplacian: in and out must not alias");
+  ED_CHECK_ARG(((uintptr_t)links % 16) == 0 && ((uintptr_t)in % 16) == 0 && ((uintptr_t)out % 16) == 0,
+               "ed_laplacian: buffers must be 16-byte aligned");
+  ED_CHECK_ARG(in_tstride >= 0 && out_tstride >= 0, "ed_laplacian: negative stride");
+  const long long dflt = 3LL * Lx * Ly * Lz * nvec;
+  if (in_tstride == 0) in_tstride = dflt;
+  if (out_tstride == 0) out_tstride = dflt;
+  ED_CHECK_ARG(prec == ED_C128 || (in_tstride % 2 == 0 && out_tstride % 2 == 0),
+               "ed_laplacian: c64 strides must keep 16-byte alignment");
+  return ed::launch_laplacian(prec, ed::Latt{Lx, Ly, Lz}, nt, nvec, links, in, in_tstride, out, out_tstride,
+                              (cudaStream_t)stream);
+}
+
+extern "C" int ed_covariant_derivative(int in_prec, int out_prec, int Lx, int Ly, int Lz, int dir, int nvec,
+                                       const void* links_c128, const void* in, void* out, void* stream) {
+  ED_CHECK_ARG((in_prec == ED_C128 || in_prec == ED_C64) && (out_prec == ED_C128 || out_prec == ED_C64),
+               "ed_covariant_derivative: bad precision");
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nvec > 0, "ed_covariant_derivative: sizes must be positive");
+  ED_CHECK_ARG(dir >= 0 && dir < 3, "ed_covariant_derivative: dir must be 0, 1 or 2");
+  ED_CHECK_ARG(links_c128 && in && out, "ed_covariant_derivative: null pointer");
+  ED_CHECK_ARG(in != out, "ed_covariant_derivative: in and out must not alias");
+  ED_CHECK_ARG(ed::ceil_div(nvec, 8) <= 65535, "ed_covariant_derivative: too many vectors");
+  return ed::launch_hop(in_prec, out_prec, ed::Latt{Lx, Ly, Lz}, dir, nvec, links_c128, in, out,
+                        (cudaStream_t)stream);
+}

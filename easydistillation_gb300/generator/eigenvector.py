@@ -1,0 +1,127 @@
+"""GB300 drop-in for ``lattice.generator.EigenvectorGenerator``.
+
+Same constructor, ``load``, ``project_SU3``, ``stout_smear`` and ``calc``
+signatures as ``lattice/generator/eigenvector.py:30-53,356-370``.  ``calc(t)``
+computes the ``Ne`` lowest eigenpairs of the 3D covariant Laplacian on
+timeslice ``t`` with the library's stencil kernel inside a GPU thick-restart
+Lanczos (FP64 basis, reorthogonalisation and Rayleigh-Ritz), sorts them
+ascending and applies the reference's renormalisation phase
+(``eigenvector.py:249-257``).  It returns device tensors
+``(evecs [Ne, Lz, Ly, Lx, 3] complex128, evals [Ne] float64)``.
+
+``stencil_precision="fp32"`` runs the Lanczos iteration with the FP32 stencil
+and then refines the result with FP64 operator applications (an FP64
+Lanczos restarted from the FP32 Ritz vectors); ``"fp64"`` (default) uses the
+FP64 stencil throughout.
+"""
+
+from __future__ import annotations
+
+from typing import List, Sequence
+
+import torch
+
+from .. import lanczos as LZ
+from ..ops import links_to_soa, laplacian, vectors_from_planes
+from .elemental import links_to_device
+
+NC = 3
+
+
+def project_su3_(U: torch.Tensor, tol: float = 1e-15, max_iter: int = 100):
+    """In-place projection of links ``[..., 3, 3]`` onto U(3) by the averaged
+    inverse iteration of ``eigenvector.py:55-65`` (``U <- (U + U^-dag)/2``)."""
+    for _ in range(max_iter):
+        Uinv = torch.linalg.inv(U)
+        Uid = Uinv.conj().transpose(-1, -2)
+        eye = torch.eye(3, dtype=U.dtype, device=U.device)
+        if (U - Uid).abs().max() <= tol and (U @ U.conj().transpose(-1, -2) - eye).abs().max() <= tol:
+            break
+        U.copy_(0.5 * (U + Uid))
+    return U
+
+
+def stout_smear_links_(U: torch.Tensor, latt_size, nstep: int, rho: float):
+    from ..stout import stout_smear_
+
+    stout_smear_(U, latt_size, nstep, rho)
+
+
+class EigenvectorGenerator:
+    def __init__(self, latt_size: List[int], gauge_field, Ne: int, tol: float, *, stencil_precision: str = "fp64",
+                 device=None) -> None:
+        if stencil_precision not in ("fp64", "fp32"):
+            raise ValueError("stencil_precision must be 'fp64' or 'fp32'")
+        self.device = torch.device(device or "cuda")
+        self.latt_size = latt_size
+        self.gauge_field = gauge_field
+        self.Ne = Ne
+        self.tol = tol
+        self.stencil_precision = stencil_precision
+        self._U = None
+        self._soa = {}
+        self.last_stats = None
+
+    def load(self, key: str):
+        self._U = links_to_device(self.gauge_field.load(key)[:], self.latt_size, self.device)
+        self._soa = {}
+
+    def project_SU3(self):
+        project_su3_(self._U)
+        self._soa = {}
+
+    def stout_smear(self, nstep: int, rho: float):
+        stout_smear_links_(self._U, self.latt_size, nstep, rho)
+        self._soa = {}
+
+    def _links(self, dtype):
+        if dtype not in self._soa:
+            self._soa[dtype] = links_to_soa(self._U, self.latt_size, dtype=dtype)
+        return self._soa[dtype]
+
+    def _matvec(self, ts: Sequence[int], dtype):
+        Lx, Ly, Lz, Lt = self.latt_size
+        V3 = Lx * Ly * Lz
+        links = self._links(dtype)
+        idx = torch.as_tensor(list(ts), device=self.device)
+        sel = links if list(ts) == list(range(Lt)) else links.index_select(0, idx)
+
+        def mv(X: torch.Tensor) -> torch.Tensor:
+            B = X.shape[0]
+            if dtype == torch.complex128:
+                F = X.view(B, 1, NC, V3)
+            else:
+                F = X.to(dtype).view(B, 1, NC, V3)
+            out = laplacian(sel, F, self.latt_size)
+            return out.view(B, NC * V3).to(torch.complex128)
+
+        return mv
+
+    def calc_batch(self, ts: Sequence[int], apply_renorm_phase: bool = True):
+        """Eigenpairs of several timeslices solved in lock step."""
+        if self._U is None:
+            raise RuntimeError("call load(key) before calc(t)")
+        Lx, Ly, Lz, Lt = self.latt_size
+        V3 = Lx * Ly * Lz
+        n = NC * V3
+        ts = list(ts)
+        B = len(ts)
+        if self.stencil_precision == "fp32":
+            r32 = LZ.trlanczos(self._matvec(ts, torch.complex64), B, n, self.Ne, max(self.tol, 1e-6),
+                               device=self.device)
+            v0 = r32.evecs.sum(dim=1)
+            res = LZ.trlanczos(self._matvec(ts, torch.complex128), B, n, self.Ne, self.tol, v0=v0,
+                               device=self.device)
+            res.matvecs += r32.matvecs
+        else:
+            res = LZ.trlanczos(self._matvec(ts, torch.complex128), B, n, self.Ne, self.tol, device=self.device)
+        self.last_stats = {"restarts": res.restarts, "matvecs": res.matvecs, "converged": res.converged}
+        evals, evecs = LZ.sort_ascending(res.evals, res.evecs)
+        if apply_renorm_phase:
+            LZ.renorm_phase_(evecs)
+        out = vectors_from_planes(evecs.reshape(B, self.Ne, NC, V3), V3)
+        return out.reshape(B, self.Ne, Lz, Ly, Lx, NC), evals
+
+    def calc(self, t: int, apply_renorm_phase: bool = True, polynomial_degree: int = 0, lambda_cut: float = 0.0):
+        evecs, evals = self.calc_batch([t], apply_renorm_phase)
+        return evecs[0], evals[0]

@@ -1,0 +1,171 @@
+"""GB300 drop-in for ``lattice.generator.ElementalGenerator``.
+
+Same constructor, ``load(key)`` and ``calc(t)`` as the reference
+(``lattice/generator/elemental.py:17-105,290-338``); the contraction runs in
+the library's CUDA kernels (covariant-derivative chains, pair contractions,
+operator combination).  ``calc`` returns the generator's internal
+``[Nderiv, Nmom, Ne, Ne]`` complex128 device buffer, which the next call
+overwrites, exactly like the reference's ``self._VPV``.
+
+Extra keyword-only arguments: ``precision`` (``"fp64"``: plain FP64
+arithmetic with V rounded to complex64, as the reference) and ``device``.
+"""
+
+from __future__ import annotations
+
+from typing import List, Tuple
+
+import numpy as np
+import torch
+
+from ..insertion import MomentumPhase, derivative, num_derivative
+from ..ops import ElementalPlan
+
+ND = 4
+NC = 3
+
+
+def _blending_coeff(Ne: int, dilution) -> np.ndarray:
+    """Stochastic blending coefficients, as ``elemental.py:61-95``."""
+    totNe_list = dilution[0]
+    if isinstance(dilution[1], int):
+        usedNe_list = [dilution[1]] * len(dilution[0])
+    else:
+        usedNe_list = list(dilution[1])
+    assert len(usedNe_list) == len(totNe_list)
+    assert (np.array(usedNe_list) <= np.array(totNe_list)).all()
+    assert sum(usedNe_list) == Ne
+    coeff = np.zeros((Ne, Ne))
+    start1 = 0
+    for nv1 in range(len(usedNe_list)):
+        used1, tot1 = usedNe_list[nv1], totNe_list[nv1]
+        start2 = 0
+        for nv2 in range(len(usedNe_list)):
+            used2, tot2 = usedNe_list[nv2], totNe_list[nv2]
+            if nv1 != nv2:
+                coeff[start1 : start1 + used1, start2 : start2 + used2] = tot1 * tot2 / used1 / used2
+            else:
+                c1 = tot1 / used1
+                c2 = c1 * (tot1 - 1) / (used1 - 1)
+                block = np.full((used1, used2), c2)
+                np.fill_diagonal(block, c1)
+                coeff[start1 : start1 + used1, start2 : start2 + used2] = block
+            start2 += used2
+        start1 += used1
+    return coeff
+
+
+def _host_array(x) -> np.ndarray:
+    if isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy()
+    if hasattr(x, "get") and not isinstance(x, np.ndarray):  # cupy arrays
+        return x.get()
+    return np.asarray(x)
+
+
+def links_to_device(gauge_data, latt_size, device) -> torch.Tensor:
+    """Load ``gauge_field.load(key)[:]`` (ILDG order ``[Lt, Lz, Ly, Lx, Nd, 3, 3]``)
+    and return the spatial links in the generators' transposed layout
+    ``[3, Lt, Lz, Ly, Lx, 3, 3]`` complex128 on the device
+    (``elemental.py:103``, ``eigenvector.py:50``)."""
+    Lx, Ly, Lz, Lt = latt_size
+    if isinstance(gauge_data, torch.Tensor):
+        U = gauge_data.to(device=device, dtype=torch.complex128)
+    else:
+        arr = np.ascontiguousarray(_host_array(gauge_data)).astype(np.complex128, copy=False)
+        U = torch.from_numpy(arr).pin_memory().to(device, non_blocking=True)
+    U = U.reshape(Lt, Lz, Ly, Lx, -1, NC, NC)
+    return U.permute(4, 0, 1, 2, 3, 5, 6)[: ND - 1].contiguous()
+
+
+class ElementalGenerator:
+    def __init__(
+        self,
+        latt_size: List[int],
+        gauge_field,
+        eigenvector,
+        num_nabla: int = 0,
+        momentum_list: List[Tuple[int]] = [(0, 0, 0)],
+        dilution: Tuple = None,
+        is_blending: bool = False,
+        *,
+        precision: str = "fp64",
+        device=None,
+    ) -> None:
+        Lx, Ly, Lz, Lt = latt_size
+        self.device = torch.device(device or "cuda")
+        self.latt_size = latt_size
+        self.gauge_field = gauge_field
+        self.eigenvector = eigenvector
+        self.num_derivative = num_derivative(num_nabla)
+        self.derivative_list = [derivative(n) for n in range(self.num_derivative)]
+        self.num_momentum = len(momentum_list)
+        self.momentum_list = momentum_list
+        Ne = eigenvector.Ne
+        self.Ne = Ne
+        self.precision = precision
+        self._U = None
+        self._VPV = torch.zeros((self.num_derivative, self.num_momentum, Ne, Ne), dtype=torch.complex128,
+                                device=self.device)
+        self._eigenvector_data = None
+        self._momentum_phase = MomentumPhase(latt_size, self.device)
+        self._plan = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, self.device)
+        self._stage = None
+
+        if is_blending and (dilution is not None):
+            self.stocastic_coeff = torch.from_numpy(_blending_coeff(Ne, dilution)).to(self.device)
+        elif is_blending:
+            raise ValueError("Dilution tuple is not defined.")
+        else:
+            self.stocastic_coeff = None
+
+    def load(self, key: str):
+        self._U = links_to_device(self.gauge_field.load(key)[:], self.latt_size, self.device)
+        self._eigenvector_data = self.eigenvector.load(key)
+
+    def _read_vectors(self, t: int) -> torch.Tensor:
+        """``V[e] = eigenvector[t, e]`` for e < Ne (``elemental.py:297-298``),
+        staged through pinned host memory into a device buffer."""
+        Lx, Ly, Lz, Lt = self.latt_size
+        Ne = self.Ne
+        data = self._eigenvector_data
+        if isinstance(data, torch.Tensor):
+            return data[t, :Ne].reshape(Ne, Lz * Ly * Lx * NC).to(self.device).contiguous()
+        if self._stage is None:
+            self._stage = torch.empty((Ne, Lz * Ly * Lx * NC), dtype=torch.complex128).pin_memory()
+        stage = self._stage.numpy()
+        block = None
+        try:
+            block = _host_array(data[t, 0:Ne])
+            if block.shape[0] != Ne or block.size != stage.size:
+                block = None
+        except Exception:
+            block = None
+        if block is not None:
+            stage[...] = block.reshape(stage.shape)
+        else:
+            for e in range(Ne):
+                stage[e] = _host_array(data[t, e]).reshape(-1)
+        return self._stage.to(self.device, non_blocking=True)
+
+    def calc(self, t: int):
+        if self._U is None:
+            raise RuntimeError("call load(key) before calc(t)")
+        Lx, Ly, Lz, Lt = self.latt_size
+        V3 = Lx * Ly * Lz
+        V = self._read_vectors(t)
+        links_t = self._U[:, t]
+        self._plan.run(links_t, dir_stride=Lt * V3 * 9, site_stride=9, evecs=V, out=self._VPV,
+                       blend=self.stocastic_coeff)
+        return self._VPV
+
+    def project_SU3(self):
+        """Iterative projection back onto SU(3) (``elemental.py:107-118``)."""
+        from .eigenvector import project_su3_
+
+        project_su3_(self._U)
+
+    def stout_smear(self, nstep: int, rho: float):
+        from .eigenvector import stout_smear_links_
+
+        stout_smear_links_(self._U, self.latt_size, nstep, rho)

@@ -1,0 +1,225 @@
+"""Torch-facing wrappers of the C ABI (device tensors in, device tensors out).
+
+Every function here launches the library's own CUDA kernels on the current
+torch stream; none has a CPU path.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import torch
+
+from . import _lib
+from ._lib import ED_C64, ED_C128, call, ptr, require_cuda, stream_handle
+
+_PREC = {torch.complex128: ED_C128, torch.complex64: ED_C64}
+_DTYPE = {ED_C128: torch.complex128, ED_C64: torch.complex64}
+
+
+def prec_of(t: torch.Tensor) -> int:
+    try:
+        return _PREC[t.dtype]
+    except KeyError:
+        raise ValueError(f"unsupported dtype {t.dtype}; expected complex128 or complex64") from None
+
+
+def links_to_soa(U: torch.Tensor, latt_size: Sequence[int], dtype=torch.complex128, layout: str = "reference"):
+    """Spatial links of every timeslice -> SoA ``[Lt, 27, V3]``.
+
+    ``U`` is complex128 on the device, either the generators' transposed
+    layout ``[Nd, Lt, Lz, Ly, Lx, 3, 3]`` (``layout="reference"``,
+    ``lattice/generator/eigenvector.py:50``) or the on-disk ILDG order
+    ``[Lt, Lz, Ly, Lx, Nd, 3, 3]`` (``layout="ildg"``)."""
+    require_cuda(U, "U")
+    if U.dtype != torch.complex128:
+        raise ValueError("links must be complex128")
+    Lx, Ly, Lz, Lt = latt_size
+    V3 = Lx * Ly * Lz
+    if layout == "reference":
+        nt = U.shape[1]
+        ts, ds, ss = V3 * 9, nt * V3 * 9, 9
+    elif layout == "ildg":
+        nt = U.shape[0]
+        ts, ds, ss = V3 * U.shape[4] * 9, 9, U.shape[4] * 9
+    else:
+        raise ValueError(f"unknown link layout {layout!r}")
+    out = torch.empty((nt, 27, V3), dtype=dtype, device=U.device)
+    call("ed_links_to_soa", _PREC[dtype], Lx, Ly, Lz, nt, ptr(U), ts, ds, ss, ptr(out), stream_handle())
+    return out
+
+
+def vectors_to_planes(V: torch.Tensor, V3: int, dtype=torch.complex128, round_c64: bool = False):
+    """``[..., V3, 3]`` -> colour planes ``[..., 3, V3]``."""
+    require_cuda(V, "V")
+    nvec = V.numel() // (3 * V3)
+    out = torch.empty(V.shape[:-2] + (3, V3) if V.dim() >= 2 else (nvec, 3, V3), dtype=dtype, device=V.device)
+    call("ed_vectors_to_planes", prec_of(V), _PREC[dtype], int(round_c64), nvec, V3, ptr(V), ptr(out), stream_handle())
+    return out
+
+
+def vectors_from_planes(P: torch.Tensor, V3: int, dtype=torch.complex128):
+    """Colour planes ``[..., 3, V3]`` -> ``[..., V3, 3]``."""
+    require_cuda(P, "P")
+    nvec = P.numel() // (3 * V3)
+    out = torch.empty(P.shape[:-2] + (V3, 3), dtype=dtype, device=P.device)
+    call("ed_vectors_from_planes", prec_of(P), _PREC[dtype], nvec, V3, ptr(P), ptr(out), stream_handle())
+    return out
+
+
+def momentum_phases(latt_size: Sequence[int], momenta, device=None) -> torch.Tensor:
+    """FP64 phase tables ``[Nmom, Lz, Ly, Lx]`` = ``exp(+2 pi i p.x / L)``
+    (``lattice/insertion/phase.py:11-13,41-46``)."""
+    Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
+    moms = [int(v) for p in momenta for v in p]
+    nmom = len(moms) // 3
+    arr = (ctypes.c_int * len(moms))(*moms)
+    out = torch.empty((nmom, Lz, Ly, Lx), dtype=torch.complex128, device=device or "cuda")
+    call("ed_momentum_phases", Lx, Ly, Lz, arr, nmom, ptr(out), stream_handle())
+    return out
+
+
+def laplacian(links_soa: torch.Tensor, F: torch.Tensor, latt_size: Sequence[int], out: torch.Tensor = None):
+    """3D covariant Laplacian (``lattice/generator/eigenvector.py:11-26``).
+
+    ``links_soa``: ``[nt, 27, V3]``; ``F``: colour planes ``[nt, nvec, 3, V3]``
+    (any leading view whose timeslice stride is uniform).  Precision follows
+    the tensors (complex128 or complex64, both the same)."""
+    Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
+    V3 = Lx * Ly * Lz
+    require_cuda(links_soa, "links")
+    if F.dim() == 2:
+        F = F.unsqueeze(0).unsqueeze(0)
+    elif F.dim() == 3:
+        F = F.unsqueeze(1)
+    nt, nvec = F.shape[0], F.shape[1]
+    if links_soa.dtype != F.dtype:
+        raise ValueError("links and vectors must share a precision")
+    if tuple(F.shape[2:]) != (3, V3) or F.stride(-1) != 1 or F.stride(-2) != V3 or F.stride(1) != 3 * V3:
+        raise ValueError("F must be colour planes [nt, nvec, 3, V3] with contiguous vectors")
+    if links_soa.shape[0] != nt:
+        raise ValueError("links and vectors disagree on the number of timeslices")
+    if out is None:
+        out = torch.empty((nt, nvec, 3, V3), dtype=F.dtype, device=F.device)
+    call(
+        "ed_laplacian",
+        prec_of(F),
+        Lx,
+        Ly,
+        Lz,
+        nt,
+        nvec,
+        ptr(links_soa),
+        ptr(F),
+        F.stride(0),
+        ptr(out),
+        out.stride(0),
+        stream_handle(),
+    )
+    return out
+
+
+def covariant_derivative(links_soa_c128: torch.Tensor, F: torch.Tensor, latt_size, direction: int, out_dtype=None):
+    """One hop ``D_d F = U_d(x) F(x+d) - U_d(x-d)^dag F(x-d)``
+    (``lattice/generator/elemental.py:282-287``); ``F`` colour planes ``[nvec, 3, V3]``."""
+    Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
+    require_cuda(F, "F")
+    require_cuda(links_soa_c128, "links")
+    out_dtype = out_dtype or F.dtype
+    nvec = F.numel() // (3 * Lx * Ly * Lz)
+    out = torch.empty_like(F, dtype=out_dtype)
+    call(
+        "ed_covariant_derivative",
+        prec_of(F),
+        _PREC[out_dtype],
+        Lx,
+        Ly,
+        Lz,
+        int(direction),
+        nvec,
+        ptr(links_soa_c128),
+        ptr(F),
+        ptr(out),
+        stream_handle(),
+    )
+    return out
+
+
+MODES = {"fp64": 0}
+
+
+class ElementalPlan:
+    """Owner of an ``ed_elemental_plan`` and its device workspace."""
+
+    def __init__(self, latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "fp64", device=None):
+        if mode not in MODES:
+            raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES)}")
+        Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
+        self.latt_size = list(latt_size)
+        self.Ne = Ne
+        self.mode = mode
+        self.num_nabla = num_nabla
+        self.momentum_list = [tuple(int(v) for v in p) for p in momentum_list]
+        moms = [v for p in self.momentum_list for v in p]
+        arr = (ctypes.c_int * len(moms))(*moms)
+        handle = ctypes.c_void_p()
+        _lib.check(
+            _lib.lib().ed_elemental_plan_create(
+                ctypes.byref(handle), Lx, Ly, Lz, Ne, num_nabla, arr, len(self.momentum_list), MODES[mode]
+            ),
+            "ed_elemental_plan_create",
+        )
+        self._h = handle
+        nbytes = ctypes.c_size_t()
+        call("ed_elemental_workspace_size", self._h, ctypes.byref(nbytes))
+        npairs = ctypes.c_int()
+        call("ed_elemental_num_pairs", self._h, ctypes.byref(npairs))
+        self.workspace_bytes = nbytes.value
+        self.num_pairs = npairs.value
+        self.device = torch.device(device or "cuda")
+        self._ws = None
+
+    def workspace(self):
+        if self._ws is None:
+            self._ws = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def run(self, links: torch.Tensor, dir_stride: int, site_stride: int, evecs: torch.Tensor, out: torch.Tensor,
+            blend: torch.Tensor = None):
+        """``links``: complex128 device view of the timeslice's spatial links
+        (element (mu, site, a, b) at mu*dir_stride + site*site_stride + 3a+b);
+        ``evecs``: ``[Ne, V3*3]``-contiguous c128/c64; ``out``: ``[Nderiv, Nmom, Ne, Ne]`` c128."""
+        ws = self.workspace()
+        require_cuda(evecs, "evecs")
+        require_cuda(out, "out")
+        if out.dtype != torch.complex128:
+            raise ValueError("out must be complex128")
+        bptr = None
+        if blend is not None:
+            require_cuda(blend, "blend")
+            bptr = ptr(blend)
+        call(
+            "ed_elemental_run",
+            self._h,
+            ptr(links),
+            dir_stride,
+            site_stride,
+            prec_of(evecs),
+            ptr(evecs),
+            bptr,
+            ptr(out),
+            ptr(ws),
+            ws.numel(),
+            stream_handle(),
+        )
+        return out
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().ed_elemental_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None

@@ -1,0 +1,135 @@
+/*
+ * easydist_gb300.h -- C ABI of the GB300 (sm_103a) distillation hot path.
+ *
+ * The library replaces the array arithmetic of two EasyDistillation
+ * generators: the 3D covariant Laplacian inside EigenvectorGenerator's
+ * per-timeslice eigensolve, and ElementalGenerator's displaced,
+ * momentum-projected contraction.  Every call:
+ *   - takes caller-owned DEVICE pointers (plain addresses) and sizes;
+ *   - is ordered on the CUDA stream passed as `stream` (a cudaStream_t, NULL
+ *     for the legacy default stream) and returns without synchronising;
+ *   - returns ED_OK (0) or a negative ED_ERR_* code; the message of the last
+ *     error on the calling host thread is available from ed_last_error();
+ *   - allocates no device memory: scratch comes from a caller-provided
+ *     workspace whose size is queried first.
+ * There is no CPU fallback: without a usable sm_103a device the calls return
+ * ED_ERR_CUDA.
+ *
+ * Data layouts (V3 = Lx*Ly*Lz, site = x + Lx*(y + Ly*z), x fastest):
+ *   reference links   : complex128, element (mu, site, a, b) at
+ *                       mu*dir_stride + site*site_stride + 3*a + b
+ *                       (ILDG order of one timeslice: dir_stride 9,
+ *                        site_stride 36; the generators' transposed order
+ *                        U[:3, t]: dir_stride 9*V3, site_stride 9)
+ *   SoA links         : [dir 3][row 3][col 3][V3] complex (c128 or c64)
+ *   reference vectors : [nvec][V3][3] complex, colour fastest
+ *   colour planes     : [nvec][3][V3] complex (c128 or c64)
+ *   elementals        : [Nderiv][Nmom][Ne][Ne] complex128
+ */
+#ifndef EASYDIST_GB300_H
+#define EASYDIST_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes */
+#define ED_OK 0
+#define ED_ERR_ARG (-1)         /* invalid argument (sizes, pointers, alignment) */
+#define ED_ERR_CUDA (-2)        /* a CUDA runtime error (launch, device) */
+#define ED_ERR_UNSUPPORTED (-3) /* valid request this build does not serve */
+#define ED_ERR_WORKSPACE (-4)   /* workspace too small */
+#define ED_ERR_TIMEOUT (-5)     /* a bounded device-side wait gave up */
+
+/* ---- storage precisions */
+#define ED_C128 0 /* complex128: double2 */
+#define ED_C64 1  /* complex64:  float2  */
+
+/* ---- elemental arithmetic modes */
+#define ED_MODE_FP64 0   /* plain FP64 SIMT contraction (V rounded to c64, all else c128) */
+
+/* Library version as 10000*major + 100*minor + patch. */
+int ed_version(void);
+
+/* Copy the last error message of this host thread into buf (NUL-terminated,
+ * truncated to len).  Returns the length of the full message. */
+int ed_last_error(char* buf, size_t len);
+
+/* Convert nt timeslices of spatial links from the reference layout into SoA.
+ * Replaces the per-timeslice slice `U[:3, t]` of
+ * lattice/generator/eigenvector.py:242-243 and elemental.py:103,320-321.
+ * in: complex128 with element (t, mu, site, a, b) at
+ *     t*t_stride + mu*dir_stride + site*site_stride + 3a + b   (complex units)
+ * out: [nt][3][3][3][V3] of precision out_prec. */
+int ed_links_to_soa(int out_prec, int Lx, int Ly, int Lz, int nt, const void* in, long long t_stride,
+                    long long dir_stride, long long site_stride, void* out, void* stream);
+
+/* Reference vectors [nvec][V3][3] (in_prec) -> colour planes [nvec][3][V3]
+ * (out_prec).  round_c64 != 0 rounds every value through complex64 first,
+ * as ElementalGenerator's complex64 buffer does (elemental.py:55,297-298). */
+int ed_vectors_to_planes(int in_prec, int out_prec, int round_c64, long long nvec, int V3, const void* in,
+                         void* out, void* stream);
+
+/* Colour planes [nvec][3][V3] -> reference vectors [nvec][V3][3]. */
+int ed_vectors_from_planes(int in_prec, int out_prec, long long nvec, int V3, const void* in, void* out,
+                           void* stream);
+
+/* Momentum phase tables exp(+2*pi*i*(px*x/Lx + py*y/Ly + pz*z/Lz)), FP64.
+ * Replaces MomentumPhase.get (lattice/insertion/phase.py:11-13,41-46).
+ * moms: HOST array [nmom][3] of ints; out: device [nmom][V3] complex128. */
+int ed_momentum_phases(int Lx, int Ly, int Lz, const int* moms, int nmom, void* out, void* stream);
+
+/* 3D covariant Laplacian on nt timeslices x nvec vectors.
+ * Replaces _Laplacian (lattice/generator/eigenvector.py:11-26).
+ * links: SoA [nt][27][V3] (prec); in/out: colour planes, vector v of
+ * timeslice t at base + t*tstride + v*3*V3 (complex units; a stride of 0
+ * means the packed 3*V3*nvec).  ED_C64 needs an even Lx and even strides.
+ * in and out must not alias. */
+int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, const void* links, const void* in,
+                 long long in_tstride, void* out, long long out_tstride, void* stream);
+
+/* One covariant-derivative hop D_dir on nvec colour-plane vectors:
+ * out = U_d(x) in(x+d) - U_d(x-d)^dag in(x-d).
+ * Replaces one iteration of ElementalGenerator._nD (elemental.py:282-287).
+ * links_c128: SoA complex128 [27][V3]; math in FP64. */
+int ed_covariant_derivative(int in_prec, int out_prec, int Lx, int Ly, int Lz, int dir, int nvec,
+                            const void* links_c128, const void* in, void* out, void* stream);
+
+/* ---- elementals (ElementalGenerator.calc, lattice/generator/elemental.py:290-338) */
+typedef struct ed_elemental_plan ed_elemental_plan;
+
+/* Plan one timeslice of elementals: derivative operators 0..Nderiv-1 with
+ * Nderiv = (3^(num_nabla+1)-1)/2 (elemental.py:48-49, derivative.py:23-33),
+ * the momenta moms[nmom][3] (host ints), Ne eigenvectors, mode ED_MODE_*.
+ * The plan is host-only state (no device memory). */
+int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne, int num_nabla,
+                             const int* moms, int nmom, int mode);
+int ed_elemental_plan_destroy(ed_elemental_plan* plan);
+
+/* Device workspace the plan needs, in bytes. */
+int ed_elemental_workspace_size(const ed_elemental_plan* plan, size_t* bytes);
+
+/* Number of distinct (left chain, right chain) contractions per momentum the
+ * plan executes (the reference evaluates 2^len subsets per operator). */
+int ed_elemental_num_pairs(const ed_elemental_plan* plan, int* npairs);
+
+/* Run one timeslice.
+ * links: reference-layout complex128 spatial links of this timeslice
+ *        (see the layout note above, dir_stride/site_stride in complex units);
+ * evecs: reference vectors [Ne][V3][3] of precision evec_prec (rounded to
+ *        complex64 as the reference does);
+ * blend: NULL or device [Ne][Ne] float64 stochastic blending coefficients,
+ *        multiplied elementwise into every (operator, momentum) block
+ *        (elemental.py:61-100,330-337);
+ * out:   device [Nderiv][Nmom][Ne][Ne] complex128 (overwritten). */
+int ed_elemental_run(const ed_elemental_plan* plan, const void* links, long long dir_stride, long long site_stride,
+                     int evec_prec, const void* evecs, const double* blend, void* out, void* workspace,
+                     size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EASYDIST_GB300_H */

@@ -1,0 +1,89 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol the
+header declares, validates arguments on the host, and plans elementals."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from tests.conftest import ROOT
+
+
+def _declared():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", h)).read()
+            names |= set(re.findall(r"^\s*int\s+(ed_\w+)\s*\(", src, re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    from easydistillation_gb300 import _lib
+
+    L = _lib.lib()
+    declared = _declared()
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(L, name), f"{name} declared in include/ but not exported"
+    assert declared <= set(_lib.exported_symbols()) | declared
+    assert set(_lib.exported_symbols()) <= declared, "binding names an undeclared symbol"
+    assert L.ed_version() >= 100
+
+
+def test_argument_validation_is_host_side():
+    from easydistillation_gb300 import _lib
+
+    L = _lib.lib()
+    # bad precision / sizes / null pointers are rejected before any CUDA call
+    assert L.ed_laplacian(7, 4, 4, 4, 1, 1, None, None, 0, None, 0, None) == _lib.ED_ERR_ARG
+    assert "prec" in _lib.last_error()
+    assert L.ed_laplacian(_lib.ED_C64, 3, 4, 4, 1, 1, 16, 32, 0, 64, 0, None) == _lib.ED_ERR_ARG
+    assert "even Lx" in _lib.last_error()
+    assert L.ed_covariant_derivative(0, 0, 4, 4, 4, 3, 1, 16, 32, 64, None) == _lib.ED_ERR_ARG
+    assert L.ed_vectors_to_planes(0, 0, 0, 0, 64, 16, 32, None) == _lib.ED_ERR_ARG
+    with pytest.raises(ValueError):
+        _lib.check(_lib.ED_ERR_ARG, "x")
+
+
+@pytest.mark.parametrize(
+    "num_nabla,moms,herm_pairs,plain_pairs",
+    [
+        (0, [(0, 0, 0)], 1, 1),
+        (1, [(0, 0, 0), (0, 0, 1), (0, 0, -1)], 4, 4 + 3),
+        (2, [(0, 0, 0), (1, 0, 0), (-1, 0, 0)], 13 + 3 + 2 + 1, 13 + 3 * 4 + 9),
+        (2, [(0, 0, 0), (0, 0, 1)], None, 13 + 3 * 4 + 9),
+    ],
+)
+def test_elemental_plan_pairs(num_nabla, moms, herm_pairs, plain_pairs):
+    """Distinct (left, right) chain contractions per momentum: 34 for
+    num_nabla=2 instead of the reference's 43 subsets, 19 when the momentum
+    list is closed under p -> -p (hermiticity)."""
+    from easydistillation_gb300.ops import ElementalPlan
+
+    plan = ElementalPlan([4, 4, 4, 8], 6, num_nabla, moms, "fp64", device="cpu")
+    expect = herm_pairs if herm_pairs is not None else plain_pairs
+    assert plan.num_pairs == expect
+    V3 = 64
+    assert plan.workspace_bytes >= (3 ** (num_nabla + 1) - 1) // 2 * 6 * 3 * V3 * 16
+
+
+def test_plan_rejects_bad_arguments():
+    from easydistillation_gb300.ops import ElementalPlan
+
+    with pytest.raises(ValueError):
+        ElementalPlan([4, 4, 4, 8], 6, 3, [(0, 0, 0)], "fp64", device="cpu")
+    with pytest.raises(ValueError):
+        ElementalPlan([4, 4, 4, 8], 0, 1, [(0, 0, 0)], "fp64", device="cpu")
+    with pytest.raises(ValueError):
+        ElementalPlan([4, 4, 4, 8], 4, 1, [(0, 0, 0)], "no-such-mode", device="cpu")
+
+
+def test_generator_metadata_matches_reference_scheme():
+    from easydistillation_gb300 import derivative, mom_dict_to_list, num_derivative
+    from oracle import restatement as R
+
+    assert [derivative(n) for n in range(40)] == [R.derivative(n) for n in range(40)]
+    assert mom_dict_to_list(3) == R.mom_dict_to_list(3)
+    assert [num_derivative(k) for k in range(3)] == [1, 4, 13]
