@@ -88,19 +88,25 @@ class ClockSampler:
         sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
         mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 3 + k and "Active" in r[3 + k]})
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 3 + k and r[3 + k] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
 
 
 # ---------------------------------------------------------------- inputs
-def make_inputs(latt, Ne, seed=2):
+def make_inputs(latt, Ne, seed=2, distinct_t=RESIDENT_T):
+    """Seeded synthetic links exp(i*0.3*A) for `distinct_t` timeslices, tiled
+    to Lt (timeslices are independent, so the timed steps see distinct data
+    as long as they rotate over fewer than `distinct_t` of them), and
+    RESIDENT_T sets of random c128 vectors of norm 1."""
     import numpy as np
 
     from oracle.restatement import synthetic_gauge  # input generation only
 
-    gauge = synthetic_gauge(latt, 0.3, 1000 + seed)
     Lx, Ly, Lz, Lt = latt
+    nt = min(Lt, distinct_t)
+    g = synthetic_gauge([Lx, Ly, Lz, nt], 0.3, 1000 + seed)
+    gauge = np.ascontiguousarray(np.tile(g, (Lt // nt + 1, 1, 1, 1, 1, 1, 1))[:Lt])
     n = Lx * Ly * Lz * 3
     rng = np.random.default_rng(seed)
     evecs = []
@@ -110,34 +116,41 @@ def make_inputs(latt, Ne, seed=2):
     return gauge, evecs
 
 
-def cpu_reference_sample(latt, Ne, threads):
+# Work units of one reference timeslice (lattice/generator/elemental.py:299-329)
+# at num_nabla = 2: 43 subsets, each rebuilding its two chains (78 hops in
+# total), and one phase-weighted zgemm per subset and momentum.
+REF_HOPS = 78
+REF_SUBSETS = 43
+
+
+def cpu_reference_sample(latt, Ne, threads, reps=2):
     """Time the oracle (CPU restatement of the reference numpy path) on a
-    bounded sample: one momentum of one timeslice with all 13 operators
-    (all chains + 43 zgemm), plus one extra zgemm to extrapolate to 27 momenta."""
+    bounded sample at full size: one covariant-derivative hop of all Ne
+    vectors and one momentum-weighted zgemm, each the median of `reps` runs,
+    scaled by the reference's counts per timeslice (78 hops, 43 x 27 zgemm)."""
     os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
     import numpy as np
 
     from oracle import restatement as R
 
-    gauge, evecs = make_inputs(latt, Ne)
+    gauge, evecs = make_inputs(latt[:3] + [1], Ne, distinct_t=1)
     U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
-    V = evecs[0].reshape(Ne, latt[2], latt[1], latt[0], 3)
-    moms = R.mom_dict_to_list(3)
-    t0 = time.perf_counter()
-    R.elemental(V, U, latt, NUM_NABLA, moms[:1])
-    t1 = time.perf_counter()
-    ph = R.momentum_phase(latt, moms[1])
-    left = V.astype(np.complex64).astype(np.complex128)
-    t2 = time.perf_counter()
-    lp = (ph[None, :, :, :, None] * left.conj()).reshape(Ne, -1)
-    _ = lp @ left.reshape(Ne, -1).T
-    t3 = time.perf_counter()
-    one_mom = t1 - t0
-    per_gemm = t3 - t2
-    pairs = 43
-    per_ts = one_mom + (NMOM - 1) * pairs * per_gemm
-    return per_ts, f"oracle ElementalGenerator.calc at {latt[0]}^3, Ne={Ne}, 13 ops x 1 momentum ({one_mom:.1f} s) " \
-                   f"+ 26 x 43 momentum GEMMs extrapolated from one ({per_gemm:.2f} s)"
+    V = evecs[0].reshape(Ne, latt[2], latt[1], latt[0], 3).astype(np.complex64).astype(np.complex128)
+    ph = R.momentum_phase(latt, (0, 0, 1))
+    th, tg = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        W = R.covariant_derivative(V, U, 1)
+        t1 = time.perf_counter()
+        lp = (-1 * ph[None, :, :, :, None] * W.conj()).reshape(Ne, -1)
+        _ = lp @ V.reshape(Ne, -1).T
+        t2 = time.perf_counter()
+        th.append(t1 - t0)
+        tg.append(t2 - t1)
+    hop, gemm = statistics.median(th), statistics.median(tg)
+    per_ts = REF_HOPS * hop + REF_SUBSETS * NMOM * gemm
+    return per_ts, (f"oracle at {latt[0]}^3, Ne={Ne}: one hop ({hop:.2f} s) and one phase-weighted zgemm "
+                    f"({gemm:.2f} s) timed, scaled by {REF_HOPS} hops + {REF_SUBSETS}x{NMOM} zgemm per timeslice")
 
 
 def run_reference(args, rank, world):

@@ -48,6 +48,8 @@ _SIGNATURES = {
     "ed_elemental_workspace_size": ([_vp, _c.POINTER(_c.c_size_t)], _i),
     "ed_elemental_num_pairs": ([_vp, _c.POINTER(_i)], _i),
     "ed_elemental_run": ([_vp, _vp, _ll, _ll, _i, _vp, _vp, _vp, _vp, _c.c_size_t, _vp], _i),
+    "ed_elemental_status": ([_vp, _vp, _c.POINTER(_i), _vp], _i),
+    "ed_elemental_set_profile_events": ([_vp, _vp, _vp], _i),
 }
 
 _lock = threading.Lock()

@@ -333,7 +333,9 @@ int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains,
     d.tile0 = tiles;
     tiles += d.mt * d.nt * P->nmom;
   }
+  if (P->prof_start) cudaEventRecord(P->prof_start, stream);
   pair_gemm_f64_kernel<<<tiles, 256, 0, stream>>>(tab, P->Ne, P->V3, P->nmom, chains, phases, G);
+  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   ED_RETURN_LAUNCH("pair GEMM (fp64)");
   return ED_OK;
 }
@@ -459,4 +461,23 @@ extern "C" int ed_elemental_run(const ed_elemental_plan* plan, const void* links
   }
   return ed::elemental_run(plan, links, dir_stride, site_stride, evec_prec, evecs, blend, out, workspace,
                            workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int ed_elemental_status(const ed_elemental_plan* plan, const void* workspace, int* code, void* stream) {
+  ED_CHECK_ARG(plan && workspace && code, "ed_elemental_status: null pointer");
+  int rc = ed::tc_read_status(plan, workspace, code, (cudaStream_t)stream);
+  if (rc != ED_OK) return rc;
+  if (*code != 0) {
+    ed::set_error("elemental: a bounded device wait gave up (code %d); the output of that run is invalid", *code);
+    return ED_ERR_TIMEOUT;
+  }
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_set_profile_events(ed_elemental_plan* plan, void* start, void* stop) {
+  ED_CHECK_ARG(plan, "ed_elemental_set_profile_events: null plan");
+  ED_CHECK_ARG((start == nullptr) == (stop == nullptr), "ed_elemental_set_profile_events: give both events or none");
+  plan->prof_start = (cudaEvent_t)start;
+  plan->prof_stop = (cudaEvent_t)stop;
+  return ED_OK;
 }

@@ -42,6 +42,7 @@ struct ed_elemental_plan {
   int tc_kind;        // 0 = none
   int tc_scale_exp;   // power-of-two scale applied before fp16 splitting
   size_t tc_bytes;    // extra workspace
+  cudaEvent_t prof_start = nullptr, prof_stop = nullptr;  // optional events around the pair GEMM
 };
 
 namespace ed {
@@ -50,4 +51,5 @@ size_t tc_extra_workspace(const ed_elemental_plan* P);
 int tc_plan_check(ed_elemental_plan* P);
 int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
                         cplx<double>* G, void* extra, cudaStream_t stream);
+int tc_read_status(const ed_elemental_plan* P, const void* workspace, int* status, cudaStream_t stream);
 }  // namespace ed

@@ -7,8 +7,12 @@ operator combination).  ``calc`` returns the generator's internal
 ``[Nderiv, Nmom, Ne, Ne]`` complex128 device buffer, which the next call
 overwrites, exactly like the reference's ``self._VPV``.
 
-Extra keyword-only arguments: ``precision`` (``"fp64"``: plain FP64
-arithmetic with V rounded to complex64, as the reference) and ``device``.
+Extra keyword-only arguments: ``precision`` and ``device``.  ``"fp64"`` is
+plain FP64 arithmetic with V rounded to complex64, as the reference.  The
+tensor-core modes ``"f16x3"``, ``"tf32x3"`` (relative error ~1e-7) and
+``"bf16x3"`` (~1e-5) store the derivative chains in complex64 and run the
+pair contractions as split-precision tcgen05 GEMMs with FP32 accumulation;
+they need ``Lx*Ly*Lz`` divisible by 32.
 """
 
 from __future__ import annotations
@@ -157,6 +161,8 @@ class ElementalGenerator:
         links_t = self._U[:, t]
         self._plan.run(links_t, dir_stride=Lt * V3 * 9, site_stride=9, evecs=V, out=self._VPV,
                        blend=self.stocastic_coeff)
+        if self.precision != "fp64":
+            self._plan.check_status()
         return self._VPV
 
     def project_SU3(self):

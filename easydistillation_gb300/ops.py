@@ -146,7 +146,8 @@ def covariant_derivative(links_soa_c128: torch.Tensor, F: torch.Tensor, latt_siz
     return out
 
 
-MODES = {"fp64": 0}
+#: elemental arithmetic modes (ED_MODE_* in include/easydist_gb300.h)
+MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3}
 
 
 class ElementalPlan:
@@ -214,6 +215,12 @@ class ElementalPlan:
             stream_handle(),
         )
         return out
+
+    def check_status(self):
+        """Synchronise and raise if a bounded device wait of the last run gave up."""
+        code = ctypes.c_int()
+        call("ed_elemental_status", self._h, ptr(self.workspace()), ctypes.byref(code), stream_handle())
+        return code.value
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -49,6 +49,9 @@ extern "C" {
 
 /* ---- elemental arithmetic modes */
 #define ED_MODE_FP64 0   /* plain FP64 SIMT contraction (V rounded to c64, all else c128) */
+#define ED_MODE_F16X3 1  /* tcgen05: scaled fp16 hi/lo split, 3 products per real product */
+#define ED_MODE_BF16X3 2 /* tcgen05: bf16 hi/lo split, 3 products per real product */
+#define ED_MODE_TF32X3 3 /* tcgen05 kind::tf32: tf32 hi/lo split, 3 products per real product */
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);
@@ -127,6 +130,18 @@ int ed_elemental_num_pairs(const ed_elemental_plan* plan, int* npairs);
 int ed_elemental_run(const ed_elemental_plan* plan, const void* links, long long dir_stride, long long site_stride,
                      int evec_prec, const void* evecs, const double* blend, void* out, void* workspace,
                      size_t workspace_bytes, void* stream);
+
+/* Record the CUDA events `start` / `stop` (cudaEvent_t, or NULL to disable)
+ * on the run's stream immediately before and after the pair-contraction
+ * kernel of every later ed_elemental_run with this plan, so a caller can time
+ * that kernel alone.  The plan keeps only the handles. */
+int ed_elemental_set_profile_events(ed_elemental_plan* plan, void* start, void* stop);
+
+/* Synchronise `stream` and report the device-side status of the last run on
+ * this workspace: ED_OK, or ED_ERR_TIMEOUT when a bounded wait inside the
+ * tensor-core kernel gave up (its output is then invalid).  *code receives
+ * the raw status word (0 = ok). */
+int ed_elemental_status(const ed_elemental_plan* plan, const void* workspace, int* code, void* stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,62 @@
+"""Split-precision tensor-core elementals (tcgen05) against the FP64 oracle.
+
+Tolerances (relative Frobenius error over the whole [Nderiv, Nmom, Ne, Ne]
+block): f16x3 and tf32x3 <= 1e-6 (the bar for the split-precision path),
+bf16x3 <= 1e-4 (two 8-bit-mantissa slices)."""
+
+import numpy as np
+import pytest
+
+from oracle import restatement as R
+from tests.helpers import MemEigen, MemGauge, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"f16x3": 1e-6, "tf32x3": 1e-6, "bf16x3": 1e-4}
+
+
+def _run(latt, Ne, num_nabla, moms, mode, t=0, seed=5):
+    from easydistillation_gb300 import ElementalGenerator
+
+    gauge = R.synthetic_gauge(latt, 0.3, seed)
+    evec = np.stack([R.random_colour_vectors(Ne, latt, seed * 10 + tt) for tt in range(latt[3])])
+    gen = ElementalGenerator(latt, MemGauge(gauge), MemEigen(evec, Ne), num_nabla, moms, precision=mode)
+    gen.load("k")
+    E = gen.calc(t).cpu().numpy()
+    U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, t]
+    return E, R.elemental(evec[t], U, latt, num_nabla, moms)
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3", "bf16x3"])
+def test_tc_small_all_operators(mode):
+    E, ref = _run([4, 4, 4, 2], 6, 2, R.mom_dict_to_list(3)[:7], mode, t=1)
+    assert rel_err(E, ref) < TOL[mode]
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3"])
+def test_tc_open_momentum_list(mode):
+    """momenta not closed under p -> -p: every (left, right) pair is computed directly"""
+    moms = [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (0, 0, 2), (0, 1, 2), (1, 1, 2)]
+    E, ref = _run([4, 4, 4, 1], 5, 2, moms, mode)
+    assert rel_err(E, ref) < TOL[mode]
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3", "bf16x3"])
+def test_tc_many_tiles(mode):
+    """Ne and momentum count that give several ragged M and N tiles."""
+    E, ref = _run([8, 8, 4, 1], 150, 1, R.mom_dict_to_list(3), mode)
+    assert rel_err(E, ref) < TOL[mode]
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3"])
+def test_tc_long_k(mode):
+    """K = 3 * 16^3 = 12288 accumulated in TMEM."""
+    E, ref = _run([16, 16, 16, 1], 24, 1, R.mom_dict_to_list(3)[:7], mode)
+    assert rel_err(E, ref) < TOL[mode]
+
+
+def test_tc_rejects_volume_not_divisible_by_32():
+    from easydistillation_gb300.ops import ElementalPlan
+
+    with pytest.raises(Exception):
+        ElementalPlan([6, 2, 2, 1], 4, 0, [(0, 0, 0)], "f16x3", device="cpu")
