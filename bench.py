@@ -50,7 +50,33 @@ def parse():
     ap.add_argument("--ne", type=int, default=NE)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison run")
     return ap.parse_args()
+
+
+def launches_per_step(mode):
+    """Kernels of one elemental timeslice: links->SoA, phases, vectors->planes,
+    12 hops, the pair GEMM, the combine; tensor-core modes add absmax, scale,
+    split and phase-scaling kernels."""
+    return 3 + 12 + 1 + 1 + (0 if mode == "fp64" else 4)
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def max_over_ranks(value, device=None):
+    from easydistillation_gb300.replicas import max_over_ranks as _m
+
+    return _m(value, device)
+
+
+def plan_group_rights(plan):
+    return plan.describe()["nright"]
 
 
 # ---------------------------------------------------------------- clocks
@@ -211,26 +237,70 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    # per-step events around the pair-contraction kernel (the dominant kernel)
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in kev:
+        a.record(stream)
+        b.record(stream)
     sampler = ClockSampler(dev.index)
     sampler.start()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     start.record(stream)
     for i in range(args.steps):
+        plan.set_profile_events(*kev[i])
         step(args.warmup + i)
     end.record(stream)
     torch.cuda.synchronize()
+    plan.set_profile_events(None, None)
     clocks = sampler.stop()
+    if args.mode != "fp64" and plan.check_status() != 0:
+        raise RuntimeError("tensor-core kernel reported a timeout")
     ms = start.elapsed_time(end)
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(ms, dev if world > 1 else None)
     ms_per_step = ms / args.steps
     value = world * args.steps / (ms / 1e3)
 
-    # dominant kernel: time the pair-contraction launch alone with events
-    roofline = None
+    # roofline of the pair-contraction kernel
+    kms = statistics.mean(a.elapsed_time(b) for a, b in kev)
+    units = plan.num_pairs * NMOM  # (pair, momentum) contractions per launch
+    alg_flop = units * 8.0 * Ne * Ne * 3 * V3
+    peaks = load_peaks()
+    if args.mode == "fp64":
+        roofline = {"bound": "fp64", "achieved": alg_flop / kms / 1e9, "peak": None, "unit": "TFLOP/s",
+                    "frac": None, "traffic": None, "kernel": "pair_gemm_f64_kernel", "kernel_ms": kms}
+    else:
+        pk, pk_src = peaks.get("bf16_tflops_sustained"), "measured bf16 sustained"
+        if pk is None:
+            pk, pk_src = 1700.0, "fallback"
+        tiles_m = sum(-(-(j * Ne) // 128) for j in plan_group_rights(plan))
+        mma_flop = tiles_m * (-(-(Ne * NMOM) // 256)) * 128 * 256 * 3 * V3 * 12 * 2.0
+        roofline = {"bound": "tensor", "achieved": alg_flop / kms / 1e9, "peak": pk, "unit": "TFLOP/s",
+                    "frac": alg_flop / kms / 1e9 / pk, "traffic": None, "peak_source": pk_src,
+                    "kernel": f"tc_pair_gemm_kernel<{args.mode}>", "kernel_ms": kms,
+                    "mma_tflops_executed": mma_flop / kms / 1e9, "mma_frac": mma_flop / kms / 1e9 / pk,
+                    "note": "achieved = algorithmic complex flops (8*Ne^2*3V3 per pair and momentum); the kernel "
+                            "issues 12 fp16/tf32 MMAs per complex multiply-add (3x) plus tile padding (mma_*)"}
+
+    # the plain FP64 GPU path on the same timeslice: speed and the split-precision error against it
+    fp64 = None
+    if args.mode != "fp64" and not args.no_fp64:
+        plan64 = ElementalPlan(latt, Ne, NUM_NABLA, moms, "fp64", dev)
+        out64 = torch.empty_like(out)
+        t_ref = (args.warmup * 7 + rank) % Lt
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        plan64.run(U[:, t_ref], Lt * V3 * 9, 9, V[args.warmup % RESIDENT_T], out64)
+        b.record(stream)
+        plan.run(U[:, t_ref], Lt * V3 * 9, 9, V[args.warmup % RESIDENT_T], out)
+        torch.cuda.synchronize()
+        ms64 = a.elapsed_time(b)
+        rel = float(torch.linalg.vector_norm(out - out64) / torch.linalg.vector_norm(out64))
+        fp64 = {"value": 1e3 / ms64, "unit": "timeslices/s", "rel_err_vs_fp64": rel,
+                "speedup_split_over_fp64": (value / world) / (1e3 / ms64)}
+        del plan64, out64
+        torch.cuda.empty_cache()
 
     # end to end through the public generator: host eigenvectors in, host elementals out
     e2e = None
@@ -280,8 +350,8 @@ def run_ours(args, rank, world):
             "config": {"workload": f"elemental {Lx}^3x{Lt}, Ne={Ne}, 13 ops x {NMOM} momenta, mode={args.mode}",
                        "pairs_per_momentum": plan.num_pairs, "l2": "inputs larger than L2 (rotating timeslices)",
                        "parallelism": f"replicas x{world}"},
-            "gpu_launches": args.steps * (4 + 12 + 1 + 1),
-            "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu,
+            "gpu_launches": args.steps * launches_per_step(args.mode),
+            "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "fp64_gpu": fp64,
         }
         print(json.dumps(line), flush=True)
 

@@ -481,3 +481,14 @@ extern "C" int ed_elemental_set_profile_events(ed_elemental_plan* plan, void* st
   plan->prof_stop = (cudaEvent_t)stop;
   return ED_OK;
 }
+
+extern "C" int ed_elemental_describe(const ed_elemental_plan* plan, int* ngroups, int* left, int* nright, int* herm) {
+  ED_CHECK_ARG(plan && ngroups && herm, "ed_elemental_describe: null pointer");
+  *ngroups = (int)plan->jobs.size();
+  *herm = plan->herm ? 1 : 0;
+  for (size_t g = 0; g < plan->jobs.size(); ++g) {
+    if (left) left[g] = plan->jobs[g].left;
+    if (nright) nright[g] = plan->jobs[g].nright;
+  }
+  return ED_OK;
+}

@@ -35,20 +35,7 @@ namespace ed {
 
 int launch_phases(Latt L, const int* moms, int nmom, cplx<double>* out, cudaStream_t stream);
 
-constexpr int TC_BM = 128;
-constexpr int TC_BN = 256;
-constexpr int TC_ROWB = 64;  // bytes of K per shared-memory row (64-byte swizzle)
-constexpr int TC_STAGES = 2;
-constexpr int TC_PWARPS = 4;
-constexpr int TC_THREADS = 64 + 32 * TC_PWARPS;
-constexpr int TC_A_BYTES = 4 * TC_BM * TC_ROWB;  // 4 planes
-constexpr int TC_B_BYTES = 4 * TC_BN * TC_ROWB;
-constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-constexpr long long TC_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
-
-// status codes written by the kernel
-constexpr int TC_ERR_FULL = 1, TC_ERR_EMPTY = 2, TC_ERR_ACC = 3;
+#include "tc_config.cuh"
 
 enum TcKind { TC_F16 = 1, TC_BF16 = 2, TC_TF32 = 3 };
 
@@ -287,6 +274,14 @@ __global__ void tc_split_kernel(const cplx<float>* __restrict__ chains, long lon
   }
 }
 
+// double-float pair results -> complex128
+__global__ void tc_df_to_c128_kernel(const float4* __restrict__ DF, long long n, cplx<double>* __restrict__ G) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 d = DF[i];
+    G[i] = mk((double)d.x + (double)d.y, (double)d.z + (double)d.w);
+  }
+}
+
 // FP64 phases -> complex64 phases scaled by 2^e
 __global__ void tc_phase_kernel(const cplx<double>* __restrict__ ph, long long n, const TcScalars* __restrict__ sc,
                                 cplx<float>* __restrict__ out) {
@@ -297,222 +292,7 @@ __global__ void tc_phase_kernel(const cplx<double>* __restrict__ ph, long long n
 
 // ------------------------------------------------------------ the GEMM kernel
 
-template <int KIND>
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_pair_gemm_kernel(const __grid_constant__ CUtensorMap amap, TcTable tab, int Ne, int nmom, int V3, long long R,
-                        const cplx<float>* __restrict__ chains, const cplx<float>* __restrict__ phases,
-                        TcScalars* __restrict__ sc, cplx<double>* __restrict__ G) {
-  constexpr int ESZ = Split<KIND>::ESZ;
-  constexpr int KE = TC_ROWB / ESZ;              // k elements per stage
-  constexpr int EPC = 16 / ESZ;                  // k elements per 16-byte chunk
-  constexpr int CPR = TC_ROWB / 16;              // chunks per row (4)
-  constexpr int KINST = 32 / ESZ;                // k elements per MMA instruction
-  constexpr uint32_t FMT = KIND == TC_F16 ? 0u : (KIND == TC_BF16 ? 1u : 2u);
-  constexpr uint32_t IDESC = umma_idesc(FMT, false);
-  constexpr uint32_t IDESC_NEG = umma_idesc(FMT, true);
-
-  extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + TC_STAGES * TC_STAGE_BYTES);
-  uint64_t* empty = full + TC_STAGES;
-  uint64_t* accf = empty + TC_STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(accf + 1);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  volatile int* status = &sc->status;
-
-  // ---- decode the tile: group, n tile (fast), m tile
-  int tile = blockIdx.x;
-  int jb = 0;
-  while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
-  const TcJob J = tab.j[jb];
-  const int local = tile - J.tile0;
-  const int mtile = local / J.nt;
-  const int ntile = local - mtile * J.nt;
-  const long long K = 3LL * V3;
-  const int nkb = (int)(K / KE);
-  const int Mrows = J.nright * Ne;
-  const int Ncols = Ne * nmom;
-  const long long row0 = (long long)J.right0 * Ne + (long long)mtile * TC_BM;  // first A row (all-chain index)
-  const int n0 = ntile * TC_BN;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_STAGES; ++s) {
-      mbar_init(&full[s], 1 + TC_PWARPS);
-      mbar_init(&empty[s], 1);
-    }
-    mbar_init(accf, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot))
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tmem_slot;
-
-  if (warp == 0) {
-    // ===================== TMA producer for A (4 planes per stage)
-    if (lane == 0) {
-      int issued_last = -1;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % TC_STAGES;
-        if (kb >= TC_STAGES && !mbar_wait(&empty[s], ((kb / TC_STAGES) + 1) & 1, status, TC_ERR_EMPTY)) break;
-        uint8_t* As = smem + s * TC_STAGE_BYTES;
-        mbar_arrive_expect_tx(&full[s], TC_A_BYTES);
-        for (int q = 0; q < 4; ++q)
-          tma_load_2d(As + q * TC_BM * TC_ROWB, &amap, &full[s], kb * KE, (int)(q * R + row0));
-        issued_last = kb;
-      }
-      // do not leave while our copies may still land in shared memory
-      if (issued_last >= 0) {
-        const int s = issued_last % TC_STAGES;
-        mbar_wait(&full[s], (issued_last / TC_STAGES) & 1, status, TC_ERR_FULL, false);
-      }
-    }
-  } else if (warp == 1) {
-    // ===================== MMA issuer
-    if (lane == 0) {
-      const uint32_t d_re = tmem, d_im = tmem + TC_BN;
-      bool ok = true;
-      for (int kb = 0; kb < nkb && ok; ++kb) {
-        const int s = kb % TC_STAGES;
-        if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, status, TC_ERR_FULL)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t a0 = smem_u32(smem + s * TC_STAGE_BYTES);
-        const uint32_t b0 = a0 + TC_A_BYTES;
-#pragma unroll
-        for (int ks = 0; ks < KE / KINST; ++ks) {
-          uint64_t A[4], B[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            A[q] = umma_desc_sw64(a0 + q * TC_BM * TC_ROWB + ks * 32);
-            B[q] = umma_desc_sw64(b0 + q * TC_BN * TC_ROWB + ks * 32);
-          }
-          const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
-          // D_re = Ar.Br - Ai.Bi
-          umma<KIND>(d_re, A[0], B[0], IDESC, acc);
-          umma<KIND>(d_re, A[0], B[1], IDESC, 1u);
-          umma<KIND>(d_re, A[1], B[0], IDESC, 1u);
-          umma<KIND>(d_re, A[2], B[2], IDESC_NEG, 1u);
-          umma<KIND>(d_re, A[2], B[3], IDESC_NEG, 1u);
-          umma<KIND>(d_re, A[3], B[2], IDESC_NEG, 1u);
-          // D_im = Ar.Bi + Ai.Br
-          umma<KIND>(d_im, A[0], B[2], IDESC, acc);
-          umma<KIND>(d_im, A[0], B[3], IDESC, 1u);
-          umma<KIND>(d_im, A[1], B[2], IDESC, 1u);
-          umma<KIND>(d_im, A[2], B[0], IDESC, 1u);
-          umma<KIND>(d_im, A[2], B[1], IDESC, 1u);
-          umma<KIND>(d_im, A[3], B[0], IDESC, 1u);
-        }
-        umma_commit(&empty[s]);  // frees this stage when the MMAs above complete
-      }
-      // Always signal: the epilogue (and the TMEM release after it) must not
-      // run while issued MMAs are still in flight.
-      umma_commit(accf);
-    }
-  } else {
-    // ===================== B producers (warps 2..5), then epilogue
-    const int pt = threadIdx.x - 64;  // 0..127
-    const float* Xb = reinterpret_cast<const float*>(chains + (long long)J.left * Ne * K);
-    bool ok = true;
-    for (int kb = 0; kb < nkb; ++kb) {
-      const int s = kb % TC_STAGES;
-      if (kb >= TC_STAGES && !warp_wait(&empty[s], ((kb / TC_STAGES) + 1) & 1, status, TC_ERR_EMPTY)) {
-        ok = false;
-        break;
-      }
-      uint8_t* Bs = smem + s * TC_STAGE_BYTES + TC_A_BYTES;
-      const long long k0 = (long long)kb * KE;
-      const int site0 = (int)(k0 % V3);
-#pragma unroll 2
-      for (int task = pt; task < TC_BN * CPR; task += 32 * TC_PWARPS) {
-        const int row = task / CPR, c = task % CPR;
-        const int n = n0 + row;
-        uint32_t hre[4], lre[4], him[4], lim[4];
-        if (n < Ncols) {
-          const int i = n / nmom, p = n - i * nmom;
-          const float* x = Xb + 2 * ((long long)i * K + k0 + c * EPC);
-          const float* ph = reinterpret_cast<const float*>(phases) + 2 * ((long long)p * V3 + site0 + c * EPC);
-          float br[EPC], bi[EPC];
-#pragma unroll
-          for (int e = 0; e < EPC; e += 2) {
-            const float4 xv = __ldg(reinterpret_cast<const float4*>(x + 2 * e));
-            const float4 pv = __ldg(reinterpret_cast<const float4*>(ph + 2 * e));
-            // conj(x) * phase
-            br[e] = xv.x * pv.x + xv.y * pv.y;
-            bi[e] = xv.x * pv.y - xv.y * pv.x;
-            br[e + 1] = xv.z * pv.z + xv.w * pv.w;
-            bi[e + 1] = xv.z * pv.w - xv.w * pv.z;
-          }
-          if constexpr (KIND == TC_TF32) {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              Split<TC_TF32>::one(br[e], hre[e], lre[e]);
-              Split<TC_TF32>::one(bi[e], him[e], lim[e]);
-            }
-          } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              Split<KIND>::pair(br[2 * e], br[2 * e + 1], hre[e], lre[e]);
-              Split<KIND>::pair(bi[2 * e], bi[2 * e + 1], him[e], lim[e]);
-            }
-          }
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e) hre[e] = lre[e] = him[e] = lim[e] = 0u;
-        }
-        const uint32_t off = row * TC_ROWB + ((c ^ ((row >> 1) & 3)) << 4);
-        uint8_t* dst = Bs + off;
-        *reinterpret_cast<uint4*>(dst + 0 * TC_BN * TC_ROWB) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-        *reinterpret_cast<uint4*>(dst + 1 * TC_BN * TC_ROWB) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
-        *reinterpret_cast<uint4*>(dst + 2 * TC_BN * TC_ROWB) = make_uint4(him[0], him[1], him[2], him[3]);
-        *reinterpret_cast<uint4*>(dst + 3 * TC_BN * TC_ROWB) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
-      }
-      fence_proxy_async();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&full[s]);
-    }
-    // ---- epilogue: TMEM -> FP64 G
-    const bool acc_ok = warp_wait(accf, 0, status, TC_ERR_ACC, false);
-    if (ok && acc_ok && *status == 0) {
-      tc_fence_after();
-      const int quarter = warp & 3;
-      const int m = quarter * 32 + lane;  // accumulator row = TMEM lane
-      const long long m_local = (long long)mtile * TC_BM + m;
-      const double inv = ldexp(1.0, -2 * sc->scale_exp);
-      const int N = J.nright * Ne;
-      for (int cc = 0; cc < TC_BN / 16; ++cc) {
-        float vr[16], vi[16];
-        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16) + cc * 16;
-        tmem_ld16(tl, vr);
-        tmem_ld16(tl + TC_BN, vi);
-        if (m_local < Mrows) {
-#pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            const int n = n0 + cc * 16 + e;
-            if (n < Ncols) {
-              const int i = n / nmom, p = n - i * nmom;
-              G[J.g_off + ((long long)p * Ne + i) * N + m_local] = mk((double)vr[e] * inv, (double)vi[e] * inv);
-            }
-          }
-        }
-      }
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 1) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
-  }
-}
+#include "tc_pair_gemm.cuh"
 
 // ------------------------------------------------------------ host side
 
@@ -540,7 +320,8 @@ size_t tc_extra_workspace(const ed_elemental_plan* P) {
   if (!kind) return 0;
   const size_t R = (size_t)P->nchain * P->Ne;
   const size_t K = 3ull * P->V3;
-  return up256(sizeof(TcScalars)) + up256((size_t)P->nmom * P->V3 * 8) + up256(4 * R * K * tc_esz(kind));
+  return up256(sizeof(TcScalars)) + up256((size_t)P->nmom * P->V3 * 8) + up256(4 * R * K * tc_esz(kind)) +
+         up256((size_t)P->g_elems * sizeof(float4));
 }
 
 int tc_plan_check(ed_elemental_plan* P) {
@@ -581,6 +362,7 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
   TcScalars* sc = (TcScalars*)X;
   cplx<float>* ph32 = (cplx<float>*)(X + up256(sizeof(TcScalars)));
   void* planes = X + up256(sizeof(TcScalars)) + up256((size_t)P->nmom * P->V3 * 8);
+  float4* DF = (float4*)((char*)planes + up256(4 * (size_t)P->nchain * P->Ne * 3 * P->V3 * ESZ));
   const long long R = (long long)P->nchain * P->Ne;
   const long long K = 3LL * P->V3;
 
@@ -632,11 +414,15 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
     if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
     attr_set[KIND] = true;
   }
+  e = cudaMemsetAsync(DF, 0, (size_t)P->g_elems * sizeof(float4), stream);
+  if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
   tc_pair_gemm_kernel<KIND><<<tiles, TC_THREADS, TC_SMEM, stream>>>(amap, tab, P->Ne, P->nmom, P->V3, R, chains,
-                                                                    ph32, sc, G);
+                                                                    ph32, sc, DF);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   ED_RETURN_LAUNCH("tensor-core pair GEMM");
+  tc_df_to_c128_kernel<<<4 * sms, 256, 0, stream>>>(DF, P->g_elems, G);
+  ED_RETURN_LAUNCH("double-float to complex128");
   return ED_OK;
 }
 

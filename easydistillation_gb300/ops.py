@@ -216,6 +216,23 @@ class ElementalPlan:
         )
         return out
 
+    def describe(self):
+        """Pair groups of the plan: left chain and number of right chains of
+        each, and whether hermiticity (p -> -p) is used."""
+        n, herm = ctypes.c_int(), ctypes.c_int()
+        left = (ctypes.c_int * 32)()
+        nright = (ctypes.c_int * 32)()
+        call("ed_elemental_describe", self._h, ctypes.byref(n), left, nright, ctypes.byref(herm))
+        return {"left": list(left[: n.value]), "nright": list(nright[: n.value]), "herm": bool(herm.value)}
+
+    def set_profile_events(self, start=None, stop=None):
+        """Have every later run record the torch CUDA events ``start``/``stop``
+        around the pair-contraction kernel (``None`` disables).  The events
+        must already hold a CUDA handle (record them once beforehand)."""
+        h0 = ctypes.c_void_p(start.cuda_event) if start is not None else None
+        h1 = ctypes.c_void_p(stop.cuda_event) if stop is not None else None
+        call("ed_elemental_set_profile_events", self._h, h0, h1)
+
     def check_status(self):
         """Synchronise and raise if a bounded device wait of the last run gave up."""
         code = ctypes.c_int()

@@ -131,6 +131,12 @@ int ed_elemental_run(const ed_elemental_plan* plan, const void* links, long long
                      int evec_prec, const void* evecs, const double* blend, void* out, void* workspace,
                      size_t workspace_bytes, void* stream);
 
+/* Describe the plan's pair groups: *ngroups groups (one per left chain); for
+ * group g, left[g] is its left chain and nright[g] its number of right chains
+ * (arrays of at least 32 ints, may be NULL); *herm = 1 when the momentum list
+ * is closed under p -> -p and hermiticity halves the work. */
+int ed_elemental_describe(const ed_elemental_plan* plan, int* ngroups, int* left, int* nright, int* herm);
+
 /* Record the CUDA events `start` / `stop` (cudaEvent_t, or NULL to disable)
  * on the run's stream immediately before and after the pair-contraction
  * kernel of every later ed_elemental_run with this plan, so a caller can time
