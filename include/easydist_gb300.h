@@ -131,6 +131,23 @@ int ed_elemental_run(const ed_elemental_plan* plan, const void* links, long long
                      int evec_prec, const void* evecs, const double* blend, void* out, void* workspace,
                      size_t workspace_bytes, void* stream);
 
+/* Size of the scratch array built into the library for
+ * ed_elemental_run_noalloc (32 MiB, held on every GPU that loads it). */
+#define ED_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* Same as ed_elemental_run, for callers that cannot allocate device memory
+ * (their GPU memory is owned by another allocator, or they are called from
+ * code that must not allocate): scratch comes from a fixed array inside the
+ * library instead of a caller workspace.  No counterpart in the reference
+ * (it is an addition of this library).  Plans needing more than
+ * ED_NOALLOC_SCRATCH_BYTES are rejected with ED_ERR_WORKSPACE.  The first call
+ * on a device resolves the array's address and should precede any stream
+ * capture; all calls share the array, so calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+int ed_elemental_run_noalloc(const ed_elemental_plan* plan, const void* links, long long dir_stride,
+                             long long site_stride, int evec_prec, const void* evecs, const double* blend, void* out,
+                             void* stream);
+
 /* Describe the plan's pair groups: *ngroups groups (one per left chain); for
  * group g, left[g] is its left chain and nright[g] its number of right chains
  * (arrays of at least 32 ints, may be NULL); *herm = 1 when the momentum list
