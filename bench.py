@@ -45,20 +45,22 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="fp64")
+    ap.add_argument("--mode", default="f16x3", help="elemental mode: f16x3 (headline), tf32x3, bf16x3, fp64")
     ap.add_argument("--lattice", default=None, help="Lx,Ly,Lz,Lt override (parity runs only)")
     ap.add_argument("--ne", type=int, default=NE)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison run")
+    ap.add_argument("--no-stencil", action="store_true", help="skip the Laplacian bandwidth measurement")
     return ap.parse_args()
 
 
 def launches_per_step(mode):
     """Kernels of one elemental timeslice: links->SoA, phases, vectors->planes,
-    12 hops, the pair GEMM, the combine; tensor-core modes add absmax, scale,
-    split and phase-scaling kernels."""
-    return 3 + 12 + 1 + 1 + (0 if mode == "fp64" else 4)
+    12 hops, the pair GEMM, the combine; tensor-core modes add complex64
+    links, absmax, scale, split, phase scaling and the double-float to
+    complex128 conversion."""
+    return 3 + 12 + 1 + 1 + (0 if mode == "fp64" else 6)
 
 
 def load_peaks():
@@ -203,6 +205,48 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def bench_stencil(U, latt, dev, reps=20):
+    """HBM roofline of the 3D Laplacian kernel as the batched Lanczos uses it:
+    one application = every timeslice x one vector.  Algorithmic bytes per
+    site: 27 link + 3 input + 3 output complex numbers (264 B at c64, 528 B at
+    c128); the 64 timeslices of links exceed L2, so every application streams
+    them from HBM."""
+    import torch
+
+    from easydistillation_gb300.ops import laplacian, links_to_soa
+
+    Lx, Ly, Lz, Lt = latt
+    V3 = Lx * Ly * Lz
+    peaks = load_peaks()
+    pk, src = (peaks["hbm_gbs"], "measured") if "hbm_gbs" in peaks else (6800.0, "fallback")
+    out = {}
+    for name, dt, s in (("c64", torch.complex64, 8), ("c128", torch.complex128, 16)):
+        links = links_to_soa(U, latt, dtype=dt)
+        F = torch.randn((Lt, 1, 3, V3), dtype=dt, device=dev)
+        G = torch.empty_like(F)
+        for _ in range(3):
+            laplacian(links, F, latt, out=G)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        for r in range(reps):
+            if r % 2 == 0:
+                laplacian(links, F, latt, out=G)
+            else:
+                laplacian(links, G, latt, out=F)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        nbytes = V3 * Lt * (27 * s + 6 * s)
+        gbs = nbytes / ms / 1e6
+        out[name] = {"bound": "hbm", "achieved": gbs, "peak": pk, "unit": "GB/s", "frac": gbs / pk,
+                     "peak_source": src, "traffic": None, "bytes_per_launch": nbytes, "kernel_ms": ms,
+                     "kernel": f"laplacian_kernel<{'float,2' if s == 8 else 'double,1'}>",
+                     "workload": f"{Lx}^3 x {Lt} timeslices x 1 vector"}
+        del links, F, G
+    return out
+
+
 # ---------------------------------------------------------------- ours
 def run_ours(args, rank, world):
     import numpy as np
@@ -302,6 +346,8 @@ def run_ours(args, rank, world):
         del plan64, out64
         torch.cuda.empty_cache()
 
+    stencil = None if args.no_stencil else bench_stencil(U, latt, dev)
+
     # end to end through the public generator: host eigenvectors in, host elementals out
     e2e = None
     if not args.no_e2e:
@@ -352,6 +398,7 @@ def run_ours(args, rank, world):
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": args.steps * launches_per_step(args.mode),
             "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "fp64_gpu": fp64,
+            "stencil_roofline": stencil,
         }
         print(json.dumps(line), flush=True)
 

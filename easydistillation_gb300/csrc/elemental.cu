@@ -29,6 +29,7 @@ int launch_to_planes(int ip, int op, int round_c64, long long nvec, int V3, cons
 int launch_phases(Latt L, const int* moms, int nmom, cplx<double>* out, cudaStream_t stream);
 int launch_hop(int in_prec, int out_prec, Latt L, int d, int nvec, const void* links_c128, const void* in,
                void* out, cudaStream_t stream);
+int launch_hop_f32(Latt L, int d, int nvec, const void* links_c64, const void* in, void* out, cudaStream_t stream);
 
 // ------------------------------------------------------------ plan (host)
 
@@ -164,6 +165,8 @@ int plan_build(ed_elemental_plan* P) {
   size_t off = 0;
   P->off_links = off;
   off = up(off + 27ull * P->V3 * 16);
+  P->off_links32 = off;
+  if (P->mode != ED_MODE_FP64) off = up(off + 27ull * P->V3 * 8);
   P->off_phase = off;
   off = up(off + (size_t)P->nmom * P->V3 * 16);
   P->off_chain = off;
@@ -381,9 +384,18 @@ int elemental_run(const ed_elemental_plan* P, const void* links, long long dir_s
   const size_t chain_bytes = (size_t)P->Ne * 3 * P->V3 * celt;
   rc = launch_to_planes(evec_prec, cprec, 1, P->Ne, P->V3, evecs, chains, stream);
   if (rc) return rc;
+  void* links32 = W + P->off_links32;
+  if (cprec == ED_C64 && P->nchain > 1) {
+    rc = launch_links_to_soa(ED_C64, L, 1, links, 0, dir_stride, site_stride, links32, stream);
+    if (rc) return rc;
+  }
   for (int c = 1; c < P->nchain; ++c) {
-    rc = launch_hop(cprec, cprec, L, P->chain_dir[c], P->Ne, links_soa, chains + P->chain_parent[c] * chain_bytes,
-                    chains + c * chain_bytes, stream);
+    const void* src = chains + P->chain_parent[c] * chain_bytes;
+    void* dst = chains + c * chain_bytes;
+    if (cprec == ED_C64)
+      rc = launch_hop_f32(L, P->chain_dir[c], P->Ne, links32, src, dst, stream);
+    else
+      rc = launch_hop(cprec, cprec, L, P->chain_dir[c], P->Ne, links_soa, src, dst, stream);
     if (rc) return rc;
   }
   cplx<double>* G = (cplx<double>*)(W + P->off_g);

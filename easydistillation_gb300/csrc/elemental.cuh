@@ -37,7 +37,7 @@ struct ed_elemental_plan {
   std::vector<int> term_start;
   long long g_elems;
   int npairs;
-  size_t off_links, off_phase, off_chain, off_g, off_extra, ws_bytes;
+  size_t off_links, off_links32, off_phase, off_chain, off_g, off_extra, ws_bytes;
   // tensor-core path parameters (filled by tc_plan_check)
   int tc_kind;        // 0 = none
   int tc_scale_exp;   // power-of-two scale applied before fp16 splitting

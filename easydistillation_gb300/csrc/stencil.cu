@@ -177,9 +177,10 @@ __global__ void __launch_bounds__(128) laplacian_kernel(Latt L, const cplx<T>* _
 
 // Covariant-derivative hop in direction d for a block of vectors.  Links are
 // held in registers (two 3x3 per site) and reused over VB vectors.  Math in
-// double; input/output storage TI/TO (c128 or c64).
-template <typename TI, typename TO, int VB>
-__global__ void __launch_bounds__(128) hop_kernel(Latt L, int d, int nvec, const cplx<double>* __restrict__ U,
+// the links' precision TM (double, or float for the complex64 chains of the
+// split-precision elemental modes); input/output storage TI/TO.
+template <typename TI, typename TO, typename TM, int VB>
+__global__ void __launch_bounds__(128) hop_kernel(Latt L, int d, int nvec, const cplx<TM>* __restrict__ U,
                                                   const cplx<TI>* __restrict__ in, cplx<TO>* __restrict__ out) {
   const int V3 = L.V3();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(128) hop_kernel(Latt L, int d, int nvec, const
     sp = s + (wrap_inc(z, L.Lz) - z) * L.Lx * L.Ly;
     sm = s + (wrap_dec(z, L.Lz) - z) * L.Lx * L.Ly;
   }
-  cplx<double> uf[9], ub[9];
+  cplx<TM> uf[9], ub[9];
 #pragma unroll
   for (int e = 0; e < 9; ++e) {
     uf[e] = ld(U + (d * 9 + e) * V3 + s);
@@ -209,15 +210,15 @@ __global__ void __launch_bounds__(128) hop_kernel(Latt L, int d, int nvec, const
   const int v1 = min(nvec, v0 + VB);
   for (int v = v0; v < v1; ++v) {
     const cplx<TI>* F = in + (long long)v * 3 * V3;
-    cplx<double> a[3], b[3], r[3];
+    cplx<TM> a[3], b[3], r[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      a[c] = cvt<double>(ld(F + c * V3 + sp));
-      b[c] = cvt<double>(ld(F + c * V3 + sm));
-      r[c] = mk(0.0, 0.0);
+      a[c] = cvt<TM>(ld(F + c * V3 + sp));
+      b[c] = cvt<TM>(ld(F + c * V3 + sm));
+      r[c] = mk(TM(0), TM(0));
     }
     mv_add(r, uf, a);
-    cplx<double> q[3] = {mk(0.0, 0.0), mk(0.0, 0.0), mk(0.0, 0.0)};
+    cplx<TM> q[3] = {mk(TM(0), TM(0)), mk(TM(0), TM(0)), mk(TM(0), TM(0))};
     mvd_add(q, ub, b);
     cplx<TO>* O = out + (long long)v * 3 * V3;
 #pragma unroll
@@ -251,18 +252,29 @@ int launch_hop(int in_prec, int out_prec, Latt L, int d, int nvec, const void* l
   dim3 grid(ceil_div(V3, 128), ceil_div(nvec, VB));
   const cplx<double>* U = (const cplx<double>*)links_c128;
   if (in_prec == ED_C128 && out_prec == ED_C128)
-    hop_kernel<double, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<double>*)in,
-                                                             (cplx<double>*)out);
+    hop_kernel<double, double, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<double>*)in,
+                                                                     (cplx<double>*)out);
   else if (in_prec == ED_C64 && out_prec == ED_C64)
-    hop_kernel<float, float, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<float>*)in,
-                                                           (cplx<float>*)out);
+    hop_kernel<float, float, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<float>*)in,
+                                                                   (cplx<float>*)out);
   else if (in_prec == ED_C64 && out_prec == ED_C128)
-    hop_kernel<float, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<float>*)in,
-                                                            (cplx<double>*)out);
+    hop_kernel<float, double, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<float>*)in,
+                                                                    (cplx<double>*)out);
   else
-    hop_kernel<double, float, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<double>*)in,
-                                                            (cplx<float>*)out);
+    hop_kernel<double, float, double, VB><<<grid, 128, 0, stream>>>(L, d, nvec, U, (const cplx<double>*)in,
+                                                                    (cplx<float>*)out);
   ED_RETURN_LAUNCH("covariant derivative hop");
+  return ED_OK;
+}
+
+// complex64 chains with FP32 links and FP32 math (split-precision elemental modes)
+int launch_hop_f32(Latt L, int d, int nvec, const void* links_c64, const void* in, void* out, cudaStream_t stream) {
+  constexpr int VB = 8;
+  const int V3 = L.V3();
+  dim3 grid(ceil_div(V3, 128), ceil_div(nvec, VB));
+  hop_kernel<float, float, float, VB><<<grid, 128, 0, stream>>>(L, d, nvec, (const cplx<float>*)links_c64,
+                                                                (const cplx<float>*)in, (cplx<float>*)out);
+  ED_RETURN_LAUNCH("covariant derivative hop (fp32)");
   return ED_OK;
 }
 

@@ -192,22 +192,40 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else {
     // ===================== B producers
+    // Each thread owns up to NT fixed (row, chunk) tasks; their row pointers
+    // are resolved once per tile, so the K loop only adds offsets.
+    constexpr int NT = (TC_BN * CPR + 32 * TC_PWARPS - 1) / (32 * TC_PWARPS);
     const int pt = threadIdx.x - 64;  // 0..191
     const float* Xb = reinterpret_cast<const float*>(chains + (long long)J.left * Ne * K);
+    const float* Pb = reinterpret_cast<const float*>(phases);
+    const float* xrow[NT];
+    const float* prow[NT];
+    uint32_t soff[NT];
+    int tstate[NT];  // 0: no task, 1: zero row (beyond the tile), 2: data row
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int task = pt + t * 32 * TC_PWARPS;
+      const int row = task / CPR, c = task % CPR;
+      const int n = n0 + row;
+      tstate[t] = task >= TC_BN * CPR ? 0 : (n < Ncols ? 2 : 1);
+      const int i = n < Ncols ? n / nmom : 0, p = n < Ncols ? n - (n / nmom) * nmom : 0;
+      xrow[t] = Xb + 2 * ((long long)i * K + c * EPC);
+      prow[t] = Pb + 2 * ((long long)p * V3 + c * EPC);
+      soff[t] = row * TC_ROWB + ((c ^ ((row >> 1) & 3)) << 4);
+    }
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % TC_STAGES;
       if (kb >= TC_STAGES && !warp_wait(&empty[s], ((kb / TC_STAGES) + 1) & 1, status, TC_ERR_EMPTY)) break;
       uint8_t* Bs = smem + s * TC_STAGE_BYTES + TC_A_BYTES;
       const long long k0 = (long long)kb * KE;
       const int site0 = (int)(k0 % V3);
-      for (int task = pt; task < TC_BN * CPR; task += 32 * TC_PWARPS) {
-        const int row = task / CPR, c = task % CPR;
-        const int n = n0 + row;
+#pragma unroll
+      for (int t = 0; t < NT; ++t) {
+        if (tstate[t] == 0) continue;
         uint32_t hre[4], lre[4], him[4], lim[4];
-        if (n < Ncols) {
-          const int i = n / nmom, p = n - i * nmom;
-          const float* x = Xb + 2 * ((long long)i * K + k0 + c * EPC);
-          const float* ph = reinterpret_cast<const float*>(phases) + 2 * ((long long)p * V3 + site0 + c * EPC);
+        if (tstate[t] == 2) {
+          const float* x = xrow[t] + 2 * k0;
+          const float* ph = prow[t] + 2 * site0;
           float br[EPC], bi[EPC];
 #pragma unroll
           for (int e = 0; e < EPC; e += 2) {
@@ -235,7 +253,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
           for (int e = 0; e < 4; ++e) hre[e] = lre[e] = him[e] = lim[e] = 0u;
         }
-        uint8_t* dst = Bs + row * TC_ROWB + ((c ^ ((row >> 1) & 3)) << 4);
+        uint8_t* dst = Bs + soff[t];
         *reinterpret_cast<uint4*>(dst + 0 * TC_BN * TC_ROWB) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
         *reinterpret_cast<uint4*>(dst + 1 * TC_BN * TC_ROWB) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
         *reinterpret_cast<uint4*>(dst + 2 * TC_BN * TC_ROWB) = make_uint4(him[0], him[1], him[2], him[3]);
