@@ -14,12 +14,13 @@ The arithmetic runs in ``libeasydist_gb300.so`` (C ABI:
 ``python -m easydistillation_gb300.build``.  There is no CPU fallback.
 """
 
-from .generator import EigenvectorGenerator, ElementalGenerator
+from .generator import DisplacementElementalGenerator, EigenvectorGenerator, ElementalGenerator
 from .insertion import MomentumPhase, derivative, mom_dict_to_list, num_derivative
 
 NC, NS, ND = 3, 4, 4
 
 __all__ = [
+    "DisplacementElementalGenerator",
     "EigenvectorGenerator",
     "ElementalGenerator",
     "MomentumPhase",

@@ -39,6 +39,7 @@ _SIGNATURES = {
     "ed_vectors_from_planes": ([_i, _i, _ll, _i, _vp, _vp, _vp], _i),
     "ed_momentum_phases": ([_i, _i, _i, _c.POINTER(_i), _i, _vp, _vp], _i),
     "ed_laplacian": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _ll, _vp, _ll, _vp], _i),
+    "ed_stout_smear_step": ([_i, _i, _i, _i, _c.c_double, _vp, _vp, _vp], _i),
     "ed_covariant_derivative": ([_i, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
     "ed_elemental_plan_create": (
         [_c.POINTER(_vp), _i, _i, _i, _i, _i, _c.POINTER(_i), _i, _i],
@@ -51,6 +52,21 @@ _SIGNATURES = {
     "ed_elemental_status": ([_vp, _vp, _c.POINTER(_i), _vp], _i),
     "ed_elemental_set_profile_events": ([_vp, _vp, _vp], _i),
     "ed_elemental_run_noalloc": ([_vp, _vp, _ll, _ll, _i, _vp, _vp, _vp, _vp], _i),
+    "ed_elemental_plan_create_batched": (
+        [_c.POINTER(_vp), _i, _i, _i, _i, _i, _c.POINTER(_i), _i, _i, _i],
+        _i,
+    ),
+    "ed_elemental_run_batch": (
+        [_vp, _i, _c.POINTER(_vp), _ll, _ll, _i, _c.POINTER(_vp), _vp, _c.POINTER(_vp), _vp, _c.c_size_t, _vp],
+        _i,
+    ),
+    "ed_parallel_transport": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
+    "ed_mean_c128": ([_i, _ll, _ll, _vp, _vp, _vp], _i),
+    "ed_pair_plan_create": (
+        [_c.POINTER(_vp), _i, _i, _i, _i, _i, _c.POINTER(_i), _i, _i, _i, _i, _i],
+        _i,
+    ),
+    "ed_pair_run": ([_vp, _vp, _vp, _vp, _c.c_size_t, _vp], _i),
     "ed_elemental_describe": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
 }
 

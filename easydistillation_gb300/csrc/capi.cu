@@ -1,6 +1,7 @@
 // Error state, layout conversions and momentum-phase tables.
 #include <cstdarg>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
@@ -212,4 +213,31 @@ extern "C" int ed_momentum_phases(int Lx, int Ly, int Lz, const int* moms, int n
   for (int i = 0; i < 3 * nmom; ++i)
     ED_CHECK_ARG(moms[i] > -1000000 && moms[i] < 1000000, "ed_momentum_phases: momentum component out of range");
   return ed::launch_phases(ed::Latt{Lx, Ly, Lz}, moms, nmom, (ed::cplx<double>*)out, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------ mean of arrays
+namespace ed {
+__global__ void mean_kernel(int nsrc, long long n, long long src_stride, const cplx<double>* __restrict__ src,
+                            cplx<double>* __restrict__ out) {
+  const double inv = 1.0 / nsrc;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int k = 0; k < nsrc; ++k) {
+      const cplx<double> v = src[k * src_stride + i];
+      re += v.re;
+      im += v.im;
+    }
+    out[i] = mk(re * inv, im * inv);
+  }
+}
+}  // namespace ed
+
+extern "C" int ed_mean_c128(int nsrc, long long n, long long src_stride, const void* src, void* out, void* stream) {
+  ED_CHECK_ARG(nsrc > 0 && n > 0 && src_stride >= n, "ed_mean_c128: bad sizes");
+  ED_CHECK_ARG(src && out, "ed_mean_c128: null pointer");
+  const int grid = (int)std::min<long long>(ed::ceil_div(n, 256), 8LL * ed::num_sms());
+  ed::mean_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(nsrc, n, src_stride, (const ed::cplx<double>*)src,
+                                                          (ed::cplx<double>*)out);
+  ED_RETURN_LAUNCH("mean");
+  return ED_OK;
 }

@@ -160,18 +160,39 @@ int plan_build(ed_elemental_plan* P) {
   P->npairs = 0;
   for (auto& j : P->jobs) P->npairs += j.nright;
 
+  // Batch of timeslices: timeslice b owns chains [b*nchain, (b+1)*nchain) and
+  // G block b; its groups repeat the first timeslice's with those offsets, so
+  // one pair-contraction launch covers the whole batch.
+  P->jobs_per_t = (int)P->jobs.size();
+  P->g_per_t = P->g_elems;
+  if ((long long)P->jobs_per_t * P->nbatch > kMaxJobs) {
+    set_error("elemental plan: %d timeslices x %d pair groups exceed the limit %d", P->nbatch, P->jobs_per_t,
+              kMaxJobs);
+    return ED_ERR_UNSUPPORTED;
+  }
+  for (int b = 1; b < P->nbatch; ++b)
+    for (int k = 0; k < P->jobs_per_t; ++k) {
+      Job j = P->jobs[k];
+      j.left += b * P->nchain;
+      j.right0 += b * P->nchain;
+      j.g_off += b * P->g_per_t;
+      P->jobs.push_back(j);
+    }
+  P->g_elems = P->g_per_t * P->nbatch;
+
   // workspace layout (256-byte aligned sections)
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+  const size_t B = (size_t)P->nbatch;
   size_t off = 0;
   P->off_links = off;
-  off = up(off + 27ull * P->V3 * 16);
+  off = up(off + B * 27ull * P->V3 * 16);
   P->off_links32 = off;
-  if (P->mode != ED_MODE_FP64) off = up(off + 27ull * P->V3 * 8);
+  if (P->mode != ED_MODE_FP64) off = up(off + B * 27ull * P->V3 * 8);
   P->off_phase = off;
   off = up(off + (size_t)P->nmom * P->V3 * 16);
   P->off_chain = off;
   const size_t chain_elt = P->mode == ED_MODE_FP64 ? 16 : 8;
-  off = up(off + (size_t)P->nchain * P->Ne * 3 * P->V3 * chain_elt);
+  off = up(off + B * (size_t)P->nchain * P->Ne * 3 * P->V3 * chain_elt);
   P->off_g = off;
   off = up(off + (size_t)P->g_elems * 16);
   P->off_extra = off;
@@ -320,9 +341,9 @@ __global__ void combine_kernel(const CombineTable tab, const cplx<double>* __res
 // ------------------------------------------------------------ run
 
 int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains, const cplx<double>* phases,
-                         cplx<double>* G, cudaStream_t stream) {
+                         cplx<double>* G, cudaStream_t stream, int njobs) {
   GemmTable tab;
-  tab.njobs = (int)P->jobs.size();
+  tab.njobs = njobs;
   int tiles = 0;
   for (int k = 0; k < tab.njobs; ++k) {
     const Job& j = P->jobs[k];
@@ -353,7 +374,7 @@ int launch_combine(const ed_elemental_plan* P, const cplx<double>* G, const doub
   tab.Ne = P->Ne;
   for (int d = 0; d <= P->nderiv; ++d) tab.start[d] = P->term_start[d];
   for (size_t q = 0; q < P->terms.size(); ++q) tab.t[q] = P->terms[q];
-  for (size_t k = 0; k < P->jobs.size(); ++k) {
+  for (int k = 0; k < P->jobs_per_t; ++k) {  // offsets within one timeslice's G block
     tab.g_off[k] = P->jobs[k].g_off;
     tab.nright[k] = P->jobs[k].nright;
   }
@@ -366,46 +387,61 @@ int launch_combine(const ed_elemental_plan* P, const cplx<double>* G, const doub
 }
 
 
-int elemental_run(const ed_elemental_plan* P, const void* links, long long dir_stride, long long site_stride,
-                  int evec_prec, const void* evecs, const double* blend, void* out, void* ws, size_t ws_bytes,
-                  cudaStream_t stream) {
+int elemental_run_batch(const ed_elemental_plan* P, int nb, const void* const* links, long long dir_stride,
+                        long long site_stride, int evec_prec, const void* const* evecs, const double* blend,
+                        void* const* outs, void* ws, size_t ws_bytes, cudaStream_t stream) {
   char* W = (char*)ws;
   const Latt L{P->Lx, P->Ly, P->Lz};
   int rc;
-  void* links_soa = W + P->off_links;
-  rc = launch_links_to_soa(ED_C128, L, 1, links, 0, dir_stride, site_stride, links_soa, stream);
-  if (rc) return rc;
   cplx<double>* phases = (cplx<double>*)(W + P->off_phase);
   rc = launch_phases(L, P->moms.data(), P->nmom, phases, stream);
   if (rc) return rc;
   const int cprec = P->mode == ED_MODE_FP64 ? ED_C128 : ED_C64;
   const size_t celt = cprec == ED_C128 ? 16 : 8;
-  char* chains = W + P->off_chain;
   const size_t chain_bytes = (size_t)P->Ne * 3 * P->V3 * celt;
-  rc = launch_to_planes(evec_prec, cprec, 1, P->Ne, P->V3, evecs, chains, stream);
-  if (rc) return rc;
-  void* links32 = W + P->off_links32;
-  if (cprec == ED_C64 && P->nchain > 1) {
-    rc = launch_links_to_soa(ED_C64, L, 1, links, 0, dir_stride, site_stride, links32, stream);
+  for (int b = 0; b < nb; ++b) {
+    void* links_soa = W + P->off_links + (size_t)b * 27 * P->V3 * 16;
+    void* links32 = W + P->off_links32 + (size_t)b * 27 * P->V3 * 8;
+    char* chains = W + P->off_chain + (size_t)b * P->nchain * chain_bytes;
+    if (cprec == ED_C128 || P->nchain == 1) {
+      rc = launch_links_to_soa(ED_C128, L, 1, links[b], 0, dir_stride, site_stride, links_soa, stream);
+      if (rc) return rc;
+    }
+    rc = launch_to_planes(evec_prec, cprec, 1, P->Ne, P->V3, evecs[b], chains, stream);
     if (rc) return rc;
-  }
-  for (int c = 1; c < P->nchain; ++c) {
-    const void* src = chains + P->chain_parent[c] * chain_bytes;
-    void* dst = chains + c * chain_bytes;
-    if (cprec == ED_C64)
-      rc = launch_hop_f32(L, P->chain_dir[c], P->Ne, links32, src, dst, stream);
-    else
-      rc = launch_hop(cprec, cprec, L, P->chain_dir[c], P->Ne, links_soa, src, dst, stream);
-    if (rc) return rc;
+    if (cprec == ED_C64 && P->nchain > 1) {
+      rc = launch_links_to_soa(ED_C64, L, 1, links[b], 0, dir_stride, site_stride, links32, stream);
+      if (rc) return rc;
+    }
+    for (int c = 1; c < P->nchain; ++c) {
+      const void* src = chains + P->chain_parent[c] * chain_bytes;
+      void* dst = chains + c * chain_bytes;
+      if (cprec == ED_C64)
+        rc = launch_hop_f32(L, P->chain_dir[c], P->Ne, links32, src, dst, stream);
+      else
+        rc = launch_hop(cprec, cprec, L, P->chain_dir[c], P->Ne, links_soa, src, dst, stream);
+      if (rc) return rc;
+    }
   }
   cplx<double>* G = (cplx<double>*)(W + P->off_g);
-  if (P->mode == ED_MODE_FP64) {
-    rc = launch_pair_gemm_f64(P, (const cplx<double>*)chains, phases, G, stream);
-  } else {
-    rc = launch_pair_gemm_tc(P, (const cplx<float>*)chains, phases, G, W + P->off_extra, stream);
-  }
+  const int njobs = nb * P->jobs_per_t;
+  if (P->mode == ED_MODE_FP64)
+    rc = launch_pair_gemm_f64(P, (const cplx<double>*)(W + P->off_chain), phases, G, stream, njobs);
+  else
+    rc = launch_pair_gemm_tc(P, (const cplx<float>*)(W + P->off_chain), phases, G, W + P->off_extra, stream, nb);
   if (rc) return rc;
-  return launch_combine(P, G, blend, (cplx<double>*)out, stream);
+  for (int b = 0; b < nb; ++b) {
+    rc = launch_combine(P, G + (size_t)b * P->g_per_t, blend, (cplx<double>*)outs[b], stream);
+    if (rc) return rc;
+  }
+  return ED_OK;
+}
+
+int elemental_run(const ed_elemental_plan* P, const void* links, long long dir_stride, long long site_stride,
+                  int evec_prec, const void* evecs, const double* blend, void* out, void* ws, size_t ws_bytes,
+                  cudaStream_t stream) {
+  return elemental_run_batch(P, 1, &links, dir_stride, site_stride, evec_prec, &evecs, blend, &out, ws, ws_bytes,
+                             stream);
 }
 
 }  // namespace ed
@@ -461,7 +497,7 @@ extern "C" int ed_elemental_num_pairs(const ed_elemental_plan* plan, int* npairs
 extern "C" int ed_elemental_run(const ed_elemental_plan* plan, const void* links, long long dir_stride,
                                 long long site_stride, int evec_prec, const void* evecs, const double* blend,
                                 void* out, void* workspace, size_t workspace_bytes, void* stream) {
-  ED_CHECK_ARG(plan, "ed_elemental_run: null plan");
+  ED_CHECK_ARG(plan && !plan->custom, "ed_elemental_run: needs a plan from ed_elemental_plan_create");
   ED_CHECK_ARG(links && evecs && out && workspace, "ed_elemental_run: null pointer");
   ED_CHECK_ARG(evec_prec == ED_C128 || evec_prec == ED_C64, "ed_elemental_run: bad eigenvector precision");
   ED_CHECK_ARG(dir_stride >= 0 && site_stride >= 0, "ed_elemental_run: negative stride");
@@ -503,4 +539,92 @@ extern "C" int ed_elemental_describe(const ed_elemental_plan* plan, int* ngroups
     if (nright) nright[g] = plan->jobs[g].nright;
   }
   return ED_OK;
+}
+
+// ------------------------------------------------------------ generic pair contractions
+// G_p[i][r*Ne + j] = sum_k conj(X_i[k]) phase_p(k) Y_{right0+r, j}[k] for caller-built
+// chains (colour planes), e.g. the displaced vectors of the displacement elemental.
+
+namespace ed {
+static int pair_plan_build(ed_elemental_plan* P, int left, int right0, int nright) {
+  P->V3 = P->Lx * P->Ly * P->Lz;
+  P->nderiv = 0;
+  P->custom = true;
+  P->negidx.assign(P->nmom, -1);
+  P->herm = false;
+  P->jobs.clear();
+  Job j;
+  j.left = left;
+  j.right0 = right0;
+  j.nright = nright;
+  j.g_off = 0;
+  P->jobs.push_back(j);
+  P->g_elems = (long long)P->nmom * P->Ne * nright * P->Ne;
+  P->terms.clear();
+  P->term_start.assign(1, 0);
+  P->npairs = nright;
+  P->nbatch = 1;
+  P->jobs_per_t = 1;
+  P->g_per_t = P->g_elems;
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+  P->off_links = P->off_links32 = P->off_chain = P->off_g = 0;
+  P->off_phase = 0;
+  size_t off = up((size_t)P->nmom * P->V3 * 16);
+  P->off_extra = off;
+  P->ws_bytes = off;  // tc_plan_check adds the tensor-core extra below
+  return ED_OK;
+}
+}  // namespace ed
+
+extern "C" int ed_pair_plan_create(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne, int nchain,
+                                   const int* moms, int nmom, int mode, int left, int right0, int nright) {
+  ED_CHECK_ARG(plan, "ed_pair_plan_create: null plan pointer");
+  *plan = nullptr;
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0 && nchain > 0 && nright > 0,
+               "ed_pair_plan_create: sizes must be positive");
+  ED_CHECK_ARG(left >= 0 && left < nchain && right0 >= 0 && right0 + nright <= nchain,
+               "ed_pair_plan_create: chain indices out of range");
+  ED_CHECK_ARG(moms, "ed_pair_plan_create: null momentum list");
+  ED_CHECK_ARG(ed::mode_supported(mode), "ed_pair_plan_create: unknown mode %d", mode);
+  auto* P = new ed_elemental_plan();
+  P->Lx = Lx;
+  P->Ly = Ly;
+  P->Lz = Lz;
+  P->Ne = Ne;
+  P->num_nabla = 0;
+  P->nmom = nmom;
+  P->mode = mode;
+  P->use_herm = false;
+  P->nchain = nchain;
+  P->moms.assign(moms, moms + 3 * nmom);
+  int rc = ed::pair_plan_build(P, left, right0, nright);
+  if (rc == ED_OK) rc = ed::tc_plan_check(P);
+  if (rc == ED_OK) P->ws_bytes = P->off_extra + ed::tc_extra_workspace(P);
+  if (rc != ED_OK) {
+    delete P;
+    return rc;
+  }
+  *plan = P;
+  return ED_OK;
+}
+
+extern "C" int ed_pair_run(const ed_elemental_plan* plan, const void* chains, void* G, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+  ED_CHECK_ARG(plan && plan->custom, "ed_pair_run: needs a plan from ed_pair_plan_create");
+  ED_CHECK_ARG(chains && G && workspace, "ed_pair_run: null pointer");
+  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0, "ed_pair_run: workspace must be 256-byte aligned");
+  if (workspace_bytes < plan->ws_bytes) {
+    ed::set_error("ed_pair_run: workspace of %zu bytes is smaller than the %zu the plan needs", workspace_bytes,
+                  plan->ws_bytes);
+    return ED_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  char* W = (char*)workspace;
+  ed::cplx<double>* phases = (ed::cplx<double>*)(W + plan->off_phase);
+  int rc = ed::launch_phases(ed::Latt{plan->Lx, plan->Ly, plan->Lz}, plan->moms.data(), plan->nmom, phases, s);
+  if (rc) return rc;
+  if (plan->mode == ED_MODE_FP64)
+    return ed::launch_pair_gemm_f64(plan, (const ed::cplx<double>*)chains, phases, (ed::cplx<double>*)G, s, 1);
+  return ed::launch_pair_gemm_tc(plan, (const ed::cplx<float>*)chains, phases, (ed::cplx<double>*)G,
+                                 W + plan->off_extra, s, 1);
 }

@@ -7,7 +7,7 @@
 
 namespace ed {
 
-constexpr int kMaxJobs = 32;   // pair groups (one per left chain)
+constexpr int kMaxJobs = 64;   // pair groups (one per left chain and timeslice of a batch)
 constexpr int kMaxTerms = 64;  // subset terms over all operators (43 for num_nabla = 2)
 constexpr int kMaxDeriv = 13;  // operators for num_nabla = 2
 constexpr int kMaxMom = 256;   // momenta for which p -> -p lookup is tabulated
@@ -29,6 +29,10 @@ struct Term {
 struct ed_elemental_plan {
   int Lx, Ly, Lz, V3, Ne, num_nabla, nderiv, nmom, mode;
   bool use_herm, herm;
+  bool custom = false;  // generic pair plan (caller-built chains, no operator terms)
+  int nbatch = 1;       // timeslices per run (batched plans)
+  int jobs_per_t = 0;   // pair groups of one timeslice
+  long long g_per_t = 0;  // G elements of one timeslice
   std::vector<int> moms, negidx;
   int nchain;
   std::vector<int> chain_parent, chain_dir;
@@ -50,6 +54,6 @@ bool mode_supported(int mode);
 size_t tc_extra_workspace(const ed_elemental_plan* P);
 int tc_plan_check(ed_elemental_plan* P);
 int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
-                        cplx<double>* G, void* extra, cudaStream_t stream);
+                        cplx<double>* G, void* extra, cudaStream_t stream, int nb);
 int tc_read_status(const ed_elemental_plan* P, const void* workspace, int* status, cudaStream_t stream);
 }  // namespace ed

@@ -1,0 +1,70 @@
+// Batched elementals: several timeslices of one lattice in one pass.
+//
+// A batched plan repeats the pair groups of one timeslice for every timeslice
+// of the batch (chain and G offsets per timeslice), so the chains of all
+// timeslices are built first and ONE pair-contraction launch then covers the
+// whole batch: the tiles of all timeslices share the GPU, which removes the
+// partial last wave a single timeslice leaves (1376 tiles = 9.05 waves of 152
+// CTAs at 32^3, Ne = 200, 27 momenta).  All launches are stream-ordered and
+// allocation-free, so the whole batch can be captured in a CUDA graph.
+#include "elemental.cuh"
+
+namespace ed {
+int plan_build(ed_elemental_plan* P);
+int elemental_run_batch(const ed_elemental_plan* P, int nb, const void* const* links, long long dir_stride,
+                        long long site_stride, int evec_prec, const void* const* evecs, const double* blend,
+                        void* const* outs, void* ws, size_t ws_bytes, cudaStream_t stream);
+}  // namespace ed
+
+extern "C" int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne,
+                                                int num_nabla, const int* moms, int nmom, int mode, int max_batch) {
+  ED_CHECK_ARG(plan, "ed_elemental_plan_create_batched: null plan pointer");
+  *plan = nullptr;
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0 && max_batch > 0,
+               "ed_elemental_plan_create_batched: sizes must be positive");
+  ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create_batched: num_nabla must be 0, 1 or 2");
+  ED_CHECK_ARG(moms, "ed_elemental_plan_create_batched: null momentum list");
+  ED_CHECK_ARG(ed::mode_supported(mode), "ed_elemental_plan_create_batched: unknown mode %d", mode);
+  ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create_batched: lattice too large");
+  auto* P = new ed_elemental_plan();
+  P->Lx = Lx;
+  P->Ly = Ly;
+  P->Lz = Lz;
+  P->Ne = Ne;
+  P->num_nabla = num_nabla;
+  P->nmom = nmom;
+  P->mode = mode;
+  P->use_herm = true;
+  P->nbatch = max_batch;
+  P->moms.assign(moms, moms + 3 * nmom);
+  int rc = ed::plan_build(P);
+  if (rc == ED_OK) rc = ed::tc_plan_check(P);
+  if (rc != ED_OK) {
+    delete P;
+    return rc;
+  }
+  *plan = P;
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_run_batch(const ed_elemental_plan* plan, int nbatch, const void* const* links,
+                                      long long dir_stride, long long site_stride, int evec_prec,
+                                      const void* const* evecs, const double* blend, void* const* outs,
+                                      void* workspace, size_t workspace_bytes, void* stream) {
+  ED_CHECK_ARG(plan && !plan->custom, "ed_elemental_run_batch: needs an elemental plan");
+  ED_CHECK_ARG(nbatch > 0 && nbatch <= plan->nbatch, "ed_elemental_run_batch: batch of %d timeslices, plan holds %d",
+               nbatch, plan->nbatch);
+  ED_CHECK_ARG(links && evecs && outs && workspace, "ed_elemental_run_batch: null pointer");
+  for (int b = 0; b < nbatch; ++b)
+    ED_CHECK_ARG(links[b] && evecs[b] && outs[b], "ed_elemental_run_batch: null pointer for timeslice %d", b);
+  ED_CHECK_ARG(evec_prec == ED_C128 || evec_prec == ED_C64, "ed_elemental_run_batch: bad eigenvector precision");
+  ED_CHECK_ARG(dir_stride >= 0 && site_stride >= 0, "ed_elemental_run_batch: negative stride");
+  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0, "ed_elemental_run_batch: workspace must be 256-byte aligned");
+  if (workspace_bytes < plan->ws_bytes) {
+    ed::set_error("ed_elemental_run_batch: workspace of %zu bytes is smaller than the %zu the plan needs",
+                  workspace_bytes, plan->ws_bytes);
+    return ED_ERR_WORKSPACE;
+  }
+  return ed::elemental_run_batch(plan, nbatch, links, dir_stride, site_stride, evec_prec, evecs, blend, outs,
+                                 workspace, workspace_bytes, (cudaStream_t)stream);
+}

@@ -62,7 +62,7 @@ int scratch_address(void** addr) {
 extern "C" int ed_elemental_run_noalloc(const ed_elemental_plan* plan, const void* links, long long dir_stride,
                                         long long site_stride, int evec_prec, const void* evecs, const double* blend,
                                         void* out, void* stream) {
-  ED_CHECK_ARG(plan, "ed_elemental_run_noalloc: null plan");
+  ED_CHECK_ARG(plan && !plan->custom, "ed_elemental_run_noalloc: needs a plan from ed_elemental_plan_create");
   ED_CHECK_ARG(links && evecs && out, "ed_elemental_run_noalloc: null pointer");
   ED_CHECK_ARG(evec_prec == ED_C128 || evec_prec == ED_C64, "ed_elemental_run_noalloc: bad eigenvector precision");
   ED_CHECK_ARG(dir_stride >= 0 && site_stride >= 0, "ed_elemental_run_noalloc: negative stride");

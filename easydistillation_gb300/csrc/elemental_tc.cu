@@ -236,10 +236,11 @@ __global__ void tc_scale_kernel(TcScalars* sc, int kind) {
 
 // right-chain planes: out[q][m][k], q = re_hi, re_lo, im_hi, im_lo
 template <int KIND>
-__global__ void tc_split_kernel(const cplx<float>* __restrict__ chains, long long R, long long K,
+__global__ void tc_split_kernel(const cplx<float>* __restrict__ chains, long long R_used, long long R, long long K,
                                 const TcScalars* __restrict__ sc, void* __restrict__ planes) {
+  // rows [0, R_used) are split; the planes keep the stride of R rows
   const float s = ldexpf(1.f, sc->scale_exp);
-  const long long total2 = R * K / 2;  // pairs of consecutive k
+  const long long total2 = R_used * K / 2;  // pairs of consecutive k
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total2;
        t += (long long)gridDim.x * blockDim.x) {
     const float4 v = reinterpret_cast<const float4*>(chains)[t];  // two complex values
@@ -318,7 +319,7 @@ static size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 size_t tc_extra_workspace(const ed_elemental_plan* P) {
   const int kind = tc_kind_of(P->mode);
   if (!kind) return 0;
-  const size_t R = (size_t)P->nchain * P->Ne;
+  const size_t R = (size_t)P->nchain * P->nbatch * P->Ne;
   const size_t K = 3ull * P->V3;
   return up256(sizeof(TcScalars)) + up256((size_t)P->nmom * P->V3 * 8) + up256(4 * R * K * tc_esz(kind)) +
          up256((size_t)P->g_elems * sizeof(float4));
@@ -331,7 +332,7 @@ int tc_plan_check(ed_elemental_plan* P) {
     set_error("tensor-core elemental modes need Lx*Ly*Lz divisible by 32 (got %d)", P->V3);
     return ED_ERR_UNSUPPORTED;
   }
-  const long long rows = 4LL * P->nchain * P->Ne;
+  const long long rows = 4LL * P->nchain * P->nbatch * P->Ne;
   if (rows >= (1LL << 31) || 3LL * P->V3 >= (1LL << 31)) {
     set_error("tensor-core elemental modes: problem too large for 32-bit TMA coordinates");
     return ED_ERR_UNSUPPORTED;
@@ -356,22 +357,24 @@ static EncodeFn get_encode() {
 
 template <int KIND>
 static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
-                       cplx<double>* G, void* extra, cudaStream_t stream) {
+                       cplx<double>* G, void* extra, cudaStream_t stream, int nb) {
   constexpr int ESZ = Split<KIND>::ESZ;
   char* X = (char*)extra;
   TcScalars* sc = (TcScalars*)X;
   cplx<float>* ph32 = (cplx<float>*)(X + up256(sizeof(TcScalars)));
   void* planes = X + up256(sizeof(TcScalars)) + up256((size_t)P->nmom * P->V3 * 8);
-  float4* DF = (float4*)((char*)planes + up256(4 * (size_t)P->nchain * P->Ne * 3 * P->V3 * ESZ));
-  const long long R = (long long)P->nchain * P->Ne;
+  // rows of all chains of the plan's batch (the plane stride), and of the nb timeslices in use
+  const long long R = (long long)P->nchain * P->nbatch * P->Ne;
+  const long long R_used = (long long)P->nchain * nb * P->Ne;
   const long long K = 3LL * P->V3;
+  float4* DF = (float4*)((char*)planes + up256(4 * (size_t)R * K * ESZ));
 
   cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(TcScalars), stream);
   if (e != cudaSuccess) return cuda_status(e, "tc scalars reset");
   const int sms = num_sms();
-  tc_absmax_kernel<<<4 * sms, 256, 0, stream>>>((const float*)chains, 2 * R * K, sc);
+  tc_absmax_kernel<<<4 * sms, 256, 0, stream>>>((const float*)chains, 2 * R_used * K, sc);
   tc_scale_kernel<<<1, 32, 0, stream>>>(sc, KIND);
-  tc_split_kernel<KIND><<<8 * sms, 256, 0, stream>>>(chains, R, K, sc, planes);
+  tc_split_kernel<KIND><<<8 * sms, 256, 0, stream>>>(chains, R_used, R, K, sc, planes);
   tc_phase_kernel<<<2 * sms, 256, 0, stream>>>(phases, (long long)P->nmom * P->V3, sc, ph32);
   ED_RETURN_LAUNCH("tensor-core operand preparation");
 
@@ -394,7 +397,7 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
   }
 
   TcTable tab;
-  tab.njobs = (int)P->jobs.size();
+  tab.njobs = nb * P->jobs_per_t;
   int tiles = 0;
   for (int k = 0; k < tab.njobs; ++k) {
     const Job& j = P->jobs[k];
@@ -408,33 +411,37 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
     d.tile0 = tiles;
     tiles += d.mt * d.nt;
   }
-  static bool attr_set[4] = {false, false, false, false};
-  if (!attr_set[KIND]) {
-    e = cudaFuncSetAttribute(tc_pair_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+  // stage the producers' rows in shared memory when they fit (see tc_pair_gemm.cuh)
+  const int xr = std::min(P->Ne, (TC_BN - 1) / P->nmom + 2);
+  const bool staged = (long long)(xr + P->nmom) * (long long)((TC_ROWB / ESZ) * 8 + TC_XP_PAD) <= TC_XP_BYTES;
+  auto kern = staged ? tc_pair_gemm_kernel<KIND, true> : tc_pair_gemm_kernel<KIND, false>;
+  static bool attr_set[4][2] = {};
+  if (!attr_set[KIND][staged]) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
-    attr_set[KIND] = true;
+    attr_set[KIND][staged] = true;
   }
-  e = cudaMemsetAsync(DF, 0, (size_t)P->g_elems * sizeof(float4), stream);
+  const long long g_used = (long long)nb * P->g_per_t;
+  e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  tc_pair_gemm_kernel<KIND><<<tiles, TC_THREADS, TC_SMEM, stream>>>(amap, tab, P->Ne, P->nmom, P->V3, R, chains,
-                                                                    ph32, sc, DF);
+  kern<<<tiles, TC_THREADS, TC_SMEM, stream>>>(amap, tab, P->Ne, P->nmom, P->V3, R, chains, ph32, sc, DF, xr);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   ED_RETURN_LAUNCH("tensor-core pair GEMM");
-  tc_df_to_c128_kernel<<<4 * sms, 256, 0, stream>>>(DF, P->g_elems, G);
+  tc_df_to_c128_kernel<<<4 * sms, 256, 0, stream>>>(DF, g_used, G);
   ED_RETURN_LAUNCH("double-float to complex128");
   return ED_OK;
 }
 
 int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
-                        cplx<double>* G, void* extra, cudaStream_t stream) {
+                        cplx<double>* G, void* extra, cudaStream_t stream, int nb) {
   switch (P->tc_kind) {
     case TC_F16:
-      return launch_kind<TC_F16>(P, chains, phases, G, extra, stream);
+      return launch_kind<TC_F16>(P, chains, phases, G, extra, stream, nb);
     case TC_BF16:
-      return launch_kind<TC_BF16>(P, chains, phases, G, extra, stream);
+      return launch_kind<TC_BF16>(P, chains, phases, G, extra, stream, nb);
     case TC_TF32:
-      return launch_kind<TC_TF32>(P, chains, phases, G, extra, stream);
+      return launch_kind<TC_TF32>(P, chains, phases, G, extra, stream, nb);
     default:
       set_error("not a tensor-core mode");
       return ED_ERR_ARG;

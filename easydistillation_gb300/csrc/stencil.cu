@@ -314,3 +314,63 @@ extern "C" int ed_covariant_derivative(int in_prec, int out_prec, int Lx, int Ly
   return ed::launch_hop(in_prec, out_prec, ed::Latt{Lx, Ly, Lz}, dir, nvec, links_c128, in, out,
                         (cudaStream_t)stream);
 }
+
+// ------------------------------------------------------------ one-sided parallel transport
+// out(x) = U_d(x) in(x+d)          (sign > 0)
+// out(x) = U_d(x-d)^dag in(x-d)    (sign < 0)
+// Straight-line displacement of DisplacementElementalGenerator._D
+// (lattice/generator/displacement_elemental.py:53-71).  FP64 math, c128 storage.
+namespace ed {
+template <int VB>
+__global__ void __launch_bounds__(128) transport_kernel(Latt L, int d, int sign, int nvec,
+                                                        const cplx<double>* __restrict__ U,
+                                                        const cplx<double>* __restrict__ in,
+                                                        cplx<double>* __restrict__ out) {
+  const int V3 = L.V3();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V3) return;
+  const int x = s % L.Lx, y = (s / L.Lx) % L.Ly, z = s / (L.Lx * L.Ly);
+  int sn;  // neighbour site
+  if (d == 0)
+    sn = s - x + (sign > 0 ? wrap_inc(x, L.Lx) : wrap_dec(x, L.Lx));
+  else if (d == 1)
+    sn = s + ((sign > 0 ? wrap_inc(y, L.Ly) : wrap_dec(y, L.Ly)) - y) * L.Lx;
+  else
+    sn = s + ((sign > 0 ? wrap_inc(z, L.Lz) : wrap_dec(z, L.Lz)) - z) * L.Lx * L.Ly;
+  const int ls = sign > 0 ? s : sn;  // site of the link
+  cplx<double> u[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) u[e] = ld(U + (d * 9 + e) * V3 + ls);
+  const int v0 = blockIdx.y * VB;
+  const int v1 = min(nvec, v0 + VB);
+  for (int v = v0; v < v1; ++v) {
+    const cplx<double>* F = in + (long long)v * 3 * V3;
+    cplx<double> a[3], r[3] = {mk(0.0, 0.0), mk(0.0, 0.0), mk(0.0, 0.0)};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) a[c] = ld(F + c * V3 + sn);
+    if (sign > 0)
+      mv_add(r, u, a);
+    else
+      mvd_add(r, u, a);
+    cplx<double>* O = out + (long long)v * 3 * V3;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) O[c * V3 + s] = r[c];
+  }
+}
+}  // namespace ed
+
+extern "C" int ed_parallel_transport(int Lx, int Ly, int Lz, int dir, int sign, int nvec, const void* links_c128,
+                                     const void* in, void* out, void* stream) {
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nvec > 0, "ed_parallel_transport: sizes must be positive");
+  ED_CHECK_ARG(dir >= 0 && dir < 3 && (sign == 1 || sign == -1), "ed_parallel_transport: bad direction or sign");
+  ED_CHECK_ARG(links_c128 && in && out && in != out, "ed_parallel_transport: null or aliasing pointers");
+  constexpr int VB = 8;
+  const int V3 = Lx * Ly * Lz;
+  ED_CHECK_ARG(ed::ceil_div(nvec, VB) <= 65535, "ed_parallel_transport: too many vectors");
+  dim3 grid(ed::ceil_div(V3, 128), ed::ceil_div(nvec, VB));
+  ed::transport_kernel<VB><<<grid, 128, 0, (cudaStream_t)stream>>>(
+      ed::Latt{Lx, Ly, Lz}, dir, sign, nvec, (const ed::cplx<double>*)links_c128, (const ed::cplx<double>*)in,
+      (ed::cplx<double>*)out);
+  ED_RETURN_LAUNCH("parallel transport");
+  return ED_OK;
+}

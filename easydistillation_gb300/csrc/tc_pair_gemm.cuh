@@ -58,11 +58,21 @@ __device__ __forceinline__ void flush_sums(float (&sre)[64], float (&sim)[64], f
   }
 }
 
-template <int KIND>
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// STAGED: the left-chain rows and all phase rows of a k-block fit the staging
+// area (xr + nmom rows); the TMA warp then copies them into shared memory and
+// the producers read them there instead of from global memory.
+template <int KIND, bool STAGED>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_pair_gemm_kernel(const __grid_constant__ CUtensorMap amap, TcTable tab, int Ne, int nmom, int V3, long long R,
                         const cplx<float>* __restrict__ chains, const cplx<float>* __restrict__ phases,
-                        TcScalars* __restrict__ sc, float4* __restrict__ DF) {
+                        TcScalars* __restrict__ sc, float4* __restrict__ DF, int xr) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;  // k elements per stage
   constexpr int EPC = 16 / ESZ;      // k elements per 16-byte chunk
@@ -79,7 +89,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint64_t* accf = empty + TC_STAGES;  // 2: accumulator buffer ready to drain
   uint64_t* acce = accf + 2;           // 2: accumulator buffer drained
   uint64_t* mma_done = acce + 2;       // every issued MMA has completed
-  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
+  uint64_t* xfull = mma_done + 1;      // TC_STAGES: staged left-chain/phase rows have landed
+  uint64_t* xempty = xfull + TC_STAGES;  // TC_STAGES: the producers are done with a staging slot
+  uint32_t* tmem_slot = (uint32_t*)(xempty + TC_STAGES);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int* status = &sc->status;
@@ -98,10 +110,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int Ncols = Ne * nmom;
   const long long row0 = (long long)J.right0 * Ne + (long long)mtile * TC_BM;
   const int n0 = ntile * TC_BN;
+  // staged rows: left-chain rows i_lo .. i_lo+nX-1, then all nmom phase rows (at row xr)
+  constexpr int XROWB = KE * 8;                 // bytes of one complex64 row chunk
+  constexpr int XSTRIDE = XROWB + TC_XP_PAD;    // padded row stride in shared memory
+  const int i_lo = n0 / nmom;
+  const int nX = min(Ne, (min(n0 + TC_BN, Ncols) - 1) / nmom + 1) - i_lo;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
-      mbar_init(&full[s], 1 + TC_PWARPS);
+      mbar_init(&full[s], 1 + TC_BWARPS);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -109,6 +126,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(&acce[b], TC_DWARPS);
     }
     mbar_init(mma_done, 1);
+    for (int st = 0; st < TC_STAGES; ++st) {
+      mbar_init(&xfull[st], 1);
+      mbar_init(&xempty[st], TC_BWARPS);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -125,7 +146,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // warpgroups 0-1: TMA, MMA and B producers give registers to the drain
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(TC_REGS_LOW));
   if (warp == 0) {
-    // ===================== TMA producer for A (4 planes per stage)
+    // ===================== TMA producer of the A planes
     if (lane == 0) {
       int issued_last = -1;
       for (int kb = 0; kb < nkb; ++kb) {
@@ -137,10 +158,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           tma_load_2d(As + q * TC_BM * TC_ROWB, &amap, &full[s], kb * KE, (int)(q * R + row0));
         issued_last = kb;
       }
-      if (issued_last >= 0) {  // do not leave while our copies may still land in shared memory
-        const int s = issued_last % TC_STAGES;
-        mbar_wait(&full[s], (issued_last / TC_STAGES) & 1, status, TC_ERR_FULL, false);
+      if (issued_last >= 0)  // do not leave while our copies may still land in shared memory
+        mbar_wait(&full[issued_last % TC_STAGES], (issued_last / TC_STAGES) & 1, status, TC_ERR_FULL, false);
+    }
+  } else if (warp == 2) {
+    // ===================== staging of the producers' input rows (left chain, phases):
+    // one 1D bulk copy per row chunk, spread over the lanes.  A slot is reused
+    // as soon as the producers have read it, independently of the MMA, so the
+    // copies run up to TC_STAGES k-blocks ahead of the producers.
+    if constexpr (STAGED) {
+      int issued_last = -1;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int d = kb % TC_STAGES;
+        if (kb >= TC_STAGES && !warp_wait(&xempty[d], ((kb / TC_STAGES) + 1) & 1, status, TC_ERR_EMPTY)) break;
+        if (lane == 0) mbar_arrive_expect_tx(&xfull[d], (uint32_t)((nX + nmom) * XROWB));
+        __syncwarp();
+        uint8_t* XP = smem + d * TC_STAGE_BYTES + TC_A_BYTES + TC_B_BYTES;
+        const long long k0 = (long long)kb * KE;
+        const long long site0 = k0 % V3;
+        const cplx<float>* Xrow = chains + ((long long)J.left * Ne + i_lo) * K + k0;
+        for (int r = lane; r < nX + nmom; r += 32) {
+          if (r < nX)
+            bulk_copy_g2s(XP + r * XSTRIDE, Xrow + (long long)r * K, XROWB, &xfull[d]);
+          else
+            bulk_copy_g2s(XP + (xr + r - nX) * XSTRIDE, phases + (long long)(r - nX) * V3 + site0, XROWB,
+                          &xfull[d]);
+        }
+        issued_last = kb;
       }
+      if (issued_last >= 0)
+        warp_wait(&xfull[issued_last % TC_STAGES], (issued_last / TC_STAGES) & 1, status, TC_ERR_XFULL, false);
     }
   } else if (warp == 1) {
     // ===================== MMA issuer
@@ -194,8 +241,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ===================== B producers
     // Each thread owns up to NT fixed (row, chunk) tasks; their row pointers
     // are resolved once per tile, so the K loop only adds offsets.
-    constexpr int NT = (TC_BN * CPR + 32 * TC_PWARPS - 1) / (32 * TC_PWARPS);
-    const int pt = threadIdx.x - 64;  // 0..191
+    constexpr int NT = (TC_BN * CPR + 32 * TC_BWARPS - 1) / (32 * TC_BWARPS);
+    const int pt = threadIdx.x - 96;  // 0..159
     const float* Xb = reinterpret_cast<const float*>(chains + (long long)J.left * Ne * K);
     const float* Pb = reinterpret_cast<const float*>(phases);
     const float* xrow[NT];
@@ -204,7 +251,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     int tstate[NT];  // 0: no task, 1: zero row (beyond the tile), 2: data row
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
-      const int task = pt + t * 32 * TC_PWARPS;
+      const int task = pt + t * 32 * TC_BWARPS;
       const int row = task / CPR, c = task % CPR;
       const int n = n0 + row;
       tstate[t] = task >= TC_BN * CPR ? 0 : (n < Ncols ? 2 : 1);
@@ -213,10 +260,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       prow[t] = Pb + 2 * ((long long)p * V3 + c * EPC);
       soff[t] = row * TC_ROWB + ((c ^ ((row >> 1) & 3)) << 4);
     }
+    // shared-memory offsets of each task's staged rows (chunk c of row i - i_lo and of phase row p)
+    uint32_t xs_off[NT], ps_off[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int task = pt + t * 32 * TC_BWARPS;
+      const int row = task / CPR, c = task % CPR;
+      const int n = min(n0 + row, Ncols - 1);
+      const int i = n / nmom, p = n - i * nmom;
+      xs_off[t] = (i - i_lo) * XSTRIDE + c * EPC * 8;
+      ps_off[t] = (xr + p) * XSTRIDE + c * EPC * 8;
+    }
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % TC_STAGES;
+      if (STAGED && !warp_wait(&xfull[s], (kb / TC_STAGES) & 1, status, TC_ERR_XFULL)) break;
       if (kb >= TC_STAGES && !warp_wait(&empty[s], ((kb / TC_STAGES) + 1) & 1, status, TC_ERR_EMPTY)) break;
       uint8_t* Bs = smem + s * TC_STAGE_BYTES + TC_A_BYTES;
+      const uint8_t* XP = Bs + TC_B_BYTES;
       const long long k0 = (long long)kb * KE;
       const int site0 = (int)(k0 % V3);
 #pragma unroll
@@ -229,8 +289,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           float br[EPC], bi[EPC];
 #pragma unroll
           for (int e = 0; e < EPC; e += 2) {
-            const float4 xv = __ldg(reinterpret_cast<const float4*>(x + 2 * e));
-            const float4 pv = __ldg(reinterpret_cast<const float4*>(ph + 2 * e));
+            float4 xv, pv;
+            if constexpr (STAGED) {
+              xv = *reinterpret_cast<const float4*>(XP + xs_off[t] + e * 8);
+              pv = *reinterpret_cast<const float4*>(XP + ps_off[t] + e * 8);
+            } else {
+              xv = __ldg(reinterpret_cast<const float4*>(x + 2 * e));
+              pv = __ldg(reinterpret_cast<const float4*>(ph + 2 * e));
+            }
             br[e] = xv.x * pv.x + xv.y * pv.y;  // conj(x) * phase
             bi[e] = xv.x * pv.y - xv.y * pv.x;
             br[e + 1] = xv.z * pv.z + xv.w * pv.w;
@@ -261,7 +327,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       fence_proxy_async();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&full[s]);
+      if (lane == 0) {
+        mbar_arrive(&full[s]);
+        if constexpr (STAGED) mbar_arrive(&xempty[s]);
+      }
     }
   }
   } else {

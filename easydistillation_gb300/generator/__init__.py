@@ -1,4 +1,5 @@
-from .elemental import ElementalGenerator
+from .displacement_elemental import DisplacementElementalGenerator
 from .eigenvector import EigenvectorGenerator
+from .elemental import ElementalGenerator
 
-__all__ = ["ElementalGenerator", "EigenvectorGenerator"]
+__all__ = ["ElementalGenerator", "EigenvectorGenerator", "DisplacementElementalGenerator"]

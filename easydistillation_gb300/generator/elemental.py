@@ -82,6 +82,23 @@ def links_to_device(gauge_data, latt_size, device) -> torch.Tensor:
     return U.permute(4, 0, 1, 2, 3, 5, 6)[: ND - 1].contiguous()
 
 
+def admit_batch(latt_size, Ne, num_nabla, momentum_list, precision="fp64", device=None, max_batch=8,
+                reserve=0.1) -> int:
+    """Largest batch of timeslices whose plan workspace fits the free HBM of
+    ``device`` (keeping a ``reserve`` fraction free), between 1 and ``max_batch``."""
+    device = torch.device(device or "cuda")
+    free, _total = torch.cuda.mem_get_info(device)
+    budget = free * (1.0 - reserve)
+    best = 1
+    for b in range(1, max_batch + 1):
+        need = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, device, batch=b).workspace_bytes
+        if need <= budget:
+            best = b
+        else:
+            break
+    return best
+
+
 class ElementalGenerator:
     def __init__(
         self,
@@ -137,6 +154,9 @@ class ElementalGenerator:
             return data[t, :Ne].reshape(Ne, Lz * Ly * Lx * NC).to(self.device).contiguous()
         if self._stage is None:
             self._stage = torch.empty((Ne, Lz * Ly * Lx * NC), dtype=torch.complex128).pin_memory()
+        # the previous host->device copy out of the pinned stage must finish before it is refilled
+        if getattr(self, "_stage_event", None) is not None:
+            self._stage_event.synchronize()
         stage = self._stage.numpy()
         block = None
         try:
@@ -150,7 +170,42 @@ class ElementalGenerator:
         else:
             for e in range(Ne):
                 stage[e] = _host_array(data[t, e]).reshape(-1)
-        return self._stage.to(self.device, non_blocking=True)
+        dev = self._stage.to(self.device, non_blocking=True)
+        if getattr(self, "_stage_event", None) is None:
+            self._stage_event = torch.cuda.Event()
+        self._stage_event.record()
+        return dev
+
+    def calc_batch(self, ts, out: torch.Tensor = None, batch: int = None):
+        """Elementals of several timeslices, ``[len(ts), Nderiv, Nmom, Ne, Ne]``.
+
+        Timeslices go through batched plans of up to ``batch`` timeslices
+        (default: as many as :func:`admit_batch` allows in free HBM, at most
+        8), one pair-contraction launch per batch."""
+        if self._U is None:
+            raise RuntimeError("call load(key) before calc_batch(ts)")
+        Lx, Ly, Lz, Lt = self.latt_size
+        V3 = Lx * Ly * Lz
+        ts = list(ts)
+        if out is None:
+            out = torch.empty((len(ts), self.num_derivative, self.num_momentum, self.Ne, self.Ne),
+                              dtype=torch.complex128, device=self.device)
+        if batch is None:
+            batch = admit_batch(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list, self.precision,
+                                self.device, max_batch=min(8, len(ts)))
+        plan = getattr(self, "_bplan", None)
+        if plan is None or plan.batch != batch:
+            plan = self._bplan = ElementalPlan(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list,
+                                               self.precision, self.device, batch=batch)
+        for s0 in range(0, len(ts), batch):
+            chunk = ts[s0 : s0 + batch]
+            vecs = [self._read_vectors(t) for t in chunk]
+            links = [self._U[:, t] for t in chunk]
+            plan.run_batch(links, Lt * V3 * 9, 9, vecs, [out[s0 + k] for k in range(len(chunk))],
+                           blend=self.stocastic_coeff)
+        if self.precision != "fp64":
+            plan.check_status()
+        return out
 
     def calc(self, t: int):
         if self._U is None:

@@ -146,6 +146,28 @@ def covariant_derivative(links_soa_c128: torch.Tensor, F: torch.Tensor, latt_siz
     return out
 
 
+def parallel_transport(links_soa_c128: torch.Tensor, F: torch.Tensor, latt_size, direction: int, sign: int,
+                       out: torch.Tensor = None):
+    """``U_d(x) F(x+d)`` (sign +1) or ``U_d(x-d)^dag F(x-d)`` (sign -1) on c128
+    colour planes ``[nvec, 3, V3]`` (``displacement_elemental.py:53-71``)."""
+    Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
+    require_cuda(F, "F")
+    nvec = F.numel() // (3 * Lx * Ly * Lz)
+    out = torch.empty_like(F) if out is None else out
+    call("ed_parallel_transport", Lx, Ly, Lz, int(direction), int(sign), nvec, ptr(links_soa_c128), ptr(F), ptr(out),
+         stream_handle())
+    return out
+
+
+def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
+    """Mean over the leading axis of a contiguous complex128 stack."""
+    require_cuda(stack, "stack")
+    n = stack[0].numel()
+    out = torch.empty_like(stack[0]) if out is None else out
+    call("ed_mean_c128", stack.shape[0], n, n, ptr(stack), ptr(out), stream_handle())
+    return out
+
+
 #: elemental arithmetic modes (ED_MODE_* in include/easydist_gb300.h)
 MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3}
 
@@ -153,7 +175,8 @@ MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3}
 class ElementalPlan:
     """Owner of an ``ed_elemental_plan`` and its device workspace."""
 
-    def __init__(self, latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "fp64", device=None):
+    def __init__(self, latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "fp64", device=None,
+                 batch: int = 1):
         if mode not in MODES:
             raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES)}")
         Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
@@ -161,16 +184,21 @@ class ElementalPlan:
         self.Ne = Ne
         self.mode = mode
         self.num_nabla = num_nabla
+        self.batch = int(batch)
         self.momentum_list = [tuple(int(v) for v in p) for p in momentum_list]
         moms = [v for p in self.momentum_list for v in p]
         arr = (ctypes.c_int * len(moms))(*moms)
         handle = ctypes.c_void_p()
-        _lib.check(
-            _lib.lib().ed_elemental_plan_create(
+        if self.batch == 1:
+            rc = _lib.lib().ed_elemental_plan_create(
                 ctypes.byref(handle), Lx, Ly, Lz, Ne, num_nabla, arr, len(self.momentum_list), MODES[mode]
-            ),
-            "ed_elemental_plan_create",
-        )
+            )
+        else:
+            rc = _lib.lib().ed_elemental_plan_create_batched(
+                ctypes.byref(handle), Lx, Ly, Lz, Ne, num_nabla, arr, len(self.momentum_list), MODES[mode],
+                self.batch
+            )
+        _lib.check(rc, "ed_elemental_plan_create")
         self._h = handle
         nbytes = ctypes.c_size_t()
         call("ed_elemental_workspace_size", self._h, ctypes.byref(nbytes))
@@ -216,6 +244,27 @@ class ElementalPlan:
         )
         return out
 
+    def run_batch(self, links, dir_stride: int, site_stride: int, evecs, outs, blend: torch.Tensor = None):
+        """Several timeslices in one pass (one pair-contraction launch).
+        ``links``/``evecs``/``outs``: equal-length lists of device tensors, each
+        as in :meth:`run`; at most ``batch`` of them."""
+        nb = len(links)
+        if not (0 < nb <= self.batch) or len(evecs) != nb or len(outs) != nb:
+            raise ValueError(f"need 1..{self.batch} timeslices with matching links, evecs and outs")
+        prec = prec_of(evecs[0])
+        for v in evecs:
+            require_cuda(v, "evecs")
+            if prec_of(v) != prec:
+                raise ValueError("all eigenvector blocks must share a precision")
+        for o in outs:
+            require_cuda(o, "out")
+        ws = self.workspace()
+        P = ctypes.c_void_p * nb
+        call("ed_elemental_run_batch", self._h, nb, P(*[ptr(t) for t in links]), dir_stride, site_stride, prec,
+             P(*[ptr(t) for t in evecs]), None if blend is None else ptr(blend), P(*[ptr(t) for t in outs]),
+             ptr(ws), ws.numel(), stream_handle())
+        return outs
+
     def describe(self):
         """Pair groups of the plan: left chain and number of right chains of
         each, and whether hermiticity (p -> -p) is used."""
@@ -238,6 +287,51 @@ class ElementalPlan:
         code = ctypes.c_int()
         call("ed_elemental_status", self._h, ptr(self.workspace()), ctypes.byref(code), stream_handle())
         return code.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().ed_elemental_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+class PairPlan:
+    """Generic pair contraction on caller-built colour-plane chains
+    (``ed_pair_plan_create`` / ``ed_pair_run``):
+    ``G[p, i, r*Ne + j] = sum_k conj(X_i[k]) phase_p(k) Y_{right0+r, j}[k]``."""
+
+    def __init__(self, latt_size, Ne: int, nchain: int, momentum_list, left: int, right0: int, nright: int,
+                 mode: str = "fp64", device=None):
+        if mode not in MODES:
+            raise ValueError(f"unknown mode {mode!r}")
+        Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
+        self.Ne, self.nright, self.mode = Ne, nright, mode
+        self.momentum_list = [tuple(int(v) for v in p) for p in momentum_list]
+        moms = [v for p in self.momentum_list for v in p]
+        arr = (ctypes.c_int * len(moms))(*moms)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().ed_pair_plan_create(ctypes.byref(h), Lx, Ly, Lz, Ne, nchain, arr,
+                                                   len(self.momentum_list), MODES[mode], left, right0, nright),
+                   "ed_pair_plan_create")
+        self._h = h
+        nbytes = ctypes.c_size_t()
+        call("ed_elemental_workspace_size", self._h, ctypes.byref(nbytes))
+        self.workspace_bytes = nbytes.value
+        self.device = torch.device(device or "cuda")
+        self._ws = None
+
+    def run(self, chains: torch.Tensor, G: torch.Tensor = None):
+        require_cuda(chains, "chains")
+        if G is None:
+            G = torch.empty((len(self.momentum_list), self.Ne, self.nright * self.Ne), dtype=torch.complex128,
+                            device=chains.device)
+        if self._ws is None:
+            self._ws = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=self.device)
+        call("ed_pair_run", self._h, ptr(chains), ptr(G), ptr(self._ws), self._ws.numel(), stream_handle())
+        return G
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -100,6 +100,24 @@ int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, const void*
 int ed_covariant_derivative(int in_prec, int out_prec, int Lx, int Ly, int Lz, int dir, int nvec,
                             const void* links_c128, const void* in, void* out, void* stream);
 
+/* One 3D stout-smearing step of the spatial links, FP64, out of place.
+ * Replaces the CUDA kernel stout_smear<double> (lattice/generator/stout_smear.cu:159-245)
+ * and its numpy form (lattice/generator/eigenvector.py:123-190).
+ * U_in/U_out: [3][nt][V3][3][3] complex128 (the generators' spatial links);
+ * they must not alias. */
+int ed_stout_smear_step(int Lx, int Ly, int Lz, int nt, double rho, const void* U_in, void* U_out, void* stream);
+
+/* One-sided parallel transport of nvec colour-plane vectors (c128, FP64):
+ * sign = +1: out(x) = U_dir(x) in(x+dir); sign = -1: out(x) = U_dir(x-dir)^dag in(x-dir).
+ * Replaces one straight-line step of DisplacementElementalGenerator._D
+ * (lattice/generator/displacement_elemental.py:53-71). links: SoA c128 [27][V3]. */
+int ed_parallel_transport(int Lx, int Ly, int Lz, int dir, int sign, int nvec, const void* links_c128,
+                          const void* in, void* out, void* stream);
+
+/* out[i] = mean over k < nsrc of src[k*src_stride + i], complex128, i < n
+ * (the `.mean(0)` of displacement_elemental.py:64,71). */
+int ed_mean_c128(int nsrc, long long n, long long src_stride, const void* src, void* out, void* stream);
+
 /* ---- elementals (ElementalGenerator.calc, lattice/generator/elemental.py:290-338) */
 typedef struct ed_elemental_plan ed_elemental_plan;
 
@@ -130,6 +148,29 @@ int ed_elemental_num_pairs(const ed_elemental_plan* plan, int* npairs);
 int ed_elemental_run(const ed_elemental_plan* plan, const void* links, long long dir_stride, long long site_stride,
                      int evec_prec, const void* evecs, const double* blend, void* out, void* workspace,
                      size_t workspace_bytes, void* stream);
+
+/* Batched elementals: a plan for up to max_batch timeslices of one lattice,
+ * run with one pair-contraction launch for the whole batch (the reference
+ * calls ElementalGenerator.calc once per timeslice, elemental.py:290).
+ * links/evecs/outs are HOST arrays of nbatch device pointers (each as in
+ * ed_elemental_run); nbatch <= max_batch.  The workspace (from
+ * ed_elemental_workspace_size) grows with max_batch. */
+int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne, int num_nabla,
+                                     const int* moms, int nmom, int mode, int max_batch);
+int ed_elemental_run_batch(const ed_elemental_plan* plan, int nbatch, const void* const* links, long long dir_stride,
+                           long long site_stride, int evec_prec, const void* const* evecs, const double* blend,
+                           void* const* outs, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Generic pair contraction on caller-built chains (the GEMM stage of
+ * elemental.py:324-329 / displacement_elemental.py:94-95):
+ *   G[p][i][r*Ne + j] = sum_k conj(X_i[k]) phase_p(k) Y_{right0+r, j}[k]
+ * with X = chain `left`.  chains: colour planes [nchain][Ne][3][V3], complex128
+ * for ED_MODE_FP64, complex64 for the tensor-core modes.  The plan is queried
+ * with ed_elemental_workspace_size and released with ed_elemental_plan_destroy. */
+int ed_pair_plan_create(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne, int nchain, const int* moms,
+                        int nmom, int mode, int left, int right0, int nright);
+int ed_pair_run(const ed_elemental_plan* plan, const void* chains, void* G, void* workspace, size_t workspace_bytes,
+                void* stream);
 
 /* Size of the scratch array built into the library for
  * ed_elemental_run_noalloc (32 MiB, held on every GPU that loads it). */
