@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--mode", default="f16x3", help="elemental mode: f16x3 (headline), tf32x3, bf16x3, fp64")
     ap.add_argument("--lattice", default=None, help="Lx,Ly,Lz,Lt override (parity runs only)")
     ap.add_argument("--ne", type=int, default=NE)
+    ap.add_argument("--batch", type=int, default=4, help="timeslices per step (one pair-contraction launch)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison run")
@@ -55,12 +56,13 @@ def parse():
     return ap.parse_args()
 
 
-def launches_per_step(mode):
-    """Kernels of one elemental timeslice: links->SoA, phases, vectors->planes,
-    12 hops, the pair GEMM, the combine; tensor-core modes add complex64
-    links, absmax, scale, split, phase scaling and the double-float to
-    complex128 conversion."""
-    return 3 + 12 + 1 + 1 + (0 if mode == "fp64" else 6)
+def launches_per_step(mode, B=1):
+    """Kernels of one batched step of B timeslices: per timeslice the links
+    to SoA, vectors to planes, 12 hops and the combine; once per batch the
+    phases and the pair GEMM; tensor-core modes add absmax, scale, split,
+    phase scaling and the double-float to complex128 conversion (the FP64
+    mode packs complex128 links, the split modes complex64 ones)."""
+    return B * (1 + 1 + 12 + 1) + 1 + 1 + (0 if mode == "fp64" else 5)
 
 
 def load_peaks():
@@ -268,13 +270,17 @@ def run_ours(args, rank, world):
     gauge, evecs_host = make_inputs(latt, Ne, seed=2 + rank)
     U = links_to_device(gauge, latt, dev)  # [3, Lt, Lz, Ly, Lx, 3, 3] c128 resident
     V = [torch.from_numpy(x).to(dev) for x in evecs_host]  # resident c128 eigenvectors
-    plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev)
-    out = torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev)
+    B = args.batch
+    plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B)
+    outs = [torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev) for _ in range(B)]
+    out = outs[0]
     stream = torch.cuda.current_stream()
 
     def step(i):
-        t = (i * 7 + rank) % Lt
-        plan.run(U[:, t], Lt * V3 * 9, 9, V[i % RESIDENT_T], out)
+        # one batch of B timeslices: one pass, one pair-contraction launch
+        ts = [((i * B + k) * 7 + rank) % Lt for k in range(B)]
+        plan.run_batch([U[:, t] for t in ts], Lt * V3 * 9, 9, [V[(i * B + k) % RESIDENT_T] for k in range(B)],
+                       outs)
 
     for i in range(args.warmup):
         step(i)
@@ -303,11 +309,11 @@ def run_ours(args, rank, world):
     ms = start.elapsed_time(end)
     ms = max_over_ranks(ms, dev if world > 1 else None)
     ms_per_step = ms / args.steps
-    value = world * args.steps / (ms / 1e3)
+    value = world * args.steps * B / (ms / 1e3)
 
     # roofline of the pair-contraction kernel
     kms = statistics.mean(a.elapsed_time(b) for a, b in kev)
-    units = plan.num_pairs * NMOM  # (pair, momentum) contractions per launch
+    units = plan.num_pairs * NMOM * B  # (pair, momentum) contractions per launch (B timeslices)
     alg_flop = units * 8.0 * Ne * Ne * 3 * V3
     peaks = load_peaks()
     if args.mode == "fp64":
@@ -317,8 +323,9 @@ def run_ours(args, rank, world):
         pk, pk_src = peaks.get("bf16_tflops_sustained"), "measured bf16 sustained"
         if pk is None:
             pk, pk_src = 1700.0, "fallback"
-        tiles_m = sum(-(-(j * Ne) // 128) for j in plan_group_rights(plan))
-        mma_flop = tiles_m * (-(-(Ne * NMOM) // 256)) * 128 * 256 * 3 * V3 * 12 * 2.0
+        # 128 x 128 tiles; 12 MMAs of 128x128x(K) per complex multiply-add
+        tiles_m = sum(-(-(j * Ne) // 128) for j in plan_group_rights(plan)[: len(plan_group_rights(plan)) // B])
+        mma_flop = B * tiles_m * (-(-(Ne * NMOM) // 128)) * 128 * 128 * 3 * V3 * 12 * 2.0
         roofline = {"bound": "tensor", "achieved": alg_flop / kms / 1e9, "peak": pk, "unit": "TFLOP/s",
                     "frac": alg_flop / kms / 1e9 / pk, "traffic": None, "peak_source": pk_src,
                     "kernel": f"tc_pair_gemm_kernel<{args.mode}>", "kernel_ms": kms,
@@ -370,17 +377,20 @@ def run_ours(args, rank, world):
         ev = np.stack([x.reshape(Ne, Lz, Ly, Lx, 3) for x in evecs_host])  # [RESIDENT_T, Ne, ...]
         gen = ElementalGenerator(latt, _Src(gauge), _Src(ev, Ne), NUM_NABLA, moms, precision=args.mode, device=dev)
         gen.load("bench")
-        host_out = torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128).pin_memory()
+        host_out = torch.empty((B, 13, NMOM, Ne, Ne), dtype=torch.complex128).pin_memory()
+        dev_out = torch.empty((B, 13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev)
+        batch_ts = [[(i * B + k) % RESIDENT_T for k in range(B)] for i in range(max(args.steps, 2))]
         for i in range(min(args.warmup, 2)):
-            host_out.copy_(gen.calc(i % RESIDENT_T))
+            host_out.copy_(gen.calc_batch(batch_ts[i], out=dev_out, batch=B))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for i in range(args.steps):
-            host_out.copy_(gen.calc(i % RESIDENT_T))
+            host_out.copy_(gen.calc_batch(batch_ts[i], out=dev_out, batch=B))
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        e2e = {"value": world * args.steps / dt, "unit": "timeslices/s",
-               "h2d_bytes_per_step": Ne * V3 * 3 * 16, "d2h_bytes_per_step": int(host_out.numel() * 16)}
+        e2e = {"value": world * args.steps * B / dt, "unit": "timeslices/s",
+               "h2d_bytes_per_step": B * Ne * V3 * 3 * 16, "d2h_bytes_per_step": int(host_out.numel() * 16),
+               "api": "ElementalGenerator.calc_batch (host eigenvectors in, host elementals out)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -393,10 +403,12 @@ def run_ours(args, rank, world):
             "metric": METRIC, "value": value, "unit": "timeslices/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128" if args.mode == "fp64" else args.mode, "data": "synthetic",
-            "config": {"workload": f"elemental {Lx}^3x{Lt}, Ne={Ne}, 13 ops x {NMOM} momenta, mode={args.mode}",
+            "config": {"workload": f"elemental {Lx}^3x{Lt}, Ne={Ne}, 13 ops x {NMOM} momenta, mode={args.mode}, "
+                                   f"{B} timeslices per step",
+                       "timeslices_per_step": B,
                        "pairs_per_momentum": plan.num_pairs, "l2": "inputs larger than L2 (rotating timeslices)",
                        "parallelism": f"replicas x{world}"},
-            "gpu_launches": args.steps * launches_per_step(args.mode),
+            "gpu_launches": args.steps * launches_per_step(args.mode, B),
             "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "fp64_gpu": fp64,
             "stencil_roofline": stencil,
         }

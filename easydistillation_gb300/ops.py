@@ -269,8 +269,8 @@ class ElementalPlan:
         """Pair groups of the plan: left chain and number of right chains of
         each, and whether hermiticity (p -> -p) is used."""
         n, herm = ctypes.c_int(), ctypes.c_int()
-        left = (ctypes.c_int * 32)()
-        nright = (ctypes.c_int * 32)()
+        left = (ctypes.c_int * 64)()  # kMaxJobs
+        nright = (ctypes.c_int * 64)()
         call("ed_elemental_describe", self._h, ctypes.byref(n), left, nright, ctypes.byref(herm))
         return {"left": list(left[: n.value]), "nright": list(nright[: n.value]), "herm": bool(herm.value)}
 
