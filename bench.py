@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison run")
     ap.add_argument("--no-stencil", action="store_true", help="skip the Laplacian bandwidth measurement")
+    ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
+    ap.add_argument("--eigen-batch", type=int, default=8)
+    ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--eigen-cpu", action="store_true", help="also time the oracle's scipy eigensolve (slow)")
     return ap.parse_args()
 
 
@@ -415,8 +419,60 @@ def run_ours(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_eigen(args):
+    """Secondary measurement (``--eigen``): EigenvectorGenerator.calc_batch on
+    ``--eigen-batch`` timeslices at ``--lattice`` (default 24^3 x 64, Ne from
+    ``--ne``, tol 1e-10), FP64 or FP32 stencil; the oracle's scipy/ARPACK
+    eigensolve of one timeslice on the host cores with ``--eigen-cpu``."""
+    import torch
+
+    from easydistillation_gb300 import EigenvectorGenerator
+
+    latt = [int(v) for v in args.lattice.split(",")] if args.lattice else [24, 24, 24, 64]
+    Ne = args.ne
+    gauge, _ = make_inputs(latt, 1, distinct_t=max(args.eigen_batch, 1))
+
+    class _G:
+        def __init__(self, a):
+            self.a = a
+            self.file = "mem"
+
+        def __getitem__(self, k):
+            return self.a[k]
+
+    class _Src:
+        def load(self, key):
+            return _G(gauge)
+
+    gen = EigenvectorGenerator(latt, _Src(), Ne, 1e-10, stencil_precision=args.eigen_precision)
+    gen.load("bench")
+    ts = list(range(args.eigen_batch))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    evecs, evals = gen.calc_batch(ts)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    line = {"metric": f"eigensolve timeslices/s {latt[0]}^3 Ne={Ne} tol 1e-10", "value": len(ts) / dt,
+            "unit": "timeslices/s", "seconds": dt, "batch": len(ts), "stencil_precision": args.eigen_precision,
+            "stats": gen.last_stats, "lowest_evals_t0": [float(v) for v in evals[0, :3].cpu()]}
+    if args.eigen_cpu:
+        from oracle import restatement as R
+
+        U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
+        t1 = time.perf_counter()
+        _, ev = R.eigensolve(U, latt, Ne, 1e-10)
+        cdt = time.perf_counter() - t1
+        line["cpu_baseline"] = {"value": 1.0 / cdt, "unit": "timeslices/s", "kind": "port",
+                                "cores": len(os.sched_getaffinity(0)), "sample": "one timeslice, scipy eigsh",
+                                "max_eval_diff": float(abs(ev - evals[0].cpu().numpy()).max())}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.eigen:
+        run_eigen(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -16,6 +16,18 @@ The arithmetic runs in ``libeasydist_gb300.so`` (C ABI:
 
 from .generator import DisplacementElementalGenerator, EigenvectorGenerator, ElementalGenerator
 from .insertion import MomentumPhase, derivative, mom_dict_to_list, num_derivative
+from .preset import (
+    EigenvectorHostmem,
+    EigenvectorNpy,
+    EigenvectorTimeSlice,
+    ElementalBinary,
+    ElementalNpy,
+    GaugeFieldBinary,
+    GaugeFieldIldg,
+    GaugeFieldTimeSlice,
+    PerambulatorBinary,
+    PerambulatorNpy,
+)
 
 NC, NS, ND = 3, 4, 4
 
@@ -27,6 +39,16 @@ __all__ = [
     "derivative",
     "mom_dict_to_list",
     "num_derivative",
+    "GaugeFieldIldg",
+    "GaugeFieldBinary",
+    "GaugeFieldTimeSlice",
+    "EigenvectorNpy",
+    "EigenvectorTimeSlice",
+    "EigenvectorHostmem",
+    "ElementalNpy",
+    "ElementalBinary",
+    "PerambulatorNpy",
+    "PerambulatorBinary",
     "NC",
     "NS",
     "ND",

@@ -60,6 +60,7 @@ _SIGNATURES = {
         [_vp, _i, _c.POINTER(_vp), _ll, _ll, _i, _c.POINTER(_vp), _vp, _c.POINTER(_vp), _vp, _c.c_size_t, _vp],
         _i,
     ),
+    "ed_link_grad": ([_i, _i, _i, _i, _i, _c.c_double, _c.c_double, _vp, _vp, _vp, _vp], _i),
     "ed_parallel_transport": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
     "ed_mean_c128": ([_i, _ll, _ll, _vp, _vp, _vp], _i),
     "ed_pair_plan_create": (

@@ -97,8 +97,16 @@ class EigenvectorGenerator:
 
         return mv
 
-    def calc_batch(self, ts: Sequence[int], apply_renorm_phase: bool = True):
-        """Eigenpairs of several timeslices solved in lock step."""
+    def calc_batch(self, ts: Sequence[int], apply_renorm_phase: bool = True, polynomial_degree: int = 0,
+                   lambda_cut: float = 0.0):
+        """Eigenpairs of several timeslices solved in lock step.
+
+        With ``polynomial_degree > 0`` and ``lambda_cut > 0`` (the reference's
+        Chebyshev acceleration, ``eigenvector.py:295-299``), the Lanczos
+        iteration runs on ``-T_deg((2L - (12 + cut)) / (12 - cut))``, which
+        maps the unwanted part of the spectrum [cut, 12] into [-1, 1] and
+        makes the wanted low modes dominant; the eigenpairs of ``L`` then
+        come from an FP64 Rayleigh-Ritz step on the converged vectors."""
         if self._U is None:
             raise RuntimeError("call load(key) before calc(t)")
         Lx, Ly, Lz, Lt = self.latt_size
@@ -106,7 +114,16 @@ class EigenvectorGenerator:
         n = NC * V3
         ts = list(ts)
         B = len(ts)
-        if self.stencil_precision == "fp32":
+        if polynomial_degree > 0 and lambda_cut > 0:
+            mv = self._matvec(ts, torch.complex64 if self.stencil_precision == "fp32" else torch.complex128)
+            # below the cut T_deg has the sign (-1)^deg: negate so the wanted modes are the smallest
+            cheb = LZ.chebyshev_operator(mv, polynomial_degree, lambda_cut, 12.0, negate=polynomial_degree % 2 == 0)
+            res = LZ.trlanczos(cheb, B, n,
+                               self.Ne, max(self.tol, 1e-12), device=self.device)
+            lam, X, resid = LZ.rayleigh_ritz(self._matvec(ts, torch.complex128), res.evecs)
+            res.evals, res.evecs, res.residuals = lam, X, resid
+            res.matvecs = res.matvecs * polynomial_degree + self.Ne
+        elif self.stencil_precision == "fp32":
             r32 = LZ.trlanczos(self._matvec(ts, torch.complex64), B, n, self.Ne, max(self.tol, 1e-6),
                                device=self.device)
             v0 = r32.evecs.sum(dim=1)
@@ -123,5 +140,5 @@ class EigenvectorGenerator:
         return out.reshape(B, self.Ne, Lz, Ly, Lx, NC), evals
 
     def calc(self, t: int, apply_renorm_phase: bool = True, polynomial_degree: int = 0, lambda_cut: float = 0.0):
-        evecs, evals = self.calc_batch([t], apply_renorm_phase)
+        evecs, evals = self.calc_batch([t], apply_renorm_phase, polynomial_degree, lambda_cut)
         return evecs[0], evals[0]

@@ -123,6 +123,24 @@ def trlanczos(
                          (beta_last.unsqueeze(1) * Y[:, ncv - 1, :nev]).abs())
 
 
+def chebyshev_operator(matvec, degree: int, a: float, b: float, negate: bool = False):
+    """``X -> T_degree((2 A - (b + a)) / (b - a)) X`` by the three-term
+    recurrence (``degree`` applications of ``matvec``); ``negate`` flips the
+    sign so that the smallest-eigenvalue Lanczos finds the modes below ``a``."""
+    if degree < 1 or not (b > a):
+        raise ValueError("need degree >= 1 and b > a")
+    alpha, beta = 2.0 / (b - a), -(b + a) / (b - a)
+
+    def op(X):
+        T0 = X
+        T1 = alpha * matvec(X) + beta * X
+        for _ in range(degree - 1):
+            T0, T1 = T1, 2.0 * (alpha * matvec(T1) + beta * T1) - T0
+        return -T1 if negate else T1
+
+    return op
+
+
 def rayleigh_ritz(matvec, X: torch.Tensor):
     """FP64 Rayleigh-Ritz on the span of X [B, k, n] (orthonormalised first).
     Returns (evals [B, k], evecs [B, k, n], residual norms [B, k])."""

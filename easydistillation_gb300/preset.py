@@ -1,0 +1,307 @@
+"""File readers with the reference's preset classes and on-disk layouts.
+
+Mirrors ``lattice/preset.py`` and ``lattice/filedata/*.py``: each preset is
+constructed as in the reference (``prefix``, ``suffix``, ``shape`` and, for
+eigenvectors/elementals/perambulators, ``totNe``) and ``load(key)`` returns a
+file-data object that is indexed like a numpy array (``[:]``, ``[t]``,
+``[t, e]``, slices).  Reads are memory-mapped; the result is a host numpy
+array with the reference's dtype conversion (ILDG data up-cast to complex128,
+``lattice/filedata/ildg.py:70``; QDP lazy-disk-map data down-cast to
+complex64, ``timeslice.py:96``).  ``to_device(key, device)`` uploads an index
+through pinned memory in one copy.
+
+Formats:
+* ILDG / LIME (``ildg.py:82-96``): records of an 8-byte magic/version word, a
+  big-endian 8-byte length, a 128-byte type string and the 8-byte padded
+  payload; ``ildg-format`` holds the XML (lx, ly, lz, lt, precision) and
+  ``ildg-binary-data`` the big-endian field.
+* ``.npy`` (``ndarray.py:17-47``): numpy header, C order.
+* raw binary (``binary.py:23-66``).
+* QDP LazyDiskMapObjFile (``timeslice.py:102-129``): magic string, version,
+  XML, a trailer with key tuples and offsets.
+"""
+
+from __future__ import annotations
+
+import mmap
+import re
+import struct
+import xml.etree.ElementTree as ET
+from time import time
+from typing import Dict, List, Tuple
+
+import numpy as np
+import torch
+
+
+class FileMetaData:
+    def __init__(self, shape: List[int], dtype: str = "<c16", extra=None):
+        self.shape = shape
+        self.dtype = dtype
+        self.extra = extra
+
+
+class _Data:
+    """Common indexing and timing of the file-data objects."""
+
+    file = None
+
+    def _array(self):  # pragma: no cover - implemented by subclasses
+        raise NotImplementedError
+
+    def _convert(self, a):
+        return a
+
+    def __getitem__(self, key):
+        s = time()
+        arr = self._array()
+        ret = self._convert(np.array(arr[key], copy=True))
+        self.time_in_sec += time() - s
+        self.size_in_byte += ret.nbytes
+        self.timeInSec, self.sizeInByte = self.time_in_sec, self.size_in_byte
+        return ret
+
+    def to_device(self, key, device=None, dtype=None):
+        a = self[key]
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        if dtype is not None:
+            t = t.to(dtype)
+        return t.pin_memory().to(device or "cuda", non_blocking=True)
+
+
+class NdarrayFileData(_Data):
+    def __init__(self, file: str, elem: FileMetaData):
+        self.file = file
+        self.shape = elem.shape if elem else None
+        self.dtype = elem.dtype if elem else None
+        self.time_in_sec = self.timeInSec = 0.0
+        self.size_in_byte = self.sizeInByte = 0
+
+    def _array(self):
+        return np.load(self.file, mmap_mode="r")
+
+
+class BinaryFileData(_Data):
+    def __init__(self, file: str, elem: FileMetaData):
+        self.file = file
+        self.shape = elem.shape
+        self.dtype = elem.dtype
+        self.time_in_sec = self.timeInSec = 0.0
+        self.size_in_byte = self.sizeInByte = 0
+
+    def _array(self):
+        return np.memmap(self.file, dtype=self.dtype, mode="r", shape=tuple(self.shape))
+
+
+def read_lime_records(path: str) -> Dict[str, Tuple[int, int]]:
+    """type -> (payload offset, padded length) of every LIME record."""
+    out = {}
+    with open(path, "rb") as f:
+        while True:
+            head = f.read(8)
+            if head == b"" or head == b"\x0A":
+                break
+            if not head.startswith(b"\x45\x67\x89\xAB\x00\x01"):
+                raise ValueError(f"{path}: not a LIME record at offset {f.tell() - 8}")
+            length = (struct.unpack(">Q", f.read(8))[0] + 7) // 8 * 8
+            rtype = f.read(128).strip(b"\x00").decode("utf-8")
+            out[rtype] = (f.tell(), length)
+            f.seek(length, 1)
+    return out
+
+
+class IldgFileData(_Data):
+    def __init__(self, file: str, elem: FileMetaData):
+        self.file = file
+        self.shape = elem.shape
+        self.dtype = elem.dtype
+        recs = read_lime_records(file)
+        self.offset, nbytes = recs["ildg-binary-data"]
+        fpos, flen = recs["ildg-format"]
+        with open(file, "rb") as f:
+            f.seek(fpos)
+            root = ET.fromstring(f.read(flen).strip(b"\x00").decode("utf-8"))
+        tag = re.match(r"\{.*\}", root.tag).group(0) if root.tag.startswith("{") else ""
+        self.latt_size = [int(root.find(f"{tag}{k}").text) for k in ("lx", "ly", "lz", "lt")]
+        self.bytes = int(re.match(r"^[<>=]?[iufc](?P<bytes>\d+)$", elem.dtype).group("bytes"))
+        if self.bytes != int(root.find(f"{tag}precision").text) // 8 * 2:
+            raise ValueError("ILDG precision does not match the preset dtype")
+        if int(np.prod(self.shape)) * self.bytes != nbytes:
+            raise ValueError("ILDG payload size does not match the preset shape")
+        self.time_in_sec = self.timeInSec = 0.0
+        self.size_in_byte = self.sizeInByte = 0
+
+    def _array(self):
+        return np.memmap(self.file, dtype=self.dtype, mode="r", offset=self.offset, shape=tuple(self.shape))
+
+    def _convert(self, a):
+        return a.astype("<c16")
+
+
+class QDPLazyDiskMapObjFileData(_Data):
+    def __init__(self, file: str, elem: FileMetaData):
+        self.file = file
+        self.extra = elem.extra
+        self.shape = elem.shape[elem.extra :]
+        self.dtype = elem.dtype
+        self.extraShape = elem.shape[: elem.extra]
+        with open(file, "rb") as f:
+            def rstr():
+                n = struct.unpack(">i", f.read(4))[0]
+                return f.read(n).decode("utf-8")
+
+            if rstr() != "XXXXQDPLazyDiskMapObjFileXXXX":
+                raise ValueError(f"{file}: not a QDP LazyDiskMapObjFile")
+            struct.unpack(">i", f.read(4))
+            ET.fromstring(rstr())
+            f.seek(struct.unpack(">qq", f.read(16))[1])
+            nrec = struct.unpack(">I", f.read(4))[0]
+            self.offsets = {}
+            for _ in range(nrec):
+                n = struct.unpack(">i", f.read(4))[0] // 4
+                key = struct.unpack(">" + "i" * n, f.read(4 * n))
+                self.offsets[key] = struct.unpack(">qq", f.read(16))[1]
+        self.time_in_sec = self.timeInSec = 0.0
+        self.size_in_byte = self.sizeInByte = 0
+
+    def __getitem__(self, key):
+        if isinstance(key, int):
+            key = (key,)
+        head = tuple(key[: self.extra])
+        if head not in self.offsets:
+            raise IndexError(f"index {key} is out of bounds for axes")
+        s = time()
+        arr = np.memmap(self.file, dtype=self.dtype, mode="r", offset=self.offsets[head], shape=tuple(self.shape))
+        ret = np.array(arr[tuple(key[self.extra :])], copy=True).astype("<c8")
+        self.time_in_sec += time() - s
+        self.size_in_byte += ret.nbytes
+        self.timeInSec, self.sizeInByte = self.time_in_sec, self.size_in_byte
+        return ret
+
+
+class _Preset:
+    _data_cls = None
+
+    def __init__(self, prefix, suffix, elem):
+        self.prefix, self.suffix, self.elem = prefix, suffix, elem
+        self._file, self.data = None, None
+
+    def load(self, key: str):
+        name = f"{self.prefix}{key}{self.suffix}"
+        if self._file != name:
+            self._file = name
+            self.data = self._data_cls(name, self.elem)
+        return self.data
+
+
+class GaugeFieldIldg(_Preset):
+    _data_cls = IldgFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 16**3, 4, 3, 3]):
+        super().__init__(prefix, ".lime" if suffix is None else suffix, FileMetaData(shape, ">c16", 0))
+
+
+class GaugeFieldBinary(_Preset):
+    _data_cls = BinaryFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 16**3, 4, 3, 3], dtype: str = "<f8"):
+        super().__init__(prefix, ".dat" if suffix is None else suffix, FileMetaData(shape, dtype, 0))
+
+
+class GaugeFieldTimeSlice(_Preset):
+    _data_cls = QDPLazyDiskMapObjFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 4, 16**3, 3, 3]):
+        super().__init__(prefix, ".stout.n20.f0.12.mod" if suffix is None else suffix, FileMetaData(shape, ">c16", 2))
+
+
+class EigenvectorNpy(_Preset):
+    _data_cls = NdarrayFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[70, 128, 16**3, 3], totNe: int = 70):
+        super().__init__(prefix, ".lime.npy" if suffix is None else suffix, FileMetaData(shape, "<c16", 2))
+        self.Ne = totNe
+
+
+class EigenvectorTimeSlice(_Preset):
+    _data_cls = QDPLazyDiskMapObjFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 70, 16**3, 3], totNe: int = 70):
+        super().__init__(prefix, ".stout.n20.f0.12.laplace_eigs.3d.mod" if suffix is None else suffix,
+                         FileMetaData(shape, ">c8", 2))
+        self.Ne = totNe
+
+
+class EigenvectorHostmem:
+    """Eigenvectors already in host memory (``lattice/preset.py:77-89``)."""
+
+    def __init__(self, host_ndarray, shape=[70, 128, 16**3, 3], totNe: int = 70):
+        if list(host_ndarray.shape) != list(shape):
+            raise ValueError(
+                f"Please check that host_ndarray shape {host_ndarray.shape} does not match expected shape "
+                f"(totNe, Lt, Lz * Ly * Lx, Nc) = {shape}"
+            )
+        self.Ne = totNe
+        self.data = host_ndarray
+
+    def load(self, key: str = None):
+        return self.data
+
+
+class ElementalNpy(_Preset):
+    _data_cls = NdarrayFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[4, 123, 128, 70, 70], totNe: int = 70):
+        super().__init__(prefix, ".stout.n20.f0.12.nev70.meson.npy" if suffix is None else suffix,
+                         FileMetaData(shape, "<c8", 0))
+        self.Ne = totNe
+
+
+class ElementalBinary(_Preset):
+    _data_cls = BinaryFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[40, 27, 128, 70, 70], totNe: int = 70):
+        super().__init__(prefix, ".stout.n20.f0.12.nev70.meson" if suffix is None else suffix,
+                         FileMetaData(shape, "<c16", 0))
+        self.Ne = totNe
+
+
+class PerambulatorNpy(_Preset):
+    _data_cls = NdarrayFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 128, 4, 4, 70, 70], totNe: int = 70):
+        super().__init__(prefix, ".stout.n20.f0.12.nev70.peram" if suffix is None else suffix,
+                         FileMetaData(shape, "<c8", 0))
+        self.Ne = totNe
+
+
+class PerambulatorBinary(_Preset):
+    _data_cls = BinaryFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 128, 4, 4, 70, 70], totNe: int = 70):
+        super().__init__(prefix, ".stout.n20.f0.12.nev70.peram" if suffix is None else suffix,
+                         FileMetaData(shape, "<c16", 0))
+        self.Ne = totNe
+
+
+def write_ildg(path: str, gauge: np.ndarray, latt_size: List[int]):
+    """Write a field ``[Lt, Lz, Ly, Lx, 4, 3, 3]`` as an ILDG/LIME file
+    (``ildg-format`` XML record + big-endian complex128 ``ildg-binary-data``)."""
+    Lx, Ly, Lz, Lt = latt_size
+    xml = (
+        '<?xml version="1.0" encoding="UTF-8"?><ildgFormat xmlns="http://www.lqcd.org/ildg">'
+        f"<version>1.0</version><field>su3gauge</field><precision>64</precision>"
+        f"<lx>{Lx}</lx><ly>{Ly}</ly><lz>{Lz}</lz><lt>{Lt}</lt></ildgFormat>"
+    ).encode()
+    payload = np.ascontiguousarray(gauge).astype(">c16").tobytes()
+
+    def record(rtype: str, data: bytes, first: bool, last: bool) -> bytes:
+        flags = (0x8000 if first else 0) | (0x4000 if last else 0)
+        head = b"\x45\x67\x89\xab" + struct.pack(">H", 1) + struct.pack(">H", flags)
+        head += struct.pack(">Q", len(data)) + rtype.encode().ljust(128, b"\x00")
+        pad = (-len(data)) % 8
+        return head + data + b"\x00" * pad
+
+    with open(path, "wb") as f:
+        f.write(record("ildg-format", xml, True, False))
+        f.write(record("ildg-binary-data", payload, False, True))

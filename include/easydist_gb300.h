@@ -118,6 +118,17 @@ int ed_parallel_transport(int Lx, int Ly, int Lz, int dir, int sign, int nvec, c
  * (the `.mean(0)` of displacement_elemental.py:64,71). */
 int ed_mean_c128(int nsrc, long long n, long long src_stride, const void* src, void* out, void* stream);
 
+/* Adjoint (link gradient) of a stencil direction, accumulated into
+ * grad_links (SoA c128 [27][V3], direction `dir` only):
+ *   grad U_dir(x) += sum_v alpha * wbar_v(x) f_v(x+dir)^dag + beta * f_v(x) wbar_v(x+dir)^dag
+ * where wbar is the adjoint seed of the stencil output and f its input
+ * (colour planes, c128, nvec vectors).  (alpha, beta) = (1, -1) gives the
+ * covariant-derivative hop of elemental.py:282-287, (-1, -1) the Laplacian of
+ * eigenvector.py:11-26; gradient convention dL = Re sum conj(grad) dU.
+ * No counterpart in the reference (it has no gradients). */
+int ed_link_grad(int Lx, int Ly, int Lz, int dir, int nvec, double alpha, double beta, const void* wbar,
+                 const void* f, void* grad_links, void* stream);
+
 /* ---- elementals (ElementalGenerator.calc, lattice/generator/elemental.py:290-338) */
 typedef struct ed_elemental_plan ed_elemental_plan;
 

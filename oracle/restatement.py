@@ -445,3 +445,49 @@ def stout_smear(U_spatial: np.ndarray, nstep: int, rho: float) -> np.ndarray:
         f = f2[..., None, None] * Q_sq + f1[..., None, None] * Q + f0[..., None, None] * eye
         U = f @ U
     return U
+
+
+# ---------------------------------------------------------------------------
+# correlators
+# ---------------------------------------------------------------------------
+
+_GAMMA_BASIS = {
+    0: [[0, 0, 0, 1j], [0, 0, 1j, 0], [0, -1j, 0, 0], [-1j, 0, 0, 0]],
+    1: [[0, 0, 0, -1], [0, 0, 1, 0], [0, 1, 0, 0], [-1, 0, 0, 0]],
+    2: [[0, 0, 1j, 0], [0, 0, 0, -1j], [-1j, 0, 0, 0], [0, 1j, 0, 0]],
+    3: [[0, 0, 1, 0], [0, 0, 0, 1], [1, 0, 0, 0], [0, 1, 0, 0]],
+}
+
+
+def gamma(n: int) -> np.ndarray:
+    """``gamma(n) = g0^(n&1) g1^(n&2) g2^(n&4) g3^(n&8)``
+    (``lattice/insertion/gamma.py:20-68,101-110``)."""
+    m = np.eye(4, dtype=np.complex128)
+    for bit in range(4):
+        if n & (1 << bit):
+            m = m @ np.array(_GAMMA_BASIS[bit], dtype=np.complex128)
+    return m
+
+
+def twopoint(phis, perambulator, timeslices, Lt, usedNe=None, is_sum_over_source_t=True):
+    """Meson two-point function (``lattice/correlator/one_particle.py:12-77``)
+    with the operator data already assembled: ``phis`` is a list of
+    ``(gammas [X,4,4], elementals [X, Lt, Ne, Ne])``; ``perambulator[t_src]`` is
+    ``[Lt, 4, 4, Ne, Ne]``."""
+    Nop = len(phis)
+    ts = list(timeslices)
+    ret = np.zeros((Nop, len(ts), Lt), np.complex128)
+    for it, t_src in enumerate(ts):
+        tau = np.asarray(perambulator[t_src])
+        if usedNe is not None:
+            tau = tau[..., :usedNe, :usedNe]
+        tau_bw = np.einsum("ii,tjiba,jj->tijab", gamma(15), tau.conj(), gamma(15))
+        for idx, (g, e) in enumerate(phis):
+            if usedNe is not None:
+                e = e[..., :usedNe, :usedNe]
+            gamma_src = np.einsum("ij,xkj,kl->xil", gamma(8), g.conj(), gamma(8))
+            ret[idx, it] = np.einsum(
+                "tijab,xjk,xtbc,tklcd,yli,yad->t", tau_bw, g, np.roll(e, -t_src, 1), tau, gamma_src,
+                e[:, t_src].conj(), optimize=True,
+            )
+    return -ret.mean(1) if is_sum_over_source_t else -ret

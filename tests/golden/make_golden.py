@@ -162,5 +162,23 @@ def main(ref_root: str):
     print("golden fixtures written to", HERE)
 
 
+def make_ildg_fixture(ref_root: str):
+    """A small ILDG file written by this package's writer and read back by the
+    reference's own reader (lattice/filedata/ildg.py), pinning the format."""
+    lattice = import_reference(ref_root)
+    from easydistillation_gb300.preset import write_ildg
+
+    latt = [2, 4, 2, 2]
+    g = synthetic_gauge(latt, 0.3, 51)
+    path = os.path.join(HERE, "small.lime")
+    write_ildg(path, g, latt)
+    Lx, Ly, Lz, Lt = latt
+    ref = lattice.GaugeFieldIldg(os.path.join(HERE, "small"), ".lime", [Lt, Lz, Ly, Lx, 4, 3, 3]).load("")
+    np.savez_compressed(os.path.join(HERE, "ildg_small.npz"), latt=latt, gauge=g, ref_read=ref[:],
+                        ref_slice=ref[1, :, 0])
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    main(root)
+    make_ildg_fixture(root)

@@ -54,3 +54,20 @@ def test_eigen_batched_timeslices_match_scipy():
     for t in range(3):
         rv, re = R.eigensolve(U[:, t], latt, Ne, 1e-10)
         _check(evecs[t].cpu().numpy(), evals[t].cpu().numpy(), rv, re, U[:, t], latt, Ne)
+
+
+@pytest.mark.parametrize("deg", [10, 7])
+def test_eigen_chebyshev_acceleration(deg):
+    """calc(t, True, polynomial_degree, lambda_cut) as the reference's test
+    calls it (tests/test_eigenvector.py:54): cut at 1.1 x the largest wanted
+    eigenvalue; same eigenpairs as the unaccelerated solve."""
+    from easydistillation_gb300 import EigenvectorGenerator
+
+    g = golden("eigen_443.npz")
+    latt = [int(v) for v in g["latt"]]
+    Ne = int(g["Ne"])
+    gen = EigenvectorGenerator(latt, MemGauge(g["gauge"]), Ne, 1e-10)
+    gen.load("mem")
+    evecs, evals = gen.calc(0, True, deg, float(g["evals0"][-1]) * 1.1)
+    U = g["gauge"].transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
+    _check(evecs.cpu().numpy(), evals.cpu().numpy(), g["evecs0"], g["evals0"], U, latt, Ne)

@@ -1,0 +1,81 @@
+"""File readers with the reference's preset classes (CPU): an ILDG file read
+exactly as the reference's own reader read it (fixture), and .npy / raw
+binary / QDP lazy-disk-map round trips."""
+
+import os
+import struct
+
+import numpy as np
+
+from tests.conftest import GOLDEN, golden
+
+
+def test_ildg_matches_reference_reader():
+    from easydistillation_gb300.preset import GaugeFieldIldg
+
+    g = golden("ildg_small.npz")
+    Lx, Ly, Lz, Lt = [int(v) for v in g["latt"]]
+    data = GaugeFieldIldg(os.path.join(GOLDEN, "small"), ".lime", [Lt, Lz, Ly, Lx, 4, 3, 3]).load("")
+    np.testing.assert_array_equal(data[:], g["ref_read"])
+    np.testing.assert_array_equal(data[1, :, 0], g["ref_slice"])
+    assert data[:].dtype == np.complex128 and data.latt_size == [Lx, Ly, Lz, Lt]
+
+
+def test_npy_and_binary_presets(tmp_path):
+    from easydistillation_gb300.preset import ElementalBinary, EigenvectorNpy, GaugeFieldBinary, PerambulatorNpy
+
+    rng = np.random.default_rng(0)
+    ev = (rng.standard_normal((3, 5, 8, 3)) + 1j * rng.standard_normal((3, 5, 8, 3))).astype(np.complex128)
+    np.save(tmp_path / "cfgA.ev.npy", ev)
+    E = EigenvectorNpy(str(tmp_path) + "/", ".ev.npy", list(ev.shape), 5)
+    d = E.load("cfgA")
+    np.testing.assert_array_equal(d[1, 2], ev[1, 2])
+    np.testing.assert_array_equal(d[2, 0:4], ev[2, 0:4])
+    assert E.Ne == 5
+    gb = rng.standard_normal((2, 8, 4, 3, 3)) + 0j
+    gb.astype("<c16").tofile(tmp_path / "cfgB.dat")
+    G = GaugeFieldBinary(str(tmp_path) + "/", ".dat", list(gb.shape), "<c16")
+    np.testing.assert_array_equal(G.load("cfgB")[:], gb)
+    el = rng.standard_normal((2, 3, 4, 5, 5)).astype(np.complex128)
+    el.astype("<c16").tofile(tmp_path / "cfgC.meson")
+    np.testing.assert_array_equal(ElementalBinary(str(tmp_path) + "/", ".meson", list(el.shape), 5).load("cfgC")[1, 2],
+                                  el[1, 2])
+    pe = rng.standard_normal((2, 2, 4, 4, 3, 3)).astype(np.complex64)
+    np.save(tmp_path / "cfgD.peram.npy", pe)
+    np.testing.assert_array_equal(PerambulatorNpy(str(tmp_path) + "/", ".peram.npy", list(pe.shape), 3).load("cfgD")[1],
+                                  pe[1])
+
+
+def _write_qdp(path, blocks, xml="<foo><lattSize>4 4 4 8</lattSize><decay_dir>3</decay_dir></foo>"):
+    """Minimal QDP LazyDiskMapObjFile writer (layout of lattice/filedata/timeslice.py:110-121)."""
+    def s(x):
+        b = x.encode()
+        return struct.pack(">i", len(b)) + b
+
+    head = s("XXXXQDPLazyDiskMapObjFileXXXX") + struct.pack(">i", 1) + s(xml)
+    data_off = len(head) + 16
+    body, offsets = b"", {}
+    for key, arr in blocks.items():
+        offsets[key] = data_off + len(body)
+        body += arr.tobytes()
+    trailer_pos = data_off + len(body)
+    trailer = struct.pack(">I", len(blocks))
+    for key, off in offsets.items():
+        trailer += struct.pack(">i", 4 * len(key)) + struct.pack(">" + "i" * len(key), *key) + struct.pack(">qq", 0, off)
+    with open(path, "wb") as f:
+        f.write(head + struct.pack(">qq", 0, trailer_pos) + body + trailer)
+
+
+def test_qdp_lazy_disk_map(tmp_path):
+    from easydistillation_gb300.preset import EigenvectorTimeSlice
+
+    rng = np.random.default_rng(1)
+    blocks = {(t, e): (rng.standard_normal((6, 3)) + 1j * rng.standard_normal((6, 3))).astype(">c8")
+              for t in range(2) for e in range(3)}
+    _write_qdp(tmp_path / "cfg.mod", blocks)
+    E = EigenvectorTimeSlice(str(tmp_path) + "/", ".mod", [2, 3, 6, 3], 3)
+    d = E.load("cfg")
+    for (t, e), arr in blocks.items():
+        out = d[t, e]
+        assert out.dtype == np.complex64
+        np.testing.assert_array_equal(out, arr.astype(np.complex64))
