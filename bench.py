@@ -135,18 +135,13 @@ def make_inputs(latt, Ne, seed=2, distinct_t=RESIDENT_T):
     RESIDENT_T sets of random c128 vectors of norm 1."""
     import numpy as np
 
-    from oracle.restatement import synthetic_gauge  # input generation only
+    from easydistillation_gb300.synthetic import colour_vectors, gauge_field
 
     Lx, Ly, Lz, Lt = latt
     nt = min(Lt, distinct_t)
-    g = synthetic_gauge([Lx, Ly, Lz, nt], 0.3, 1000 + seed)
+    g = gauge_field([Lx, Ly, Lz, nt], 0.3, 1000 + seed)
     gauge = np.ascontiguousarray(np.tile(g, (Lt // nt + 1, 1, 1, 1, 1, 1, 1))[:Lt])
-    n = Lx * Ly * Lz * 3
-    rng = np.random.default_rng(seed)
-    evecs = []
-    for t in range(RESIDENT_T):
-        X = (rng.standard_normal((Ne, n)) + 1j * rng.standard_normal((Ne, n))) / np.sqrt(2 * n)
-        evecs.append(X)
+    evecs = [colour_vectors(Ne, latt, seed * 100 + t) for t in range(RESIDENT_T)]
     return gauge, evecs
 
 
@@ -268,7 +263,7 @@ def run_ours(args, rank, world):
     Lx, Ly, Lz, Lt = latt
     V3 = Lx * Ly * Lz
     Ne = args.ne
-    from oracle.restatement import mom_dict_to_list  # momentum list only
+    from easydistillation_gb300.insertion import mom_dict_to_list
 
     moms = mom_dict_to_list(3)[:NMOM]
     gauge, evecs_host = make_inputs(latt, Ne, seed=2 + rank)

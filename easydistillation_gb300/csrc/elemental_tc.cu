@@ -6,19 +6,18 @@
 // (left chain X, right chains Y0..Y0+nR-1), all momenta at once:
 //   A (M side, 128 rows per CTA)  : right-chain vectors m = (r, j), loaded by TMA
 //                                   from pre-split planes in HBM;
-//   B (N side, 256 rows per CTA)  : n = (i, p) = i*Nmom + p, produced in shared
+//   B (N side, 128 rows per CTA)  : n = (i, p) = i*Nmom + p, produced in shared
 //                                   memory by producer warps as conj(X_i) * phase_p;
 //   D[m][n] = G_p[i][m] accumulated in TMEM: D_re = Ar.Br - Ai.Bi, D_im = Ar.Bi + Ai.Br
 //   (4 real products per complex product; the 3-multiplication Gauss form would
-//   need three 256-column accumulators, more than TMEM's 512 columns).
+//   need three 128-column accumulators per buffer, which does not fit two
+//   buffers into TMEM's 512 columns).
 // Every real operand is split into hi + lo parts of a narrow type and each real
 // product is hi.hi + hi.lo + lo.hi (three MMAs, FP32 accumulation):
 //   f16x3 : fp16 parts of the operand scaled by 2^e (fp16 range); error ~2^-22
 //   bf16x3: bf16 parts, no scaling;                                 error ~2^-16
 //   tf32x3: tf32 parts (kind::tf32);                                error ~2^-22
-// Warp roles (192 threads, one CTA per SM): warp 0 issues TMA, warp 1 owns TMEM
-// and issues tcgen05.mma from one lane, warps 2-5 produce B and afterwards
-// drain the accumulators (tcgen05.ld) into the FP64 G buffer.
+// Warp roles and the accumulation scheme are described in tc_pair_gemm.cuh.
 // Shared memory rows are 64 bytes with the 64-byte swizzle (TMA and UMMA agree
 // on it; the producers apply it by hand).  Every mbarrier wait is bounded: on
 // timeout the kernel records an error code in a status word and leaves.
