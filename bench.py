@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison run")
+    ap.add_argument("--no-factor", action="store_true",
+                    help="keep the on-chip phase GEMM although the 27 momenta factorise")
     ap.add_argument("--no-stencil", action="store_true", help="skip the Laplacian bandwidth measurement")
     ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
     ap.add_argument("--eigen-batch", type=int, default=8)
@@ -60,13 +62,16 @@ def parse():
     return ap.parse_args()
 
 
-def launches_per_step(mode, B=1):
+def launches_per_step(mode, B=1, factorised=False):
     """Kernels of one batched step of B timeslices: per timeslice the links
     to SoA, vectors to planes, 12 hops and the combine; once per batch the
     phases and the pair GEMM; tensor-core modes add absmax, scale, split,
     phase scaling and the double-float to complex128 conversion (the FP64
-    mode packs complex128 links, the split modes complex64 ones)."""
-    return B * (1 + 1 + 12 + 1) + 1 + 1 + (0 if mode == "fp64" else 5)
+    mode packs complex128 links, the split modes complex64 ones); the
+    factorised-phase GEMM splits two operands and builds two factor tables
+    (absmax, scale, 2 factor phases, 2 scalings, 2 splits, conversion)."""
+    extra = 0 if mode == "fp64" else (9 if factorised else 5)
+    return B * (1 + 1 + 12 + 1) + 1 + 1 + extra
 
 
 def load_peaks():
@@ -270,7 +275,7 @@ def run_ours(args, rank, world):
     U = links_to_device(gauge, latt, dev)  # [3, Lt, Lz, Ly, Lx, 3, 3] c128 resident
     V = [torch.from_numpy(x).to(dev) for x in evecs_host]  # resident c128 eigenvectors
     B = args.batch
-    plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B)
+    plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=not args.no_factor)
     outs = [torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev) for _ in range(B)]
     out = outs[0]
     stream = torch.cuda.current_stream()
@@ -312,7 +317,10 @@ def run_ours(args, rank, world):
 
     # roofline of the pair-contraction kernel
     kms = statistics.mean(a.elapsed_time(b) for a, b in kev)
-    units = plan.num_pairs * NMOM * B  # (pair, momentum) contractions per launch (B timeslices)
+    # algorithmic work: the reference's 43 chain-pair subsets (num_nabla = 2) per
+    # momentum, 8*Ne^2*3V3 real flops each; this implementation evaluates only
+    # plan.num_pairs distinct pair products per momentum and combines them.
+    units = REF_SUBSETS * NMOM * B
     alg_flop = units * 8.0 * Ne * Ne * 3 * V3
     peaks = load_peaks()
     if args.mode == "fp64":
@@ -323,14 +331,23 @@ def run_ours(args, rank, world):
         if pk is None:
             pk, pk_src = 1700.0, "fallback"
         # 128 x 128 tiles; 12 MMAs of 128x128x(K) per complex multiply-add
-        tiles_m = sum(-(-(j * Ne) // 128) for j in plan_group_rights(plan)[: len(plan_group_rights(plan)) // B])
-        mma_flop = B * tiles_m * (-(-(Ne * NMOM) // 128)) * 128 * 128 * 3 * V3 * 12 * 2.0
+        rights = plan_group_rights(plan)[: len(plan_group_rights(plan)) // B]
+        if plan.factorised:
+            pxy, pz = plan.factorised
+            tiles = sum(-(-(j * pz * Ne) // 128) for j in rights) * (-(-(pxy * Ne) // 128))
+            kname = f"tc_fac_gemm_kernel<{args.mode}>"
+        else:
+            tiles = sum(-(-(j * Ne) // 128) for j in rights) * (-(-(Ne * NMOM) // 128))
+            kname = f"tc_pair_gemm_kernel<{args.mode}>"
+        mma_flop = B * tiles * 128 * 128 * 3 * V3 * 12 * 2.0
         roofline = {"bound": "tensor", "achieved": alg_flop / kms / 1e9, "peak": pk, "unit": "TFLOP/s",
                     "frac": alg_flop / kms / 1e9 / pk, "traffic": None, "peak_source": pk_src,
-                    "kernel": f"tc_pair_gemm_kernel<{args.mode}>", "kernel_ms": kms,
+                    "kernel": kname, "kernel_ms": kms,
                     "mma_tflops_executed": mma_flop / kms / 1e9, "mma_frac": mma_flop / kms / 1e9 / pk,
-                    "note": "achieved = algorithmic complex flops (8*Ne^2*3V3 per pair and momentum); the kernel "
-                            "issues 12 fp16/tf32 MMAs per complex multiply-add (3x) plus tile padding (mma_*)"}
+                    "pairs_evaluated_per_momentum": plan.num_pairs, "ref_subsets_per_momentum": REF_SUBSETS,
+                    "note": "achieved = algorithmic flops 8*Ne^2*3V3*Nmom*43 per timeslice (the reference's subset "
+                            "count); the kernel evaluates 19 distinct chain pairs per momentum and issues 12 "
+                            "fp16/tf32 MMAs per complex multiply-add (3x) plus tile padding (mma_*)"}
 
     # the plain FP64 GPU path on the same timeslice: speed and the split-precision error against it
     fp64 = None
@@ -374,7 +391,8 @@ def run_ours(args, rank, world):
                 return self.d
 
         ev = np.stack([x.reshape(Ne, Lz, Ly, Lx, 3) for x in evecs_host])  # [RESIDENT_T, Ne, ...]
-        gen = ElementalGenerator(latt, _Src(gauge), _Src(ev, Ne), NUM_NABLA, moms, precision=args.mode, device=dev)
+        gen = ElementalGenerator(latt, _Src(gauge), _Src(ev, Ne), NUM_NABLA, moms, precision=args.mode, device=dev,
+                                 factorise=not args.no_factor)
         gen.load("bench")
         host_out = torch.empty((B, 13, NMOM, Ne, Ne), dtype=torch.complex128).pin_memory()
         dev_out = torch.empty((B, 13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev)
@@ -405,9 +423,10 @@ def run_ours(args, rank, world):
             "config": {"workload": f"elemental {Lx}^3x{Lt}, Ne={Ne}, 13 ops x {NMOM} momenta, mode={args.mode}, "
                                    f"{B} timeslices per step",
                        "timeslices_per_step": B,
+                       "factorised_phases": plan.factorised,
                        "pairs_per_momentum": plan.num_pairs, "l2": "inputs larger than L2 (rotating timeslices)",
                        "parallelism": f"replicas x{world}"},
-            "gpu_launches": args.steps * launches_per_step(args.mode, B),
+            "gpu_launches": args.steps * launches_per_step(args.mode, B, plan.factorised is not None),
             "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "fp64_gpu": fp64,
             "stencil_roofline": stencil,
         }

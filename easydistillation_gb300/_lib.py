@@ -69,6 +69,7 @@ _SIGNATURES = {
     ),
     "ed_pair_run": ([_vp, _vp, _vp, _vp, _c.c_size_t, _vp], _i),
     "ed_elemental_describe": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
+    "ed_elemental_factorised": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
 }
 
 _lock = threading.Lock()

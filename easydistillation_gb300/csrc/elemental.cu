@@ -179,6 +179,7 @@ int plan_build(ed_elemental_plan* P) {
       P->jobs.push_back(j);
     }
   P->g_elems = P->g_per_t * P->nbatch;
+  tc_fac_setup(P);
 
   // workspace layout (256-byte aligned sections)
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
@@ -455,7 +456,8 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0, "ed_elemental_plan_create: sizes must be positive");
   ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create: num_nabla must be 0, 1 or 2");
   ED_CHECK_ARG(moms, "ed_elemental_plan_create: null momentum list");
-  ED_CHECK_ARG(ed::mode_supported(mode), "ed_elemental_plan_create: unknown mode %d", mode);
+  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR)) == 0,
+               "ed_elemental_plan_create: unknown mode %d", mode);
   ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create: lattice too large");
   auto* P = new ed_elemental_plan();
   P->Lx = Lx;
@@ -464,7 +466,8 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   P->Ne = Ne;
   P->num_nabla = num_nabla;
   P->nmom = nmom;
-  P->mode = mode;
+  P->mode = mode & 0xff;
+  P->no_factor = (mode & ED_MODE_FLAG_NO_FACTOR) != 0;
   P->use_herm = true;
   P->moms.assign(moms, moms + 3 * nmom);
   int rc = ed::plan_build(P);
@@ -538,6 +541,14 @@ extern "C" int ed_elemental_describe(const ed_elemental_plan* plan, int* ngroups
     if (left) left[g] = plan->jobs[g].left;
     if (nright) nright[g] = plan->jobs[g].nright;
   }
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_factorised(const ed_elemental_plan* plan, int* factorised, int* pxy, int* pz) {
+  ED_CHECK_ARG(plan && factorised, "ed_elemental_factorised: null pointer");
+  *factorised = plan->fac ? 1 : 0;
+  if (pxy) *pxy = plan->fac_pxy;
+  if (pz) *pz = plan->fac_pz;
   return ED_OK;
 }
 

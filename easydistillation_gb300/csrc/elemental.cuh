@@ -46,11 +46,20 @@ struct ed_elemental_plan {
   int tc_kind;        // 0 = none
   int tc_scale_exp;   // power-of-two scale applied before fp16 splitting
   size_t tc_bytes;    // extra workspace
+  // factorised phases: momenta = {(px,py)} x {pz} up to a few unused combinations
+  bool no_factor = false;       // ED_MODE_FLAG_NO_FACTOR given at creation
+  bool fac = false;             // the factorised-phase GEMM serves this plan
+  int fac_pxy = 0, fac_pz = 0;  // distinct (px, py) pairs and pz values
+  std::vector<int> fac_xy, fac_z;       // their values: fac_xy[2a], fac_xy[2a+1]; fac_z[c]
+  std::vector<signed char> fac_pidx;    // momentum index of (a, c), -1 if not in the list
+  std::vector<int> fac_lchain;          // left-chain slots of one timeslice -> chain index
+  std::vector<int> fac_lslot;           // chain index -> left-chain slot (-1 if never a left chain)
   cudaEvent_t prof_start = nullptr, prof_stop = nullptr;  // optional events around the pair GEMM
 };
 
 namespace ed {
 bool mode_supported(int mode);
+void tc_fac_setup(ed_elemental_plan* P);
 size_t tc_extra_workspace(const ed_elemental_plan* P);
 int tc_plan_check(ed_elemental_plan* P);
 int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,

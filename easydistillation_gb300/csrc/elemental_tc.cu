@@ -129,7 +129,7 @@ __device__ __forceinline__ uint64_t umma_desc_sw64(uint32_t saddr) {
 }
 
 // Instruction descriptor: D fp32, A/B format `fmt` (f16 0, bf16 1, tf32 2), K-major,
-// M = 128, N = 256, optional negation of A.
+// M = TC_BM, N = TC_BN, optional negation of A.
 __host__ __device__ constexpr uint32_t umma_idesc(uint32_t fmt, bool neg_a) {
   return (1u << 4) | (fmt << 7) | (fmt << 10) | ((neg_a ? 1u : 0u) << 13) | ((uint32_t)(TC_BN >> 3) << 17) |
          ((uint32_t)(TC_BM >> 4) << 24);
@@ -290,9 +290,86 @@ __global__ void tc_phase_kernel(const cplx<double>* __restrict__ ph, long long n
     out[i] = mk((float)(ph[i].re * s), (float)(ph[i].im * s));
 }
 
-// ------------------------------------------------------------ the GEMM kernel
+// ------------------------------------------------------------ the GEMM kernels
 
 #include "tc_pair_gemm.cuh"
+#include "tc_fac_gemm.cuh"
+
+// ------------------------------------------------------------ factorised-phase operands
+
+// Rows of the left (B) and right (A) variant planes.  Left slot sl of the
+// batch (timeslice sl / nl) holds chain lchain[sl % nl] of that timeslice;
+// right slot sl is chain sl of the chain buffer.
+struct TcFacSlots {
+  int nl;      // left-chain slots per timeslice (0 for the right side)
+  int nchain;  // chains per timeslice
+  int lchain[kMaxDeriv];
+};
+
+// out row (slot*nvar + a)*Ne + i of the planes <- conj(X_i) f_a   (LEFT)
+//                                              or f_a Y_i         (right)
+// for input row (slot, i) of the chain buffer; f_a = factor table a in
+// complex64, already scaled by 2^e (tc_phase_kernel).
+template <int KIND, bool LEFT>
+__global__ void tc_fac_split_kernel(const cplx<float>* __restrict__ chains, TcFacSlots sl, int nrows, int Ne,
+                                    int nvar, const cplx<float>* __restrict__ fac, int V3, long long Rplane,
+                                    void* __restrict__ planes) {
+  const long long K = 3LL * V3;
+  const int K2 = (int)(K / 2);
+  for (int row = blockIdx.y; row < nrows; row += gridDim.y) {
+    const int slot = row / Ne, i = row - (row / Ne) * Ne;
+    const int chain = LEFT ? (slot / sl.nl) * sl.nchain + sl.lchain[slot % sl.nl] : slot;
+    const float4* src = reinterpret_cast<const float4*>(chains + ((long long)chain * Ne + i) * K);
+    for (int kp = blockIdx.x * blockDim.x + threadIdx.x; kp < K2; kp += gridDim.x * blockDim.x) {
+      const float4 v = src[kp];
+      const int site = (2 * kp) % V3;  // V3 is even: both elements lie in one colour plane
+      for (int a = 0; a < nvar; ++a) {
+        const float4 f = *reinterpret_cast<const float4*>(fac + (long long)a * V3 + site);
+        const float fr0 = f.x, fi0 = f.y, fr1 = f.z, fi1 = f.w;
+        float re0, im0, re1, im1;
+        if constexpr (LEFT) {  // conj(x) * f
+          re0 = v.x * fr0 + v.y * fi0;
+          im0 = v.x * fi0 - v.y * fr0;
+          re1 = v.z * fr1 + v.w * fi1;
+          im1 = v.z * fi1 - v.w * fr1;
+        } else {  // f * y
+          re0 = fr0 * v.x - fi0 * v.y;
+          im0 = fr0 * v.y + fi0 * v.x;
+          re1 = fr1 * v.z - fi1 * v.w;
+          im1 = fr1 * v.w + fi1 * v.z;
+        }
+        const long long orow = ((long long)slot * nvar + a) * Ne + i;
+        if constexpr (KIND == TC_TF32) {
+          uint32_t* P = (uint32_t*)planes;
+          const long long plane = Rplane * K, e0 = orow * K + 2 * kp;
+          uint32_t h, l;
+          Split<TC_TF32>::one(re0, h, l);
+          P[e0] = h;
+          P[plane + e0] = l;
+          Split<TC_TF32>::one(re1, h, l);
+          P[e0 + 1] = h;
+          P[plane + e0 + 1] = l;
+          Split<TC_TF32>::one(im0, h, l);
+          P[2 * plane + e0] = h;
+          P[3 * plane + e0] = l;
+          Split<TC_TF32>::one(im1, h, l);
+          P[2 * plane + e0 + 1] = h;
+          P[3 * plane + e0 + 1] = l;
+        } else {
+          uint32_t* P = (uint32_t*)planes;  // 16-bit elements, pairs as words
+          const long long plane = Rplane * K2, w = orow * K2 + kp;
+          uint32_t h, l;
+          Split<KIND>::pair(re0, re1, h, l);
+          P[w] = h;
+          P[plane + w] = l;
+          Split<KIND>::pair(im0, im1, h, l);
+          P[2 * plane + w] = h;
+          P[3 * plane + w] = l;
+        }
+      }
+    }
+  }
+}
 
 // ------------------------------------------------------------ host side
 
@@ -315,9 +392,79 @@ static size_t tc_esz(int kind) { return kind == TC_TF32 ? 4 : 2; }
 
 static size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 
+// Decide whether the factorised-phase GEMM serves the plan: every momentum
+// is a distinct (px, py) x pz combination and at most a quarter of the
+// Pxy * Pz combinations the GEMM forms are not requested.
+void tc_fac_setup(ed_elemental_plan* P) {
+  P->fac = false;
+  if (!tc_kind_of(P->mode) || P->custom || P->no_factor || P->nmom > 127) return;
+  std::vector<int> xy, z, ai(P->nmom), ci(P->nmom);
+  for (int m = 0; m < P->nmom; ++m) {
+    const int px = P->moms[3 * m], py = P->moms[3 * m + 1], pz = P->moms[3 * m + 2];
+    int a = 0, c = 0;
+    while (a < (int)xy.size() / 2 && !(xy[2 * a] == px && xy[2 * a + 1] == py)) ++a;
+    if (a == (int)xy.size() / 2) xy.insert(xy.end(), {px, py});
+    while (c < (int)z.size() && z[c] != pz) ++c;
+    if (c == (int)z.size()) z.push_back(pz);
+    ai[m] = a;
+    ci[m] = c;
+  }
+  const int pxy = (int)xy.size() / 2, pz = (int)z.size();
+  if (pxy * pz > kMaxFac || 4 * pxy * pz > 5 * P->nmom) return;
+  std::vector<signed char> pidx(pxy * pz, -1);
+  for (int m = 0; m < P->nmom; ++m) {
+    signed char& e = pidx[ai[m] * pz + ci[m]];
+    if (e >= 0) return;  // a repeated momentum
+    e = (signed char)m;
+  }
+  std::vector<int> lchain, lslot(P->nchain, -1);
+  for (int k = 0; k < P->jobs_per_t; ++k) {
+    const int l = P->jobs[k].left;
+    if (lslot[l] < 0) {
+      lslot[l] = (int)lchain.size();
+      lchain.push_back(l);
+    }
+  }
+  const long long rb = (long long)P->nbatch * (long long)lchain.size() * pxy * P->Ne;
+  const long long ra = (long long)P->nbatch * P->nchain * pz * P->Ne;
+  if (4 * rb >= (1LL << 31) || 4 * ra >= (1LL << 31) || (int)lchain.size() > kMaxDeriv) return;
+  P->fac = true;
+  P->fac_pxy = pxy;
+  P->fac_pz = pz;
+  P->fac_xy = xy;
+  P->fac_z = z;
+  P->fac_pidx = pidx;
+  P->fac_lchain = lchain;
+  P->fac_lslot = lslot;
+}
+
+// Extra workspace of the factorised-phase GEMM, in this order: scalars, FP64
+// factor tables f_a (Pxy x V3) and g_c (Pz x V3), their scaled complex64
+// copies, B planes [4][RB][K], A planes [4][RA][K], double-float results.
+struct FacLayout {
+  long long rb, ra;
+  size_t fxy, fz, fxy32, fz32, bpl, apl, df, total;
+};
+static FacLayout fac_layout(const ed_elemental_plan* P) {
+  FacLayout L;
+  const size_t K = 3ull * P->V3, esz = tc_esz(tc_kind_of(P->mode));
+  L.rb = (long long)P->nbatch * (long long)P->fac_lchain.size() * P->fac_pxy * P->Ne;
+  L.ra = (long long)P->nbatch * P->nchain * P->fac_pz * P->Ne;
+  L.fxy = up256(sizeof(TcScalars));
+  L.fz = L.fxy + up256((size_t)P->fac_pxy * P->V3 * 16);
+  L.fxy32 = L.fz + up256((size_t)P->fac_pz * P->V3 * 16);
+  L.fz32 = L.fxy32 + up256((size_t)P->fac_pxy * P->V3 * 8);
+  L.bpl = L.fz32 + up256((size_t)P->fac_pz * P->V3 * 8);
+  L.apl = L.bpl + up256(4 * (size_t)L.rb * K * esz);
+  L.df = L.apl + up256(4 * (size_t)L.ra * K * esz);
+  L.total = L.df + up256((size_t)P->g_elems * sizeof(float4));
+  return L;
+}
+
 size_t tc_extra_workspace(const ed_elemental_plan* P) {
   const int kind = tc_kind_of(P->mode);
   if (!kind) return 0;
+  if (P->fac) return fac_layout(P).total;
   const size_t R = (size_t)P->nchain * P->nbatch * P->Ne;
   const size_t K = 3ull * P->V3;
   return up256(sizeof(TcScalars)) + up256((size_t)P->nmom * P->V3 * 8) + up256(4 * R * K * tc_esz(kind)) +
@@ -432,8 +579,134 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
   return ED_OK;
 }
 
+static int encode_planes(CUtensorMap* map, int kind, void* base, long long K, long long rows) {
+  EncodeFn enc = get_encode();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled is unavailable from the driver");
+    return ED_ERR_CUDA;
+  }
+  const size_t esz = tc_esz(kind);
+  cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)(K * esz)};
+  cuuint32_t box[2] = {(cuuint32_t)(TC_ROWB / esz), (cuuint32_t)TC_BM};
+  cuuint32_t estride[2] = {1, 1};
+  CUresult cr = enc(map, kind == TC_TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, base,
+                    gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+    return ED_ERR_CUDA;
+  }
+  return ED_OK;
+}
+
+// Factorised-phase path: factor tables, left/right variant planes, one GEMM
+// launch over all groups of the nb timeslices, double-float -> complex128.
+template <int KIND>
+static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cplx<double>* G, void* extra,
+                      cudaStream_t stream, int nb) {
+  const FacLayout lay = fac_layout(P);
+  char* X = (char*)extra;
+  TcScalars* sc = (TcScalars*)X;
+  cplx<double>* fxy = (cplx<double>*)(X + lay.fxy);
+  cplx<double>* fz = (cplx<double>*)(X + lay.fz);
+  cplx<float>* fxy32 = (cplx<float>*)(X + lay.fxy32);
+  cplx<float>* fz32 = (cplx<float>*)(X + lay.fz32);
+  void* bpl = X + lay.bpl;
+  void* apl = X + lay.apl;
+  float4* DF = (float4*)(X + lay.df);
+  const long long K = 3LL * P->V3;
+  const int nl = (int)P->fac_lchain.size(), pxy = P->fac_pxy, pz = P->fac_pz, Ne = P->Ne;
+  const Latt L{P->Lx, P->Ly, P->Lz};
+
+  cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(TcScalars), stream);
+  if (e != cudaSuccess) return cuda_status(e, "tc scalars reset");
+  const int sms = num_sms();
+  const long long R_used = (long long)P->nchain * nb * Ne;
+  tc_absmax_kernel<<<4 * sms, 256, 0, stream>>>((const float*)chains, 2 * R_used * K, sc);
+  tc_scale_kernel<<<1, 32, 0, stream>>>(sc, KIND);
+  ED_RETURN_LAUNCH("tensor-core operand scale");
+  std::vector<int> m3;
+  for (int a = 0; a < pxy; ++a) m3.insert(m3.end(), {P->fac_xy[2 * a], P->fac_xy[2 * a + 1], 0});
+  int rc = launch_phases(L, m3.data(), pxy, fxy, stream);
+  if (rc) return rc;
+  m3.clear();
+  for (int c = 0; c < pz; ++c) m3.insert(m3.end(), {0, 0, P->fac_z[c]});
+  rc = launch_phases(L, m3.data(), pz, fz, stream);
+  if (rc) return rc;
+  tc_phase_kernel<<<sms, 256, 0, stream>>>(fxy, (long long)pxy * P->V3, sc, fxy32);
+  tc_phase_kernel<<<sms, 256, 0, stream>>>(fz, (long long)pz * P->V3, sc, fz32);
+  ED_RETURN_LAUNCH("factor tables");
+
+  TcFacSlots sl;
+  sl.nl = nl;
+  sl.nchain = P->nchain;
+  for (int s = 0; s < nl; ++s) sl.lchain[s] = P->fac_lchain[s];
+  const int kx = (int)ceil_div(K / 2, 256);
+  const int lrows = nb * nl * Ne, rrows = nb * P->nchain * Ne;
+  tc_fac_split_kernel<KIND, true><<<dim3(kx, std::min(lrows, 65535)), 256, 0, stream>>>(
+      chains, sl, lrows, Ne, pxy, fxy32, P->V3, lay.rb, bpl);
+  tc_fac_split_kernel<KIND, false><<<dim3(kx, std::min(rrows, 65535)), 256, 0, stream>>>(
+      chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
+  ED_RETURN_LAUNCH("variant planes");
+
+  CUtensorMap amap, bmap;
+  if ((rc = encode_planes(&amap, KIND, apl, K, 4 * lay.ra))) return rc;
+  if ((rc = encode_planes(&bmap, KIND, bpl, K, 4 * lay.rb))) return rc;
+
+  TcFacTable tab;
+  tab.njobs = nb * P->jobs_per_t;
+  tab.pxy = pxy;
+  tab.pz = pz;
+  for (int q = 0; q < kMaxFac; ++q) tab.pidx[q] = q < pxy * pz ? P->fac_pidx[q] : (signed char)-1;
+  int tiles = 0;
+  for (int k = 0; k < tab.njobs; ++k) {
+    const Job& j = P->jobs[k];
+    const int b = k / P->jobs_per_t;
+    const int slot = b * nl + P->fac_lslot[P->jobs[k % P->jobs_per_t].left];
+    TcFacJob& d = tab.j[k];
+    d.arow0 = j.right0 * pz * Ne;
+    d.brow0 = slot * pxy * Ne;
+    d.nright = j.nright;
+    d.g_off = j.g_off;
+    d.mt = (int)ceil_div((long long)j.nright * pz * Ne, TC_BM);
+    d.nt = (int)ceil_div((long long)pxy * Ne, TC_BN);
+    d.tile0 = tiles;
+    tiles += d.mt * d.nt;
+  }
+  static bool attr_set[4] = {};
+  if (!attr_set[KIND]) {
+    e = cudaFuncSetAttribute(tc_fac_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, TCF_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
+    attr_set[KIND] = true;
+  }
+  const long long g_used = (long long)nb * P->g_per_t;
+  e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
+  if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
+  if (P->prof_start) cudaEventRecord(P->prof_start, stream);
+  tc_fac_gemm_kernel<KIND><<<tiles, TC_THREADS, TCF_SMEM, stream>>>(amap, bmap, tab, Ne, P->V3, (int)lay.ra,
+                                                                     (int)lay.rb, sc, DF);
+  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
+  ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");
+  tc_df_to_c128_kernel<<<4 * sms, 256, 0, stream>>>(DF, g_used, G);
+  ED_RETURN_LAUNCH("double-float to complex128");
+  return ED_OK;
+}
+
 int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
                         cplx<double>* G, void* extra, cudaStream_t stream, int nb) {
+  if (P->fac) {
+    switch (P->tc_kind) {
+      case TC_F16:
+        return launch_fac<TC_F16>(P, chains, G, extra, stream, nb);
+      case TC_BF16:
+        return launch_fac<TC_BF16>(P, chains, G, extra, stream, nb);
+      case TC_TF32:
+        return launch_fac<TC_TF32>(P, chains, G, extra, stream, nb);
+      default:
+        break;
+    }
+  }
   switch (P->tc_kind) {
     case TC_F16:
       return launch_kind<TC_F16>(P, chains, phases, G, extra, stream, nb);

@@ -1,0 +1,278 @@
+// Factorised-phase pair contraction (included by elemental_tc.cu).
+//
+// When the momentum list is (close to) a product set {(px, py)} x {pz}, the
+// phase factorises, phase_p(x, y, z) = f_a(x, y) * g_c(z) with a = (px, py)
+// and c = pz, and
+//   G_p(X, Y)[i, j] = sum_k (conj(X_i) f_a)[k] * (g_c Y_j)[k]
+// becomes one plain complex GEMM between
+//   B, the left variants  conj(X_i) f_a   (N side, rows n = a*Ne + i) and
+//   A, the right variants g_c Y_j         (M side, rows m = (r*Pz + c)*Ne + j),
+// covering all Pxy x Pz momenta of a chain pair at once.  Both operands are
+// formed and split into hi/lo planes once per timeslice (tc_fac_split_kernel)
+// and reach shared memory by TMA, so the K loop has no producer warps.  The
+// accumulation scheme (per-k-block TMEM buffers, FP32 register sums,
+// double-float flushes) is the one of tc_pair_gemm.cuh.
+//
+// Warp roles (512 threads, one CTA per SM):
+//   warp 0      : TMA of the four A and the four B planes of each stage
+//   warp 1      : TMEM owner, tcgen05.mma issue (one lane)
+//   warps 2-7   : idle
+//   warps 8-15  : drain (two warps per TMEM lane quarter, 64 + 64 columns each)
+// Register split: warpgroups 0-1 drop to 56 registers and the drain
+// warpgroups rise to 200 (256*56 + 256*200 = 512*128), enough to keep two
+// 32-column TMEM loads in flight per wait.
+
+constexpr int TCF_STAGES = 3;
+constexpr int TCF_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;  // 64 KB
+constexpr int TCF_SMEM = TCF_STAGES * TCF_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+static_assert(TCF_SMEM <= 232448, "shared memory per block");
+constexpr int TCF_REGS_LOW = 56, TCF_REGS_HIGH = 200;
+static_assert(256 * TCF_REGS_LOW + 256 * TCF_REGS_HIGH == TC_THREADS * TC_LAUNCH_REGS, "register split");
+constexpr int kMaxFac = 128;  // Pxy * Pz
+
+struct TcFacJob {
+  int arow0;   // first A row (right variants of the group's first right chain) within a plane
+  int brow0;   // first B row (left variants of the group's left chain) within a plane
+  int nright;  // right chains of the group
+  int tile0, mt, nt;
+  long long g_off;
+};
+struct TcFacTable {
+  int njobs, pxy, pz;
+  TcFacJob j[kMaxJobs];
+  signed char pidx[kMaxFac];  // momentum index of (a, c) = pidx[a*pz + c], -1 if not requested
+};
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Add the 64 register sums of one drain thread (row m, columns n0c..n0c+63)
+// into the double-float results and clear them.
+__device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64], float4* __restrict__ DF,
+                                               const TcFacTable& tab, const TcFacJob& J, int Ne, int n0c,
+                                               int m_local, int Mrows, float inv) {
+  const int Ncols = tab.pxy * Ne;
+  const int N = J.nright * Ne;  // row length of G_p[i][.] within the group
+  const bool row_ok = m_local < Mrows;
+  const int per_r = tab.pz * Ne;
+  const int r_local = m_local / per_r;
+  const int rem = m_local - r_local * per_r;
+  const int c = rem / Ne;
+  const int j = rem - c * Ne;
+#pragma unroll
+  for (int q = 0; q < 64; ++q) {
+    const int n = n0c + q;
+    if (row_ok && n < Ncols) {
+      const int a = n / Ne, i = n - (n / Ne) * Ne;
+      const int p = tab.pidx[a * tab.pz + c];
+      if (p >= 0) {
+        float4* dst = DF + J.g_off + ((long long)p * Ne + i) * N + (long long)r_local * Ne + j;
+        float4 d = *dst;
+        df_add(d.x, d.y, sre[q] * inv);
+        df_add(d.z, d.w, sim[q] * inv);
+        *dst = d;
+      }
+    }
+    sre[q] = 0.f;
+    sim[q] = 0.f;
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_fac_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
+                       const __grid_constant__ TcFacTable tab, int Ne, int V3, int RA, int RB,
+                       TcScalars* __restrict__ sc, float4* __restrict__ DF) {
+  constexpr int ESZ = Split<KIND>::ESZ;
+  constexpr int KE = TC_ROWB / ESZ;   // k elements per stage
+  constexpr int KINST = 32 / ESZ;     // k elements per MMA instruction
+  constexpr uint32_t FMT = KIND == TC_F16 ? 0u : (KIND == TC_BF16 ? 1u : 2u);
+  constexpr uint32_t IDESC = umma_idesc(FMT, false);
+  constexpr uint32_t IDESC_NEG = umma_idesc(FMT, true);
+
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + TCF_STAGES * TCF_STAGE_BYTES);
+  uint64_t* empty = full + TCF_STAGES;
+  uint64_t* accf = empty + TCF_STAGES;  // 2: accumulator buffer ready to drain
+  uint64_t* acce = accf + 2;            // 2: accumulator buffer drained
+  uint64_t* mma_done = acce + 2;        // every issued MMA has completed
+  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  volatile int* status = &sc->status;
+
+  // ---- decode the tile: group, n tile (fast), m tile
+  const int tile = blockIdx.x;
+  int jb = 0;
+  while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
+  const TcFacJob& J = tab.j[jb];
+  const int local = tile - J.tile0;
+  const int mtile = local / J.nt;
+  const int ntile = local - mtile * J.nt;
+  const long long K = 3LL * V3;
+  const int nkb = (int)(K / KE);
+  const int Mrows = J.nright * tab.pz * Ne;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TCF_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], TC_DWARPS);
+    }
+    mbar_init(mma_done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < 8) {
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(TCF_REGS_LOW));
+    if (warp == 0) {
+      // ===================== TMA of the A and B planes
+      if (lane == 0) {
+        const int ay = J.arow0 + mtile * TC_BM;
+        const int by = J.brow0 + ntile * TC_BN;
+        int issued_last = -1;
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int s = kb % TCF_STAGES;
+          if (kb >= TCF_STAGES && !mbar_wait(&empty[s], ((kb / TCF_STAGES) + 1) & 1, status, TC_ERR_EMPTY)) break;
+          uint8_t* As = smem + s * TCF_STAGE_BYTES;
+          uint8_t* Bs = As + TC_A_BYTES;
+          mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+          for (int q = 0; q < 4; ++q) {
+            tma_load_2d(As + q * TC_BM * TC_ROWB, &amap, &full[s], kb * KE, q * RA + ay);
+            tma_load_2d(Bs + q * TC_BN * TC_ROWB, &bmap, &full[s], kb * KE, q * RB + by);
+          }
+          issued_last = kb;
+        }
+        if (issued_last >= 0)  // do not leave while our copies may still land in shared memory
+          mbar_wait(&full[issued_last % TCF_STAGES], (issued_last / TCF_STAGES) & 1, status, TC_ERR_FULL, false);
+      }
+    } else if (warp == 1) {
+      // ===================== MMA issuer (same product order as tc_pair_gemm_kernel)
+      if (lane == 0) {
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int s = kb % TCF_STAGES;
+          const int b = kb & 1;
+          if (!mbar_wait(&full[s], (kb / TCF_STAGES) & 1, status, TC_ERR_FULL)) break;
+          if (kb >= 2 && !mbar_wait(&acce[b], ((kb >> 1) + 1) & 1, status, TC_ERR_ACCE)) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(smem + s * TCF_STAGE_BYTES);
+          const uint32_t b0 = a0 + TC_A_BYTES;
+          const uint32_t d_re = tmem + b * 256, d_im = d_re + TC_BN;
+#pragma unroll
+          for (int ks = 0; ks < KE / KINST; ++ks) {
+            const uint32_t acc = ks > 0 ? 1u : 0u;
+            const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
+            const uint64_t A0 = umma_desc_sw64(ao), A1 = umma_desc_sw64(ao + TC_BM * TC_ROWB);
+            const uint64_t A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB), A3 = umma_desc_sw64(ao + 3 * TC_BM * TC_ROWB);
+            const uint64_t B0 = umma_desc_sw64(bo), B1 = umma_desc_sw64(bo + TC_BN * TC_ROWB);
+            const uint64_t B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB), B3 = umma_desc_sw64(bo + 3 * TC_BN * TC_ROWB);
+            umma<KIND>(d_re, A0, B1, IDESC, acc);
+            umma<KIND>(d_re, A1, B0, IDESC, 1u);
+            umma<KIND>(d_re, A2, B3, IDESC_NEG, 1u);
+            umma<KIND>(d_re, A3, B2, IDESC_NEG, 1u);
+            umma<KIND>(d_im, A0, B3, IDESC, acc);
+            umma<KIND>(d_im, A1, B2, IDESC, 1u);
+            umma<KIND>(d_im, A2, B1, IDESC, 1u);
+            umma<KIND>(d_im, A3, B0, IDESC, 1u);
+          }
+#pragma unroll
+          for (int ks = 0; ks < KE / KINST; ++ks) {
+            const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
+            const uint64_t A0 = umma_desc_sw64(ao), A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB);
+            const uint64_t B0 = umma_desc_sw64(bo), B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB);
+            umma<KIND>(d_re, A0, B0, IDESC, 1u);
+            umma<KIND>(d_re, A2, B2, IDESC_NEG, 1u);
+            umma<KIND>(d_im, A0, B2, IDESC, 1u);
+            umma<KIND>(d_im, A2, B0, IDESC, 1u);
+          }
+          umma_commit(&empty[s]);  // frees the stage when these MMAs complete
+          umma_commit(&accf[b]);   // the buffer is ready to drain
+        }
+        umma_commit(mma_done);  // arrives once every MMA issued above has completed
+      }
+    }
+  } else {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(TCF_REGS_HIGH));
+    // ===================== drain: TMEM -> FP32 register sums -> double-float result
+    const int dw = warp - 8;         // 0..7
+    const int quarter = warp & 3;    // TMEM lane quarter this warp may access
+    const int half = dw >> 2;        // which 64 of the 128 columns
+    const int m = quarter * 32 + lane;
+    const int m_local = mtile * TC_BM + m;
+    const int n0c = ntile * TC_BN + half * 64;
+    const float inv = ldexpf(1.f, -2 * sc->scale_exp);
+    float sre[64], sim[64];
+#pragma unroll
+    for (int c = 0; c < 64; ++c) sre[c] = sim[c] = 0.f;
+    bool ok = true;
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int b = kb & 1;
+      if (!warp_wait(&accf[b], (kb >> 1) & 1, status, TC_ERR_ACC)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16) + b * 256 + half * 64;
+      {
+        uint32_t r0[32], r1[32];
+        tmem_ld32(tl, r0);
+        tmem_ld32(tl + 32, r1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+          sre[e] += __uint_as_float(r0[e]);
+          sre[32 + e] += __uint_as_float(r1[e]);
+        }
+      }
+      {
+        uint32_t r0[32], r1[32];
+        tmem_ld32(tl + TC_BN, r0);
+        tmem_ld32(tl + TC_BN + 32, r1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+          sim[e] += __uint_as_float(r0[e]);
+          sim[32 + e] += __uint_as_float(r1[e]);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
+      if ((kb & (TC_FLUSH_KB - 1)) == TC_FLUSH_KB - 1 || kb == nkb - 1)
+        flush_sums_fac(sre, sim, DF, tab, J, Ne, n0c, m_local, Mrows, inv);
+    }
+    if (!ok) {
+      // wait (without aborting on the error flag) until every issued MMA is
+      // done before the block releases TMEM
+      warp_wait(mma_done, 0, status, TC_ERR_ACC, false);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}

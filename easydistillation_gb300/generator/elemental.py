@@ -7,12 +7,16 @@ operator combination).  ``calc`` returns the generator's internal
 ``[Nderiv, Nmom, Ne, Ne]`` complex128 device buffer, which the next call
 overwrites, exactly like the reference's ``self._VPV``.
 
-Extra keyword-only arguments: ``precision`` and ``device``.  ``"fp64"`` is
-plain FP64 arithmetic with V rounded to complex64, as the reference.  The
-tensor-core modes ``"f16x3"``, ``"tf32x3"`` (relative error ~1e-7) and
-``"bf16x3"`` (~1e-5) store the derivative chains in complex64 and run the
-pair contractions as split-precision tcgen05 GEMMs with FP32 accumulation;
-they need ``Lx*Ly*Lz`` divisible by 32.
+Extra keyword-only arguments: ``precision``, ``device`` and ``factorise``.
+``"fp64"`` is plain FP64 arithmetic with V rounded to complex64, as the
+reference.  The tensor-core modes ``"f16x3"``, ``"tf32x3"`` (relative error
+~1e-7) and ``"bf16x3"`` (~1e-5) store the derivative chains in complex64 and
+run the pair contractions as split-precision tcgen05 GEMMs with FP32
+accumulation; they need ``Lx*Ly*Lz`` divisible by 32.  When the momentum list
+is a product set {(px, py)} x {pz} (e.g. all 27 momenta with |p|^2 <= 3),
+those GEMMs use the factorised phase exp(2 pi i p.x / L) = f(px, py) g(pz)
+with both operands prepared in HBM; ``factorise=False`` keeps the kernel
+that forms the phase-weighted operand on chip.
 """
 
 from __future__ import annotations
@@ -83,7 +87,7 @@ def links_to_device(gauge_data, latt_size, device) -> torch.Tensor:
 
 
 def admit_batch(latt_size, Ne, num_nabla, momentum_list, precision="fp64", device=None, max_batch=8,
-                reserve=0.1) -> int:
+                reserve=0.1, factorise: bool = True) -> int:
     """Largest batch of timeslices whose plan workspace fits the free HBM of
     ``device`` (keeping a ``reserve`` fraction free), between 1 and ``max_batch``."""
     device = torch.device(device or "cuda")
@@ -91,7 +95,8 @@ def admit_batch(latt_size, Ne, num_nabla, momentum_list, precision="fp64", devic
     budget = free * (1.0 - reserve)
     best = 1
     for b in range(1, max_batch + 1):
-        need = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, device, batch=b).workspace_bytes
+        need = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, device, batch=b,
+                             factorise=factorise).workspace_bytes
         if need <= budget:
             best = b
         else:
@@ -112,6 +117,7 @@ class ElementalGenerator:
         *,
         precision: str = "fp64",
         device=None,
+        factorise: bool = True,
     ) -> None:
         Lx, Ly, Lz, Lt = latt_size
         self.device = torch.device(device or "cuda")
@@ -125,12 +131,14 @@ class ElementalGenerator:
         Ne = eigenvector.Ne
         self.Ne = Ne
         self.precision = precision
+        self.factorise = factorise
         self._U = None
         self._VPV = torch.zeros((self.num_derivative, self.num_momentum, Ne, Ne), dtype=torch.complex128,
                                 device=self.device)
         self._eigenvector_data = None
         self._momentum_phase = MomentumPhase(latt_size, self.device)
-        self._plan = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, self.device)
+        self._plan = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, self.device,
+                                   factorise=factorise)
         self._stage = None
 
         if is_blending and (dilution is not None):
@@ -192,11 +200,11 @@ class ElementalGenerator:
                               dtype=torch.complex128, device=self.device)
         if batch is None:
             batch = admit_batch(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list, self.precision,
-                                self.device, max_batch=min(8, len(ts)))
+                                self.device, max_batch=min(8, len(ts)), factorise=self.factorise)
         plan = getattr(self, "_bplan", None)
         if plan is None or plan.batch != batch:
             plan = self._bplan = ElementalPlan(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list,
-                                               self.precision, self.device, batch=batch)
+                                               self.precision, self.device, batch=batch, factorise=self.factorise)
         for s0 in range(0, len(ts), batch):
             chunk = ts[s0 : s0 + batch]
             vecs = [self._read_vectors(t) for t in chunk]

@@ -176,9 +176,13 @@ class ElementalPlan:
     """Owner of an ``ed_elemental_plan`` and its device workspace."""
 
     def __init__(self, latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "fp64", device=None,
-                 batch: int = 1):
+                 batch: int = 1, factorise: bool = True):
+        """``factorise=False`` keeps the tensor-core GEMM that forms the
+        phase-weighted operand inside the kernel even when the momentum list
+        factorises (ED_MODE_FLAG_NO_FACTOR)."""
         if mode not in MODES:
             raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES)}")
+        cmode = MODES[mode] | (0 if factorise else 0x100)
         Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
         self.latt_size = list(latt_size)
         self.Ne = Ne
@@ -191,11 +195,11 @@ class ElementalPlan:
         handle = ctypes.c_void_p()
         if self.batch == 1:
             rc = _lib.lib().ed_elemental_plan_create(
-                ctypes.byref(handle), Lx, Ly, Lz, Ne, num_nabla, arr, len(self.momentum_list), MODES[mode]
+                ctypes.byref(handle), Lx, Ly, Lz, Ne, num_nabla, arr, len(self.momentum_list), cmode
             )
         else:
             rc = _lib.lib().ed_elemental_plan_create_batched(
-                ctypes.byref(handle), Lx, Ly, Lz, Ne, num_nabla, arr, len(self.momentum_list), MODES[mode],
+                ctypes.byref(handle), Lx, Ly, Lz, Ne, num_nabla, arr, len(self.momentum_list), cmode,
                 self.batch
             )
         _lib.check(rc, "ed_elemental_plan_create")
@@ -206,6 +210,10 @@ class ElementalPlan:
         call("ed_elemental_num_pairs", self._h, ctypes.byref(npairs))
         self.workspace_bytes = nbytes.value
         self.num_pairs = npairs.value
+        fac, pxy, pz = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        call("ed_elemental_factorised", self._h, ctypes.byref(fac), ctypes.byref(pxy), ctypes.byref(pz))
+        #: (Pxy, Pz) when the factorised-phase GEMM serves this plan, else None
+        self.factorised = (pxy.value, pz.value) if fac.value else None
         self.device = torch.device(device or "cuda")
         self._ws = None
 

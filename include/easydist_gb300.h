@@ -52,6 +52,11 @@ extern "C" {
 #define ED_MODE_F16X3 1  /* tcgen05: scaled fp16 hi/lo split, 3 products per real product */
 #define ED_MODE_BF16X3 2 /* tcgen05: bf16 hi/lo split, 3 products per real product */
 #define ED_MODE_TF32X3 3 /* tcgen05 kind::tf32: tf32 hi/lo split, 3 products per real product */
+/* Flag OR-ed into a tensor-core mode at plan creation: keep the GEMM whose
+ * phase-weighted operand is formed inside the kernel even when the momentum
+ * list factorises into {(px,py)} x {pz} (by default such plans use the
+ * factorised-phase GEMM, whose operands are both prepared in HBM). */
+#define ED_MODE_FLAG_NO_FACTOR 0x100
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);
@@ -205,6 +210,13 @@ int ed_elemental_run_noalloc(const ed_elemental_plan* plan, const void* links, l
  * (arrays of at least 32 ints, may be NULL); *herm = 1 when the momentum list
  * is closed under p -> -p and hermiticity halves the work. */
 int ed_elemental_describe(const ed_elemental_plan* plan, int* ngroups, int* left, int* nright, int* herm);
+
+/* *factorised = 1 when the plan runs the factorised-phase tensor-core GEMM:
+ * its momenta are (up to a quarter of unused combinations) the product set
+ * of *pxy distinct (px, py) pairs and *pz distinct pz values, and both GEMM
+ * operands (conj(X) f_(px,py) and g_pz Y) are prepared in HBM.  pxy and pz
+ * may be NULL.  No counterpart in the reference (an execution detail). */
+int ed_elemental_factorised(const ed_elemental_plan* plan, int* factorised, int* pxy, int* pz);
 
 /* Record the CUDA events `start` / `stop` (cudaEvent_t, or NULL to disable)
  * on the run's stream immediately before and after the pair-contraction

@@ -60,3 +60,67 @@ def test_tc_rejects_volume_not_divisible_by_32():
 
     with pytest.raises(Exception):
         ElementalPlan([6, 2, 2, 1], 4, 0, [(0, 0, 0)], "f16x3", device="cpu")
+
+
+# ---------------------------------------------------------------- factorised phases
+def _run_fac(latt, Ne, num_nabla, moms, mode, factorise, t=0, seed=5):
+    from easydistillation_gb300 import ElementalGenerator
+
+    gauge = R.synthetic_gauge(latt, 0.3, seed)
+    evec = np.stack([R.random_colour_vectors(Ne, latt, seed * 10 + tt) for tt in range(latt[3])])
+    gen = ElementalGenerator(latt, MemGauge(gauge), MemEigen(evec, Ne), num_nabla, moms, precision=mode,
+                             factorise=factorise)
+    gen.load("k")
+    E = gen.calc(t).cpu().numpy()
+    U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, t]
+    return gen, E, R.elemental(evec[t], U, latt, num_nabla, moms)
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3", "bf16x3"])
+def test_fac_all_27_momenta(mode):
+    """|p|^2 <= 3: the 27 momenta are {(px,py)} x {pz} = 9 x 3, every operator"""
+    gen, E, ref = _run_fac([4, 4, 4, 2], 6, 2, R.mom_dict_to_list(3), mode, True, t=1)
+    assert gen._plan.factorised == (9, 3)
+    assert rel_err(E, ref) < TOL[mode]
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3"])
+def test_fac_matches_on_chip_phase_kernel(mode):
+    """the factorised and the on-chip-phase GEMMs agree with each other and the oracle"""
+    moms = R.mom_dict_to_list(3)
+    g1, E1, ref = _run_fac([8, 4, 4, 1], 40, 2, moms, mode, True)
+    g2, E2, _ = _run_fac([8, 4, 4, 1], 40, 2, moms, mode, False)
+    assert g1._plan.factorised == (9, 3) and g2._plan.factorised is None
+    assert rel_err(E1, ref) < TOL[mode] and rel_err(E2, ref) < TOL[mode]
+    assert rel_err(E1, E2) < 2 * TOL[mode]
+
+
+def test_fac_open_product_list():
+    """a product list not closed under p -> -p (no hermiticity): 4 x 3 momenta"""
+    moms = [(px, py, pz) for px in (0, 1) for py in (0, 2) for pz in (0, 1, 3)]
+    gen, E, ref = _run_fac([4, 4, 4, 1], 5, 2, moms, "f16x3", True)
+    assert gen._plan.factorised == (4, 3)
+    assert rel_err(E, ref) < TOL["f16x3"]
+
+
+def test_fac_with_unrequested_combinations():
+    """25 of the 27 product momenta (two combinations formed but not stored)"""
+    moms = [p for p in R.mom_dict_to_list(3) if p not in ((1, 1, 1), (-1, -1, -1))]
+    gen, E, ref = _run_fac([4, 4, 4, 1], 7, 1, moms, "f16x3", True)
+    assert gen._plan.factorised == (9, 3)
+    assert rel_err(E, ref) < TOL["f16x3"]
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3"])
+def test_fac_many_ragged_tiles(mode):
+    """Ne = 150: 9*150 B rows and 3*150 A rows per chain, ragged in both tile directions"""
+    gen, E, ref = _run_fac([8, 8, 4, 1], 150, 1, R.mom_dict_to_list(3), mode, True)
+    assert gen._plan.factorised == (9, 3)
+    assert rel_err(E, ref) < TOL[mode]
+
+
+def test_fac_long_k():
+    """K = 3 * 16^3 = 12288"""
+    gen, E, ref = _run_fac([16, 16, 16, 1], 24, 1, R.mom_dict_to_list(3), "f16x3", True)
+    assert gen._plan.factorised == (9, 3)
+    assert rel_err(E, ref) < TOL["f16x3"]

@@ -87,3 +87,30 @@ def test_generator_metadata_matches_reference_scheme():
     assert [derivative(n) for n in range(40)] == [R.derivative(n) for n in range(40)]
     assert mom_dict_to_list(3) == R.mom_dict_to_list(3)
     assert [num_derivative(k) for k in range(3)] == [1, 4, 13]
+
+
+@pytest.mark.parametrize(
+    "moms, mode, factorise, expect",
+    [
+        ("all27", "f16x3", True, (9, 3)),
+        ("all27", "tf32x3", True, (9, 3)),
+        ("all27", "f16x3", False, None),
+        ("all27", "fp64", True, None),
+        ("first7", "f16x3", True, None),  # 5 x 3 combinations for 7 momenta: too many unused
+        ([(px, py, pz) for px in (0, 1) for py in (0, 2) for pz in (0, 1, 3)], "bf16x3", True, (4, 3)),
+        ([(0, 0, 0), (0, 0, 1), (0, 0, 0)], "f16x3", True, None),  # a repeated momentum
+    ],
+)
+def test_factorised_phase_selection(moms, mode, factorise, expect):
+    """Plans pick the factorised-phase GEMM exactly for product momentum sets."""
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.ops import ElementalPlan
+
+    lists = {"all27": mom_dict_to_list(3), "first7": mom_dict_to_list(3)[:7]}
+    moms = lists.get(moms, moms) if isinstance(moms, str) else moms
+    p = ElementalPlan([8, 8, 4, 2], 10, 2, moms, mode, device="cpu", factorise=factorise)
+    assert p.factorised == expect
+    if expect:
+        # the factorised workspace holds both variant operands: larger than the on-chip-phase one
+        q = ElementalPlan([8, 8, 4, 2], 10, 2, moms, mode, device="cpu", factorise=False)
+        assert q.factorised is None and p.workspace_bytes > q.workspace_bytes
