@@ -56,10 +56,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Add the 64 register sums of one drain thread (row m, columns n0c..n0c+63)
-// into the double-float results and clear them.
+// into the double-float results and clear them.  The read-modify-writes go
+// in groups of 8: all loads of a group are issued before its stores, so a
+// flush waits for 8 memory round trips instead of 64.
 __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64], float4* __restrict__ DF,
                                                const TcFacTable& tab, const TcFacJob& J, int Ne, int n0c,
                                                int m_local, int Mrows, float inv) {
+  constexpr int G = 8;
   const int Ncols = tab.pxy * Ne;
   const int N = J.nright * Ne;  // row length of G_p[i][.] within the group
   const bool row_ok = m_local < Mrows;
@@ -68,22 +71,32 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
   const int rem = m_local - r_local * per_r;
   const int c = rem / Ne;
   const int j = rem - c * Ne;
+  float4* const base = DF + J.g_off + (long long)r_local * Ne + j;
 #pragma unroll
-  for (int q = 0; q < 64; ++q) {
-    const int n = n0c + q;
-    if (row_ok && n < Ncols) {
-      const int a = n / Ne, i = n - (n / Ne) * Ne;
-      const int p = tab.pidx[a * tab.pz + c];
-      if (p >= 0) {
-        float4* dst = DF + J.g_off + ((long long)p * Ne + i) * N + (long long)r_local * Ne + j;
-        float4 d = *dst;
-        df_add(d.x, d.y, sre[q] * inv);
-        df_add(d.z, d.w, sim[q] * inv);
-        *dst = d;
+  for (int q0 = 0; q0 < 64; q0 += G) {
+    long long off[G];
+    float4 d[G];
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      const int n = n0c + q0 + u;
+      off[u] = -1;
+      if (row_ok && n < Ncols) {
+        const int a = n / Ne, i = n - (n / Ne) * Ne;
+        const int p = tab.pidx[a * tab.pz + c];
+        if (p >= 0) off[u] = ((long long)p * Ne + i) * N;
       }
+      if (off[u] >= 0) d[u] = base[off[u]];
     }
-    sre[q] = 0.f;
-    sim[q] = 0.f;
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      if (off[u] >= 0) {
+        df_add(d[u].x, d[u].y, sre[q0 + u] * inv);
+        df_add(d[u].z, d[u].w, sim[q0 + u] * inv);
+        base[off[u]] = d[u];
+      }
+      sre[q0 + u] = 0.f;
+      sim[q0 + u] = 0.f;
+    }
   }
 }
 

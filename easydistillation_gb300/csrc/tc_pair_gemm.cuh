@@ -37,24 +37,37 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
 }
 
 // Add this thread's 64 register sums into the double-float result
-// DF[elem] = (re_hi, re_lo, im_hi, im_lo) and clear them.
+// DF[elem] = (re_hi, re_lo, im_hi, im_lo) and clear them.  The
+// read-modify-writes go in pairs (both loads before the stores).
 __device__ __forceinline__ void flush_sums(float (&sre)[64], float (&sim)[64], float4* __restrict__ DF,
                                            long long gbase, int N, int n0c, int Ncols, int nmom, int Ne,
                                            long long m_local, int Mrows, float inv) {
+  constexpr int G = 2;
   const bool row_ok = m_local < Mrows;
 #pragma unroll
-  for (int c = 0; c < 64; ++c) {
-    const int n = n0c + c;
-    if (row_ok && n < Ncols) {
-      const int i = n / nmom, p = n - i * nmom;
-      float4* dst = DF + gbase + ((long long)p * Ne + i) * N + m_local;
-      float4 d = *dst;
-      df_add(d.x, d.y, sre[c] * inv);
-      df_add(d.z, d.w, sim[c] * inv);
-      *dst = d;
+  for (int q0 = 0; q0 < 64; q0 += G) {
+    long long off[G];
+    float4 d[G];
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      const int n = n0c + q0 + u;
+      off[u] = -1;
+      if (row_ok && n < Ncols) {
+        const int i = n / nmom, p = n - (n / nmom) * nmom;
+        off[u] = gbase + ((long long)p * Ne + i) * N + m_local;
+        d[u] = DF[off[u]];
+      }
     }
-    sre[c] = 0.f;
-    sim[c] = 0.f;
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      if (off[u] >= 0) {
+        df_add(d[u].x, d[u].y, sre[q0 + u] * inv);
+        df_add(d[u].z, d[u].w, sim[q0 + u] * inv);
+        DF[off[u]] = d[u];
+      }
+      sre[q0 + u] = 0.f;
+      sim[q0 + u] = 0.f;
+    }
   }
 }
 
