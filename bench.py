@@ -59,6 +59,11 @@ def parse():
     ap.add_argument("--eigen-batch", type=int, default=8)
     ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--eigen-cpu", action="store_true", help="also time the oracle's scipy eigensolve (slow)")
+    ap.add_argument("--eigen-poly", type=int, default=0, help="Chebyshev degree for --eigen (0: plain Lanczos)")
+    ap.add_argument("--mixed", action="store_true",
+                    help="measure graphed batches over mixed volumes (16^3 Ne=64, 24^3 Ne=128, 32^3 Ne=256)")
+    ap.add_argument("--grad", action="store_true",
+                    help="measure the correlator-loss gradient (24^3x48, Ne=100) with a finite-difference check")
     return ap.parse_args()
 
 
@@ -433,6 +438,132 @@ def run_ours(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_mixed(args):
+    """Secondary measurement (``--mixed``): 96 timeslices, 32 each of 16^3
+    (Ne=64), 24^3 (Ne=128) and 32^3 (Ne=256), links exp(i eps A) with eps
+    alternating 0.1 / 0.3 over timeslices, 4 operators x 7 momenta, split
+    precision.  Each volume runs as CUDA-graph replays of one batched plan
+    (batch admitted by HBM footprint); inputs resident in HBM."""
+    import torch
+
+    from easydistillation_gb300.batch import GraphedElementalBatch, admit_batch
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.synthetic import gauge_field
+
+    dev = torch.device("cuda", 0)
+    mode = args.mode
+    moms = mom_dict_to_list(3)[:7]
+    vols = [([16, 16, 16, 32], 64), ([24, 24, 24, 32], 128), ([32, 32, 32, 32], 256)]
+    gen = torch.Generator(device=dev).manual_seed(3003)
+    runners, inputs = [], []
+    for latt, Ne in vols:
+        Lx, Ly, Lz, Lt = latt
+        V3 = Lx * Ly * Lz
+        # 2 distinct timeslices per eps, tiled (timeslices are independent)
+        g = [gauge_field([Lx, Ly, Lz, 2], eps, 1000 + 3 + k) for k, eps in enumerate((0.1, 0.3))]
+        U = torch.stack([links_to_device(x, [Lx, Ly, Lz, 2], dev) for x in g], dim=2)  # [3, 2, eps, ...]
+        U = U.reshape(3, 4, Lz, Ly, Lx, 3, 3)  # t' = 2*t + eps index: eps alternates
+        V = torch.complex(torch.randn((4, Ne, V3 * 3), generator=gen, device=dev, dtype=torch.float64),
+                          torch.randn((4, Ne, V3 * 3), generator=gen, device=dev, dtype=torch.float64))
+        V /= (2 * V3 * 3) ** 0.5
+        B = admit_batch(latt, Ne, 1, moms, mode, dev, max_batch=8)
+        r = GraphedElementalBatch(latt, Ne, 1, moms, mode, batch=B, device=dev)
+        runners.append(r)
+        inputs.append((U, V, Lt))
+
+    def sweep():
+        n = 0
+        for r, (U, V, Lt) in zip(runners, inputs):
+            for s0 in range(0, Lt, r.batch):
+                ts = list(range(s0, min(Lt, s0 + r.batch)))
+                r.run([U[:, t % 4] for t in ts], [V[t % 4] for t in ts])
+                n += len(ts)
+        return n
+
+    sweep()  # captures the graphs
+    torch.cuda.synchronize()
+    reps = max(1, args.steps)
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(reps):
+        n += sweep()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    for r in runners:
+        if mode != "fp64":
+            r.plan.check_status()
+    line = {"metric": "mixed-volume elemental timeslices/s (96 timeslices: 16^3 Ne=64, 24^3 Ne=128, 32^3 Ne=256; "
+                      "4 ops x 7 momenta)", "value": n / dt, "unit": "timeslices/s", "seconds_per_sweep": dt / reps,
+            "mode": mode, "batches": {f"{v[0][0]}^3": r.batch for v, r in zip(vols, runners)},
+            "graph_replays_per_sweep": sum(-(-inp[2] // r.batch) for r, inp in zip(runners, inputs)),
+            "data": "synthetic, resident in HBM"}
+    print(json.dumps(line), flush=True)
+
+
+def run_grad(args):
+    """Secondary measurement (``--grad``): gradient of the correlator
+    log-ratio loss (t = 6, 12; operator nabla_x, p = 0; gamma_5) with respect
+    to the profile weights w_k and the links at 24^3 x 48, Ne = 100, through
+    the hand-written adjoints; a central finite difference (h = 1e-6) along a
+    random link direction and a random weight direction checks it."""
+    import numpy as np
+    import torch
+
+    from easydistillation_gb300.autograd import correlator_log_ratio
+    from easydistillation_gb300.correlator import gamma
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.synthetic import gauge_field
+
+    dev = torch.device("cuda", 0)
+    latt = [24, 24, 24, 48]
+    Lx, Ly, Lz, Lt = latt
+    V3 = Lx * Ly * Lz
+    Ne = 100
+    g = gauge_field([Lx, Ly, Lz, 4], 0.3, 1004)
+    U4 = links_to_device(g, [Lx, Ly, Lz, 4], dev)
+    U = U4[:, torch.arange(Lt, device=dev) % 4].contiguous()
+    gen = torch.Generator(device=dev).manual_seed(4006)
+    V = torch.complex(torch.randn((Lt, Ne, V3 * 3), generator=gen, device=dev, dtype=torch.float64),
+                      torch.randn((Lt, Ne, V3 * 3), generator=gen, device=dev, dtype=torch.float64)) / (2 * V3 * 3) ** 0.5
+    rng = np.random.default_rng(4004)
+    w = torch.from_numpy(rng.uniform(0.5, 1.5, Ne)).to(dev)
+    evals = torch.from_numpy(np.sort(rng.uniform(0.2, 0.6, (Lt, Ne)), axis=1)).to(dev)
+    rng5 = np.random.default_rng(4005)
+    tau = torch.from_numpy(rng5.standard_normal((Lt, 4, 4, Ne, Ne)) + 1j * rng5.standard_normal((Lt, 4, 4, Ne, Ne))).to(dev)
+    g5 = gamma(15, dev)
+
+    def loss(U_, w_):
+        return correlator_log_ratio(U_, V, evals, w_, tau, latt, g5, d=1, t1=6, t2=12)
+
+    times = []
+    for _ in range(max(2, args.steps + 1)):
+        U1 = U.clone().requires_grad_(True)
+        w1 = w.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L = loss(U1, w1)
+        L.backward()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    h = 1e-6
+    dU = torch.randn(U.shape, generator=gen, device=dev, dtype=torch.complex128)
+    dw = torch.randn(w.shape, generator=gen, device=dev, dtype=torch.float64)
+    with torch.no_grad():
+        fdU = float((loss(U + h * dU, w) - loss(U - h * dU, w)) / (2 * h))
+        fdw = float((loss(U, w + h * dw) - loss(U, w - h * dw)) / (2 * h))
+    anU = float((U1.grad.conj() * dU).real.sum())
+    anw = float((w1.grad * dw).sum())
+    line = {"metric": "correlator-loss gradient (dL/dw, dL/dU) 24^3x48 Ne=100", "value": 1.0 / min(times[1:]),
+            "unit": "loss+gradient evaluations/s", "seconds": min(times[1:]), "loss": float(L),
+            "fd_check": {"h": h, "dU_directional": [anU, fdU], "dw_directional": [anw, fdw],
+                         "rel_err_U": abs(anU - fdU) / max(abs(fdU), 1e-30),
+                         "rel_err_w": abs(anw - fdw) / max(abs(fdw), 1e-30)},
+            "data": "synthetic: links exp(i 0.3 A), Gaussian vectors and perambulator [48,4,4,100,100], "
+                    "w ~ U(0.5, 1.5), sigma = 1"}
+    print(json.dumps(line), flush=True)
+
+
 def run_eigen(args):
     """Secondary measurement (``--eigen``): EigenvectorGenerator.calc_batch on
     ``--eigen-batch`` timeslices at ``--lattice`` (default 24^3 x 64, Ne from
@@ -463,11 +594,20 @@ def run_eigen(args):
     ts = list(range(args.eigen_batch))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    evecs, evals = gen.calc_batch(ts)
+    if args.eigen_poly > 0:
+        # lambda_cut: 15 % above the largest wanted eigenvalue, from a first plain solve of one timeslice
+        _, ev0 = gen.calc_batch(ts[:1])
+        cut = 1.15 * float(ev0[0, -1])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        evecs, evals = gen.calc_batch(ts, polynomial_degree=args.eigen_poly, lambda_cut=cut)
+    else:
+        evecs, evals = gen.calc_batch(ts)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     line = {"metric": f"eigensolve timeslices/s {latt[0]}^3 Ne={Ne} tol 1e-10", "value": len(ts) / dt,
             "unit": "timeslices/s", "seconds": dt, "batch": len(ts), "stencil_precision": args.eigen_precision,
+            "polynomial_degree": args.eigen_poly,
             "stats": gen.last_stats, "lowest_evals_t0": [float(v) for v in evals[0, :3].cpu()]}
     if args.eigen_cpu:
         from oracle import restatement as R
@@ -486,6 +626,12 @@ def main():
     args = parse()
     if args.eigen:
         run_eigen(args)
+        return
+    if args.mixed:
+        run_mixed(args)
+        return
+    if args.grad:
+        run_grad(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
