@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="f16x3", help="elemental mode: f16x3 (headline), tf32x3, bf16x3, fp64")
+    ap.add_argument("--mode", default="f16x3",
+                    help="elemental mode: f16x3 (headline), tf32x3, bf16x3, ozaki_i8, fp64")
     ap.add_argument("--lattice", default=None, help="Lx,Ly,Lz,Lt override (parity runs only)")
     ap.add_argument("--ne", type=int, default=NE)
     ap.add_argument("--batch", type=int, default=4, help="timeslices per step (one pair-contraction launch)")
@@ -75,6 +76,8 @@ def launches_per_step(mode, B=1, factorised=False):
     mode packs complex128 links, the split modes complex64 ones); the
     factorised-phase GEMM splits two operands and builds two factor tables
     (absmax, scale, 2 factor phases, 2 scalings, 2 splits, conversion)."""
+    if mode == "ozaki_i8":  # 2 factor phases, 2 scalings, 2 row maxima, 2 digit splits; no absmax/conversion
+        return B * (1 + 1 + 12 + 1) + 1 + 1 + 8
     extra = 0 if mode == "fp64" else (9 if factorised else 5)
     return B * (1 + 1 + 12 + 1) + 1 + 1 + extra
 
@@ -328,7 +331,18 @@ def run_ours(args, rank, world):
     units = REF_SUBSETS * NMOM * B
     alg_flop = units * 8.0 * Ne * Ne * 3 * V3
     peaks = load_peaks()
-    if args.mode == "fp64":
+    if args.mode == "ozaki_i8":
+        pxy, pz = plan.factorised
+        rights = plan_group_rights(plan)[: len(plan_group_rights(plan)) // B]
+        tiles = sum(-(-(j * pz * Ne) // 64) for j in rights) * (-(-(pxy * Ne) // 64))
+        iops = B * tiles * 64 * 64 * 3 * V3 * 40 * 2.0  # 10 slice pairs x 4 real products, 2 ops per MAC
+        roofline = {"bound": "int8 tensor (mma.sync)", "achieved": alg_flop / kms / 1e9, "peak": None,
+                    "unit": "TFLOP/s", "frac": None, "traffic": None, "kernel": "tc_ozaki_gemm_kernel",
+                    "kernel_ms": kms, "int8_tops_executed": iops / kms / 1e9,
+                    "note": "achieved in the 43-subset flop count; the kernel issues 40 int8 products per complex "
+                            "multiply-add (10 slice pairs x 4); mma.sync int8 measured at 158 TOPS on this part "
+                            "by a register-only probe (tcgen05 has no kind::i8 on sm_103a)"}
+    elif args.mode == "fp64":
         roofline = {"bound": "fp64", "achieved": alg_flop / kms / 1e9, "peak": None, "unit": "TFLOP/s",
                     "frac": None, "traffic": None, "kernel": "pair_gemm_f64_kernel", "kernel_ms": kms}
     else:
@@ -395,24 +409,32 @@ def run_ours(args, rank, world):
             def load(self, key):
                 return self.d
 
-        ev = np.stack([x.reshape(Ne, Lz, Ly, Lx, 3) for x in evecs_host])  # [RESIDENT_T, Ne, ...]
-        gen = ElementalGenerator(latt, _Src(gauge), _Src(ev, Ne), NUM_NABLA, moms, precision=args.mode, device=dev,
+        # eigenvectors in pinned host memory ([RESIDENT_T, Ne, Lz, Ly, Lx, 3] c128), elementals back into
+        # pinned host memory; one calc_batch call over all timed steps, whose batches pipeline the copies
+        ev = torch.from_numpy(np.stack([x.reshape(Ne, Lz, Ly, Lx, 3) for x in evecs_host])).pin_memory()
+        class _TSrc:  # eigenvector source whose load() returns the pinned tensor itself
+            def __init__(self, t, Ne):
+                self.t, self.Ne = t, Ne
+
+            def load(self, key):
+                return self.t
+
+        gen = ElementalGenerator(latt, _Src(gauge), _TSrc(ev, Ne), NUM_NABLA, moms, precision=args.mode, device=dev,
                                  factorise=not args.no_factor)
         gen.load("bench")
-        host_out = torch.empty((B, 13, NMOM, Ne, Ne), dtype=torch.complex128).pin_memory()
-        dev_out = torch.empty((B, 13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev)
-        batch_ts = [[(i * B + k) % RESIDENT_T for k in range(B)] for i in range(max(args.steps, 2))]
-        for i in range(min(args.warmup, 2)):
-            host_out.copy_(gen.calc_batch(batch_ts[i], out=dev_out, batch=B))
+        nts = args.steps * B
+        host_out = torch.empty((nts, 13, NMOM, Ne, Ne), dtype=torch.complex128).pin_memory()
+        ts_all = [k % RESIDENT_T for k in range(nts)]
+        gen.calc_batch(ts_all[:B], out=host_out[:B], batch=B)  # warm-up: plans, buffers, streams
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for i in range(args.steps):
-            host_out.copy_(gen.calc_batch(batch_ts[i], out=dev_out, batch=B))
+        gen.calc_batch(ts_all, out=host_out, batch=B)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        e2e = {"value": world * args.steps * B / dt, "unit": "timeslices/s",
-               "h2d_bytes_per_step": B * Ne * V3 * 3 * 16, "d2h_bytes_per_step": int(host_out.numel() * 16),
-               "api": "ElementalGenerator.calc_batch (host eigenvectors in, host elementals out)"}
+        e2e = {"value": world * nts / dt, "unit": "timeslices/s",
+               "h2d_bytes_per_step": B * Ne * V3 * 3 * 16, "d2h_bytes_per_step": int(host_out[:B].numel() * 16),
+               "api": "ElementalGenerator.calc_batch over all timed steps (pinned host eigenvectors in, pinned host "
+                      "elementals out; host<->device copies of batch k+-1 overlap the compute of batch k)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

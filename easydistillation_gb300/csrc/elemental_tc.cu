@@ -36,7 +36,7 @@ int launch_phases(Latt L, const int* moms, int nmom, cplx<double>* out, cudaStre
 
 #include "tc_config.cuh"
 
-enum TcKind { TC_F16 = 1, TC_BF16 = 2, TC_TF32 = 3 };
+enum TcKind { TC_F16 = 1, TC_BF16 = 2, TC_TF32 = 3, TC_OZAKI = 4 };
 
 struct TcJob {
   int left, right0, nright, tile0, mt, nt;
@@ -294,6 +294,7 @@ __global__ void tc_phase_kernel(const cplx<double>* __restrict__ ph, long long n
 
 #include "tc_pair_gemm.cuh"
 #include "tc_fac_gemm.cuh"
+#include "tc_ozaki_gemm.cuh"
 
 // ------------------------------------------------------------ factorised-phase operands
 
@@ -381,6 +382,8 @@ static int tc_kind_of(int mode) {
       return TC_BF16;
     case ED_MODE_TF32X3:
       return TC_TF32;
+    case ED_MODE_OZAKI_I8:
+      return TC_OZAKI;
     default:
       return 0;
   }
@@ -397,7 +400,8 @@ static size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 // Pxy * Pz combinations the GEMM forms are not requested.
 void tc_fac_setup(ed_elemental_plan* P) {
   P->fac = false;
-  if (!tc_kind_of(P->mode) || P->custom || P->no_factor || P->nmom > 127) return;
+  const bool ozaki = tc_kind_of(P->mode) == TC_OZAKI;  // runs on factorised operands only
+  if (!tc_kind_of(P->mode) || P->custom || (P->no_factor && !ozaki) || P->nmom > 127) return;
   std::vector<int> xy, z, ai(P->nmom), ci(P->nmom);
   for (int m = 0; m < P->nmom; ++m) {
     const int px = P->moms[3 * m], py = P->moms[3 * m + 1], pz = P->moms[3 * m + 2];
@@ -410,7 +414,8 @@ void tc_fac_setup(ed_elemental_plan* P) {
     ci[m] = c;
   }
   const int pxy = (int)xy.size() / 2, pz = (int)z.size();
-  if (pxy * pz > kMaxFac || 4 * pxy * pz > 5 * P->nmom) return;
+  if (pxy * pz > kMaxFac || (!ozaki && 4 * pxy * pz > 5 * P->nmom)) return;
+  if (ozaki && (pxy > OZ_MAX_VAR || pz > OZ_MAX_VAR)) return;  // the row-maximum kernel keeps <= 16 per row
   std::vector<signed char> pidx(pxy * pz, -1);
   for (int m = 0; m < P->nmom; ++m) {
     signed char& e = pidx[ai[m] * pz + ci[m]];
@@ -427,7 +432,7 @@ void tc_fac_setup(ed_elemental_plan* P) {
   }
   const long long rb = (long long)P->nbatch * (long long)lchain.size() * pxy * P->Ne;
   const long long ra = (long long)P->nbatch * P->nchain * pz * P->Ne;
-  if (4 * rb >= (1LL << 31) || 4 * ra >= (1LL << 31) || (int)lchain.size() > kMaxDeriv) return;
+  if (OZ_BP * rb >= (1LL << 31) || OZ_AP * ra >= (1LL << 31) || (int)lchain.size() > kMaxDeriv) return;
   P->fac = true;
   P->fac_pxy = pxy;
   P->fac_pz = pz;
@@ -461,9 +466,35 @@ static FacLayout fac_layout(const ed_elemental_plan* P) {
   return L;
 }
 
+// Extra workspace of the Ozaki path: scalars, FP64 and complex64 factor
+// tables (as fac_layout), per-row maxima of A and B, the A digit planes
+// [8][RA][K] and B digit planes [12][RB][K] (int8).  The pair results go
+// straight to the plan's complex128 G buffer.
+struct OzLayout {
+  long long rb, ra;
+  size_t fxy, fz, fxy32, fz32, amax, bmax, apl, bpl, total;
+};
+static OzLayout oz_layout(const ed_elemental_plan* P) {
+  OzLayout L;
+  const size_t K = 3ull * P->V3;
+  L.rb = (long long)P->nbatch * (long long)P->fac_lchain.size() * P->fac_pxy * P->Ne;
+  L.ra = (long long)P->nbatch * P->nchain * P->fac_pz * P->Ne;
+  L.fxy = up256(sizeof(TcScalars));
+  L.fz = L.fxy + up256((size_t)P->fac_pxy * P->V3 * 16);
+  L.fxy32 = L.fz + up256((size_t)P->fac_pz * P->V3 * 16);
+  L.fz32 = L.fxy32 + up256((size_t)P->fac_pxy * P->V3 * 8);
+  L.amax = L.fz32 + up256((size_t)P->fac_pz * P->V3 * 8);
+  L.bmax = L.amax + up256((size_t)L.ra * 4);
+  L.apl = L.bmax + up256((size_t)L.rb * 4);
+  L.bpl = L.apl + up256((size_t)OZ_AP * L.ra * K);
+  L.total = L.bpl + up256((size_t)OZ_BP * L.rb * K);
+  return L;
+}
+
 size_t tc_extra_workspace(const ed_elemental_plan* P) {
   const int kind = tc_kind_of(P->mode);
   if (!kind) return 0;
+  if (kind == TC_OZAKI) return P->fac ? oz_layout(P).total : 0;
   if (P->fac) return fac_layout(P).total;
   const size_t R = (size_t)P->nchain * P->nbatch * P->Ne;
   const size_t K = 3ull * P->V3;
@@ -477,6 +508,18 @@ int tc_plan_check(ed_elemental_plan* P) {
   if (P->V3 % 32 != 0) {
     set_error("tensor-core elemental modes need Lx*Ly*Lz divisible by 32 (got %d)", P->V3);
     return ED_ERR_UNSUPPORTED;
+  }
+  if (P->tc_kind == TC_OZAKI) {
+    if (!P->fac) {
+      set_error("the Ozaki int8 mode needs a distinct momentum list of at most %d (px,py) x pz combinations "
+                "(and not a generic pair plan)", kMaxFac);
+      return ED_ERR_UNSUPPORTED;
+    }
+    if (3LL * P->V3 > OZ_MAX_K) {
+      set_error("the Ozaki int8 mode keeps int32 sums exact for 3*Lx*Ly*Lz <= %lld (got %lld)", OZ_MAX_K,
+                3LL * P->V3);
+      return ED_ERR_UNSUPPORTED;
+    }
   }
   const long long rows = 4LL * P->nchain * P->nbatch * P->Ne;
   if (rows >= (1LL << 31) || 3LL * P->V3 >= (1LL << 31)) {
@@ -693,8 +736,238 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   return ED_OK;
 }
 
+// ---- Ozaki int8 path
+// Per-row maxima of the variant rows: one block per input row (slot, i), all
+// nvar variants of that row; max over k of |re|, |im| of the FP32 product.
+template <bool LEFT>
+__global__ void oz_rowmax_kernel(const cplx<float>* __restrict__ chains, TcFacSlots sl, int Ne, int nvar,
+                                 const cplx<float>* __restrict__ fac, int V3, float* __restrict__ rowmax) {
+  __shared__ float red[OZ_MAX_VAR][8];
+  const int row = blockIdx.x;
+  const int slot = row / Ne, i = row - (row / Ne) * Ne;
+  const int chain = LEFT ? (slot / sl.nl) * sl.nchain + sl.lchain[slot % sl.nl] : slot;
+  const float4* src = reinterpret_cast<const float4*>(chains + ((long long)chain * Ne + i) * 3LL * V3);
+  const int K2 = 3 * V3 / 2;
+  float m[OZ_MAX_VAR];
+#pragma unroll
+  for (int a = 0; a < OZ_MAX_VAR; ++a) m[a] = 0.f;
+  for (int kp = threadIdx.x; kp < K2; kp += blockDim.x) {
+    const float4 v = src[kp];
+    const int site = (2 * kp) % V3;
+#pragma unroll
+    for (int a = 0; a < OZ_MAX_VAR; ++a) {
+      if (a >= nvar) break;
+      const float4 f = *reinterpret_cast<const float4*>(fac + (long long)a * V3 + site);
+      float r0, i0, r1, i1;
+      if constexpr (LEFT) {
+        r0 = v.x * f.x + v.y * f.y;
+        i0 = v.x * f.y - v.y * f.x;
+        r1 = v.z * f.z + v.w * f.w;
+        i1 = v.z * f.w - v.w * f.z;
+      } else {
+        r0 = f.x * v.x - f.y * v.y;
+        i0 = f.x * v.y + f.y * v.x;
+        r1 = f.z * v.z - f.w * v.w;
+        i1 = f.z * v.w + f.w * v.z;
+      }
+      m[a] = fmaxf(m[a], fmaxf(fmaxf(fabsf(r0), fabsf(i0)), fmaxf(fabsf(r1), fabsf(i1))));
+    }
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int a = 0; a < OZ_MAX_VAR; ++a) {
+    if (a >= nvar) break;
+    float x = m[a];
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (lane == 0) red[a][warp] = x;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nvar) {
+    float x = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x = fmaxf(x, red[threadIdx.x][w]);
+    rowmax[((long long)slot * nvar + threadIdx.x) * Ne + i] = x;
+  }
+}
+
+// four signed 6-bit digits of v in (-1, 1): v = sum_s d_s 2^(-6(s+1)) up to
+// 2^-25; every step is exact in FP32 (x - rint(x) keeps the fraction bits of x)
+__device__ __forceinline__ void oz_digits(float v, int (&d)[OZ_S]) {
+  float x = v * 64.f;
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) {
+    const float r = rintf(x);
+    d[s] = (int)r;
+    x = (x - r) * 64.f;
+  }
+}
+
+// Digit planes of the variant rows: each thread handles 4 consecutive k of
+// one input row and writes 4-byte words (4 int8 digits) per plane.
+//   A (right, !LEFT): planes q = s*2 + {re, im};  B (LEFT): q = s*3 + {re, im, -im}
+template <bool LEFT>
+__global__ void oz_digit_kernel(const cplx<float>* __restrict__ chains, TcFacSlots sl, int nrows, int Ne, int nvar,
+                                const cplx<float>* __restrict__ fac, int V3, const float* __restrict__ rowmax,
+                                long long Rplane, int8_t* __restrict__ planes) {
+  constexpr int NP = LEFT ? 3 : 2;
+  const long long K = 3LL * V3;
+  const int K4 = (int)(K / 4);
+  for (int row = blockIdx.y; row < nrows; row += gridDim.y) {
+    const int slot = row / Ne, i = row - (row / Ne) * Ne;
+    const int chain = LEFT ? (slot / sl.nl) * sl.nchain + sl.lchain[slot % sl.nl] : slot;
+    const float4* src = reinterpret_cast<const float4*>(chains + ((long long)chain * Ne + i) * K);
+    for (int kq = blockIdx.x * blockDim.x + threadIdx.x; kq < K4; kq += gridDim.x * blockDim.x) {
+      const float4 v0 = src[2 * kq], v1 = src[2 * kq + 1];
+      const float xr[4] = {v0.x, v0.z, v1.x, v1.z}, xi[4] = {v0.y, v0.w, v1.y, v1.w};
+      const int site = (4 * kq) % V3;  // 4 | V3: the four elements share a colour plane
+      for (int a = 0; a < nvar; ++a) {
+        const long long orow = ((long long)slot * nvar + a) * Ne + i;
+        int e = 0;
+        const float mx = rowmax[orow];
+        if (mx > 0.f) frexpf(mx, &e);
+        const float4 f0 = *reinterpret_cast<const float4*>(fac + (long long)a * V3 + site);
+        const float4 f1 = *reinterpret_cast<const float4*>(fac + (long long)a * V3 + site + 2);
+        const float fr[4] = {f0.x, f0.z, f1.x, f1.z}, fi[4] = {f0.y, f0.w, f1.y, f1.w};
+        uint32_t wre[OZ_S] = {}, wim[OZ_S] = {}, wneg[OZ_S] = {};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          float re, im;
+          if constexpr (LEFT) {
+            re = xr[u] * fr[u] + xi[u] * fi[u];
+            im = xr[u] * fi[u] - xi[u] * fr[u];
+          } else {
+            re = fr[u] * xr[u] - fi[u] * xi[u];
+            im = fr[u] * xi[u] + fi[u] * xr[u];
+          }
+          int dr[OZ_S], di[OZ_S];
+          oz_digits(ldexpf(re, -e), dr);
+          oz_digits(ldexpf(im, -e), di);
+#pragma unroll
+          for (int s = 0; s < OZ_S; ++s) {
+            wre[s] |= (uint32_t)(dr[s] & 0xff) << (8 * u);
+            wim[s] |= (uint32_t)(di[s] & 0xff) << (8 * u);
+            wneg[s] |= (uint32_t)((-di[s]) & 0xff) << (8 * u);
+          }
+        }
+        uint32_t* P = reinterpret_cast<uint32_t*>(planes);
+        const long long w = orow * (K / 4) + kq, plane = Rplane * (K / 4);
+#pragma unroll
+        for (int s = 0; s < OZ_S; ++s) {
+          P[(s * NP + 0) * plane + w] = wre[s];
+          P[(s * NP + 1) * plane + w] = wim[s];
+          if constexpr (LEFT) P[(s * NP + 2) * plane + w] = wneg[s];
+        }
+      }
+    }
+  }
+}
+
+static int encode_i8(CUtensorMap* map, void* base, long long K, long long rows) {
+  EncodeFn enc = get_encode();
+  if (!enc) {
+    set_error("cuTensorMapEncodeTiled is unavailable from the driver");
+    return ED_ERR_CUDA;
+  }
+  cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)K};
+  cuuint32_t box[2] = {(cuuint32_t)OZ_KS, (cuuint32_t)OZ_BM};
+  cuuint32_t estride[2] = {1, 1};
+  CUresult cr = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, gdim, gstride, box, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+    return ED_ERR_CUDA;
+  }
+  return ED_OK;
+}
+
+static int launch_ozaki(const ed_elemental_plan* P, const cplx<float>* chains, cplx<double>* G, void* extra,
+                        cudaStream_t stream, int nb) {
+  const OzLayout lay = oz_layout(P);
+  char* X = (char*)extra;
+  TcScalars* sc = (TcScalars*)X;
+  cplx<double>* fxy = (cplx<double>*)(X + lay.fxy);
+  cplx<double>* fz = (cplx<double>*)(X + lay.fz);
+  cplx<float>* fxy32 = (cplx<float>*)(X + lay.fxy32);
+  cplx<float>* fz32 = (cplx<float>*)(X + lay.fz32);
+  float* amax = (float*)(X + lay.amax);
+  float* bmax = (float*)(X + lay.bmax);
+  int8_t* apl = (int8_t*)(X + lay.apl);
+  int8_t* bpl = (int8_t*)(X + lay.bpl);
+  const long long K = 3LL * P->V3;
+  const int nl = (int)P->fac_lchain.size(), pxy = P->fac_pxy, pz = P->fac_pz, Ne = P->Ne;
+  const Latt L{P->Lx, P->Ly, P->Lz};
+
+  cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(TcScalars), stream);  // scale 2^0, status 0
+  if (e != cudaSuccess) return cuda_status(e, "tc scalars reset");
+  const int sms = num_sms();
+  std::vector<int> m3;
+  for (int a = 0; a < pxy; ++a) m3.insert(m3.end(), {P->fac_xy[2 * a], P->fac_xy[2 * a + 1], 0});
+  int rc = launch_phases(L, m3.data(), pxy, fxy, stream);
+  if (rc) return rc;
+  m3.clear();
+  for (int c = 0; c < pz; ++c) m3.insert(m3.end(), {0, 0, P->fac_z[c]});
+  rc = launch_phases(L, m3.data(), pz, fz, stream);
+  if (rc) return rc;
+  tc_phase_kernel<<<sms, 256, 0, stream>>>(fxy, (long long)pxy * P->V3, sc, fxy32);
+  tc_phase_kernel<<<sms, 256, 0, stream>>>(fz, (long long)pz * P->V3, sc, fz32);
+  ED_RETURN_LAUNCH("factor tables");
+
+  TcFacSlots sl;
+  sl.nl = nl;
+  sl.nchain = P->nchain;
+  for (int s = 0; s < nl; ++s) sl.lchain[s] = P->fac_lchain[s];
+  const int lrows = nb * nl * Ne, rrows = nb * P->nchain * Ne;
+  oz_rowmax_kernel<true><<<lrows, 256, 0, stream>>>(chains, sl, Ne, pxy, fxy32, P->V3, bmax);
+  oz_rowmax_kernel<false><<<rrows, 256, 0, stream>>>(chains, sl, Ne, pz, fz32, P->V3, amax);
+  const int kx = (int)ceil_div(K / 4, 256);
+  oz_digit_kernel<true><<<dim3(kx, std::min(lrows, 65535)), 256, 0, stream>>>(chains, sl, lrows, Ne, pxy, fxy32,
+                                                                               P->V3, bmax, lay.rb, bpl);
+  oz_digit_kernel<false><<<dim3(kx, std::min(rrows, 65535)), 256, 0, stream>>>(chains, sl, rrows, Ne, pz, fz32,
+                                                                                P->V3, amax, lay.ra, apl);
+  ED_RETURN_LAUNCH("Ozaki digit planes");
+
+  CUtensorMap amap, bmap;
+  if ((rc = encode_i8(&amap, apl, K, OZ_AP * lay.ra))) return rc;
+  if ((rc = encode_i8(&bmap, bpl, K, OZ_BP * lay.rb))) return rc;
+
+  TcFacTable tab;
+  tab.njobs = nb * P->jobs_per_t;
+  tab.pxy = pxy;
+  tab.pz = pz;
+  for (int q = 0; q < kMaxFac; ++q) tab.pidx[q] = q < pxy * pz ? P->fac_pidx[q] : (signed char)-1;
+  int tiles = 0;
+  for (int k = 0; k < tab.njobs; ++k) {
+    const Job& j = P->jobs[k];
+    const int b = k / P->jobs_per_t;
+    const int slot = b * nl + P->fac_lslot[P->jobs[k % P->jobs_per_t].left];
+    TcFacJob& d = tab.j[k];
+    d.arow0 = j.right0 * pz * Ne;
+    d.brow0 = slot * pxy * Ne;
+    d.nright = j.nright;
+    d.g_off = j.g_off;
+    d.mt = (int)ceil_div((long long)j.nright * pz * Ne, OZ_BM);
+    d.nt = (int)ceil_div((long long)pxy * Ne, OZ_BN);
+    d.tile0 = tiles;
+    tiles += d.mt * d.nt;
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    e = cudaFuncSetAttribute(tc_ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "Ozaki kernel smem attribute");
+    attr_set = true;
+  }
+  if (P->prof_start) cudaEventRecord(P->prof_start, stream);
+  tc_ozaki_gemm_kernel<<<tiles, OZ_THREADS, OZ_SMEM, stream>>>(amap, bmap, tab, Ne, P->V3, (int)lay.ra, (int)lay.rb,
+                                                              amax, bmax, sc, G);
+  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
+  ED_RETURN_LAUNCH("Ozaki int8 pair GEMM");
+  return ED_OK;
+}
+
 int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
                         cplx<double>* G, void* extra, cudaStream_t stream, int nb) {
+  if (P->tc_kind == TC_OZAKI) return launch_ozaki(P, chains, G, extra, stream, nb);
   if (P->fac) {
     switch (P->tc_kind) {
       case TC_F16:

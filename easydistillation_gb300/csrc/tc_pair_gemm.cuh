@@ -10,7 +10,7 @@
 // products first and the four dominant hi.hi products last, so only those
 // four additions round at the partial's full magnitude.  Eight drain warps
 // read every finished buffer (tcgen05.ld), add it into FP32 register sums
-// (round-to-nearest) and hand the buffer back; every 64 k-blocks the register
+// (round-to-nearest) and hand the buffer back; every TC_FLUSH_KB k-blocks the register
 // sums are added into a double-float (hi, lo FP32 pair) result in global
 // memory with two-sum arithmetic (FP64 units are too slow on this part for a
 // per-flush FP64 update), converted to complex128 after the kernel.

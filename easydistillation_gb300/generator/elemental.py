@@ -184,20 +184,42 @@ class ElementalGenerator:
         self._stage_event.record()
         return dev
 
+    def _fetch_chunk(self, chunk, slot, stream):
+        """Eigenvectors of the timeslices in ``chunk`` into the device input
+        buffers of ``slot``: direct asynchronous copies on ``stream`` when the
+        eigenvector data is a (pinned) torch tensor, else through the pinned
+        stage (:meth:`_read_vectors`)."""
+        Lx, Ly, Lz, Lt = self.latt_size
+        Ne, n = self.Ne, Lx * Ly * Lz * NC
+        data = self._eigenvector_data
+        bufs = self._in_bufs[slot]
+        with torch.cuda.stream(stream):
+            for k, t in enumerate(chunk):
+                if isinstance(data, torch.Tensor):
+                    bufs[k].copy_(data[t, :Ne].reshape(Ne, n), non_blocking=True)
+                else:
+                    bufs[k].copy_(self._read_vectors(t))
+        return bufs[: len(chunk)]
+
     def calc_batch(self, ts, out: torch.Tensor = None, batch: int = None):
         """Elementals of several timeslices, ``[len(ts), Nderiv, Nmom, Ne, Ne]``.
 
         Timeslices go through batched plans of up to ``batch`` timeslices
         (default: as many as :func:`admit_batch` allows in free HBM, at most
-        8), one pair-contraction launch per batch."""
+        8), one pair-contraction launch per batch.  The batches are pipelined:
+        the eigenvectors of batch k+1 are copied to the device on one stream
+        and, when ``out`` is a host tensor (pinned for asynchronous copies),
+        the elementals of batch k-1 are copied back on another while batch k
+        computes."""
         if self._U is None:
             raise RuntimeError("call load(key) before calc_batch(ts)")
         Lx, Ly, Lz, Lt = self.latt_size
         V3 = Lx * Ly * Lz
         ts = list(ts)
+        shape = (self.num_derivative, self.num_momentum, self.Ne, self.Ne)
         if out is None:
-            out = torch.empty((len(ts), self.num_derivative, self.num_momentum, self.Ne, self.Ne),
-                              dtype=torch.complex128, device=self.device)
+            out = torch.empty((len(ts),) + shape, dtype=torch.complex128, device=self.device)
+        host_out = out.device.type == "cpu"
         if batch is None:
             batch = admit_batch(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list, self.precision,
                                 self.device, max_batch=min(8, len(ts)), factorise=self.factorise)
@@ -205,14 +227,61 @@ class ElementalGenerator:
         if plan is None or plan.batch != batch:
             plan = self._bplan = ElementalPlan(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list,
                                                self.precision, self.device, batch=batch, factorise=self.factorise)
-        for s0 in range(0, len(ts), batch):
-            chunk = ts[s0 : s0 + batch]
-            vecs = [self._read_vectors(t) for t in chunk]
+        evdt = self._eigenvector_data.dtype if isinstance(self._eigenvector_data, torch.Tensor) else torch.complex128
+        if getattr(self, "_in_bufs", None) is None or len(self._in_bufs[0]) != batch or \
+                self._in_bufs[0][0].dtype != evdt:
+            self._in_bufs = [[torch.empty((self.Ne, V3 * NC), dtype=evdt, device=self.device) for _ in range(batch)]
+                             for _ in range(2)]
+            self._streams = (torch.cuda.Stream(self.device), torch.cuda.Stream(self.device))
+        if host_out and (getattr(self, "_out_bufs", None) is None or self._out_bufs[0].shape[0] != batch):
+            self._out_bufs = [torch.empty((batch,) + shape, dtype=torch.complex128, device=self.device)
+                              for _ in range(2)]
+        h2d, d2h = self._streams
+        compute = torch.cuda.current_stream(self.device)
+        chunks = [ts[s0 : s0 + batch] for s0 in range(0, len(ts), batch)]
+        in_ready = [torch.cuda.Event(), torch.cuda.Event()]
+        in_free = [None, None]   # compute finished reading the input slot
+        out_free = [None, None]  # the host copy of an output slot finished
+        h2d.wait_stream(compute)  # links and earlier work on the compute stream come first
+        vecs = self._fetch_chunk(chunks[0], 0, h2d)
+        in_ready[0].record(h2d)
+        for k, chunk in enumerate(chunks):
+            slot = k % 2
+            if k + 1 < len(chunks):  # prefetch the next batch into the other slot
+                nslot = 1 - slot
+                if in_free[nslot] is not None:
+                    h2d.wait_event(in_free[nslot])
+                nvecs = self._fetch_chunk(chunks[k + 1], nslot, h2d)
+                in_ready[nslot].record(h2d)
+            compute.wait_event(in_ready[slot])
+            if host_out:
+                if out_free[slot] is not None:
+                    compute.wait_event(out_free[slot])
+                outs = [self._out_bufs[slot][j] for j in range(len(chunk))]
+            else:
+                s0 = k * batch
+                outs = [out[s0 + j] for j in range(len(chunk))]
             links = [self._U[:, t] for t in chunk]
-            plan.run_batch(links, Lt * V3 * 9, 9, vecs, [out[s0 + k] for k in range(len(chunk))],
-                           blend=self.stocastic_coeff)
+            plan.run_batch(links, Lt * V3 * 9, 9, vecs, outs, blend=self.stocastic_coeff)
+            ev = torch.cuda.Event()
+            ev.record(compute)
+            in_free[slot] = ev
+            if host_out:
+                d2h.wait_event(ev)
+                with torch.cuda.stream(d2h):
+                    out[k * batch : k * batch + len(chunk)].copy_(self._out_bufs[slot][: len(chunk)],
+                                                                  non_blocking=True)
+                e2 = torch.cuda.Event()
+                e2.record(d2h)
+                out_free[slot] = e2
+            if k + 1 < len(chunks):
+                vecs = nvecs
+        compute.wait_stream(h2d)
+        compute.wait_stream(d2h)
         if self.precision != "fp64":
-            plan.check_status()
+            plan.check_status()  # synchronises the compute stream
+        elif host_out:
+            compute.synchronize()
         return out
 
     def calc(self, t: int):

@@ -169,7 +169,7 @@ def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
 
 
 #: elemental arithmetic modes (ED_MODE_* in include/easydist_gb300.h)
-MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3}
+MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3, "ozaki_i8": 4}
 
 
 class ElementalPlan:

@@ -52,6 +52,11 @@ extern "C" {
 #define ED_MODE_F16X3 1  /* tcgen05: scaled fp16 hi/lo split, 3 products per real product */
 #define ED_MODE_BF16X3 2 /* tcgen05: bf16 hi/lo split, 3 products per real product */
 #define ED_MODE_TF32X3 3 /* tcgen05 kind::tf32: tf32 hi/lo split, 3 products per real product */
+#define ED_MODE_OZAKI_I8 4 /* Ozaki scheme: per-row scaled operands cut into four signed 6-bit
+                            * int8 slices, slice products with s+t <= 3 accumulated exactly in
+                            * int32 (mma.sync s8), recombined in FP64.  Needs a momentum list that
+                            * factorises into distinct (px,py) x pz combinations (at most 128)
+                            * and 3*Lx*Ly*Lz <= 163840. */
 /* Flag OR-ed into a tensor-core mode at plan creation: keep the GEMM whose
  * phase-weighted operand is formed inside the kernel even when the momentum
  * list factorises into {(px,py)} x {pz} (by default such plans use the

@@ -1,8 +1,9 @@
-"""Split-precision tensor-core elementals (tcgen05) against the FP64 oracle.
+"""Split-precision tensor-core elementals (tcgen05) and the Ozaki int8-slice
+variant against the FP64 oracle.
 
 Tolerances (relative Frobenius error over the whole [Nderiv, Nmom, Ne, Ne]
-block): f16x3 and tf32x3 <= 1e-6 (the bar for the split-precision path),
-bf16x3 <= 1e-4 (two 8-bit-mantissa slices)."""
+block): f16x3, tf32x3 and ozaki_i8 <= 1e-6 (the bar for the split-precision
+path), bf16x3 <= 1e-4 (two 8-bit-mantissa slices)."""
 
 import numpy as np
 import pytest
@@ -13,6 +14,7 @@ from tests.helpers import MemEigen, MemGauge, rel_err
 pytestmark = pytest.mark.gpu
 
 TOL = {"f16x3": 1e-6, "tf32x3": 1e-6, "bf16x3": 1e-4}
+TOL_OZAKI = 1e-6  # four signed 6-bit slices of the complex64 operands, products with s + t <= 3
 
 
 def _run(latt, Ne, num_nabla, moms, mode, t=0, seed=5):
@@ -124,3 +126,26 @@ def test_fac_long_k():
     gen, E, ref = _run_fac([16, 16, 16, 1], 24, 1, R.mom_dict_to_list(3), "f16x3", True)
     assert gen._plan.factorised == (9, 3)
     assert rel_err(E, ref) < TOL["f16x3"]
+
+
+# ---------------------------------------------------------------- Ozaki int8 slices
+@pytest.mark.parametrize("num_nabla, moms", [(2, "all27"), (1, "first7")])
+def test_ozaki_small(num_nabla, moms):
+    """int8 slice products with exact int32 sums: 27 momenta (9 x 3 variants) and the
+    7 momenta with |p|^2 <= 1 (5 x 3 variants, 8 of the 15 combinations unused)"""
+    m = R.mom_dict_to_list(3) if moms == "all27" else R.mom_dict_to_list(3)[:7]
+    gen, E, ref = _run_fac([4, 4, 4, 2], 6, num_nabla, m, "ozaki_i8", True, t=1)
+    assert gen._plan.factorised is not None
+    assert rel_err(E, ref) < TOL_OZAKI
+
+
+def test_ozaki_many_ragged_tiles():
+    """Ne = 150: 64 x 64 tiles ragged in both directions"""
+    gen, E, ref = _run_fac([8, 8, 4, 1], 150, 1, R.mom_dict_to_list(3), "ozaki_i8", True)
+    assert rel_err(E, ref) < TOL_OZAKI
+
+
+def test_ozaki_long_k():
+    """K = 3 * 16^3 = 12288 exact int32 accumulation"""
+    gen, E, ref = _run_fac([16, 16, 16, 1], 24, 1, R.mom_dict_to_list(3), "ozaki_i8", True)
+    assert rel_err(E, ref) < TOL_OZAKI

@@ -114,3 +114,14 @@ def test_factorised_phase_selection(moms, mode, factorise, expect):
         # the factorised workspace holds both variant operands: larger than the on-chip-phase one
         q = ElementalPlan([8, 8, 4, 2], 10, 2, moms, mode, device="cpu", factorise=False)
         assert q.factorised is None and p.workspace_bytes > q.workspace_bytes
+
+
+def test_ozaki_plan_limits():
+    """The Ozaki int8 mode needs factorising momenta (any unused share) and K <= 163840."""
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.ops import ElementalPlan
+
+    p = ElementalPlan([8, 8, 4, 2], 10, 1, mom_dict_to_list(3)[:7], "ozaki_i8", device="cpu")
+    assert p.factorised == (5, 3)
+    with pytest.raises(Exception):
+        ElementalPlan([40, 40, 36, 2], 10, 1, [(0, 0, 0)], "ozaki_i8", device="cpu")
