@@ -163,6 +163,9 @@ def make_inputs(latt, Ne, seed=2, distinct_t=RESIDENT_T):
 # total), and one phase-weighted zgemm per subset and momentum.
 REF_HOPS = 78
 REF_SUBSETS = 43
+# FP64 FMA throughput of this part (register-resident DFMA loop on all SMs)
+FP64_PEAK_TFLOPS = 1.25
+FP64_PEAK_SOURCE = "nominal GB300 FP64"
 
 
 def cpu_reference_sample(latt, Ne, threads, reps=2):
@@ -227,14 +230,18 @@ def bench_stencil(U, latt, dev, reps=20):
     them from HBM."""
     import torch
 
-    from easydistillation_gb300.ops import laplacian, links_to_soa
+    from easydistillation_gb300.ops import laplacian, laplacian_config, laplacian_status, links_to_soa
 
     Lx, Ly, Lz, Lt = latt
     V3 = Lx * Ly * Lz
     peaks = load_peaks()
     pk, src = (peaks["hbm_gbs"], "measured") if "hbm_gbs" in peaks else (6800.0, "fallback")
     out = {}
-    for name, dt, s in (("c64", torch.complex64, 8), ("c128", torch.complex128, 16)):
+    variants = (("c64", torch.complex64, 8, False, "laplacian_kernel<float,2>"),
+                ("c64_tma", torch.complex64, 8, True, "laplacian_tma_kernel (input planes staged by TMA)"),
+                ("c128", torch.complex128, 16, False, "laplacian_kernel<double,1>"))
+    for name, dt, s, tma, kname in variants:
+        laplacian_config(tma)
         links = links_to_soa(U, latt, dtype=dt)
         F = torch.randn((Lt, 1, 3, V3), dtype=dt, device=dev)
         G = torch.empty_like(F)
@@ -250,14 +257,20 @@ def bench_stencil(U, latt, dev, reps=20):
                 laplacian(links, G, latt, out=F)
         b.record()
         torch.cuda.synchronize()
+        laplacian_status()
         ms = a.elapsed_time(b) / reps
         nbytes = V3 * Lt * (27 * s + 6 * s)
         gbs = nbytes / ms / 1e6
         out[name] = {"bound": "hbm", "achieved": gbs, "peak": pk, "unit": "GB/s", "frac": gbs / pk,
                      "peak_source": src, "traffic": None, "bytes_per_launch": nbytes, "kernel_ms": ms,
-                     "kernel": f"laplacian_kernel<{'float,2' if s == 8 else 'double,1'}>",
-                     "workload": f"{Lx}^3 x {Lt} timeslices x 1 vector"}
+                     "kernel": kname, "workload": f"{Lx}^3 x {Lt} timeslices x 1 vector"}
+        if s == 16:
+            # FP64 arithmetic, not HBM, bounds the complex128 stencil on this part: 444 flops per site
+            fl = 444.0 * V3 * Lt / ms / 1e9
+            out[name].update({"bound": "fp64", "fp64_tflops": fl, "fp64_peak_tflops": FP64_PEAK_TFLOPS,
+                              "fp64_frac": fl / FP64_PEAK_TFLOPS, "fp64_peak_source": FP64_PEAK_SOURCE})
         del links, F, G
+    laplacian_config(False)
     return out
 
 

@@ -69,6 +69,8 @@ _SIGNATURES = {
     ),
     "ed_pair_run": ([_vp, _vp, _vp, _vp, _c.c_size_t, _vp], _i),
     "ed_elemental_describe": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
+    "ed_laplacian_config": ([_i], _i),
+    "ed_laplacian_status": ([_c.POINTER(_i), _vp], _i),
     "ed_elemental_factorised": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
 }
 

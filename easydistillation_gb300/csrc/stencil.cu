@@ -11,9 +11,22 @@
 // 3 output complex numbers per site.  Every thread handles S consecutive
 // x-sites so that every plane access is one 128-bit load (S=1 for c128 =
 // double2, S=2 for c64 = float4).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace ed {
+
+// 1: complex64 Laplacians go through the TMA-staged kernel where it applies.
+// Off by default: at 32^3 x 64 timeslices it reaches 68 % of the measured HBM
+// copy bandwidth against 83 % for the kernel that reads neighbours through
+// L1/L2 (the links, 27 of the 33 complex numbers per site, dominate the
+// traffic, and the per-plane block barrier costs latency hiding).
+static int g_stencil_tma = 0;
+static bool laplacian_tma_enabled() { return g_stencil_tma != 0; }
 
 template <typename T, int S>
 struct Pack;
@@ -226,12 +239,254 @@ __global__ void __launch_bounds__(128) hop_kernel(Latt L, int d, int nvec, const
   }
 }
 
+// ------------------------------------------------------------ TMA-staged Laplacian (complex64)
+// One block marches through a slab of z planes of one (timeslice, vector).
+// The input colour planes of z-1, z and z+1 sit in a ring of four shared-memory
+// slots that TMA fills (plane z+2 lands while z computes), so every input
+// value is read from HBM once per slab (plus one halo plane at each end);
+// links are read with 128-bit loads, the backward links of x and y from the
+// neighbouring sites of the same plane and those of z from the plane just
+// finished (both L1/L2 resident).  Waits on the slot barriers are bounded: a
+// timeout sets the error word that ed_laplacian_status reports.
+
+constexpr int LT_THREADS = 256, LT_SLOTS = 4;
+constexpr long long LT_WAIT_CYCLES = 4000000000LL;  // ~2 s
+__device__ int g_stencil_error = 0;
+
+__device__ __forceinline__ uint32_t st_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool st_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(st_smem(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool st_wait(uint64_t* bar, uint32_t parity) {
+  if (st_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!st_try_wait(bar, parity))
+    if (clock64() - t0 > LT_WAIT_CYCLES) return false;
+  return true;
+}
+
+__global__ void __launch_bounds__(LT_THREADS) laplacian_tma_kernel(const __grid_constant__ CUtensorMap fmap, Latt L,
+                                                                   int zb, const cplx<float>* __restrict__ links,
+                                                                   long long link_tstride, cplx<float>* __restrict__ out,
+                                                                   long long out_tstride, float diag, int slot_bytes) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  uint64_t* bar = (uint64_t*)(sm + LT_SLOTS * slot_bytes);
+  __shared__ int failed;
+  const int Lx = L.Lx, Ly = L.Ly, Lz = L.Lz, V3 = L.V3(), P = Lx * Ly;
+  const int t = blockIdx.z, v = blockIdx.y;
+  const int z0 = blockIdx.x * zb, z1 = min(Lz, z0 + zb);
+  const int nplanes = (z1 - z0) + 2;  // plane j holds z = z0 - 1 + j (periodic)
+  if (threadIdx.x == 0) {
+    failed = 0;
+    for (int s = 0; s < LT_SLOTS; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st_smem(&bar[s])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int j) {
+    const int z = (z0 - 1 + j + Lz) % Lz;
+    const int s = j % LT_SLOTS;
+    uint8_t* dst = sm + s * slot_bytes;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(st_smem(&bar[s])), "r"(3 * P * 8)
+                 : "memory");
+    for (int c = 0; c < 3; ++c)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+          "[%2];" ::"r"(st_smem(dst + c * P * 8)),
+          "l"(&fmap), "r"(st_smem(&bar[s])), "r"(0), "r"(((v * 3 + c) * Lz + z) * Ly), "r"(t)
+          : "memory");
+  };
+  int issued_hi = -1;
+  if (threadIdx.x == 0)
+    for (int j = 0; j < LT_SLOTS && j < nplanes; ++j) {
+      issue(j);
+      issued_hi = j;
+    }
+  const cplx<float>* U = links + (long long)t * link_tstride;
+  cplx<float>* O = out + (long long)t * out_tstride + (long long)v * 3 * V3;
+  for (int z = z0; z < z1; ++z) {
+    const int jc = z - z0 + 1;
+    if (threadIdx.x == 0)
+      for (int j = jc - 1; j <= jc + 1; ++j)
+        if (!st_wait(&bar[j % LT_SLOTS], (j / LT_SLOTS) & 1)) failed = 1;
+    __syncthreads();
+    if (failed) break;
+    const float2* Fm = (const float2*)(sm + ((jc - 1) % LT_SLOTS) * slot_bytes);  // [c][y][x]
+    const float2* Fc = (const float2*)(sm + (jc % LT_SLOTS) * slot_bytes);
+    const float2* Fp = (const float2*)(sm + ((jc + 1) % LT_SLOTS) * slot_bytes);
+    const int zm = wrap_dec(z, Lz), zp = wrap_inc(z, Lz);
+    for (int q = threadIdx.x; q < P / 2; q += LT_THREADS) {
+      const int x0 = (2 * q) % Lx, y = (2 * q) / Lx;
+      const int p0 = y * Lx + x0;  // in-plane index of the first of the two sites
+      const int s0 = z * P + p0;
+      const int xm = wrap_dec(x0, Lx), xp2 = (x0 + 2) % Lx;
+      const int ym = wrap_dec(y, Ly), yp = wrap_inc(y, Ly);
+      cplx<float> f[3][2], hop[2][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float4 a = *reinterpret_cast<const float4*>(Fc + c * P + p0);
+        f[c][0] = mk(a.x, a.y);
+        f[c][1] = mk(a.z, a.w);
+      }
+#pragma unroll
+      for (int s = 0; s < 2; ++s)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) hop[s][c] = mk(0.f, 0.f);
+      // ---- x: forward links at s0 (both sites), backward U_x(x0-1) for site 0, U_x(x0) for site 1
+      {
+        cplx<float> uf[9][2], ubm[9], fxp[3], fxm[3];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) Pack<float, 2>::load(U + (0 * 9 + e) * V3 + s0, uf[e]);
+#pragma unroll
+        for (int e = 0; e < 9; ++e) ubm[e] = ld(U + (0 * 9 + e) * V3 + z * P + y * Lx + xm);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float2 a = Fc[c * P + y * Lx + xp2], b = Fc[c * P + y * Lx + xm];
+          fxp[c] = mk(a.x, a.y);
+          fxm[c] = mk(b.x, b.y);
+        }
+        cplx<float> u[9], w[3];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) u[e] = uf[e][0];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) w[c] = f[c][1];
+        mv_add(hop[0], u, w);       // U_x(x0) F(x0+1)
+        mvd_add(hop[0], ubm, fxm);  // U_x(x0-1)^dag F(x0-1)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) w[c] = f[c][0];
+        mvd_add(hop[1], u, w);      // U_x(x0)^dag F(x0)
+#pragma unroll
+        for (int e = 0; e < 9; ++e) u[e] = uf[e][1];
+        mv_add(hop[1], u, fxp);     // U_x(x0+1) F(x0+2)
+      }
+      // ---- y and z: forward links at s0, backward links at the neighbour sites
+#pragma unroll
+      for (int mu = 1; mu < 3; ++mu) {
+        const int sm_site = mu == 1 ? z * P + ym * Lx + x0 : zm * P + p0;
+        const float2* Fpl = mu == 1 ? Fc + yp * Lx + x0 : Fp + p0;
+        const float2* Fml = mu == 1 ? Fc + ym * Lx + x0 : Fm + p0;
+        cplx<float> uf[9][2], ub[9][2], fp[3][2], fm[3][2];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+          Pack<float, 2>::load(U + (mu * 9 + e) * V3 + s0, uf[e]);
+          Pack<float, 2>::load(U + (mu * 9 + e) * V3 + sm_site, ub[e]);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float4 a = *reinterpret_cast<const float4*>(Fpl + c * P);
+          const float4 b = *reinterpret_cast<const float4*>(Fml + c * P);
+          fp[c][0] = mk(a.x, a.y);
+          fp[c][1] = mk(a.z, a.w);
+          fm[c][0] = mk(b.x, b.y);
+          fm[c][1] = mk(b.z, b.w);
+        }
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          cplx<float> u[9], w[9], a[3], b[3];
+#pragma unroll
+          for (int e = 0; e < 9; ++e) {
+            u[e] = uf[e][s];
+            w[e] = ub[e][s];
+          }
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            a[c] = fp[c][s];
+            b[c] = fm[c][s];
+          }
+          mv_add(hop[s], u, a);
+          mvd_add(hop[s], w, b);
+        }
+      }
+      (void)zp;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        cplx<float> o[2];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) o[s] = mk(diag * f[c][s].re - hop[s][c].re, diag * f[c][s].im - hop[s][c].im);
+        Pack<float, 2>::store(O + c * V3 + s0, o);
+      }
+    }
+    __syncthreads();  // every thread is done with plane jc - 1
+    if (threadIdx.x == 0 && jc - 1 + LT_SLOTS < nplanes) {
+      issue(jc - 1 + LT_SLOTS);
+      issued_hi = jc - 1 + LT_SLOTS;
+    }
+  }
+  if (threadIdx.x == 0 && failed) {
+    atomicExch(&g_stencil_error, 1);
+    // let the copies still in flight land before the block's shared memory is released
+    for (int j = issued_hi; j >= 0 && j > issued_hi - LT_SLOTS; --j) st_wait(&bar[j % LT_SLOTS], (j / LT_SLOTS) & 1);
+  }
+}
+
+using StEncodeFn = PFN_cuTensorMapEncodeTiled_v12000;
+static StEncodeFn st_encoder() {
+  static StEncodeFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (StEncodeFn)p;
+  }
+  return fn;
+}
+
+// The TMA path serves complex64 when four planes fit in shared memory and the
+// plane rows meet the tensor-map limits; returns -1 when it does not apply.
+static int launch_laplacian_tma(Latt L, int nt, int nvec, const void* links, const void* in, long long its,
+                                void* out, long long ots, cudaStream_t stream) {
+  const int P = L.Lx * L.Ly;
+  const int slot_bytes = (3 * P * 8 + 127) / 128 * 128;
+  const int smem = LT_SLOTS * slot_bytes + 64;
+  if (L.Lx % 2 || 2 * L.Lx > 256 || L.Ly > 256 || smem > 200 * 1024 || (its * 8) % 16 || (P * 8) % 128) return -1;
+  if ((long long)3 * nvec * L.Lz * L.Ly >= (1LL << 31)) return -1;
+  StEncodeFn enc = st_encoder();
+  if (!enc) return -1;
+  CUtensorMap map;
+  cuuint64_t gdim[3] = {(cuuint64_t)(2 * L.Lx), (cuuint64_t)(3LL * nvec * L.Lz * L.Ly), (cuuint64_t)nt};
+  cuuint64_t gstride[2] = {(cuuint64_t)(8LL * L.Lx), (cuuint64_t)(its * 8)};
+  cuuint32_t box[3] = {(cuuint32_t)(2 * L.Lx), (cuuint32_t)L.Ly, 1};
+  cuuint32_t estride[3] = {1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(in), gdim, gstride, box, estride,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return -1;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(laplacian_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+        cudaSuccess)
+      return -1;
+    attr = true;
+  }
+  // about two waves of blocks (two blocks per SM when the planes are small)
+  const long long want = 4LL * num_sms();
+  int zb = (int)std::max(1LL, std::min<long long>(L.Lz, (long long)L.Lz * nt * nvec / want));
+  const int nslab = ceil_div(L.Lz, zb);
+  dim3 grid(nslab, nvec, nt);
+  laplacian_tma_kernel<<<grid, LT_THREADS, smem, stream>>>(map, L, zb, (const cplx<float>*)links, 27LL * L.V3(),
+                                                           (cplx<float>*)out, ots, 6.0f, slot_bytes);
+  ED_RETURN_LAUNCH("laplacian (TMA-staged)");
+  return ED_OK;
+}
+
 // ------------------------------------------------------------ launchers
 
 int launch_laplacian(int prec, Latt L, int nt, int nvec, const void* links, const void* in, long long its,
                      void* out, long long ots, cudaStream_t stream) {
   const int V3 = L.V3();
   const long long lts = 27LL * V3;
+  if (prec == ED_C64 && laplacian_tma_enabled()) {
+    const int rc = launch_laplacian_tma(L, nt, nvec, links, in, its, out, ots, stream);
+    if (rc != -1) return rc;
+  }
   if (prec == ED_C128) {
     dim3 grid(ceil_div(V3, 128), nvec, nt);
     laplacian_kernel<double, 1><<<grid, 128, 0, stream>>>(L, (const cplx<double>*)links, (const cplx<double>*)in,
@@ -300,6 +555,29 @@ extern "C" int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, 
                "ed_laplacian: c64 strides must keep 16-byte alignment");
   return ed::launch_laplacian(prec, ed::Latt{Lx, Ly, Lz}, nt, nvec, links, in, in_tstride, out, out_tstride,
                               (cudaStream_t)stream);
+}
+
+extern "C" int ed_laplacian_config(int use_tma) {
+  ED_CHECK_ARG(use_tma == 0 || use_tma == 1, "ed_laplacian_config: use_tma must be 0 or 1");
+  ed::g_stencil_tma = use_tma;
+  return ED_OK;
+}
+
+extern "C" int ed_laplacian_status(int* code, void* stream) {
+  ED_CHECK_ARG(code, "ed_laplacian_status: null pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  int zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbolAsync(code, ed::g_stencil_error, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && *code != 0) e = cudaMemcpyToSymbolAsync(ed::g_stencil_error, &zero, sizeof(int), 0,
+                                                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return ed::cuda_status(e, "reading the stencil status word");
+  if (*code != 0) {
+    ed::set_error("laplacian: a bounded wait of the TMA-staged kernel gave up; that output is invalid");
+    return ED_ERR_TIMEOUT;
+  }
+  return ED_OK;
 }
 
 extern "C" int ed_covariant_derivative(int in_prec, int out_prec, int Lx, int Ly, int Lz, int dir, int nvec,

@@ -120,6 +120,21 @@ def laplacian(links_soa: torch.Tensor, F: torch.Tensor, latt_size: Sequence[int]
     return out
 
 
+def laplacian_config(use_tma: bool = False):
+    """Select the complex64 Laplacian kernel process-wide: the TMA-staged
+    one (used where its shape limits allow) or the default one reading all
+    neighbours through L1/L2 (faster on GB300)."""
+    call("ed_laplacian_config", 1 if use_tma else 0)
+
+
+def laplacian_status():
+    """Synchronise the current stream and raise if a bounded wait of the
+    TMA-staged Laplacian gave up since the last check."""
+    code = ctypes.c_int()
+    call("ed_laplacian_status", ctypes.byref(code), stream_handle())
+    return code.value
+
+
 def covariant_derivative(links_soa_c128: torch.Tensor, F: torch.Tensor, latt_size, direction: int, out_dtype=None):
     """One hop ``D_d F = U_d(x) F(x+d) - U_d(x-d)^dag F(x-d)``
     (``lattice/generator/elemental.py:282-287``); ``F`` colour planes ``[nvec, 3, V3]``."""

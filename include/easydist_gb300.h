@@ -103,6 +103,18 @@ int ed_momentum_phases(int Lx, int Ly, int Lz, const int* moms, int nmom, void* 
 int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, const void* links, const void* in,
                  long long in_tstride, void* out, long long out_tstride, void* stream);
 
+/* Choose the complex64 Laplacian kernel: use_tma = 1 stages the input colour
+ * planes of z-1, z, z+1 through TMA into shared memory (when 4 planes fit, Lx
+ * is even, Lx <= 128, Ly <= 256 and Lx*Ly is a multiple of 16); 0 (default,
+ * faster on GB300) reads every neighbour through L1/L2.  Process-wide
+ * setting.  No counterpart in the reference. */
+int ed_laplacian_config(int use_tma);
+
+/* Status of the TMA-staged Laplacian's bounded waits since the last call
+ * (synchronises `stream`): ED_OK, or ED_ERR_TIMEOUT when a wait gave up (the
+ * output of that launch is invalid).  The status word is cleared. */
+int ed_laplacian_status(int* code, void* stream);
+
 /* One covariant-derivative hop D_dir on nvec colour-plane vectors:
  * out = U_d(x) in(x+d) - U_d(x-d)^dag in(x-d).
  * Replaces one iteration of ElementalGenerator._nD (elemental.py:282-287).

@@ -123,3 +123,34 @@ def test_momentum_phases_golden():
     latt = list(g["latt"])
     out = momentum_phases(latt, [tuple(p) for p in g["moms"]]).cpu().numpy()
     assert np.abs(out - g["phase"]).max() < 1e-15 * 8
+
+
+@pytest.mark.parametrize("latt, nvec", [([8, 8, 6, 3], 2), ([16, 16, 16, 2], 1), ([32, 32, 32, 2], 1),
+                                        ([24, 24, 24, 1], 3), ([4, 4, 3, 2], 2)])
+def test_laplacian_tma_matches_plain_and_oracle(latt, nvec):
+    """complex64: the TMA-staged kernel (input planes z-1, z, z+1 in shared
+    memory, several z slabs per (timeslice, vector)) against the plain kernel
+    and the FP64 oracle, with a padded timeslice stride."""
+    from easydistillation_gb300.ops import laplacian, laplacian_config, laplacian_status, links_to_soa
+
+    Lx, Ly, Lz, Lt = latt
+    V3 = Lx * Ly * Lz
+    gauge = R.synthetic_gauge(latt, 0.3, 8)
+    links = links_to_soa(torch.from_numpy(gauge).cuda(), latt, dtype=torch.complex64, layout="ildg")
+    rng = np.random.default_rng(3)
+    F = rng.standard_normal((Lt, nvec, V3 * 3)) + 1j * rng.standard_normal((Lt, nvec, V3 * 3))
+    big = torch.zeros((Lt, nvec + 1, 3, V3), dtype=torch.complex64, device="cuda")
+    big[:, :nvec] = torch.from_numpy(np.stack([_planes(F[t].T, latt) for t in range(Lt)])).to(torch.complex64)
+    try:
+        laplacian_config(True)
+        o_tma = laplacian(links, big[:, :nvec], latt).cpu().numpy()
+        assert laplacian_status() == 0
+        laplacian_config(False)
+        o_plain = laplacian(links, big[:, :nvec], latt).cpu().numpy()
+    finally:
+        laplacian_config(False)
+    assert rel_err(o_tma, o_plain) < 1e-6
+    for t in range(Lt):
+        Ut = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, t]
+        ref = _planes(R.laplacian(F[t].T, Ut, latt), latt)
+        assert rel_err(o_tma[t], ref) < 3e-6
