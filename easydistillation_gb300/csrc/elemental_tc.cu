@@ -718,18 +718,39 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
     tiles += d.mt * d.nt;
   }
   static bool attr_set[4] = {};
+  static int resident[4] = {};
   if (!attr_set[KIND]) {
     e = cudaFuncSetAttribute(tc_fac_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, TCF_SMEM);
     if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[KIND], tc_fac_gemm_kernel<KIND>, TC_THREADS,
+                                                      TCF_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "tc kernel occupancy");
+    if (resident[KIND] < 1) {
+      set_error("the factorised tensor-core GEMM does not fit on an SM");
+      return ED_ERR_UNSUPPORTED;
+    }
     attr_set[KIND] = true;
   }
   const long long g_used = (long long)nb * P->g_per_t;
   e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
+  // persistent grid: every CTA co-resident (the step counter of the kernel relies on it)
+  const int grid = std::min(tiles, resident[KIND] * sms);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(TC_THREADS);
+  cfg.dynamicSmemBytes = TCF_SMEM;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  tc_fac_gemm_kernel<KIND><<<tiles, TC_THREADS, TCF_SMEM, stream>>>(amap, bmap, tab, Ne, P->V3, (int)lay.ra,
-                                                                     (int)lay.rb, sc, DF);
+  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, tab, Ne, P->V3, (int)lay.ra, (int)lay.rb, sc,
+                         DF, tiles, TC_FLUSH_KB);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
+  if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");
   tc_df_to_c128_kernel<<<4 * sms, 256, 0, stream>>>(DF, g_used, G);
   ED_RETURN_LAUNCH("double-float to complex128");

@@ -100,11 +100,24 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
   }
 }
 
+// Persistent schedule.  The grid is one co-resident CTA per SM (cooperative
+// launch).  The work is the list of steps (K slab s, tile): CTA c owns tiles
+// c, c + G, c + 2G, ... and walks step q = s*J + j (tile j*G + c, the k-blocks
+// of slab s).  At any moment the G CTAs work on the same K slab of G
+// consecutive tiles, which share their A and B operand rows, so those rows
+// come from HBM once and from L2 for the other CTAs; with every CTA running
+// one tile over the whole K instead, the CTAs drift apart along K and the
+// operand streams were re-read from HBM (736 GB per 4-timeslice launch at
+// 32^3, Ne = 200).  To keep the CTAs in step, the TMA warp of each CTA counts
+// every step it starts on a global counter and starts step q only when every
+// CTA has started step q - 1 (a bounded wait).  The FP32 register sums are
+// flushed into the double-float results at the end of every step, so a tile
+// is only ever touched by its owner CTA.
 template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fac_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
                        const __grid_constant__ TcFacTable tab, int Ne, int V3, int RA, int RB,
-                       TcScalars* __restrict__ sc, float4* __restrict__ DF) {
+                       TcScalars* __restrict__ sc, float4* __restrict__ DF, int ntiles, int slab_kb) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;   // k elements per stage
   constexpr int KINST = 32 / ESZ;     // k elements per MMA instruction
@@ -123,18 +136,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int* status = &sc->status;
+  unsigned int* progress = reinterpret_cast<unsigned int*>(&sc->pad[0]);  // zeroed with the scalars
 
-  // ---- decode the tile: group, n tile (fast), m tile
-  const int tile = blockIdx.x;
-  int jb = 0;
-  while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
-  const TcFacJob& J = tab.j[jb];
-  const int local = tile - J.tile0;
-  const int mtile = local / J.nt;
-  const int ntile = local - mtile * J.nt;
+  const int G = gridDim.x, cta = blockIdx.x;
+  const int J = (ntiles + G - 1) / G;  // tiles per CTA (steps per slab)
   const long long K = 3LL * V3;
   const int nkb = (int)(K / KE);
-  const int Mrows = J.nright * tab.pz * Ne;
+  const int NS = (nkb + slab_kb - 1) / slab_kb;
+  const int nsteps = NS * J;
+  // tile of step q (>= ntiles: nothing to do) and its k-block range
+  auto step_tile = [&](int q) { return (q % J) * G + cta; };
+  auto step_kb0 = [&](int q) { return (q / J) * slab_kb; };
+  auto step_kb1 = [&](int q) { return min(nkb, (q / J + 1) * slab_kb); };
+  auto decode = [&](int tile, int& jb, int& mtile, int& ntile) {
+    jb = 0;
+    while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
+    const int local = tile - tab.j[jb].tile0;
+    mtile = local / tab.j[jb].nt;
+    ntile = local - mtile * tab.j[jb].nt;
+  };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TCF_STAGES; ++s) {
@@ -161,120 +181,164 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp < 8) {
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(TCF_REGS_LOW));
     if (warp == 0) {
-      // ===================== TMA of the A and B planes
+      // ===================== TMA of the A and B planes, step by step
       if (lane == 0) {
-        const int ay = J.arow0 + mtile * TC_BM;
-        const int by = J.brow0 + ntile * TC_BN;
-        int issued_last = -1;
-        for (int kb = 0; kb < nkb; ++kb) {
-          const int s = kb % TCF_STAGES;
-          if (kb >= TCF_STAGES && !mbar_wait(&empty[s], ((kb / TCF_STAGES) + 1) & 1, status, TC_ERR_EMPTY)) break;
-          uint8_t* As = smem + s * TCF_STAGE_BYTES;
-          uint8_t* Bs = As + TC_A_BYTES;
-          mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
-          for (int q = 0; q < 4; ++q) {
-            tma_load_2d(As + q * TC_BM * TC_ROWB, &amap, &full[s], kb * KE, q * RA + ay);
-            tma_load_2d(Bs + q * TC_BN * TC_ROWB, &bmap, &full[s], kb * KE, q * RB + by);
+        long long g = 0, issued_last = -1;
+        bool ok = true;
+        for (int q = 0; q < nsteps && ok; ++q) {
+          atomicAdd(progress, 1u);  // this CTA starts step q
+          if (q > 0) {              // ... once every CTA has started step q - 1
+            const unsigned int need = (unsigned int)q * (unsigned int)G;
+            const long long t0 = clock64();
+            while (*(volatile unsigned int*)progress < need) {
+              if (*status != 0 || clock64() - t0 > TC_WAIT_CYCLES) {
+                atomicCAS((int*)status, 0, TC_ERR_SYNC);
+                ok = false;
+                break;
+              }
+            }
+            if (!ok) break;
           }
-          issued_last = kb;
+          const int tile = step_tile(q);
+          if (tile >= ntiles) continue;
+          int jb, mtile, ntile;
+          decode(tile, jb, mtile, ntile);
+          const int ay = tab.j[jb].arow0 + mtile * TC_BM;
+          const int by = tab.j[jb].brow0 + ntile * TC_BN;
+          const int kb1 = step_kb1(q);
+          for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
+            const int s = (int)(g % TCF_STAGES);
+            if (g >= TCF_STAGES &&
+                !mbar_wait(&empty[s], (uint32_t)(((g / TCF_STAGES) + 1) & 1), status, TC_ERR_EMPTY)) {
+              ok = false;
+              break;
+            }
+            uint8_t* As = smem + s * TCF_STAGE_BYTES;
+            uint8_t* Bs = As + TC_A_BYTES;
+            mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+            for (int p = 0; p < 4; ++p) {
+              tma_load_2d(As + p * TC_BM * TC_ROWB, &amap, &full[s], kb * KE, p * RA + ay);
+              tma_load_2d(Bs + p * TC_BN * TC_ROWB, &bmap, &full[s], kb * KE, p * RB + by);
+            }
+            issued_last = g;
+          }
         }
         if (issued_last >= 0)  // do not leave while our copies may still land in shared memory
-          mbar_wait(&full[issued_last % TCF_STAGES], (issued_last / TCF_STAGES) & 1, status, TC_ERR_FULL, false);
+          mbar_wait(&full[issued_last % TCF_STAGES], (uint32_t)((issued_last / TCF_STAGES) & 1), status,
+                    TC_ERR_FULL, false);
       }
     } else if (warp == 1) {
       // ===================== MMA issuer (same product order as tc_pair_gemm_kernel)
       if (lane == 0) {
-        for (int kb = 0; kb < nkb; ++kb) {
-          const int s = kb % TCF_STAGES;
-          const int b = kb & 1;
-          if (!mbar_wait(&full[s], (kb / TCF_STAGES) & 1, status, TC_ERR_FULL)) break;
-          if (kb >= 2 && !mbar_wait(&acce[b], ((kb >> 1) + 1) & 1, status, TC_ERR_ACCE)) break;
-          tc_fence_after();
-          const uint32_t a0 = smem_u32(smem + s * TCF_STAGE_BYTES);
-          const uint32_t b0 = a0 + TC_A_BYTES;
-          const uint32_t d_re = tmem + b * 256, d_im = d_re + TC_BN;
+        long long g = 0;  // stages consumed == accumulator buffers filled
+        bool ok = true;
+        for (int q = 0; q < nsteps && ok; ++q) {
+          if (step_tile(q) >= ntiles) continue;
+          const int kb1 = step_kb1(q);
+          for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
+            const int s = (int)(g % TCF_STAGES);
+            const int b = (int)(g & 1);
+            if (!mbar_wait(&full[s], (uint32_t)((g / TCF_STAGES) & 1), status, TC_ERR_FULL) ||
+                (g >= 2 && !mbar_wait(&acce[b], (uint32_t)(((g >> 1) + 1) & 1), status, TC_ERR_ACCE))) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(smem + s * TCF_STAGE_BYTES);
+            const uint32_t b0 = a0 + TC_A_BYTES;
+            const uint32_t d_re = tmem + b * 256, d_im = d_re + TC_BN;
 #pragma unroll
-          for (int ks = 0; ks < KE / KINST; ++ks) {
-            const uint32_t acc = ks > 0 ? 1u : 0u;
-            const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
-            const uint64_t A0 = umma_desc_sw64(ao), A1 = umma_desc_sw64(ao + TC_BM * TC_ROWB);
-            const uint64_t A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB), A3 = umma_desc_sw64(ao + 3 * TC_BM * TC_ROWB);
-            const uint64_t B0 = umma_desc_sw64(bo), B1 = umma_desc_sw64(bo + TC_BN * TC_ROWB);
-            const uint64_t B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB), B3 = umma_desc_sw64(bo + 3 * TC_BN * TC_ROWB);
-            umma<KIND>(d_re, A0, B1, IDESC, acc);
-            umma<KIND>(d_re, A1, B0, IDESC, 1u);
-            umma<KIND>(d_re, A2, B3, IDESC_NEG, 1u);
-            umma<KIND>(d_re, A3, B2, IDESC_NEG, 1u);
-            umma<KIND>(d_im, A0, B3, IDESC, acc);
-            umma<KIND>(d_im, A1, B2, IDESC, 1u);
-            umma<KIND>(d_im, A2, B1, IDESC, 1u);
-            umma<KIND>(d_im, A3, B0, IDESC, 1u);
-          }
+            for (int ks = 0; ks < KE / KINST; ++ks) {
+              const uint32_t acc = ks > 0 ? 1u : 0u;
+              const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
+              const uint64_t A0 = umma_desc_sw64(ao), A1 = umma_desc_sw64(ao + TC_BM * TC_ROWB);
+              const uint64_t A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB), A3 = umma_desc_sw64(ao + 3 * TC_BM * TC_ROWB);
+              const uint64_t B0 = umma_desc_sw64(bo), B1 = umma_desc_sw64(bo + TC_BN * TC_ROWB);
+              const uint64_t B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB), B3 = umma_desc_sw64(bo + 3 * TC_BN * TC_ROWB);
+              umma<KIND>(d_re, A0, B1, IDESC, acc);
+              umma<KIND>(d_re, A1, B0, IDESC, 1u);
+              umma<KIND>(d_re, A2, B3, IDESC_NEG, 1u);
+              umma<KIND>(d_re, A3, B2, IDESC_NEG, 1u);
+              umma<KIND>(d_im, A0, B3, IDESC, acc);
+              umma<KIND>(d_im, A1, B2, IDESC, 1u);
+              umma<KIND>(d_im, A2, B1, IDESC, 1u);
+              umma<KIND>(d_im, A3, B0, IDESC, 1u);
+            }
 #pragma unroll
-          for (int ks = 0; ks < KE / KINST; ++ks) {
-            const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
-            const uint64_t A0 = umma_desc_sw64(ao), A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB);
-            const uint64_t B0 = umma_desc_sw64(bo), B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB);
-            umma<KIND>(d_re, A0, B0, IDESC, 1u);
-            umma<KIND>(d_re, A2, B2, IDESC_NEG, 1u);
-            umma<KIND>(d_im, A0, B2, IDESC, 1u);
-            umma<KIND>(d_im, A2, B0, IDESC, 1u);
+            for (int ks = 0; ks < KE / KINST; ++ks) {
+              const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
+              const uint64_t A0 = umma_desc_sw64(ao), A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB);
+              const uint64_t B0 = umma_desc_sw64(bo), B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB);
+              umma<KIND>(d_re, A0, B0, IDESC, 1u);
+              umma<KIND>(d_re, A2, B2, IDESC_NEG, 1u);
+              umma<KIND>(d_im, A0, B2, IDESC, 1u);
+              umma<KIND>(d_im, A2, B0, IDESC, 1u);
+            }
+            umma_commit(&empty[s]);  // frees the stage when these MMAs complete
+            umma_commit(&accf[b]);   // the buffer is ready to drain
           }
-          umma_commit(&empty[s]);  // frees the stage when these MMAs complete
-          umma_commit(&accf[b]);   // the buffer is ready to drain
         }
         umma_commit(mma_done);  // arrives once every MMA issued above has completed
       }
     }
   } else {
     asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(TCF_REGS_HIGH));
-    // ===================== drain: TMEM -> FP32 register sums -> double-float result
+    // ===================== drain: TMEM -> FP32 register sums -> double-float result per step
     const int dw = warp - 8;         // 0..7
     const int quarter = warp & 3;    // TMEM lane quarter this warp may access
     const int half = dw >> 2;        // which 64 of the 128 columns
     const int m = quarter * 32 + lane;
-    const int m_local = mtile * TC_BM + m;
-    const int n0c = ntile * TC_BN + half * 64;
     const float inv = ldexpf(1.f, -2 * sc->scale_exp);
     float sre[64], sim[64];
-#pragma unroll
-    for (int c = 0; c < 64; ++c) sre[c] = sim[c] = 0.f;
     bool ok = true;
-    for (int kb = 0; kb < nkb; ++kb) {
-      const int b = kb & 1;
-      if (!warp_wait(&accf[b], (kb >> 1) & 1, status, TC_ERR_ACC)) {
-        ok = false;
-        break;
-      }
-      tc_fence_after();
-      const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16) + b * 256 + half * 64;
-      {
-        uint32_t r0[32], r1[32];
-        tmem_ld32(tl, r0);
-        tmem_ld32(tl + 32, r1);
-        tmem_wait_ld();
+    long long g = 0;
+    for (int q = 0; q < nsteps && ok; ++q) {
+      const int tile = step_tile(q);
+      if (tile >= ntiles) continue;
+      int jb, mtile, ntile;
+      decode(tile, jb, mtile, ntile);
+      const TcFacJob& J = tab.j[jb];
+      const int m_local = mtile * TC_BM + m;
+      const int n0c = ntile * TC_BN + half * 64;
+      const int Mrows = J.nright * tab.pz * Ne;
 #pragma unroll
-        for (int e = 0; e < 32; ++e) {
-          sre[e] += __uint_as_float(r0[e]);
-          sre[32 + e] += __uint_as_float(r1[e]);
+      for (int c = 0; c < 64; ++c) sre[c] = sim[c] = 0.f;
+      const int kb1 = step_kb1(q);
+      for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
+        const int b = (int)(g & 1);
+        if (!warp_wait(&accf[b], (uint32_t)((g >> 1) & 1), status, TC_ERR_ACC)) {
+          ok = false;
+          break;
         }
-      }
-      {
-        uint32_t r0[32], r1[32];
-        tmem_ld32(tl + TC_BN, r0);
-        tmem_ld32(tl + TC_BN + 32, r1);
-        tmem_wait_ld();
+        tc_fence_after();
+        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16) + b * 256 + half * 64;
+        {
+          uint32_t r0[32], r1[32];
+          tmem_ld32(tl, r0);
+          tmem_ld32(tl + 32, r1);
+          tmem_wait_ld();
 #pragma unroll
-        for (int e = 0; e < 32; ++e) {
-          sim[e] += __uint_as_float(r0[e]);
-          sim[32 + e] += __uint_as_float(r1[e]);
+          for (int e = 0; e < 32; ++e) {
+            sre[e] += __uint_as_float(r0[e]);
+            sre[32 + e] += __uint_as_float(r1[e]);
+          }
         }
+        {
+          uint32_t r0[32], r1[32];
+          tmem_ld32(tl + TC_BN, r0);
+          tmem_ld32(tl + TC_BN + 32, r1);
+          tmem_wait_ld();
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            sim[e] += __uint_as_float(r0[e]);
+            sim[32 + e] += __uint_as_float(r1[e]);
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[b]);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acce[b]);
-      if ((kb & (TC_FLUSH_KB - 1)) == TC_FLUSH_KB - 1 || kb == nkb - 1)
-        flush_sums_fac(sre, sim, DF, tab, J, Ne, n0c, m_local, Mrows, inv);
+      if (ok) flush_sums_fac(sre, sim, DF, tab, J, Ne, n0c, m_local, Mrows, inv);
     }
     if (!ok) {
       // wait (without aborting on the error flag) until every issued MMA is

@@ -56,3 +56,26 @@ def test_mixed_volumes_f16x3_vs_oracle():
         for t in range(latt[3]):
             ref = R.elemental(evec[t], U[:, t], latt, 1, moms)
             assert rel_err(out[name][t].cpu().numpy(), ref) < 1e-6
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "ozaki_i8"])
+def test_graphed_factorised_modes(mode):
+    """CUDA graph capture and replay of the factorised-phase GEMM (a persistent
+    cooperative launch) and of the Ozaki int8 GEMM, against the oracle."""
+    from easydistillation_gb300.batch import GraphedElementalBatch
+
+    latt = [8, 4, 4, 3]
+    Ne, moms = 9, R.mom_dict_to_list(3)
+    gauge, evec = _inputs(latt, Ne, 0.3, 11)
+    U = torch.from_numpy(gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3].copy()).cuda()
+    V = torch.from_numpy(evec.reshape(latt[3], Ne, -1)).cuda()
+    runner = GraphedElementalBatch(latt, Ne, 2, moms, mode, batch=2)
+    assert runner.plan.factorised == (9, 3)
+    Uh = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3]
+    for chunk in ([0, 1], [2, 0], [1, 2]):
+        out = runner.run([U[:, t] for t in chunk], [V[t] for t in chunk]).cpu().numpy()
+        for k, t in enumerate(chunk):
+            ref = R.elemental(evec[t], Uh[:, t], latt, 2, moms)
+            assert rel_err(out[k], ref) < 1e-6
+    runner.plan.check_status()
+    assert runner.graph is not None
