@@ -109,6 +109,14 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
@@ -340,9 +348,11 @@ __global__ void tc_fac_split_kernel(const cplx<float>* __restrict__ chains, TcFa
           im1 = fr1 * v.w + fi1 * v.z;
         }
         const long long orow = ((long long)slot * nvar + a) * Ne + i;
+        // k-block-major planes: element (row, k) of a plane at ((k / KB) * Rplane + row) * KB + k % KB,
+        // KB = the k elements of one 64-byte TMA row, so each (128-row, k-block) box is contiguous
         if constexpr (KIND == TC_TF32) {
           uint32_t* P = (uint32_t*)planes;
-          const long long plane = Rplane * K, e0 = orow * K + 2 * kp;
+          const long long plane = Rplane * K, e0 = ((2LL * kp / 16) * Rplane + orow) * 16 + (2 * kp) % 16;
           uint32_t h, l;
           Split<TC_TF32>::one(re0, h, l);
           P[e0] = h;
@@ -357,8 +367,8 @@ __global__ void tc_fac_split_kernel(const cplx<float>* __restrict__ chains, TcFa
           P[2 * plane + e0 + 1] = h;
           P[3 * plane + e0 + 1] = l;
         } else {
-          uint32_t* P = (uint32_t*)planes;  // 16-bit elements, pairs as words
-          const long long plane = Rplane * K2, w = orow * K2 + kp;
+          uint32_t* P = (uint32_t*)planes;  // 16-bit elements, pairs as words (16 words per 64-byte row)
+          const long long plane = Rplane * K2, w = (((long long)kp / 16) * Rplane + orow) * 16 + kp % 16;
           uint32_t h, l;
           Split<KIND>::pair(re0, re1, h, l);
           P[w] = h;
@@ -622,18 +632,22 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
   return ED_OK;
 }
 
-static int encode_planes(CUtensorMap* map, int kind, void* base, long long K, long long rows) {
+// Tensor map over four k-block-major planes of R rows: dimensions (k within
+// the 64-byte row, row, plane*nkb + k-block); a box is 128 rows of one
+// k-block, 8 KB contiguous in HBM.
+static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, long long R) {
   EncodeFn enc = get_encode();
   if (!enc) {
     set_error("cuTensorMapEncodeTiled is unavailable from the driver");
     return ED_ERR_CUDA;
   }
   const size_t esz = tc_esz(kind);
-  cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  cuuint64_t gstride[1] = {(cuuint64_t)(K * esz)};
-  cuuint32_t box[2] = {(cuuint32_t)(TC_ROWB / esz), (cuuint32_t)TC_BM};
-  cuuint32_t estride[2] = {1, 1};
-  CUresult cr = enc(map, kind == TC_TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, base,
+  const long long KB = TC_ROWB / (long long)esz, nkb = K / KB;
+  cuuint64_t gdim[3] = {(cuuint64_t)KB, (cuuint64_t)R, (cuuint64_t)(4 * nkb)};
+  cuuint64_t gstride[2] = {(cuuint64_t)TC_ROWB, (cuuint64_t)(R * TC_ROWB)};
+  cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)TC_BM, 1};
+  cuuint32_t estride[3] = {1, 1, 1};
+  CUresult cr = enc(map, kind == TC_TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, base,
                     gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS) {
@@ -694,8 +708,8 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   ED_RETURN_LAUNCH("variant planes");
 
   CUtensorMap amap, bmap;
-  if ((rc = encode_planes(&amap, KIND, apl, K, 4 * lay.ra))) return rc;
-  if ((rc = encode_planes(&bmap, KIND, bpl, K, 4 * lay.rb))) return rc;
+  if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra))) return rc;
+  if ((rc = encode_kmajor(&bmap, KIND, bpl, K, lay.rb))) return rc;
 
   TcFacTable tab;
   tab.njobs = nb * P->jobs_per_t;

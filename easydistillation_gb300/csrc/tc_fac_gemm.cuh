@@ -216,9 +216,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             uint8_t* As = smem + s * TCF_STAGE_BYTES;
             uint8_t* Bs = As + TC_A_BYTES;
             mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
-            for (int p = 0; p < 4; ++p) {
-              tma_load_2d(As + p * TC_BM * TC_ROWB, &amap, &full[s], kb * KE, p * RA + ay);
-              tma_load_2d(Bs + p * TC_BN * TC_ROWB, &bmap, &full[s], kb * KE, p * RB + by);
+            for (int p = 0; p < 4; ++p) {  // k-block-major planes: one contiguous 8 KB box each
+              tma_load_3d(As + p * TC_BM * TC_ROWB, &amap, &full[s], 0, ay, p * nkb + kb);
+              tma_load_3d(Bs + p * TC_BN * TC_ROWB, &bmap, &full[s], 0, by, p * nkb + kb);
             }
             issued_last = g;
           }
