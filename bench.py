@@ -163,6 +163,9 @@ def make_inputs(latt, Ne, seed=2, distinct_t=RESIDENT_T):
 # total), and one phase-weighted zgemm per subset and momentum.
 REF_HOPS = 78
 REF_SUBSETS = 43
+# DRAM bytes (read + write) of one tc_fac_gemm_kernel<f16x3> launch on the default workload (32^3, Ne = 200,
+# 4 timeslices), from one ncu capture (profiles/tc_fac_gemm_f16x3_32cube_dram.md)
+FAC_TRAFFIC_BYTES = 414.10e9 + 15.97e9
 # FP64 FMA throughput of this part (register-resident DFMA loop on all SMs)
 FP64_PEAK_TFLOPS = 1.25
 FP64_PEAK_SOURCE = "nominal GB300 FP64"
@@ -372,8 +375,12 @@ def run_ours(args, rank, world):
             tiles = sum(-(-(j * Ne) // 128) for j in rights) * (-(-(Ne * NMOM) // 128))
             kname = f"tc_pair_gemm_kernel<{args.mode}>"
         mma_flop = B * tiles * 128 * 128 * 3 * V3 * 12 * 2.0
+        default_workload = (plan.factorised is not None and args.mode == "f16x3" and B == 4 and Ne == NE
+                            and list(latt[:3]) == LATT[:3])
         roofline = {"bound": "tensor", "achieved": alg_flop / kms / 1e9, "peak": pk, "unit": "TFLOP/s",
-                    "frac": alg_flop / kms / 1e9 / pk, "traffic": None, "peak_source": pk_src,
+                    "frac": alg_flop / kms / 1e9 / pk,
+                    "traffic": FAC_TRAFFIC_BYTES if default_workload else None,
+                    "traffic_unit": "bytes per launch (DRAM read + write, ncu)", "peak_source": pk_src,
                     "kernel": kname, "kernel_ms": kms,
                     "mma_tflops_executed": mma_flop / kms / 1e9, "mma_frac": mma_flop / kms / 1e9 / pk,
                     "pairs_evaluated_per_momentum": plan.num_pairs, "ref_subsets_per_momentum": REF_SUBSETS,
