@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--eigen-cpu", action="store_true", help="also time the oracle's scipy eigensolve (slow)")
     ap.add_argument("--eigen-poly", type=int, default=0, help="Chebyshev degree for --eigen (0: plain Lanczos)")
+    ap.add_argument("--eigen-ncv", type=int, default=None, help="Krylov dimension for --eigen")
     ap.add_argument("--mixed", action="store_true",
                     help="measure graphed batches over mixed volumes (16^3 Ne=64, 24^3 Ne=128, 32^3 Ne=256)")
     ap.add_argument("--grad", action="store_true",
@@ -631,7 +632,7 @@ def run_eigen(args):
         def load(self, key):
             return _G(gauge)
 
-    gen = EigenvectorGenerator(latt, _Src(), Ne, 1e-10, stencil_precision=args.eigen_precision)
+    gen = EigenvectorGenerator(latt, _Src(), Ne, 1e-10, stencil_precision=args.eigen_precision, ncv=args.eigen_ncv)
     gen.load("bench")
     ts = list(range(args.eigen_batch))
     torch.cuda.synchronize()
@@ -649,7 +650,7 @@ def run_eigen(args):
     dt = time.perf_counter() - t0
     line = {"metric": f"eigensolve timeslices/s {latt[0]}^3 Ne={Ne} tol 1e-10", "value": len(ts) / dt,
             "unit": "timeslices/s", "seconds": dt, "batch": len(ts), "stencil_precision": args.eigen_precision,
-            "polynomial_degree": args.eigen_poly,
+            "polynomial_degree": args.eigen_poly, "ncv": gen.ncv,
             "stats": gen.last_stats, "lowest_evals_t0": [float(v) for v in evals[0, :3].cpu()]}
     if args.eigen_cpu:
         from oracle import restatement as R

@@ -761,8 +761,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, tab, Ne, P->V3, (int)lay.ra, (int)lay.rb, sc,
-                         DF, tiles, TC_FLUSH_KB);
+  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, tab, Ne, P->V3, sc, DF, tiles, TC_FLUSH_KB);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");

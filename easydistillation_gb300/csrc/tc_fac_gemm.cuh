@@ -116,8 +116,8 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
 template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fac_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
-                       const __grid_constant__ TcFacTable tab, int Ne, int V3, int RA, int RB,
-                       TcScalars* __restrict__ sc, float4* __restrict__ DF, int ntiles, int slab_kb) {
+                       const __grid_constant__ TcFacTable tab, int Ne, int V3, TcScalars* __restrict__ sc,
+                       float4* __restrict__ DF, int ntiles, int slab_kb) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;   // k elements per stage
   constexpr int KINST = 32 / ESZ;     // k elements per MMA instruction

@@ -49,9 +49,12 @@ def stout_smear_links_(U: torch.Tensor, latt_size, nstep: int, rho: float):
 
 class EigenvectorGenerator:
     def __init__(self, latt_size: List[int], gauge_field, Ne: int, tol: float, *, stencil_precision: str = "fp64",
-                 device=None) -> None:
+                 device=None, ncv: int = None) -> None:
+        """``ncv``: Krylov dimension of the thick-restart Lanczos (default
+        max(3 Ne, Ne + 32), capped by the problem size)."""
         if stencil_precision not in ("fp64", "fp32"):
             raise ValueError("stencil_precision must be 'fp64' or 'fp32'")
+        self.ncv = ncv
         self.device = torch.device(device or "cuda")
         self.latt_size = latt_size
         self.gauge_field = gauge_field
@@ -119,19 +122,20 @@ class EigenvectorGenerator:
             # below the cut T_deg has the sign (-1)^deg: negate so the wanted modes are the smallest
             cheb = LZ.chebyshev_operator(mv, polynomial_degree, lambda_cut, 12.0, negate=polynomial_degree % 2 == 0)
             res = LZ.trlanczos(cheb, B, n,
-                               self.Ne, max(self.tol, 1e-12), device=self.device)
+                               self.Ne, max(self.tol, 1e-12), ncv=self.ncv, device=self.device)
             lam, X, resid = LZ.rayleigh_ritz(self._matvec(ts, torch.complex128), res.evecs)
             res.evals, res.evecs, res.residuals = lam, X, resid
             res.matvecs = res.matvecs * polynomial_degree + self.Ne
         elif self.stencil_precision == "fp32":
             r32 = LZ.trlanczos(self._matvec(ts, torch.complex64), B, n, self.Ne, max(self.tol, 1e-6),
-                               device=self.device)
+                               ncv=self.ncv, device=self.device)
             v0 = r32.evecs.sum(dim=1)
             res = LZ.trlanczos(self._matvec(ts, torch.complex128), B, n, self.Ne, self.tol, v0=v0,
-                               device=self.device)
+                               ncv=self.ncv, device=self.device)
             res.matvecs += r32.matvecs
         else:
-            res = LZ.trlanczos(self._matvec(ts, torch.complex128), B, n, self.Ne, self.tol, device=self.device)
+            res = LZ.trlanczos(self._matvec(ts, torch.complex128), B, n, self.Ne, self.tol, ncv=self.ncv,
+                               device=self.device)
         self.last_stats = {"restarts": res.restarts, "matvecs": res.matvecs, "converged": res.converged}
         evals, evecs = LZ.sort_ascending(res.evals, res.evecs)
         if apply_renorm_phase:

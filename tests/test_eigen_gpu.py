@@ -71,3 +71,22 @@ def test_eigen_chebyshev_acceleration(deg):
     evecs, evals = gen.calc(0, True, deg, float(g["evals0"][-1]) * 1.1)
     U = g["gauge"].transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
     _check(evecs.cpu().numpy(), evals.cpu().numpy(), g["evecs0"], g["evals0"], U, latt, Ne)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_eigen_larger_volume_against_scipy(prec):
+    """12^3 (n = 5184), Ne = 40, tol 1e-10, two timeslices in one batch: several
+    thick restarts, so the reorthogonalisation is exercised over many steps."""
+    from easydistillation_gb300 import EigenvectorGenerator
+
+    latt = [12, 12, 12, 2]
+    Ne = 40
+    gauge = R.synthetic_gauge(latt, 0.3, 17)
+    gen = EigenvectorGenerator(latt, MemGauge(gauge), Ne, 1e-10, stencil_precision=prec)
+    gen.load("k")
+    evecs, evals = gen.calc_batch(range(2))
+    assert gen.last_stats["converged"]
+    U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3]
+    for t in range(2):
+        rv, re = R.eigensolve(U[:, t], latt, Ne, 1e-10)
+        _check(evecs[t].cpu().numpy(), evals[t].cpu().numpy(), rv, re, U[:, t], latt, Ne)
