@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--no-factor", action="store_true",
                     help="keep the on-chip phase GEMM although the 27 momenta factorise")
     ap.add_argument("--no-stencil", action="store_true", help="skip the Laplacian bandwidth measurement")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="build the plans with the built-in defaults instead of the autotuner's choice (which is "
+                         "measured before the timed region and cached per device and shape)")
     ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
     ap.add_argument("--eigen-batch", type=int, default=8)
     ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
@@ -300,7 +303,19 @@ def run_ours(args, rank, world):
     U = links_to_device(gauge, latt, dev)  # [3, Lt, Lz, Ly, Lx, 3, 3] c128 resident
     V = [torch.from_numpy(x).to(dev) for x in evecs_host]  # resident c128 eigenvectors
     B = args.batch
-    plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=not args.no_factor)
+    tuned = None
+    if args.no_factor:
+        args.autotune = False  # an explicit GEMM form
+    if args.autotune:
+        from easydistillation_gb300.tune import tune_elemental
+
+        t0 = time.perf_counter()
+        res = tune_elemental(latt, Ne, NUM_NABLA, moms, args.mode, B, dev)
+        tuned = {"cached": res.cached, "seconds": time.perf_counter() - t0, "trials": res.trials}
+        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=res.best.factorise,
+                             tuning=res.best.tuning)
+    else:
+        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=not args.no_factor)
     outs = [torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev) for _ in range(B)]
     out = outs[0]
     stream = torch.cuda.current_stream()
@@ -392,7 +407,15 @@ def run_ours(args, rank, world):
     # the plain FP64 GPU path on the same timeslice: speed and the split-precision error against it
     fp64 = None
     if args.mode != "fp64" and not args.no_fp64:
-        plan64 = ElementalPlan(latt, Ne, NUM_NABLA, moms, "fp64", dev)
+        t_tune = None
+        if args.autotune:
+            from easydistillation_gb300.tune import tuned_plan
+
+            t_tune = time.perf_counter()
+            plan64 = tuned_plan(latt, Ne, NUM_NABLA, moms, "fp64", dev)
+            t_tune = time.perf_counter() - t_tune
+        else:
+            plan64 = ElementalPlan(latt, Ne, NUM_NABLA, moms, "fp64", dev)
         out64 = torch.empty_like(out)
         t_ref = (args.warmup * 7 + rank) % Lt
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -405,7 +428,8 @@ def run_ours(args, rank, world):
         ms64 = a.elapsed_time(b)
         rel = float(torch.linalg.vector_norm(out - out64) / torch.linalg.vector_norm(out64))
         fp64 = {"value": 1e3 / ms64, "unit": "timeslices/s", "rel_err_vs_fp64": rel,
-                "speedup_split_over_fp64": (value / world) / (1e3 / ms64)}
+                "speedup_split_over_fp64": (value / world) / (1e3 / ms64), "plan_settings": plan64.tuning(),
+                "autotune_seconds": t_tune}
         del plan64, out64
         torch.cuda.empty_cache()
 
@@ -441,7 +465,7 @@ def run_ours(args, rank, world):
                 return self.t
 
         gen = ElementalGenerator(latt, _Src(gauge), _TSrc(ev, Ne), NUM_NABLA, moms, precision=args.mode, device=dev,
-                                 factorise=not args.no_factor)
+                                 factorise=not args.no_factor, autotune=args.autotune)
         gen.load("bench")
         nts = args.steps * B
         host_out = torch.empty((nts, 13, NMOM, Ne, Ne), dtype=torch.complex128).pin_memory()
@@ -472,12 +496,15 @@ def run_ours(args, rank, world):
                                    f"{B} timeslices per step",
                        "timeslices_per_step": B,
                        "factorised_phases": plan.factorised,
+                       "plan_settings": {"factorise": plan.factorise, **plan.tuning()},
                        "pairs_per_momentum": plan.num_pairs, "l2": "inputs larger than L2 (rotating timeslices)",
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": args.steps * launches_per_step(args.mode, B, plan.factorised is not None),
             "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "fp64_gpu": fp64,
             "stencil_roofline": stencil,
         }
+        if tuned is not None:
+            line["autotune"] = tuned
         print(json.dumps(line), flush=True)
 
 
@@ -485,11 +512,12 @@ def run_mixed(args):
     """Secondary measurement (``--mixed``): 96 timeslices, 32 each of 16^3
     (Ne=64), 24^3 (Ne=128) and 32^3 (Ne=256), links exp(i eps A) with eps
     alternating 0.1 / 0.3 over timeslices, 4 operators x 7 momenta, split
-    precision.  Each volume runs as CUDA-graph replays of one batched plan
-    (batch admitted by HBM footprint); inputs resident in HBM."""
+    precision.  All 96 timeslices are one CUDA-graph replay: per volume a
+    batched plan (batch admitted by HBM footprint) reads the resident inputs
+    in place; the plans take the autotuner's choice (``--no-autotune``: defaults)."""
     import torch
 
-    from easydistillation_gb300.batch import GraphedElementalBatch, admit_batch
+    from easydistillation_gb300.batch import MixedVolumeGraph, VolumeBinding
     from easydistillation_gb300.generator.elemental import links_to_device
     from easydistillation_gb300.insertion import mom_dict_to_list
     from easydistillation_gb300.synthetic import gauge_field
@@ -499,7 +527,7 @@ def run_mixed(args):
     moms = mom_dict_to_list(3)[:7]
     vols = [([16, 16, 16, 32], 64), ([24, 24, 24, 32], 128), ([32, 32, 32, 32], 256)]
     gen = torch.Generator(device=dev).manual_seed(3003)
-    runners, inputs = [], []
+    bindings = []
     for latt, Ne in vols:
         Lx, Ly, Lz, Lt = latt
         V3 = Lx * Ly * Lz
@@ -510,36 +538,30 @@ def run_mixed(args):
         V = torch.complex(torch.randn((4, Ne, V3 * 3), generator=gen, device=dev, dtype=torch.float64),
                           torch.randn((4, Ne, V3 * 3), generator=gen, device=dev, dtype=torch.float64))
         V /= (2 * V3 * 3) ** 0.5
-        B = admit_batch(latt, Ne, 1, moms, mode, dev, max_batch=8)
-        r = GraphedElementalBatch(latt, Ne, 1, moms, mode, batch=B, device=dev)
-        runners.append(r)
-        inputs.append((U, V, Lt))
-
-    def sweep():
-        n = 0
-        for r, (U, V, Lt) in zip(runners, inputs):
-            for s0 in range(0, Lt, r.batch):
-                ts = list(range(s0, min(Lt, s0 + r.batch)))
-                r.run([U[:, t % 4] for t in ts], [V[t % 4] for t in ts])
-                n += len(ts)
-        return n
-
-    sweep()  # captures the graphs
+        bindings.append(VolumeBinding(latt, Ne, U, V, [t % 4 for t in range(Lt)]))
+    t0 = time.perf_counter()
+    mv = MixedVolumeGraph(bindings, 1, moms, mode, max_batch=8, device=dev, autotune=args.autotune)
+    setup_s = time.perf_counter() - t0
+    mv.capture()
     torch.cuda.synchronize()
     reps = max(1, args.steps)
-    t0 = time.perf_counter()
-    n = 0
+    n_per = sum(len(b.timeslices) for b in bindings)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
     for _ in range(reps):
-        n += sweep()
+        mv.run()
+    b.record()
     torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    for r in runners:
-        if mode != "fp64":
-            r.plan.check_status()
+    dt = a.elapsed_time(b) / 1e3
+    mv.check_status()
     line = {"metric": "mixed-volume elemental timeslices/s (96 timeslices: 16^3 Ne=64, 24^3 Ne=128, 32^3 Ne=256; "
-                      "4 ops x 7 momenta)", "value": n / dt, "unit": "timeslices/s", "seconds_per_sweep": dt / reps,
-            "mode": mode, "batches": {f"{v[0][0]}^3": r.batch for v, r in zip(vols, runners)},
-            "graph_replays_per_sweep": sum(-(-inp[2] // r.batch) for r, inp in zip(runners, inputs)),
+                      "4 ops x 7 momenta)", "value": reps * n_per / dt, "unit": "timeslices/s",
+            "seconds_per_sweep": dt / reps, "mode": mode,
+            "batches": {f"{v[0][0]}^3": p.batch for v, p in zip(vols, mv.plans)},
+            "plan_settings": {f"{v[0][0]}^3": {"factorise": p.factorise, "factorised": p.factorised, **p.tuning()}
+                              for v, p in zip(vols, mv.plans)},
+            "autotune": args.autotune, "plan_setup_seconds": setup_s,
+            "graph_replays_per_sweep": 1, "batched_passes_per_sweep": mv.passes(),
             "data": "synthetic, resident in HBM"}
     print(json.dumps(line), flush=True)
 

@@ -72,6 +72,8 @@ _SIGNATURES = {
     "ed_laplacian_config": ([_i], _i),
     "ed_laplacian_status": ([_c.POINTER(_i), _vp], _i),
     "ed_elemental_factorised": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
+    "ed_elemental_set_tuning": ([_vp, _i, _i], _i),
+    "ed_elemental_get_tuning": ([_vp, _i, _c.POINTER(_i)], _i),
 }
 
 _lock = threading.Lock()

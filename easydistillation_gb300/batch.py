@@ -50,10 +50,11 @@ class GraphedElementalBatch:
     (``links[b]``: complex128 ``[3, Lz, Ly, Lx, 3, 3]`` spatial links,
     ``evecs[b]``: ``[Ne, V3*3]`` c128/c64 reference-layout vectors) into the
     static buffers, replays the graph and returns the static output
-    ``[batch, Nderiv, Nmom, Ne, Ne]`` (valid for the first len(links) rows)."""
+    ``[batch, Nderiv, Nmom, Ne, Ne]`` (valid for the first len(links) rows).
+    ``autotune`` builds the plan with the autotuner's choice for its shape."""
 
     def __init__(self, latt_size, Ne, num_nabla, momentum_list, precision="f16x3", batch=None, device=None,
-                 evec_dtype=torch.complex128):
+                 evec_dtype=torch.complex128, autotune=False):
         self.device = torch.device(device or "cuda")
         self.latt_size = list(latt_size)
         Lx, Ly, Lz, Lt = latt_size
@@ -62,7 +63,13 @@ class GraphedElementalBatch:
         if batch is None:
             batch = admit_batch(latt_size, Ne, num_nabla, momentum_list, precision, self.device)
         self.batch = batch
-        self.plan = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, self.device, batch=batch)
+        if autotune:
+            from .tune import tuned_plan
+
+            self.plan = tuned_plan(latt_size, Ne, num_nabla, momentum_list, precision, self.device, batch=batch,
+                                   evec_dtype=evec_dtype)
+        else:
+            self.plan = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, self.device, batch=batch)
         nd, nm = num_derivative(num_nabla), len(momentum_list)
         self.links = torch.zeros((batch, 3, Lz, Ly, Lx, 3, 3), dtype=torch.complex128, device=self.device)
         eye = torch.eye(3, dtype=torch.complex128, device=self.device)
@@ -110,27 +117,124 @@ class VolumeGroup:
     timeslices: List[int]
 
 
+@dataclass
+class VolumeBinding:
+    """One lattice volume of a :class:`MixedVolumeGraph`, bound to caller-owned
+    device tensors: ``links`` complex128 ``[3, T, Lz, Ly, Lx, 3, 3]`` (the
+    generators' spatial-link layout), ``evecs`` ``[T, Ne, 3*V3]`` c128/c64,
+    ``timeslices`` indices into T (repeats allowed), ``out`` complex128
+    ``[len(timeslices), Nderiv, Nmom, Ne, Ne]`` (allocated when None)."""
+
+    latt_size: List[int]
+    Ne: int
+    links: torch.Tensor
+    evecs: torch.Tensor
+    timeslices: List[int]
+    out: torch.Tensor = None
+
+
+class MixedVolumeGraph:
+    """Every timeslice of several lattice volumes (each with its own Ne) in
+    ONE captured CUDA graph.
+
+    Each volume gets a batched plan (batch admitted by HBM footprint, the
+    volumes' workspaces held at once, largest volume first); the graph holds,
+    volume by volume, one batched pass per chunk of timeslices, reading the
+    bound input tensors in place and writing the bound outputs, so a replay
+    (``run()``) recomputes everything from the tensors' current contents with
+    one host call.  ``autotune`` builds each plan with the autotuner's choice
+    for its shape (``easydistillation_gb300.tune``)."""
+
+    def __init__(self, volumes: Sequence[VolumeBinding], num_nabla, momentum_list, precision="f16x3",
+                 max_batch=8, device=None, autotune=False, reserve=0.1):
+        self.device = torch.device(device or "cuda")
+        self.precision = precision
+        self.volumes = list(volumes)
+        nd, nm = num_derivative(num_nabla), len(momentum_list)
+        self.plans = []
+        order = sorted(range(len(self.volumes)), key=lambda i: -self._v3(self.volumes[i]) * self.volumes[i].Ne)
+        plans = [None] * len(self.volumes)
+        for i in order:
+            v = self.volumes[i]
+            if v.links.dim() != 7 or v.links.shape[0] != 3 or v.links.dtype != torch.complex128:
+                raise ValueError("links must be complex128 [3, T, Lz, Ly, Lx, 3, 3]")
+            if v.links.stride(-1) != 1 or v.links.stride(-2) != 3 or v.links.stride(-3) != 9:
+                raise ValueError("links must have contiguous 3x3 matrices with unit site stride 9")
+            V3 = self._v3(v)
+            if v.links.stride(3) != 9 * v.latt_size[0] or v.links.stride(2) != 9 * V3 // v.latt_size[2]:
+                raise ValueError("links must be contiguous over the sites of a timeslice")
+            if v.out is None:
+                v.out = torch.empty((len(v.timeslices), nd, nm, v.Ne, v.Ne), dtype=torch.complex128,
+                                    device=self.device)
+            n = len(v.timeslices)
+            b = min(max_batch, n, admit_batch(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device,
+                                              max_batch=max_batch, reserve=reserve, static_buffers=False))
+            if autotune:
+                from .tune import tuned_plan
+
+                plan = tuned_plan(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device, batch=b,
+                                  evec_dtype=v.evecs.dtype)
+            else:
+                plan = ElementalPlan(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device, batch=b)
+            plan.workspace()  # held now, so the next volume's admission sees it
+            plans[i] = plan
+        self.plans = plans
+        self.graph = None
+
+    @staticmethod
+    def _v3(v):
+        return v.latt_size[0] * v.latt_size[1] * v.latt_size[2]
+
+    def _launch(self):
+        for v, plan in zip(self.volumes, self.plans):
+            ts = list(v.timeslices)
+            for s0 in range(0, len(ts), plan.batch):
+                chunk = ts[s0 : s0 + plan.batch]
+                plan.run_batch([v.links[:, t] for t in chunk], v.links.stride(0), 9,
+                               [v.evecs[t] for t in chunk], [v.out[s0 + j] for j in range(len(chunk))])
+
+    def capture(self):
+        self._launch()  # warm-up outside the capture
+        torch.cuda.synchronize(self.device)
+        self.check_status()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self._launch()
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self.graph = g
+        return g
+
+    def run(self):
+        """Replay the graph (captured on first use); returns the bound outputs."""
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+        return [v.out for v in self.volumes]
+
+    def passes(self) -> int:
+        """Batched passes in the graph."""
+        return sum(-(-len(v.timeslices) // p.batch) for v, p in zip(self.volumes, self.plans))
+
+    def check_status(self):
+        if self.precision != "fp64":
+            for p in self.plans:
+                p.check_status()
+
+
 def run_mixed_volumes(groups: Dict[str, VolumeGroup], links: Dict[str, torch.Tensor],
                       evecs: Dict[str, torch.Tensor], num_nabla, momentum_list, precision="f16x3",
-                      max_batch=8, device=None):
-    """Elementals for several lattice volumes (each with its own Ne): each
-    volume gets a graphed batch sized by HBM admission; its timeslices are
-    processed batch by batch.  ``links[name]``: ``[3, Lt, Lz, Ly, Lx, 3, 3]``;
-    ``evecs[name]``: ``[Lt, Ne, V3*3]``.  Returns {name: [n_t, Nderiv, Nmom, Ne, Ne]}."""
-    out = {}
-    for name, g in groups.items():
-        runner = GraphedElementalBatch(g.latt_size, g.Ne, num_nabla, momentum_list, precision,
-                                       batch=min(max_batch, admit_batch(g.latt_size, g.Ne, num_nabla, momentum_list,
-                                                                        precision, device, max_batch)),
-                                       device=device)
-        res = []
-        ts = list(g.timeslices)
-        for s0 in range(0, len(ts), runner.batch):
-            chunk = ts[s0 : s0 + runner.batch]
-            r = runner.run([links[name][:, t] for t in chunk], [evecs[name][t] for t in chunk])
-            res.append(r.clone())
-        out[name] = torch.cat(res)
-        if precision != "fp64":
-            runner.plan.check_status()
-        del runner
-    return out
+                      max_batch=8, device=None, autotune=False):
+    """Elementals for several lattice volumes (each with its own Ne), all in
+    one graphed pass (:class:`MixedVolumeGraph`).  ``links[name]``:
+    ``[3, Lt, Lz, Ly, Lx, 3, 3]``; ``evecs[name]``: ``[Lt, Ne, V3*3]``.
+    Returns {name: [n_t, Nderiv, Nmom, Ne, Ne]}."""
+    names = list(groups)
+    vols = [VolumeBinding(groups[n].latt_size, groups[n].Ne, links[n], evecs[n], list(groups[n].timeslices))
+            for n in names]
+    mv = MixedVolumeGraph(vols, num_nabla, momentum_list, precision, max_batch, device, autotune)
+    outs = mv.run()
+    mv.check_status()
+    return dict(zip(names, outs))

@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "elemental.cuh"
+#include "tc_config.cuh"
 
 namespace ed {
 
@@ -213,17 +214,22 @@ struct GemmTable {
   GemmJobDev j[kMaxJobs];
 };
 
-constexpr int F64_BM = 64, F64_BN = 64, F64_BK = 8;
+constexpr int F64_BK = 8;
 
-// One CTA = a 64x64 tile of G_p(X, Y-range) for one (group, momentum).
-// 256 threads as 16x16, each owning 4x4 complex outputs.  The left operand is
-// multiplied by the phase while staged: A[i][k] = conj(X_i[k]) * phase_p(k mod V3).
+// One CTA = a (16*TM) x (16*TN) tile of G_p(X, Y-range) for one (group,
+// momentum).  256 threads as 16x16, each owning TM x TN complex outputs.  The
+// left operand is multiplied by the phase while staged:
+// A[i][k] = conj(X_i[k]) * phase_p(k mod V3).  The tile shape is a plan
+// setting (ED_TUNE_F64_TILE): smaller tiles waste less on an Ne that is not a
+// multiple of 64 and give more CTAs for small Ne.
+template <int TM, int TN>
 __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int Ne, int V3, int nmom,
                                                             const cplx<double>* __restrict__ chains,
                                                             const cplx<double>* __restrict__ phases,
                                                             cplx<double>* __restrict__ G) {
-  __shared__ cplx<double> As[F64_BK][F64_BM + 1];
-  __shared__ cplx<double> Bs[F64_BK][F64_BN + 1];
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  __shared__ cplx<double> As[F64_BK][BM + 1];
+  __shared__ cplx<double> Bs[F64_BK][BN + 1];
   int tile = blockIdx.x;
   int jb = 0;
   while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
@@ -243,24 +249,28 @@ __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int N
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int lk = tid & 7, lr = tid >> 3;  // loader: 8 consecutive k per row, 32 rows per pass
-  cplx<double> acc[4][4];
+  cplx<double> acc[TM][TN];
 #pragma unroll
-  for (int a = 0; a < 4; ++a)
+  for (int a = 0; a < TM; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = mk(0.0, 0.0);
+    for (int b = 0; b < TN; ++b) acc[a][b] = mk(0.0, 0.0);
 
   for (long long k0 = 0; k0 < K; k0 += F64_BK) {
     const long long k = k0 + lk;
     cplx<double> phk = mk(0.0, 0.0);
     if (k < K) phk = ld(ph + (k % V3));
 #pragma unroll
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < BM / 32; ++pass) {
       const int r = lr + 32 * pass;
-      const int gi = mtile * F64_BM + r;
+      const int gi = mtile * BM + r;
       cplx<double> a = mk(0.0, 0.0);
       if (gi < M && k < K) a = cmul_conj(ld(Lc + (long long)gi * K + k), phk);
       As[lk][r] = a;
-      const int gj = ntile * F64_BN + r;
+    }
+#pragma unroll
+    for (int pass = 0; pass < BN / 32; ++pass) {
+      const int r = lr + 32 * pass;
+      const int gj = ntile * BN + r;
       cplx<double> b = mk(0.0, 0.0);
       if (gj < N && k < K) b = ld(Rc + (long long)gj * K + k);
       Bs[lk][r] = b;
@@ -268,26 +278,26 @@ __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int N
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < F64_BK; ++kk) {
-      cplx<double> av[4], bv[4];
+      cplx<double> av[TM], bv[TN];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) av[a] = As[kk][ty + 16 * a];
+      for (int a = 0; a < TM; ++a) av[a] = As[kk][ty + 16 * a];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx + 16 * b];
+      for (int b = 0; b < TN; ++b) bv[b] = Bs[kk][tx + 16 * b];
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+      for (int a = 0; a < TM; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) cfma(acc[a][b], av[a], bv[b]);
+        for (int b = 0; b < TN; ++b) cfma(acc[a][b], av[a], bv[b]);
     }
     __syncthreads();
   }
   cplx<double>* Gp = G + J.g_off + (long long)p * M * N;
 #pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const int gi = mtile * F64_BM + ty + 16 * a;
+  for (int a = 0; a < TM; ++a) {
+    const int gi = mtile * BM + ty + 16 * a;
     if (gi >= M) continue;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const int gj = ntile * F64_BN + tx + 16 * b;
+    for (int b = 0; b < TN; ++b) {
+      const int gj = ntile * BN + tx + 16 * b;
       if (gj < N) Gp[(long long)gi * N + gj] = acc[a][b];
     }
   }
@@ -343,6 +353,9 @@ __global__ void combine_kernel(const CombineTable tab, const cplx<double>* __res
 
 int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains, const cplx<double>* phases,
                          cplx<double>* G, cudaStream_t stream, int njobs) {
+  // tile shapes of ED_TUNE_F64_TILE: rows x cols = 64x64, 32x64, 64x32, 32x32
+  static const int kBM[4] = {64, 32, 64, 32}, kBN[4] = {64, 64, 32, 32};
+  const int shape = P->f64_tile;
   GemmTable tab;
   tab.njobs = njobs;
   int tiles = 0;
@@ -353,13 +366,17 @@ int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains,
     d.right0 = j.right0;
     d.nright = j.nright;
     d.g_off = j.g_off;
-    d.mt = ceil_div(P->Ne, F64_BM);
-    d.nt = ceil_div((long long)j.nright * P->Ne, F64_BN);
+    d.mt = ceil_div(P->Ne, kBM[shape]);
+    d.nt = ceil_div((long long)j.nright * P->Ne, kBN[shape]);
     d.tile0 = tiles;
     tiles += d.mt * d.nt * P->nmom;
   }
+  auto kern = shape == 0   ? pair_gemm_f64_kernel<4, 4>
+              : shape == 1 ? pair_gemm_f64_kernel<2, 4>
+              : shape == 2 ? pair_gemm_f64_kernel<4, 2>
+                           : pair_gemm_f64_kernel<2, 2>;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  pair_gemm_f64_kernel<<<tiles, 256, 0, stream>>>(tab, P->Ne, P->V3, P->nmom, chains, phases, G);
+  kern<<<tiles, 256, 0, stream>>>(tab, P->Ne, P->V3, P->nmom, chains, phases, G);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   ED_RETURN_LAUNCH("pair GEMM (fp64)");
   return ED_OK;
@@ -456,7 +473,8 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0, "ed_elemental_plan_create: sizes must be positive");
   ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create: num_nabla must be 0, 1 or 2");
   ED_CHECK_ARG(moms, "ed_elemental_plan_create: null momentum list");
-  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR)) == 0,
+  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) == 0 &&
+                   (~mode & (ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) != 0,
                "ed_elemental_plan_create: unknown mode %d", mode);
   ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create: lattice too large");
   auto* P = new ed_elemental_plan();
@@ -468,6 +486,7 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   P->nmom = nmom;
   P->mode = mode & 0xff;
   P->no_factor = (mode & ED_MODE_FLAG_NO_FACTOR) != 0;
+  P->force_factor = (mode & ED_MODE_FLAG_FORCE_FACTOR) != 0;
   P->use_herm = true;
   P->moms.assign(moms, moms + 3 * nmom);
   int rc = ed::plan_build(P);
@@ -550,6 +569,47 @@ extern "C" int ed_elemental_factorised(const ed_elemental_plan* plan, int* facto
   if (pxy) *pxy = plan->fac_pxy;
   if (pz) *pz = plan->fac_pz;
   return ED_OK;
+}
+
+extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int value) {
+  ED_CHECK_ARG(plan, "ed_elemental_set_tuning: null plan");
+  switch (key) {
+    case ED_TUNE_F64_TILE:
+      ED_CHECK_ARG(value >= 0 && value <= 3, "ed_elemental_set_tuning: FP64 tile shape %d not in 0..3", value);
+      plan->f64_tile = value;
+      return ED_OK;
+    case ED_TUNE_TC_SLAB_KB:
+      ED_CHECK_ARG(value >= 0 && value <= TC_FLUSH_KB && (value & (value - 1)) == 0,
+                   "ed_elemental_set_tuning: slab of %d k-blocks (need 0 or a power of two <= %d)", value,
+                   TC_FLUSH_KB);
+      plan->tc_slab_kb = value;
+      return ED_OK;
+    case ED_TUNE_TC_GRID:
+      ED_CHECK_ARG(value >= 0 && value <= (1 << 20), "ed_elemental_set_tuning: grid of %d CTAs", value);
+      plan->tc_grid = value;
+      return ED_OK;
+    default:
+      ED_CHECK_ARG(false, "ed_elemental_set_tuning: unknown key %d", key);
+  }
+  return ED_ERR_ARG;
+}
+
+extern "C" int ed_elemental_get_tuning(const ed_elemental_plan* plan, int key, int* value) {
+  ED_CHECK_ARG(plan && value, "ed_elemental_get_tuning: null pointer");
+  switch (key) {
+    case ED_TUNE_F64_TILE:
+      *value = plan->f64_tile;
+      return ED_OK;
+    case ED_TUNE_TC_SLAB_KB:
+      *value = plan->tc_slab_kb;
+      return ED_OK;
+    case ED_TUNE_TC_GRID:
+      *value = plan->tc_grid;
+      return ED_OK;
+    default:
+      ED_CHECK_ARG(false, "ed_elemental_get_tuning: unknown key %d", key);
+  }
+  return ED_ERR_ARG;
 }
 
 // ------------------------------------------------------------ generic pair contractions

@@ -48,6 +48,7 @@ struct ed_elemental_plan {
   size_t tc_bytes;    // extra workspace
   // factorised phases: momenta = {(px,py)} x {pz} up to a few unused combinations
   bool no_factor = false;       // ED_MODE_FLAG_NO_FACTOR given at creation
+  bool force_factor = false;    // ED_MODE_FLAG_FORCE_FACTOR: factorise however many combinations go unused
   bool fac = false;             // the factorised-phase GEMM serves this plan
   int fac_pxy = 0, fac_pz = 0;  // distinct (px, py) pairs and pz values
   std::vector<int> fac_xy, fac_z;       // their values: fac_xy[2a], fac_xy[2a+1]; fac_z[c]
@@ -55,6 +56,10 @@ struct ed_elemental_plan {
   std::vector<int> fac_lchain;          // left-chain slots of one timeslice -> chain index
   std::vector<int> fac_lslot;           // chain index -> left-chain slot (-1 if never a left chain)
   cudaEvent_t prof_start = nullptr, prof_stop = nullptr;  // optional events around the pair GEMM
+  // launch settings (ed_elemental_set_tuning); 0 everywhere is the built-in default
+  int f64_tile = 0;    // FP64 pair GEMM tile, rows x cols: 0 = 64x64, 1 = 32x64, 2 = 64x32, 3 = 32x32
+  int tc_slab_kb = 0;  // k-blocks per lock-step slab of the factorised GEMM (0 = TC_FLUSH_KB)
+  int tc_grid = 0;     // CTAs of the persistent factorised GEMM (0 = every co-resident CTA)
 };
 
 namespace ed {

@@ -424,7 +424,7 @@ void tc_fac_setup(ed_elemental_plan* P) {
     ci[m] = c;
   }
   const int pxy = (int)xy.size() / 2, pz = (int)z.size();
-  if (pxy * pz > kMaxFac || (!ozaki && 4 * pxy * pz > 5 * P->nmom)) return;
+  if (pxy * pz > kMaxFac || (!ozaki && !P->force_factor && 4 * pxy * pz > 5 * P->nmom)) return;
   if (ozaki && (pxy > OZ_MAX_VAR || pz > OZ_MAX_VAR)) return;  // the row-maximum kernel keeps <= 16 per row
   std::vector<signed char> pidx(pxy * pz, -1);
   for (int m = 0; m < P->nmom; ++m) {
@@ -749,7 +749,9 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
   // persistent grid: every CTA co-resident (the step counter of the kernel relies on it)
-  const int grid = std::min(tiles, resident[KIND] * sms);
+  int grid = std::min(tiles, resident[KIND] * sms);
+  if (P->tc_grid > 0) grid = std::min(grid, P->tc_grid);
+  const int slab_kb = P->tc_slab_kb > 0 ? P->tc_slab_kb : TC_FLUSH_KB;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(TC_THREADS);
@@ -761,7 +763,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, tab, Ne, P->V3, sc, DF, tiles, TC_FLUSH_KB);
+  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, tab, Ne, P->V3, sc, DF, tiles, slab_kb);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");

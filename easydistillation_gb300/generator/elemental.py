@@ -7,7 +7,8 @@ operator combination).  ``calc`` returns the generator's internal
 ``[Nderiv, Nmom, Ne, Ne]`` complex128 device buffer, which the next call
 overwrites, exactly like the reference's ``self._VPV``.
 
-Extra keyword-only arguments: ``precision``, ``device`` and ``factorise``.
+Extra keyword-only arguments: ``precision``, ``device``, ``factorise`` and
+``autotune``.
 ``"fp64"`` is plain FP64 arithmetic with V rounded to complex64, as the
 reference.  The tensor-core modes ``"f16x3"``, ``"tf32x3"`` (relative error
 ~1e-7) and ``"bf16x3"`` (~1e-5) store the derivative chains in complex64 and
@@ -16,7 +17,12 @@ accumulation; they need ``Lx*Ly*Lz`` divisible by 32.  When the momentum list
 is a product set {(px, py)} x {pz} (e.g. all 27 momenta with |p|^2 <= 3),
 those GEMMs use the factorised phase exp(2 pi i p.x / L) = f(px, py) g(pz)
 with both operands prepared in HBM; ``factorise=False`` keeps the kernel
-that forms the phase-weighted operand on chip.
+that forms the phase-weighted operand on chip, ``factorise="force"``
+factorises however many (px, py) x pz combinations go unused.
+``autotune=True`` replaces ``factorise``: each plan (one per batch size) takes
+the GEMM form and launch settings that the autotuner
+(``easydistillation_gb300.tune``) measured fastest for its shape on this
+device, cached per device and shape.
 """
 
 from __future__ import annotations
@@ -117,7 +123,8 @@ class ElementalGenerator:
         *,
         precision: str = "fp64",
         device=None,
-        factorise: bool = True,
+        factorise=True,
+        autotune: bool = False,
     ) -> None:
         Lx, Ly, Lz, Lt = latt_size
         self.device = torch.device(device or "cuda")
@@ -132,13 +139,14 @@ class ElementalGenerator:
         self.Ne = Ne
         self.precision = precision
         self.factorise = factorise
+        self.autotune = autotune
         self._U = None
         self._VPV = torch.zeros((self.num_derivative, self.num_momentum, Ne, Ne), dtype=torch.complex128,
                                 device=self.device)
         self._eigenvector_data = None
         self._momentum_phase = MomentumPhase(latt_size, self.device)
-        self._plan = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, self.device,
-                                   factorise=factorise)
+        self._num_nabla = num_nabla
+        self._plan = self._make_plan(1)
         self._stage = None
 
         if is_blending and (dilution is not None):
@@ -147,6 +155,18 @@ class ElementalGenerator:
             raise ValueError("Dilution tuple is not defined.")
         else:
             self.stocastic_coeff = None
+
+    def _make_plan(self, batch: int) -> ElementalPlan:
+        """The plan for ``batch`` timeslices per run: built as ``factorise``
+        says, or, with ``autotune``, in the form and with the launch settings
+        the autotuner measured fastest for this shape (cached per device)."""
+        if self.autotune:
+            from ..tune import tuned_plan
+
+            return tuned_plan(self.latt_size, self.Ne, self._num_nabla, self.momentum_list, self.precision,
+                              self.device, batch=batch)
+        return ElementalPlan(self.latt_size, self.Ne, self._num_nabla, self.momentum_list, self.precision,
+                             self.device, batch=batch, factorise=self.factorise)
 
     def load(self, key: str):
         self._U = links_to_device(self.gauge_field.load(key)[:], self.latt_size, self.device)
@@ -221,12 +241,13 @@ class ElementalGenerator:
             out = torch.empty((len(ts),) + shape, dtype=torch.complex128, device=self.device)
         host_out = out.device.type == "cpu"
         if batch is None:
-            batch = admit_batch(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list, self.precision,
-                                self.device, max_batch=min(8, len(ts)), factorise=self.factorise)
+            # with autotune the GEMM form is chosen per batch size: admit what every form fits
+            forms = (True, False, "force") if self.autotune else (self.factorise,)
+            batch = min(admit_batch(self.latt_size, self.Ne, self._num_nabla, self.momentum_list, self.precision,
+                                    self.device, max_batch=min(8, len(ts)), factorise=f) for f in forms)
         plan = getattr(self, "_bplan", None)
         if plan is None or plan.batch != batch:
-            plan = self._bplan = ElementalPlan(self.latt_size, self.Ne, self._plan.num_nabla, self.momentum_list,
-                                               self.precision, self.device, batch=batch, factorise=self.factorise)
+            plan = self._bplan = self._make_plan(batch)
         evdt = self._eigenvector_data.dtype if isinstance(self._eigenvector_data, torch.Tensor) else torch.complex128
         if getattr(self, "_in_bufs", None) is None or len(self._in_bufs[0]) != batch or \
                 self._in_bufs[0][0].dtype != evdt:

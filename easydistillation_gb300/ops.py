@@ -185,19 +185,30 @@ def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
 
 #: elemental arithmetic modes (ED_MODE_* in include/easydist_gb300.h)
 MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3, "ozaki_i8": 4}
+_FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR = 0x100, 0x200
+#: plan launch settings (ED_TUNE_* keys)
+TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3}
+#: FP64 pair GEMM tile shapes (rows, cols) by ED_TUNE_F64_TILE value
+F64_TILES = {0: (64, 64), 1: (32, 64), 2: (64, 32), 3: (32, 32)}
 
 
 class ElementalPlan:
     """Owner of an ``ed_elemental_plan`` and its device workspace."""
 
     def __init__(self, latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "fp64", device=None,
-                 batch: int = 1, factorise: bool = True):
+                 batch: int = 1, factorise=True, tuning=None):
         """``factorise=False`` keeps the tensor-core GEMM that forms the
         phase-weighted operand inside the kernel even when the momentum list
-        factorises (ED_MODE_FLAG_NO_FACTOR)."""
+        factorises (ED_MODE_FLAG_NO_FACTOR); ``factorise="force"`` factorises
+        however many (px,py) x pz combinations the list leaves unused
+        (ED_MODE_FLAG_FORCE_FACTOR).  ``tuning``: launch settings
+        ``{"f64_tile", "tc_slab_kb", "tc_grid"}`` (see ``set_tuning``)."""
         if mode not in MODES:
             raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES)}")
-        cmode = MODES[mode] | (0 if factorise else 0x100)
+        if factorise not in (True, False, "force"):
+            raise ValueError(f"factorise must be True, False or 'force', not {factorise!r}")
+        cmode = MODES[mode] | {True: 0, False: _FLAG_NO_FACTOR, "force": _FLAG_FORCE_FACTOR}[factorise]
+        self.factorise = factorise
         Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
         self.latt_size = list(latt_size)
         self.Ne = Ne
@@ -231,6 +242,25 @@ class ElementalPlan:
         self.factorised = (pxy.value, pz.value) if fac.value else None
         self.device = torch.device(device or "cuda")
         self._ws = None
+        if tuning:
+            self.set_tuning(**tuning)
+
+    def set_tuning(self, **settings):
+        """Launch settings of later runs: ``f64_tile`` (0..3, see ``F64_TILES``),
+        ``tc_slab_kb`` (0 or a power of two <= 256), ``tc_grid`` (0 or a CTA
+        bound).  0 restores the built-in default."""
+        for name, value in settings.items():
+            if name not in TUNING_KEYS:
+                raise ValueError(f"unknown tuning setting {name!r}; available: {sorted(TUNING_KEYS)}")
+            call("ed_elemental_set_tuning", self._h, TUNING_KEYS[name], int(value))
+
+    def tuning(self) -> dict:
+        out = {}
+        for name, key in TUNING_KEYS.items():
+            v = ctypes.c_int()
+            call("ed_elemental_get_tuning", self._h, key, ctypes.byref(v))
+            out[name] = v.value
+        return out
 
     def workspace(self):
         if self._ws is None:

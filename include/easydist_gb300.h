@@ -62,6 +62,23 @@ extern "C" {
  * list factorises into {(px,py)} x {pz} (by default such plans use the
  * factorised-phase GEMM, whose operands are both prepared in HBM). */
 #define ED_MODE_FLAG_NO_FACTOR 0x100
+/* Flag OR-ed into a tensor-core mode at plan creation: use the factorised-phase
+ * GEMM whenever the momentum list fits {(px,py)} x {pz} (at most 128
+ * combinations), however many of those combinations the list leaves unused
+ * (by default at most a quarter may go unused).  Excludes
+ * ED_MODE_FLAG_NO_FACTOR.  An autotuner measures both forms. */
+#define ED_MODE_FLAG_FORCE_FACTOR 0x200
+
+/* ---- launch settings of a plan (ed_elemental_set_tuning keys) */
+#define ED_TUNE_F64_TILE 1   /* FP64 pair GEMM tile, rows x cols: 0 = 64x64 (default), 1 = 32x64,
+                              * 2 = 64x32, 3 = 32x32 */
+#define ED_TUNE_TC_SLAB_KB 2 /* k-blocks (of 32 fp16 / 16 tf32 elements) per lock-step slab of the
+                              * persistent factorised tensor-core GEMM: 0 (default, 256) or a power
+                              * of two <= 256.  The FP32 register sums are flushed to the
+                              * double-float results once per slab, so smaller slabs also shorten
+                              * the FP32 sums. */
+#define ED_TUNE_TC_GRID 3    /* CTAs of the persistent factorised GEMM: 0 (default: every CTA that
+                              * fits on the device at once) or an upper bound on that number */
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);
@@ -234,6 +251,17 @@ int ed_elemental_describe(const ed_elemental_plan* plan, int* ngroups, int* left
  * operands (conj(X) f_(px,py) and g_pz Y) are prepared in HBM.  pxy and pz
  * may be NULL.  No counterpart in the reference (an execution detail). */
 int ed_elemental_factorised(const ed_elemental_plan* plan, int* factorised, int* pxy, int* pz);
+
+/* Set / read one launch setting of a plan (ED_TUNE_* key).  Settings change
+ * how later runs are launched, never what they compute beyond rounding: the
+ * FP64 tile shape leaves every sum in the same order (bit-identical results);
+ * the slab length changes where the tensor-core path's FP32 sums are cut
+ * (results agree to the mode's tolerance).  Host-side only, no device call.
+ * ED_ERR_ARG for an unknown key or a value out of range.  No counterpart in
+ * the reference (its GEMMs are library calls); the project's autotuner
+ * (easydistillation_gb300/tune.py) picks the values by measurement. */
+int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int value);
+int ed_elemental_get_tuning(const ed_elemental_plan* plan, int key, int* value);
 
 /* Record the CUDA events `start` / `stop` (cudaEvent_t, or NULL to disable)
  * on the run's stream immediately before and after the pair-contraction

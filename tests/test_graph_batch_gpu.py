@@ -79,3 +79,37 @@ def test_graphed_factorised_modes(mode):
             assert rel_err(out[k], ref) < 1e-6
     runner.plan.check_status()
     assert runner.graph is not None
+
+
+def test_mixed_volume_graph_one_replay():
+    """Two volumes with their own Ne in ONE captured graph, bound to the input
+    tensors in place (repeated timeslices allowed); a second replay after the
+    inputs change recomputes everything."""
+    from easydistillation_gb300.batch import MixedVolumeGraph, VolumeBinding
+    from easydistillation_gb300.generator.elemental import links_to_device
+
+    moms = R.mom_dict_to_list(3)
+    specs = [([8, 4, 4, 2], 10, 0.3, 31, [0, 1, 1, 0, 1]), ([4, 4, 4, 3], 6, 0.1, 32, [2, 0, 1])]
+    vols, host = [], []
+    for latt, Ne, eps, seed, ts in specs:
+        gauge, evec = _inputs(latt, Ne, eps, seed)
+        vols.append(VolumeBinding(latt, Ne, links_to_device(gauge, latt, "cuda"),
+                                  torch.from_numpy(evec.reshape(latt[3], Ne, -1)).cuda(), ts))
+        host.append((gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3], evec))
+    mv = MixedVolumeGraph(vols, 2, moms, "f16x3", max_batch=2)
+    assert mv.passes() == 3 + 2
+
+    def check():
+        outs = [o.cpu().numpy() for o in mv.run()]
+        mv.check_status()
+        for (latt, Ne, eps, seed, ts), (Uh, evec), out in zip(specs, host, outs):
+            for k, t in enumerate(ts):
+                assert rel_err(out[k], R.elemental(evec[t], Uh[:, t], latt, 2, moms)) < 1e-6
+
+    check()
+    assert mv.graph is not None
+    rng = np.random.default_rng(5)
+    for v, (Uh, evec) in zip(vols, host):
+        evec *= np.exp(1j * rng.uniform(0, 2 * np.pi, evec.shape[:2]))[..., None, None, None, None]
+        v.evecs.copy_(torch.from_numpy(evec.reshape(evec.shape[0], evec.shape[1], -1)))
+    check()
