@@ -8,7 +8,9 @@ followed by one full classical Gram-Schmidt pass; two passes at the first
 step after a restart, where the new vector couples to every kept Ritz
 vector), the Rayleigh-Ritz step and the residual estimates are FP64.  The
 operator application is a callback (the library's Laplacian kernel, FP64 or
-FP32).  Convergence follows ARPACK's rule: a Ritz pair is accepted when
+FP32); the projected matrix (arrowhead + tridiagonal after a thick restart)
+is diagonalised by the library's batched FP64 eigensolver (``ed_arrow_eigh``).
+Convergence follows ARPACK's rule: a Ritz pair is accepted when
 ``|beta_m * y_m| <= tol * |theta|``.
 
 Several timeslices are solved in lock step (batch dimension B): every matvec
@@ -76,11 +78,18 @@ def trlanczos(
     v0: Optional[torch.Tensor] = None,
     device=None,
     seed: int = 12345,
+    small_eigh: str = "arrow",
 ) -> LanczosResult:
     """Thick-restart Lanczos (Wu & Simon) for the ``nev`` smallest eigenpairs.
 
     ``matvec(X)`` maps ``[B, n]`` complex128 to ``[B, n]`` complex128.
-    ``v0``: optional ``[B, n]`` start vectors (random otherwise)."""
+    ``v0``: optional ``[B, n]`` start vectors (random otherwise).
+    ``small_eigh``: how the projected matrix is diagonalised at each restart:
+    ``"arrow"`` (the library's batched arrowhead + tridiagonal eigensolver,
+    ``ops.arrow_eigh``, only the pairs the restart keeps) or ``"dense"``
+    (``torch.linalg.eigh``)."""
+    if small_eigh not in ("arrow", "dense"):
+        raise ValueError(f"small_eigh must be 'arrow' or 'dense', not {small_eigh!r}")
     device = torch.device(device or "cuda")
     ncv = ncv or default_ncv(nev, n)
     if not (nev < ncv < n + 1):
@@ -96,6 +105,18 @@ def trlanczos(
         v = v0.to(device=device, dtype=c128).clone()
     V[:, 0] = v / torch.linalg.vector_norm(v, dim=1, keepdim=True)
     T = torch.zeros((B, ncv, ncv), dtype=f64, device=device)
+    # Ritz pairs kept at a thick restart: the wanted ones plus half the rest
+    kk = min(ncv - 1, nev + max(1, (ncv - nev) // 2))
+
+    def projected_eigh(k):
+        if small_eigh == "dense":
+            return torch.linalg.eigh(T)
+        from .ops import arrow_eigh
+
+        d = torch.diagonal(T, dim1=1, dim2=2)
+        e = torch.diagonal(T, offset=1, dim1=1, dim2=2)
+        return arrow_eigh(d, e, T[:, :k, k] if k > 0 else None, nwant=kk)
+
     k = 0
     matvecs = 0
     beta_last = torch.zeros(B, dtype=f64, device=device)
@@ -127,7 +148,7 @@ def trlanczos(
                 T[:, j + 1, j] = beta
             else:
                 beta_last = beta
-        theta, Y = torch.linalg.eigh(T)
+        theta, Y = projected_eigh(k)
         resid = (beta_last.unsqueeze(1) * Y[:, ncv - 1, :]).abs()
         scale = torch.clamp(theta.abs(), min=torch.finfo(f64).eps ** (2.0 / 3.0))
         ok = resid[:, :nev] <= tol * scale[:, :nev]
@@ -137,7 +158,6 @@ def trlanczos(
         if restarts == max_restarts:
             break
         # thick restart: keep the kk smallest Ritz vectors plus the residual direction
-        kk = min(ncv - 1, nev + max(1, (ncv - nev) // 2))
         V[:, :kk] = _rotate(Y[:, :, :kk], V[:, :ncv])
         V[:, kk] = V[:, ncv]
         T.zero_()

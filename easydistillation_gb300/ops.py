@@ -135,6 +135,36 @@ def laplacian_status():
     return code.value
 
 
+def arrow_eigh(d: torch.Tensor, e: torch.Tensor, s: torch.Tensor = None, nwant: int = None):
+    """Lowest ``nwant`` eigenpairs of the batched arrowhead + tridiagonal
+    matrices of thick-restart Lanczos (``ed_arrow_eigh``): ``d`` [B, m] the
+    diagonal, ``e`` [B, m-1] the off-diagonal ``T[j, j+1]`` (used from row
+    ``ka`` on), ``s`` [B, ka] the border ``T[j, ka]`` (None: tridiagonal).
+    FP64 device tensors.  Returns (evals [B, nwant] ascending, evecs [B, m, nwant])."""
+    if d.dim() != 2 or d.dtype != torch.float64:
+        raise ValueError("d must be float64 [B, m]")
+    d = d.contiguous()
+    require_cuda(d, "d")
+    B, m = d.shape
+    nwant = m if nwant is None else int(nwant)
+    ka = 0 if s is None else s.shape[1]
+    e = e.contiguous() if m > 1 else torch.zeros((B, 1), dtype=torch.float64, device=d.device)
+    if e.dtype != torch.float64 or e.shape[0] != B or (m > 1 and e.shape[1] != m - 1):
+        raise ValueError("e must be float64 [B, m-1]")
+    if s is not None:
+        s = s.contiguous()
+        if s.dtype != torch.float64 or s.shape[0] != B:
+            raise ValueError("s must be float64 [B, ka]")
+    nbytes = ctypes.c_size_t()
+    call("ed_arrow_eigh_workspace", B, m, nwant, ctypes.byref(nbytes))
+    ws = torch.empty(nbytes.value // 8 + 1, dtype=torch.float64, device=d.device)
+    evals = torch.empty((B, nwant), dtype=torch.float64, device=d.device)
+    evecs = torch.empty((B, m, nwant), dtype=torch.float64, device=d.device)
+    call("ed_arrow_eigh", B, m, ka, nwant, ptr(d), None if s is None else ptr(s), ptr(e), ptr(evals), ptr(evecs),
+         ptr(ws), ws.numel() * 8, stream_handle())
+    return evals, evecs
+
+
 def covariant_derivative(links_soa_c128: torch.Tensor, F: torch.Tensor, latt_size, direction: int, out_dtype=None):
     """One hop ``D_d F = U_d(x) F(x+d) - U_d(x-d)^dag F(x-d)``
     (``lattice/generator/elemental.py:282-287``); ``F`` colour planes ``[nvec, 3, V3]``."""

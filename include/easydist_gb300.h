@@ -132,6 +132,24 @@ int ed_laplacian_config(int use_tma);
  * output of that launch is invalid).  The status word is cleared. */
 int ed_laplacian_status(int* code, void* stream);
 
+/* ---- projected eigenproblem of thick-restart Lanczos (eigenvector.py:234-257: the
+ *      dense eigensolve inside ARPACK / cupyx eigsh at every restart) */
+
+/* Lowest nwant eigenpairs of B real symmetric matrices of order m with the
+ * arrowhead + tridiagonal structure of a thick-restart Lanczos matrix:
+ *   T[j][j] = d[j];  T[j][ka] = T[ka][j] = s[j] (j < ka);
+ *   T[j][j+1] = T[j+1][j] = e[j] (ka <= j < m-1);  every other entry 0.
+ * ka = 0 is a plain tridiagonal matrix.  Device arrays, FP64: d [B][m],
+ * s [B][ka] (NULL when ka = 0), e [B][m-1] (entries below ka ignored).
+ * Out: evals [B][nwant] ascending, evecs [B][m][nwant] (column i is the unit
+ * eigenvector of evals[i]; the columns are orthonormal).  Bisection on Sturm
+ * counts, inverse iteration (clusters closer than 1e-7 ||T|| orthogonalised
+ * in order), two Gram-Schmidt passes; no host synchronisation.
+ * workspace: ed_arrow_eigh_workspace bytes of device memory, 8-byte aligned. */
+int ed_arrow_eigh_workspace(int B, int m, int nwant, size_t* bytes);
+int ed_arrow_eigh(int B, int m, int ka, int nwant, const double* d, const double* s, const double* e,
+                  double* evals, double* evecs, void* workspace, size_t workspace_bytes, void* stream);
+
 /* One covariant-derivative hop D_dir on nvec colour-plane vectors:
  * out = U_d(x) in(x+d) - U_d(x-d)^dag in(x-d).
  * Replaces one iteration of ElementalGenerator._nD (elemental.py:282-287).

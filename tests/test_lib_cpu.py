@@ -45,6 +45,13 @@ def test_argument_validation_is_host_side():
     assert L.ed_vectors_to_planes(0, 0, 0, 0, 64, 16, 32, None) == _lib.ED_ERR_ARG
     with pytest.raises(ValueError):
         _lib.check(_lib.ED_ERR_ARG, "x")
+    # the arrow eigensolver checks its sizes on the host
+    nb = ctypes.c_size_t()
+    assert L.ed_arrow_eigh_workspace(2, 10, 4, ctypes.byref(nb)) == _lib.ED_OK and nb.value == 2 * 10 * 4 * 6 * 8
+    assert L.ed_arrow_eigh_workspace(2, 10, 11, ctypes.byref(nb)) == _lib.ED_ERR_ARG
+    assert L.ed_arrow_eigh(2, 10, 10, 4, 8, 8, 8, 8, 8, 8, 1 << 20, None) == _lib.ED_ERR_ARG  # ka >= m
+    assert L.ed_arrow_eigh(2, 10, 3, 4, 8, None, 8, 8, 8, 8, 1 << 20, None) == _lib.ED_ERR_ARG  # no border
+    assert L.ed_arrow_eigh(2, 10, 0, 4, 8, None, 8, 8, 8, 8, 100, None) == _lib.ED_ERR_WORKSPACE
 
 
 @pytest.mark.parametrize(
