@@ -260,7 +260,7 @@ __global__ void arrow_invit_kernel(int B, int m, int ka, int nwant, const double
 
 // Two classical Gram-Schmidt passes per vector, in eigenvalue order; one
 // block per matrix.  Q [nwant][m] (vector-contiguous) -> evecs [m][nwant].
-constexpr int MGS_THREADS = 256;
+constexpr int MGS_THREADS = 1024;
 __global__ void __launch_bounds__(MGS_THREADS) arrow_mgs_kernel(int m, int nwant, double* __restrict__ Q,
                                                                 double* __restrict__ evecs) {
   extern __shared__ double h[];  // [nwant] projections, then 32 partial sums

@@ -43,19 +43,26 @@ def default_ncv(nev: int, n: int) -> int:
     return min(max(3 * nev, nev + 32), n - 1)
 
 
-def _reorth(Vj: torch.Tensor, w: torch.Tensor):
-    """Two passes of classical Gram-Schmidt of w [B, n] against rows of Vj [B, j, n]."""
-    h = torch.bmm(w.unsqueeze(1).conj(), Vj.transpose(1, 2)).conj()  # [B, 1, j] = V^H w
-    w = w - torch.bmm(h, Vj).squeeze(1)
-    h2 = torch.bmm(w.unsqueeze(1).conj(), Vj.transpose(1, 2)).conj()
-    w = w - torch.bmm(h2, Vj).squeeze(1)
-    return w, (h + h2).squeeze(1)
+def _reorth_once(Vj: torch.Tensor, w: torch.Tensor, kernel: bool = True):
+    """One classical Gram-Schmidt pass of w [B, n] against the rows of Vj [B, j, n]:
+    the library's batched kernel (``ops.cgs_pass``, which also returns the new
+    norm) or two torch batched GEMVs.  Returns (w, h, ||w||)."""
+    if kernel:
+        from .ops import cgs_pass
 
-
-def _reorth_once(Vj: torch.Tensor, w: torch.Tensor):
-    """One classical Gram-Schmidt pass of w [B, n] against the rows of Vj [B, j, n]."""
+        w = w.contiguous()
+        h, nrm = cgs_pass(Vj, Vj.shape[1], w, norm=True)
+        return w, h, nrm
     h = torch.bmm(w.unsqueeze(1).conj(), Vj.transpose(1, 2)).conj()  # [B, 1, j]
-    return w - torch.bmm(h, Vj).squeeze(1), h.squeeze(1)
+    w = w - torch.bmm(h, Vj).squeeze(1)
+    return w, h.squeeze(1), torch.linalg.vector_norm(w, dim=1)
+
+
+def _reorth(Vj: torch.Tensor, w: torch.Tensor, kernel: bool = True):
+    """Two passes of classical Gram-Schmidt of w [B, n] against rows of Vj [B, j, n]."""
+    w, h, _ = _reorth_once(Vj, w, kernel)
+    w, h2, nrm = _reorth_once(Vj, w, kernel)
+    return w, h + h2, nrm
 
 
 def _rotate(Y: torch.Tensor, V: torch.Tensor) -> torch.Tensor:
@@ -79,6 +86,8 @@ def trlanczos(
     device=None,
     seed: int = 12345,
     small_eigh: str = "arrow",
+    gs_kernel: bool = True,
+    graph: bool = True,
 ) -> LanczosResult:
     """Thick-restart Lanczos (Wu & Simon) for the ``nev`` smallest eigenpairs.
 
@@ -87,7 +96,13 @@ def trlanczos(
     ``small_eigh``: how the projected matrix is diagonalised at each restart:
     ``"arrow"`` (the library's batched arrowhead + tridiagonal eigensolver,
     ``ops.arrow_eigh``, only the pairs the restart keeps) or ``"dense"``
-    (``torch.linalg.eigh``)."""
+    (``torch.linalg.eigh``).  ``gs_kernel``: Gram-Schmidt passes by the
+    library's batched kernel (``ed_cgs_pass``) rather than torch GEMVs.
+    ``graph``: replay the Lanczos steps of a restart cycle (identical from the
+    second restart on) from a captured CUDA graph instead of issuing them one
+    by one from Python; ``matvec`` must then be capturable (stream-ordered,
+    no host synchronisation), as the library's stencil and Chebyshev
+    operators are."""
     if small_eigh not in ("arrow", "dense"):
         raise ValueError(f"small_eigh must be 'arrow' or 'dense', not {small_eigh!r}")
     device = torch.device(device or "cuda")
@@ -117,20 +132,16 @@ def trlanczos(
         e = torch.diagonal(T, offset=1, dim1=1, dim2=2)
         return arrow_eigh(d, e, T[:, :k, k] if k > 0 else None, nwant=kk)
 
-    k = 0
-    matvecs = 0
     beta_last = torch.zeros(B, dtype=f64, device=device)
-    theta = Y = None
-    converged = False
-    restarts = 0
-    for restarts in range(1, max_restarts + 1):
+
+    def cycle(k):
+        """Lanczos steps k .. ncv-1, in place on V, T and beta_last."""
         for j in range(k, ncv):
             w = matvec(V[:, j])
-            matvecs += 1
             if j == k:
                 # first step after a (re)start: w couples to every kept vector
                 # (the arrow of the thick restart), so project fully, twice
-                w, h = _reorth(V[:, : j + 1], w)
+                w, h, beta = _reorth(V[:, : j + 1], w, gs_kernel)
                 T[:, j, j] = h[:, j].real
             else:
                 # three-term recurrence, then one full Gram-Schmidt pass that
@@ -138,16 +149,40 @@ def trlanczos(
                 vj = V[:, j]
                 alpha = torch.sum(vj.conj() * w, dim=1).real
                 w = w - alpha.unsqueeze(1).to(w.dtype) * vj - T[:, j - 1, j].unsqueeze(1).to(w.dtype) * V[:, j - 1]
-                w, h = _reorth_once(V[:, : j + 1], w)
+                w, h, beta = _reorth_once(V[:, : j + 1], w, gs_kernel)
                 T[:, j, j] = alpha + h[:, j].real
-            beta = torch.linalg.vector_norm(w, dim=1)
             safe = torch.where(beta > 0, beta, torch.ones_like(beta))
             V[:, j + 1] = w / safe.unsqueeze(1)
             if j + 1 < ncv:
                 T[:, j, j + 1] = beta
                 T[:, j + 1, j] = beta
             else:
-                beta_last = beta
+                beta_last.copy_(beta)
+
+    use_graph = graph and device.type == "cuda"
+    cycle_graph = None
+    restart_cycles = 0
+    k = 0
+    matvecs = 0
+    theta = Y = None
+    converged = False
+    restarts = 0
+    for restarts in range(1, max_restarts + 1):
+        if k == 0 or not use_graph or restart_cycles == 0:
+            cycle(k)  # the first restart cycle also warms up everything the capture will record
+        else:
+            if cycle_graph is None:
+                cycle_graph = torch.cuda.CUDAGraph()
+                cs = torch.cuda.Stream(device)
+                cs.wait_stream(torch.cuda.current_stream(device))
+                with torch.cuda.stream(cs):
+                    with torch.cuda.graph(cycle_graph, stream=cs):
+                        cycle(k)
+                torch.cuda.current_stream(device).wait_stream(cs)
+            cycle_graph.replay()
+        if k > 0:
+            restart_cycles += 1
+        matvecs += ncv - k
         theta, Y = projected_eigh(k)
         resid = (beta_last.unsqueeze(1) * Y[:, ncv - 1, :]).abs()
         scale = torch.clamp(theta.abs(), min=torch.finfo(f64).eps ** (2.0 / 3.0))

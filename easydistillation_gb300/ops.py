@@ -135,6 +135,29 @@ def laplacian_status():
     return code.value
 
 
+def cgs_pass(V: torch.Tensor, r: int, w: torch.Tensor, h: torch.Tensor = None, norm: bool = False):
+    """One classical Gram-Schmidt pass (``ed_cgs_pass``): ``h = V[:, :r]^H w``,
+    ``w -= V[:, :r] h`` in place.  ``V``: complex128 [B, rows, n] with
+    contiguous rows (any batch stride), ``w``: contiguous complex128 [B, n].
+    Returns ``h`` [B, r], and with ``norm`` also ``||w||`` [B] float64 of the
+    updated w (from the kernel's per-block partial sums)."""
+    if V.dtype != torch.complex128 or w.dtype != torch.complex128:
+        raise ValueError("cgs_pass works on complex128")
+    if not (V.is_cuda and w.is_cuda) or not w.is_contiguous():
+        raise ValueError("V and w must be CUDA tensors, w contiguous")
+    B, rows, n = V.shape
+    if V.stride(2) != 1 or V.stride(1) != n or not (0 < r <= rows) or tuple(w.shape) != (B, n):
+        raise ValueError("V must be [B, rows, n] with contiguous rows, w [B, n], 0 < r <= rows")
+    if h is None:
+        h = torch.empty((B, r), dtype=torch.complex128, device=w.device)
+    part = torch.empty((B, (n + 255) // 256), dtype=torch.float64, device=w.device) if norm else None
+    call("ed_cgs_pass", B, r, n, ptr(V), V.stride(0), ptr(w), ptr(h), h.stride(0),
+         None if part is None else ptr(part), stream_handle())
+    if norm:
+        return h, torch.sqrt(part.sum(dim=1))
+    return h
+
+
 def arrow_eigh(d: torch.Tensor, e: torch.Tensor, s: torch.Tensor = None, nwant: int = None):
     """Lowest ``nwant`` eigenpairs of the batched arrowhead + tridiagonal
     matrices of thick-restart Lanczos (``ed_arrow_eigh``): ``d`` [B, m] the

@@ -146,6 +146,19 @@ int ed_laplacian_status(int* code, void* stream);
  * counts, inverse iteration (clusters closer than 1e-7 ||T|| orthogonalised
  * in order), two Gram-Schmidt passes; no host synchronisation.
  * workspace: ed_arrow_eigh_workspace bytes of device memory, 8-byte aligned. */
+/* One classical Gram-Schmidt pass of the Lanczos reorthogonalisation, batched
+ * over B problems, complex128 (double2):
+ *   h[b][i] = sum_x conj(V[b][i][x]) w[b][x]   (i < r),  then
+ *   w[b][x] -= sum_i h[b][i] V[b][i][x].
+ * V: r rows of length n per problem, problem b at V + b*v_bstride (rows
+ * contiguous, row stride n); w [B][n] updated in place; h [B][ldh].  Pointers
+ * 16-byte aligned.  norm_part (optional, NULL to skip): [B][ceil(n/256)]
+ * partial sums of |w_new|^2, whose row sums are ||w_new||^2.  Two kernels,
+ * each streaming V once; on GB300 they are bound by the FP64 pipe (8 flops
+ * per 16-byte element: about 2.5 TB/s at the FP64 peak), not by HBM. */
+int ed_cgs_pass(int B, int r, long long n, const void* V, long long v_bstride, void* w, void* h, int ldh,
+                double* norm_part, void* stream);
+
 int ed_arrow_eigh_workspace(int B, int m, int nwant, size_t* bytes);
 int ed_arrow_eigh(int B, int m, int ka, int nwant, const double* d, const double* s, const double* e,
                   double* evals, double* evecs, void* workspace, size_t workspace_bytes, void* stream);

@@ -99,3 +99,43 @@ def test_lanczos_arrow_matches_dense_eigh():
     x0 = a.evecs[:, 0]
     res = torch.linalg.vector_norm(mv(x0) - a.evals[:, :1].to(x0.dtype) * x0, dim=1)
     assert float(res.max()) < 1e-9
+
+
+@pytest.mark.parametrize("B,rows,r,n", [(3, 9, 7, 1000), (2, 40, 33, 3 * 216), (1, 5, 5, 17), (2, 1500, 1100, 64)])
+def test_cgs_pass_matches_torch(B, rows, r, n):
+    """The batched Gram-Schmidt kernel against torch GEMVs, on a basis view
+    whose batch stride exceeds r*n (rows beyond r are never read)."""
+    from easydistillation_gb300.ops import cgs_pass
+
+    g = torch.Generator(device="cuda").manual_seed(r)
+    V = torch.randn((B, rows + 1, n), dtype=torch.complex128, device="cuda", generator=g)
+    w = torch.randn((B, n), dtype=torch.complex128, device="cuda", generator=g)
+    Vj = V[:, :r]
+    h_ref = torch.bmm(w.unsqueeze(1).conj(), Vj.transpose(1, 2)).conj().squeeze(1)
+    w_ref = w - torch.bmm(h_ref.unsqueeze(1), Vj).squeeze(1)
+    w2 = w.clone()
+    h, nrm = cgs_pass(Vj, r, w2, norm=True)
+    scale = float(torch.linalg.vector_norm(w)) * float(torch.linalg.vector_norm(Vj))
+    assert float(torch.linalg.vector_norm(h - h_ref)) <= 1e-13 * scale
+    assert float(torch.linalg.vector_norm(w2 - w_ref)) <= 1e-13 * scale * r ** 0.5
+    assert torch.allclose(nrm, torch.linalg.vector_norm(w2, dim=1), rtol=1e-13, atol=0)
+
+
+def test_lanczos_gs_kernel_matches_torch_gemv():
+    from easydistillation_gb300.lanczos import trlanczos
+    from easydistillation_gb300.ops import laplacian, links_to_soa
+    from oracle import restatement as R
+
+    latt = [6, 6, 6, 2]
+    V3 = 216
+    g = R.synthetic_gauge(latt, 0.3, 4)
+    U = torch.from_numpy(np.ascontiguousarray(g.transpose(4, 0, 1, 2, 3, 5, 6))).cuda()
+    L = links_to_soa(U, latt)
+
+    def mv(X):
+        return laplacian(L, X.contiguous().view(2, 1, 3, V3), latt).view(2, 3 * V3)
+
+    a = trlanczos(mv, 2, 3 * V3, 16, 1e-11, ncv=40, gs_kernel=True)
+    b = trlanczos(mv, 2, 3 * V3, 16, 1e-11, ncv=40, gs_kernel=False)
+    assert a.converged and b.converged
+    assert torch.allclose(a.evals, b.evals, rtol=1e-11, atol=0)

@@ -52,6 +52,9 @@ def test_argument_validation_is_host_side():
     assert L.ed_arrow_eigh(2, 10, 10, 4, 8, 8, 8, 8, 8, 8, 1 << 20, None) == _lib.ED_ERR_ARG  # ka >= m
     assert L.ed_arrow_eigh(2, 10, 3, 4, 8, None, 8, 8, 8, 8, 1 << 20, None) == _lib.ED_ERR_ARG  # no border
     assert L.ed_arrow_eigh(2, 10, 0, 4, 8, None, 8, 8, 8, 8, 100, None) == _lib.ED_ERR_WORKSPACE
+    assert L.ed_cgs_pass(2, 5, 100, 16, 400, 16, 16, 5, None, None) == _lib.ED_ERR_ARG  # batch stride < r*n
+    assert L.ed_cgs_pass(2, 5, 100, 8, 500, 16, 16, 5, None, None) == _lib.ED_ERR_ARG  # misaligned V
+    assert L.ed_cgs_pass(2, 5, 100, 16, 500, 16, 16, 4, None, None) == _lib.ED_ERR_ARG  # ldh < r
 
 
 @pytest.mark.parametrize(
