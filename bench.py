@@ -60,6 +60,8 @@ def parse():
                     help="build the plans with the built-in defaults instead of the autotuner's choice (which is "
                          "measured before the timed region and cached per device and shape)")
     ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
+    ap.add_argument("--stencil", action="store_true",
+                    help="measure only the Laplacian kernels (c64, c64 TMA-staged, c128) at --lattice")
     ap.add_argument("--eigen-batch", type=int, default=8)
     ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--eigen-cpu", action="store_true", help="also time the oracle's scipy eigensolve (slow)")
@@ -629,6 +631,23 @@ def run_grad(args):
     print(json.dumps(line), flush=True)
 
 
+def run_stencil(args):
+    """Secondary measurement (``--stencil``): the HBM roofline of the Laplacian
+    kernels alone (the lines ``bench_stencil`` adds to the main JSON line), at
+    ``--lattice`` (default 32^3 x 64) on 4 distinct timeslices of links tiled
+    over Lt."""
+    import torch
+
+    from easydistillation_gb300.generator.elemental import links_to_device
+
+    latt = [int(v) for v in args.lattice.split(",")] if args.lattice else LATT
+    dev = torch.device("cuda", 0)
+    gauge, _ = make_inputs(latt, 1, distinct_t=4)
+    U = links_to_device(gauge, latt, dev)
+    print(json.dumps({"metric": "laplacian HBM roofline", "stencil_roofline": bench_stencil(U, latt, dev)}),
+          flush=True)
+
+
 def run_eigen(args):
     """Secondary measurement (``--eigen``): EigenvectorGenerator.calc_batch on
     ``--eigen-batch`` timeslices at ``--lattice`` (default 24^3 x 64, Ne from
@@ -658,19 +677,16 @@ def run_eigen(args):
     gen = EigenvectorGenerator(latt, _Src(), Ne, 1e-10, stencil_precision=args.eigen_precision, ncv=args.eigen_ncv)
     gen.load("bench")
     ts = list(range(args.eigen_batch))
-    if args.warmup > 0:
-        gen.calc_batch(ts)  # one untimed solve of the same batch: first-use setup of the kernels and libraries
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    kw = {}
     if args.eigen_poly > 0:
         # lambda_cut: 15 % above the largest wanted eigenvalue, from a first plain solve of one timeslice
         _, ev0 = gen.calc_batch(ts[:1])
-        cut = 1.15 * float(ev0[0, -1])
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        evecs, evals = gen.calc_batch(ts, polynomial_degree=args.eigen_poly, lambda_cut=cut)
-    else:
-        evecs, evals = gen.calc_batch(ts)
+        kw = {"polynomial_degree": args.eigen_poly, "lambda_cut": 1.15 * float(ev0[0, -1])}
+    if args.warmup > 0:
+        gen.calc_batch(ts, **kw)  # one untimed solve of the same call: first-use setup of kernels and libraries
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    evecs, evals = gen.calc_batch(ts, **kw)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     line = {"metric": f"eigensolve timeslices/s {latt[0]}^3 Ne={Ne} tol 1e-10", "value": len(ts) / dt,
@@ -700,6 +716,9 @@ def main():
         return
     if args.grad:
         run_grad(args)
+        return
+    if args.stencil:
+        run_stencil(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -205,7 +205,7 @@ def _synthetic_inputs(latt_size, Ne, device, evec_dtype, seed=7):
 #: the FP64 tile shapes are timed on a lattice of at most this extent per
 #: direction (the tile choice depends on Ne and the pair groups; the time of
 #: every shape grows in proportion to K = 3 V3)
-FP64_PROXY_EXTENT = 16
+FP64_PROXY_EXTENT = 12
 
 
 def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "f16x3", batch: int = 1,
@@ -231,6 +231,7 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
     meas_latt = list(latt_size[:3]) + list(latt_size[3:])
     if mode == "fp64":
         meas_latt[:3] = [min(FP64_PROXY_EXTENT, int(L)) for L in latt_size[:3]]
+        reps = min(reps, 2)  # the tile shapes differ by tens of percent
     links, vecs = _synthetic_inputs(meas_latt, Ne, device, evec_dtype)
     V3 = meas_latt[0] * meas_latt[1] * meas_latt[2]
     outs = [torch.empty((nd, nm, Ne, Ne), dtype=torch.complex128, device=device) for _ in range(batch)]
