@@ -70,7 +70,7 @@ __device__ __forceinline__ void mvd_add(cplx<T> (&y)[3], const cplx<T> (&U)[9], 
 
 // One launch covers nt timeslices x nvec vectors; grid (sites/S/128, nvec, nt).
 template <typename T, int S>
-__global__ void __launch_bounds__(128) laplacian_kernel(Latt L, const cplx<T>* __restrict__ links,
+__global__ void __launch_bounds__(128, 8) laplacian_kernel(Latt L, const cplx<T>* __restrict__ links,
                                                         const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out,
                                                         long long link_tstride, long long in_tstride,
                                                         long long out_tstride, T diag) {
