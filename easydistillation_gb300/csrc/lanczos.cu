@@ -1,0 +1,545 @@
+// Native thick-restart Lanczos for the lowest eigenpairs of the 3D covariant
+// Laplacian, batched over timeslices (ed_lanczos_tr).
+//
+// This is the eigensolve of EigenvectorGenerator.calc
+// (lattice/generator/eigenvector.py:234-257: scipy / cupyx
+// eigsh(LinearOperator, k=Ne, which="SA", tol), with the QUDA path's Chebyshev
+// acceleration at :295-299), written as a host loop over the library's
+// kernels: one FP64 stencil launch per Lanczos step for all timeslices
+// (launch_laplacian), the three-term recurrence and one classical
+// Gram-Schmidt pass per step (two at the first step after a restart) by
+// ed_cgs_pass, the projected arrowhead + tridiagonal matrix diagonalised by
+// ed_arrow_eigh at each restart, the restart rotation Y^T V as one cuBLAS
+// DGEMM on the (re, im) pairs of the basis.  Everything is FP64 on the GPU;
+// the host reads one convergence counter per restart.  Convergence follows
+// ARPACK's rule: Ritz pair i is accepted when |beta_m y_{m,i}| <= tol |theta_i|.
+//
+// With a Chebyshev degree the iteration runs on -T_deg((2L - (12 + cut)) /
+// (12 - cut)) (sign flipped for even degree so the wanted modes are the
+// smallest), which keeps L's eigenvectors and their order below the cut; the
+// eigenvalues returned are then the Rayleigh quotients x^H L x.
+
+#include <cublas_v2.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace ed {
+namespace {
+
+constexpr int LZ_THREADS = 256;
+
+// ED_OK, or the library's CUDA error status for a failed call
+inline int lz_chk(cudaError_t e, const char* what) { return e == cudaSuccess ? ED_OK : cuda_status(e, what); }
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int q = 0; q < LZ_THREADS / 32; ++q) t += red[q];
+  __syncthreads();
+  return t;
+}
+
+// sum of the nblk partials of problem b, in a fixed order (every block gets the same value); thread 0 sums,
+// the block shares the result
+__device__ __forceinline__ double sum_parts(const double* part, int b, int nblk) {
+  __shared__ double total;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < nblk; ++q) t += part[(long long)b * nblk + q];
+    total = t;
+  }
+  __syncthreads();
+  return total;
+}
+
+// w[b] = pseudo-random start vector (integer hash of (b, x), values in [-1, 1))
+__global__ void lz_random_kernel(int B, long long n, double2* __restrict__ w, unsigned seed) {
+  const int b = blockIdx.y;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)x * 0x9E3779B1u ^ ((uint32_t)b * 0x85EBCA77u + seed);
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    uint32_t g = h * 0x9E3779B1u + 0x7F4A7C15u;
+    g ^= g >> 13;
+    g *= 0x5BD1E995u;
+    g ^= g >> 15;
+    w[(long long)b * n + x] = make_double2((double)(h >> 8) * (2.0 / 16777216.0) - 1.0,
+                                           (double)(g >> 8) * (2.0 / 16777216.0) - 1.0);
+  }
+}
+
+// part[b][blk] = partial of Re(sum_x conj(a[b][x]) c[b][x])
+__global__ void __launch_bounds__(LZ_THREADS) lz_dot_kernel(long long n, const double2* __restrict__ a, long long ab,
+                                                            const double2* __restrict__ c, long long cb,
+                                                            double* __restrict__ part) {
+  __shared__ double red[LZ_THREADS / 32];
+  const int b = blockIdx.y;
+  double acc = 0.0;
+  for (long long x = (long long)blockIdx.x * LZ_THREADS + threadIdx.x; x < n; x += (long long)gridDim.x * LZ_THREADS) {
+    const double2 u = a[(long long)b * ab + x], v = c[(long long)b * cb + x];
+    acc = fma(u.x, v.x, fma(u.y, v.y, acc));
+  }
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) part[(long long)b * gridDim.x + blockIdx.x] = t;
+}
+
+// dst[b] = src[b] / sqrt(sum of part[b])
+__global__ void lz_normalise_kernel(long long n, const double2* __restrict__ src, const double* __restrict__ part,
+                                    int nblk, double2* __restrict__ dst, long long db) {
+  const int b = blockIdx.y;
+  const double nrm = sqrt(sum_parts(part, b, nblk));
+  const double inv = nrm > 0.0 ? 1.0 / nrm : 1.0;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    const double2 v = src[(long long)b * n + x];
+    dst[(long long)b * db + x] = make_double2(v.x * inv, v.y * inv);
+  }
+}
+
+// alpha = sum of part[b] (= Re <v_j, w>); d[j] = alpha; w -= alpha v_j + e[j-1] v_{j-1}
+__global__ void lz_three_term_kernel(long long n, const double2* __restrict__ V, long long vb, int j,
+                                     double2* __restrict__ w, const double* __restrict__ part, int nblk,
+                                     double* __restrict__ d, const double* __restrict__ e, int ncv) {
+  const int b = blockIdx.y;
+  const double alpha = sum_parts(part, b, nblk);
+  const double beta = e[(long long)b * (ncv - 1) + j - 1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) d[(long long)b * ncv + j] = alpha;
+  const double2* vj = V + (long long)b * vb + (long long)j * n;
+  const double2* vm = vj - n;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    double2 o = w[(long long)b * n + x];
+    const double2 a = vj[x], c = vm[x];
+    o.x -= alpha * a.x + beta * c.x;
+    o.y -= alpha * a.y + beta * c.y;
+    w[(long long)b * n + x] = o;
+  }
+}
+
+// End of step j: beta = ||w|| (from the Gram-Schmidt norm partials);
+// d[j] (+)= Re h[j] (+ Re h2[j]); e[j] = beta (or beta_last at the last step);
+// V[j+1] = w / beta.
+__global__ void lz_finish_kernel(long long n, double2* __restrict__ V, long long vb, int j, const double2* __restrict__ w,
+                                 const double2* __restrict__ h, const double2* __restrict__ h2, int ldh,
+                                 const double* __restrict__ npart, int nblk, double* __restrict__ d,
+                                 double* __restrict__ e, double* __restrict__ beta_last, int ncv, int first) {
+  const int b = blockIdx.y;
+  const double beta = sqrt(sum_parts(npart, b, nblk));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double dj = h[(long long)b * ldh + j].x + (h2 ? h2[(long long)b * ldh + j].x : 0.0);
+    if (!first) dj += d[(long long)b * ncv + j];
+    d[(long long)b * ncv + j] = dj;
+    if (j + 1 < ncv)
+      e[(long long)b * (ncv - 1) + j] = beta;
+    else
+      beta_last[b] = beta;
+  }
+  const double inv = beta > 0.0 ? 1.0 / beta : 1.0;
+  double2* dst = V + (long long)b * vb + (long long)(j + 1) * n;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    const double2 v = w[(long long)b * n + x];
+    dst[x] = make_double2(v.x * inv, v.y * inv);
+  }
+}
+
+// Chebyshev recurrence step: out = s * (f (a Lx + c x) - prev) with f = 2 (or 1 and no prev for the first step);
+// x and prev may be strided (xb, pb elements per problem), Lx and out are [B][n].
+__global__ void lz_cheb_kernel(long long n, const double2* __restrict__ Lx, const double2* __restrict__ x, long long xb,
+                               const double2* __restrict__ prev, long long pb, double2* __restrict__ out, double a,
+                               double c, double f, double s) {
+  const int b = blockIdx.y;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 l = Lx[(long long)b * n + i], v = x[(long long)b * xb + i];
+    double re = f * (a * l.x + c * v.x), im = f * (a * l.y + c * v.y);
+    if (prev) {
+      const double2 p = prev[(long long)b * pb + i];
+      re -= p.x;
+      im -= p.y;
+    }
+    out[(long long)b * n + i] = make_double2(s * re, s * im);
+  }
+}
+
+// Count the wanted Ritz pairs that fail |beta_last y_{m-1,i}| <= tol max(|theta_i|, eps^(2/3)).
+__global__ void lz_converged_kernel(int B, int ncv, int kk, int nev, const double* __restrict__ theta,
+                                    const double* __restrict__ Y, const double* __restrict__ beta_last, double tol,
+                                    int* __restrict__ nbad) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * nev) return;
+  const int b = idx / nev, i = idx - b * nev;
+  const double r = fabs(beta_last[b] * Y[((long long)b * ncv + ncv - 1) * kk + i]);
+  const double sc = fmax(fabs(theta[(long long)b * kk + i]), 3.6e-11 /* eps^(2/3) */);
+  if (!(r <= tol * sc)) atomicAdd(nbad, 1);
+}
+
+// Thick restart: d[i] = theta_i, s[i] = beta_last y_{m-1,i} for the kk kept pairs.
+__global__ void lz_restart_kernel(int B, int ncv, int kk, const double* __restrict__ theta,
+                                  const double* __restrict__ Y, const double* __restrict__ beta_last,
+                                  double* __restrict__ d, double* __restrict__ s) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * kk) return;
+  const int b = idx / kk, i = idx - b * kk;
+  d[(long long)b * ncv + i] = theta[(long long)b * kk + i];
+  s[(long long)b * kk + i] = beta_last[b] * Y[((long long)b * ncv + ncv - 1) * kk + i];
+}
+
+// Rayleigh quotients Re(x^H L x) / ||x||^2, one block per (problem, vector).
+__global__ void __launch_bounds__(LZ_THREADS) lz_rq_kernel(long long n, const double2* __restrict__ X,
+                                                           const double2* __restrict__ LX, double* __restrict__ rq) {
+  __shared__ double red[LZ_THREADS / 32];
+  const long long v = blockIdx.x;
+  double num = 0.0, den = 0.0;
+  for (long long i = threadIdx.x; i < n; i += LZ_THREADS) {
+    const double2 x = X[v * n + i], l = LX[v * n + i];
+    num = fma(x.x, l.x, fma(x.y, l.y, num));
+    den = fma(x.x, x.x, fma(x.y, x.y, den));
+  }
+  num = block_sum(num, red);
+  den = block_sum(den, red);
+  if (threadIdx.x == 0) rq[v] = den > 0.0 ? num / den : 0.0;
+}
+
+// Sort each problem's nev values ascending (insertion sort, one thread per problem) and record the order.
+__global__ void lz_sort_kernel(int B, int nev, double* __restrict__ vals, int* __restrict__ perm) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  double* v = vals + (long long)b * nev;
+  int* p = perm + (long long)b * nev;
+  for (int i = 0; i < nev; ++i) p[i] = i;
+  for (int i = 1; i < nev; ++i) {
+    const double key = v[i];
+    const int kp = p[i];
+    int q = i - 1;
+    while (q >= 0 && v[q] > key) {
+      v[q + 1] = v[q];
+      p[q + 1] = p[q];
+      --q;
+    }
+    v[q + 1] = key;
+    p[q + 1] = kp;
+  }
+}
+
+// dst[b][i] = src[b][perm[b][i]] (vectors of n values)
+__global__ void lz_gather_kernel(int nev, long long n, const double2* __restrict__ src, const int* __restrict__ perm,
+                                 double2* __restrict__ dst) {
+  const int b = blockIdx.z, i = blockIdx.y;
+  const int from = perm[(long long)b * nev + i];
+  const double2* s = src + ((long long)b * nev + from) * n;
+  double2* o = dst + ((long long)b * nev + i) * n;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x)
+    o[x] = s[x];
+}
+
+// Workspace carve-up (all offsets 256-byte aligned).
+struct LzLayout {
+  size_t V, w, t0, t1, t2, lbuf, rot, hA, hB, part, npart, d, e, s, bl, theta, Y, arrow, nbad, rq, perm, total;
+  size_t arrow_bytes;
+};
+
+size_t al(size_t v) { return (v + 255) / 256 * 256; }
+
+LzLayout lz_layout(int B, long long n, int ncv, int kk, int nev, int nblk) {
+  LzLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = o;
+    o += al(bytes);
+    return at;
+  };
+  const size_t vec = (size_t)B * n * 16;
+  L.V = take((size_t)B * (ncv + 1) * n * 16);
+  L.w = take(vec);
+  L.t0 = take(vec);
+  L.t1 = take(vec);
+  L.t2 = take(vec);
+  L.lbuf = take(vec);
+  L.rot = take((size_t)B * kk * n * 16);
+  L.hA = take((size_t)B * (ncv + 1) * 16);
+  L.hB = take((size_t)B * (ncv + 1) * 16);
+  L.part = take((size_t)B * nblk * 8);
+  L.npart = take((size_t)B * nblk * 8);
+  L.d = take((size_t)B * ncv * 8);
+  L.e = take((size_t)B * ncv * 8);  // [B][ncv-1] used: T[j][j+1], the layout ed_arrow_eigh reads
+  L.s = take((size_t)B * kk * 8);
+  L.bl = take((size_t)B * 8);
+  L.theta = take((size_t)B * kk * 8);
+  L.Y = take((size_t)B * ncv * kk * 8);
+  size_t ab = 0;
+  ed_arrow_eigh_workspace(B, ncv, kk, &ab);
+  L.arrow_bytes = ab;
+  L.arrow = take(ab);
+  L.nbad = take(16);
+  L.rq = take((size_t)B * nev * 8);
+  L.perm = take((size_t)B * nev * 4);
+  L.total = o;
+  return L;
+}
+
+int lz_kept(int nev, int ncv) { return std::min(ncv - 1, nev + std::max(1, (ncv - nev) / 2)); }
+
+std::mutex g_blas_mu;
+cublasHandle_t blas_handle(int dev) {
+  static std::vector<cublasHandle_t> handles;
+  std::lock_guard<std::mutex> lk(g_blas_mu);
+  if ((int)handles.size() <= dev) handles.resize(dev + 1, nullptr);
+  if (!handles[dev]) {
+    if (cublasCreate(&handles[dev]) != CUBLAS_STATUS_SUCCESS) handles[dev] = nullptr;
+  }
+  return handles[dev];
+}
+
+// C[b] (2n x nkeep, column-major, ldc 2n) = Vr[b] (2n x m) * Y[b]^T-slice: the first nkeep columns of the
+// row-major [m][ldy] Ritz coefficients.  Vr[b] = the first m basis vectors as 2n doubles each.
+int lz_rotate(cudaStream_t st, int B, long long n, int m, int nkeep, const double* V, long long vb,
+              const double* Y, int ldy, long long yb, double* C, long long cb) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cublasHandle_t h = blas_handle(dev);
+  if (!h) {
+    set_error("ed_lanczos_tr: cuBLAS handle creation failed");
+    return ED_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lk(g_blas_mu);
+  cublasSetStream(h, st);
+  const double one = 1.0, zero = 0.0;
+  const cublasStatus_t s =
+      cublasDgemmStridedBatched(h, CUBLAS_OP_N, CUBLAS_OP_T, (int)(2 * n), nkeep, m, &one, V, (int)(2 * n), 2 * vb, Y,
+                                ldy, yb, &zero, C, (int)(2 * n), 2 * cb, B);
+  if (s != CUBLAS_STATUS_SUCCESS) {
+    set_error("ed_lanczos_tr: cuBLAS DGEMM failed (status %d)", (int)s);
+    return ED_ERR_CUDA;
+  }
+  return ED_OK;
+}
+
+}  // namespace
+}  // namespace ed
+
+extern "C" int ed_lanczos_workspace(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, size_t* bytes) {
+  ED_CHECK_ARG(bytes, "ed_lanczos_workspace: null pointer");
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_workspace: bad sizes");
+  const long long n = 3LL * Lx * Ly * Lz;
+  ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_workspace: need Ne < ncv <= 3*Lx*Ly*Lz");
+  const int nblk = (int)((n + ed::LZ_THREADS - 1) / ed::LZ_THREADS);
+  *bytes = ed::lz_layout(nt, n, ncv, ed::lz_kept(Ne, ncv), Ne, nblk).total;
+  return ED_OK;
+}
+
+extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, double tol, int ncv,
+                             int max_restarts, int poly_deg, double lambda_cut, void* evecs, double* evals, int* status,
+                             void* workspace, size_t workspace_bytes, void* stream) {
+  using namespace ed;
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr: bad sizes");
+  const long long n = 3LL * Lx * Ly * Lz;
+  ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr: need Ne < ncv <= 3*Lx*Ly*Lz");
+  ED_CHECK_ARG(tol > 0.0 && max_restarts > 0, "ed_lanczos_tr: need tol > 0 and max_restarts > 0");
+  ED_CHECK_ARG(poly_deg >= 0 && (poly_deg == 0 || (lambda_cut > 0.0 && lambda_cut < 12.0)),
+               "ed_lanczos_tr: a Chebyshev degree needs 0 < lambda_cut < 12");
+  ED_CHECK_ARG(links && evecs && evals && status && workspace, "ed_lanczos_tr: null pointer");
+  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0 && ((uintptr_t)evecs % 16) == 0 && ((uintptr_t)links % 16) == 0,
+               "ed_lanczos_tr: workspace must be 256-byte aligned, links and evecs 16-byte aligned");
+  const int B = nt, kk = lz_kept(Ne, ncv);
+  // elementwise grids: one element per thread; the Gram-Schmidt update kernel writes its ||w||^2 partials on the
+  // same grid (ceil(n / 256) blocks per problem)
+  const int nblk = (int)((n + LZ_THREADS - 1) / LZ_THREADS);
+  const LzLayout Lw = lz_layout(B, n, ncv, kk, Ne, nblk);
+  if (workspace_bytes < Lw.total) {
+    set_error("ed_lanczos_tr: workspace of %zu bytes is smaller than the %zu needed", workspace_bytes, Lw.total);
+    return ED_ERR_WORKSPACE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* W = (uint8_t*)workspace;
+  double2* V = (double2*)(W + Lw.V);
+  double2* w = (double2*)(W + Lw.w);
+  double2* t0 = (double2*)(W + Lw.t0);
+  double2* t1 = (double2*)(W + Lw.t1);
+  double2* t2 = (double2*)(W + Lw.t2);
+  double2* lbuf = (double2*)(W + Lw.lbuf);
+  double2* rot = (double2*)(W + Lw.rot);
+  double2* hA = (double2*)(W + Lw.hA);
+  double2* hB = (double2*)(W + Lw.hB);
+  double* part = (double*)(W + Lw.part);
+  double* npart = (double*)(W + Lw.npart);
+  double* d = (double*)(W + Lw.d);
+  double* e = (double*)(W + Lw.e);
+  double* s = (double*)(W + Lw.s);
+  double* bl = (double*)(W + Lw.bl);
+  double* theta = (double*)(W + Lw.theta);
+  double* Y = (double*)(W + Lw.Y);
+  int* nbad = (int*)(W + Lw.nbad);
+  double* rq = (double*)(W + Lw.rq);
+  int* perm = (int*)(W + Lw.perm);
+  const long long vb = (long long)(ncv + 1) * n;
+  const dim3 vgrid((unsigned)nblk, (unsigned)B);
+  int rc = ED_OK;
+#define LZ_TRY(expr)               \
+  do {                             \
+    rc = (expr);                   \
+    if (rc != ED_OK) return rc;    \
+  } while (0)
+#define LZ_LAUNCHED(what) LZ_TRY(lz_chk(cudaGetLastError(), what))
+
+  // the operator: L, or -(+)T_deg of the spectrum map [cut, 12] -> [-1, 1]
+  const double ca = poly_deg ? 2.0 / (12.0 - lambda_cut) : 0.0, cc = poly_deg ? -(12.0 + lambda_cut) / (12.0 - lambda_cut) : 0.0;
+  const double sgn = (poly_deg % 2 == 0) ? -1.0 : 1.0;
+  long long matvecs = 0;
+  cudaStream_t sr = st;  // the stream the Lanczos steps go to (a capture stream while a restart cycle is recorded)
+  auto apply = [&](const double2* x, long long xb, double2* out) -> int {
+    int r = ed_laplacian(ED_C128, Lx, Ly, Lz, B, 1, links, x, xb, poly_deg ? lbuf : out, n, sr);
+    if (r != ED_OK || poly_deg == 0) return r;
+    // T_0 = x, T_1 = A x, T_{k+1} = 2 A T_k - T_{k-1} with A = a L + c; the last step writes out, signed
+    double2* bufs[3] = {t0, t1, t2};
+    int ci = 1, pi = -1;  // T_k in bufs[ci]; T_{k-1} in bufs[pi], or x itself while pi < 0
+    lz_cheb_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, lbuf, x, xb, nullptr, 0, poly_deg == 1 ? out : bufs[ci], ca, cc,
+                                                  1.0, poly_deg == 1 ? sgn : 1.0);
+    if ((r = lz_chk(cudaGetLastError(), "Chebyshev step")) != ED_OK) return r;
+    for (int kd = 2; kd <= poly_deg; ++kd) {
+      if ((r = ed_laplacian(ED_C128, Lx, Ly, Lz, B, 1, links, bufs[ci], n, lbuf, n, sr)) != ED_OK) return r;
+      const int ni = pi < 0 ? (ci + 1) % 3 : 3 - ci - pi;
+      const bool last = kd == poly_deg;
+      lz_cheb_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, lbuf, bufs[ci], n, pi < 0 ? x : bufs[pi], pi < 0 ? xb : n,
+                                                    last ? out : bufs[ni], ca, cc, 2.0, last ? sgn : 1.0);
+      if ((r = lz_chk(cudaGetLastError(), "Chebyshev step")) != ED_OK) return r;
+      pi = ci;
+      ci = ni;
+    }
+    return ED_OK;
+  };
+
+  // Lanczos steps k .. ncv-1 on stream sr
+  auto cycle = [&](int k) -> int {
+    int r;
+    for (int j = k; j < ncv; ++j) {
+      if ((r = apply(V + (long long)j * n, vb, w)) != ED_OK) return r;
+      if (j == k) {
+        if ((r = ed_cgs_pass(B, j + 1, n, V, vb, w, hA, ncv + 1, nullptr, sr)) != ED_OK) return r;
+        if ((r = ed_cgs_pass(B, j + 1, n, V, vb, w, hB, ncv + 1, npart, sr)) != ED_OK) return r;
+        lz_finish_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V, vb, j, w, hA, hB, ncv + 1, npart, nblk, d, e, bl, ncv, 1);
+        if ((r = lz_chk(cudaGetLastError(), "Lanczos step end")) != ED_OK) return r;
+      } else {
+        lz_dot_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V + (long long)j * n, vb, w, n, part);
+        if ((r = lz_chk(cudaGetLastError(), "Lanczos alpha")) != ED_OK) return r;
+        lz_three_term_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V, vb, j, w, part, nblk, d, e, ncv);
+        if ((r = lz_chk(cudaGetLastError(), "Lanczos recurrence")) != ED_OK) return r;
+        if ((r = ed_cgs_pass(B, j + 1, n, V, vb, w, hA, ncv + 1, npart, sr)) != ED_OK) return r;
+        lz_finish_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V, vb, j, w, hA, nullptr, ncv + 1, npart, nblk, d, e, bl,
+                                                        ncv, 0);
+        if ((r = lz_chk(cudaGetLastError(), "Lanczos step end")) != ED_OK) return r;
+      }
+    }
+    return ED_OK;
+  };
+
+  // From the second restart on every cycle runs the same launches (steps kk .. ncv-1): they are recorded once
+  // on a private stream into a CUDA graph and replayed on the caller's stream.
+  struct GraphRes {
+    cudaStream_t cs = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    ~GraphRes() {
+      if (x) cudaGraphExecDestroy(x);
+      if (g) cudaGraphDestroy(g);
+      if (cs) cudaStreamDestroy(cs);
+    }
+  } gr;
+  auto cycle_replayed = [&](int k) -> int {
+    if (!gr.x) {
+      int r = lz_chk(cudaStreamCreateWithFlags(&gr.cs, cudaStreamNonBlocking), "Lanczos capture stream");
+      if (r != ED_OK) return r;
+      if ((r = lz_chk(cudaStreamBeginCapture(gr.cs, cudaStreamCaptureModeThreadLocal), "Lanczos capture")) != ED_OK)
+        return r;
+      sr = gr.cs;
+      r = cycle(k);
+      sr = st;
+      const int r2 = lz_chk(cudaStreamEndCapture(gr.cs, &gr.g), "Lanczos capture end");
+      if (r != ED_OK) return r;
+      if (r2 != ED_OK) return r2;
+      if ((r = lz_chk(cudaGraphInstantiate(&gr.x, gr.g, 0), "Lanczos graph instantiation")) != ED_OK) return r;
+    }
+    return lz_chk(cudaGraphLaunch(gr.x, st), "Lanczos graph launch");
+  };
+
+  // start vectors
+  lz_random_kernel<<<vgrid, LZ_THREADS, 0, st>>>(B, n, w, 12345u);
+  LZ_LAUNCHED("Lanczos start vector");
+  lz_dot_kernel<<<vgrid, LZ_THREADS, 0, st>>>(n, w, n, w, n, part);
+  LZ_LAUNCHED("Lanczos start norm");
+  lz_normalise_kernel<<<vgrid, LZ_THREADS, 0, st>>>(n, w, part, nblk, V, vb);
+  LZ_LAUNCHED("Lanczos start normalise");
+
+  int k = 0, restarts = 0, converged = 0, restart_cycles = 0;
+  for (restarts = 1; restarts <= max_restarts; ++restarts) {
+    if (k == 0 || restart_cycles == 0)
+      LZ_TRY(cycle(k));  // the first restart cycle also warms up what the graph records
+    else
+      LZ_TRY(cycle_replayed(k));
+    if (k > 0) ++restart_cycles;
+    matvecs += (long long)(ncv - k) * (poly_deg ? poly_deg : 1);
+    LZ_TRY(ed_arrow_eigh(B, ncv, k, kk, d, k > 0 ? s : nullptr, e, theta, Y, W + Lw.arrow, Lw.arrow_bytes, st));
+    LZ_TRY(lz_chk(cudaMemsetAsync(nbad, 0, sizeof(int), st), "Lanczos convergence counter"));
+    lz_converged_kernel<<<(B * Ne + 127) / 128, 128, 0, st>>>(B, ncv, kk, Ne, theta, Y, bl, tol, nbad);
+    LZ_LAUNCHED("Lanczos convergence test");
+    int hbad = -1;
+    LZ_TRY(lz_chk(cudaMemcpyAsync(&hbad, nbad, sizeof(int), cudaMemcpyDeviceToHost, st), "Lanczos counter read"));
+    LZ_TRY(lz_chk(cudaStreamSynchronize(st), "Lanczos synchronise"));
+    if (hbad == 0) {
+      converged = 1;
+      break;
+    }
+    if (restarts == max_restarts) break;
+    // thick restart: V[:, :kk] = Y[:, :kk]^T V[:, :ncv], V[:, kk] = V[:, ncv]
+    LZ_TRY(lz_rotate(st, B, n, ncv, kk, (const double*)V, vb, Y, kk, (long long)ncv * kk, (double*)rot,
+                     (long long)kk * n));
+    LZ_TRY(lz_chk(cudaMemcpy2DAsync(V, vb * 16, rot, (size_t)kk * n * 16, (size_t)kk * n * 16, B,
+                                         cudaMemcpyDeviceToDevice, st),
+                       "Lanczos restart copy"));
+    LZ_TRY(lz_chk(cudaMemcpy2DAsync(V + (long long)kk * n, vb * 16, V + (long long)ncv * n, vb * 16, (size_t)n * 16,
+                                         B, cudaMemcpyDeviceToDevice, st),
+                       "Lanczos residual vector copy"));
+    lz_restart_kernel<<<(B * kk + 127) / 128, 128, 0, st>>>(B, ncv, kk, theta, Y, bl, d, s);
+    LZ_LAUNCHED("Lanczos restart");
+    k = kk;
+  }
+  if (restarts > max_restarts) restarts = max_restarts;
+  // Ritz vectors X = Y[:, :Ne]^T V and values
+  LZ_TRY(lz_rotate(st, B, n, ncv, Ne, (const double*)V, vb, Y, kk, (long long)ncv * kk, (double*)evecs,
+                   (long long)Ne * n));
+  if (poly_deg == 0) {
+    LZ_TRY(lz_chk(cudaMemcpy2DAsync(evals, (size_t)Ne * 8, theta, (size_t)kk * 8, (size_t)Ne * 8, B,
+                                         cudaMemcpyDeviceToDevice, st),
+                       "Lanczos eigenvalues"));
+  } else {
+    // eigenvalues of L: Rayleigh quotients, then ascending order
+    double2* LX = rot;  // [B][Ne][n] (Ne <= kk)
+    LZ_TRY(ed_laplacian(ED_C128, Lx, Ly, Lz, B, Ne, links, evecs, (long long)Ne * n, LX, (long long)Ne * n, st));
+    matvecs += Ne;
+    lz_rq_kernel<<<(unsigned)(B * Ne), LZ_THREADS, 0, st>>>(n, (const double2*)evecs, LX, rq);
+    LZ_LAUNCHED("Rayleigh quotients");
+    lz_sort_kernel<<<(B + 63) / 64, 64, 0, st>>>(B, Ne, rq, perm);
+    LZ_LAUNCHED("eigenvalue sort");
+    lz_gather_kernel<<<dim3((unsigned)std::min<long long>((n + 255) / 256, 64), Ne, B), 256, 0, st>>>(
+        Ne, n, (const double2*)evecs, perm, LX);
+    LZ_LAUNCHED("eigenvector reorder");
+    LZ_TRY(lz_chk(
+        cudaMemcpyAsync(evecs, LX, (size_t)B * Ne * n * 16, cudaMemcpyDeviceToDevice, st), "eigenvector copy"));
+    LZ_TRY(lz_chk(cudaMemcpyAsync(evals, rq, (size_t)B * Ne * 8, cudaMemcpyDeviceToDevice, st),
+                       "eigenvalue copy"));
+  }
+  status[0] = converged;
+  status[1] = restarts;
+  status[2] = (int)std::min<long long>(matvecs, 2147483647LL);
+#undef LZ_TRY
+#undef LZ_LAUNCHED
+  return ED_OK;
+}

@@ -22,7 +22,7 @@ from typing import List, Sequence
 import torch
 
 from .. import lanczos as LZ
-from ..ops import links_to_soa, laplacian, vectors_from_planes
+from ..ops import lanczos_tr, links_to_soa, laplacian, vectors_from_planes
 from .elemental import links_to_device
 
 NC = 3
@@ -49,11 +49,18 @@ def stout_smear_links_(U: torch.Tensor, latt_size, nstep: int, rho: float):
 
 class EigenvectorGenerator:
     def __init__(self, latt_size: List[int], gauge_field, Ne: int, tol: float, *, stencil_precision: str = "fp64",
-                 device=None, ncv: int = None) -> None:
+                 device=None, ncv: int = None, driver: str = "native") -> None:
         """``ncv``: Krylov dimension of the thick-restart Lanczos (default
-        max(3 Ne, Ne + 32), capped by the problem size)."""
+        max(3 Ne, Ne + 32), 2 Ne with Chebyshev acceleration, capped by the
+        problem size).  ``driver``: ``"native"`` runs the FP64-stencil
+        eigensolve in the library (``ed_lanczos_tr``); ``"python"`` drives the
+        same kernels from ``lanczos.trlanczos`` (the FP32-stencil mode always
+        does)."""
         if stencil_precision not in ("fp64", "fp32"):
             raise ValueError("stencil_precision must be 'fp64' or 'fp32'")
+        if driver not in ("native", "python"):
+            raise ValueError("driver must be 'native' or 'python'")
+        self.driver = driver
         self.ncv = ncv
         self.device = torch.device(device or "cuda")
         self.latt_size = latt_size
@@ -117,6 +124,18 @@ class EigenvectorGenerator:
         n = NC * V3
         ts = list(ts)
         B = len(ts)
+        if self.driver == "native" and self.stencil_precision == "fp64":
+            links = self._links(torch.complex128)
+            sel = links if ts == list(range(Lt)) else links.index_select(0, torch.as_tensor(ts, device=self.device))
+            poly = polynomial_degree if (polynomial_degree > 0 and lambda_cut > 0) else 0
+            evals, planes, stats = lanczos_tr(sel, self.latt_size, self.Ne, max(self.tol, 1e-12) if poly else self.tol,
+                                              ncv=self.ncv, poly_deg=poly, lambda_cut=lambda_cut if poly else 0.0)
+            self.last_stats = {k: stats[k] for k in ("restarts", "matvecs", "converged")}
+            evecs = planes.reshape(B, self.Ne, n)
+            if apply_renorm_phase:
+                LZ.renorm_phase_(evecs)
+            out = vectors_from_planes(evecs.reshape(B, self.Ne, NC, V3), V3)
+            return out.reshape(B, self.Ne, Lz, Ly, Lx, NC), evals
         if polynomial_degree > 0 and lambda_cut > 0:
             mv = self._matvec(ts, torch.complex64 if self.stencil_precision == "fp32" else torch.complex128)
             # below the cut T_deg has the sign (-1)^deg: negate so the wanted modes are the smallest

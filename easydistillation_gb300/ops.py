@@ -135,6 +135,36 @@ def laplacian_status():
     return code.value
 
 
+def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int = None, max_restarts: int = None,
+               poly_deg: int = 0, lambda_cut: float = 0.0):
+    """Native batched thick-restart Lanczos (``ed_lanczos_tr``) for the lowest
+    ``Ne`` eigenpairs of the FP64 Laplacian of every timeslice of
+    ``links_soa`` (complex128 ``[nt, 27, V3]``).  Returns (evals ``[nt, Ne]``
+    float64 ascending, evecs ``[nt, Ne, 3, V3]`` complex128 colour planes,
+    stats ``{"converged", "restarts", "matvecs"}``)."""
+    require_cuda(links_soa, "links")
+    if links_soa.dtype != torch.complex128:
+        raise ValueError("the native Lanczos works on complex128 links")
+    Lx, Ly, Lz = (int(v) for v in latt_size[:3])
+    nt, V3 = links_soa.shape[0], Lx * Ly * Lz
+    if tuple(links_soa.shape[1:]) != (27, V3):
+        raise ValueError("links must be [nt, 27, Lx*Ly*Lz]")
+    n = 3 * V3
+    if ncv is None:
+        ncv = min(max((2 if poly_deg > 0 else 3) * Ne, Ne + 32), n)
+    if max_restarts is None:
+        max_restarts = max(30, 10 * n // max(1, ncv - Ne))
+    nbytes = ctypes.c_size_t()
+    call("ed_lanczos_workspace", Lx, Ly, Lz, nt, Ne, ncv, ctypes.byref(nbytes))
+    ws = torch.empty(nbytes.value, dtype=torch.uint8, device=links_soa.device)
+    evecs = torch.empty((nt, Ne, 3, V3), dtype=torch.complex128, device=links_soa.device)
+    evals = torch.empty((nt, Ne), dtype=torch.float64, device=links_soa.device)
+    st = (ctypes.c_int * 3)()
+    call("ed_lanczos_tr", Lx, Ly, Lz, nt, ptr(links_soa), Ne, float(tol), ncv, max_restarts, int(poly_deg),
+         float(lambda_cut), ptr(evecs), ptr(evals), st, ptr(ws), ws.numel(), stream_handle())
+    return evals, evecs, {"converged": bool(st[0]), "restarts": int(st[1]), "matvecs": int(st[2]), "ncv": ncv}
+
+
 def cgs_pass(V: torch.Tensor, r: int, w: torch.Tensor, h: torch.Tensor = None, norm: bool = False):
     """One classical Gram-Schmidt pass (``ed_cgs_pass``): ``h = V[:, :r]^H w``,
     ``w -= V[:, :r] h`` in place.  ``V``: complex128 [B, rows, n] with

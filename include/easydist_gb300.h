@@ -159,6 +159,25 @@ int ed_laplacian_status(int* code, void* stream);
 int ed_cgs_pass(int B, int r, long long n, const void* V, long long v_bstride, void* w, void* h, int ldh,
                 double* norm_part, void* stream);
 
+/* Lowest Ne eigenpairs of the FP64 3D covariant Laplacian of nt timeslices by
+ * batched thick-restart Lanczos: the eigsh call of
+ * lattice/generator/eigenvector.py:234-257 (and, with poly_deg > 0, the QUDA
+ * path's Chebyshev acceleration of :295-299).  links: complex128 SoA
+ * [nt][27][V3] (ed_links_to_soa); evecs out: complex128 colour planes
+ * [nt][Ne][3][V3], unit norm; evals out: [nt][Ne] ascending; status (host,
+ * int[3]): converged (1/0), restarts, operator applications.  ncv: Krylov
+ * dimension (Ne < ncv <= 3*V3); the kept Ritz pairs at a restart are
+ * min(ncv-1, Ne + max(1, (ncv-Ne)/2)).  Convergence: |beta y_m,i| <= tol
+ * |theta_i| for every wanted pair (ARPACK's test).  poly_deg > 0 iterates on
+ * the Chebyshev filter of degree poly_deg that maps [lambda_cut, 12] to
+ * [-1, 1] and returns Rayleigh quotients as eigenvalues.  Synchronises the
+ * stream once per restart.  Needs ed_lanczos_workspace bytes (256-byte
+ * aligned). */
+int ed_lanczos_workspace(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, size_t* bytes);
+int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, double tol, int ncv, int max_restarts,
+                  int poly_deg, double lambda_cut, void* evecs, double* evals, int* status, void* workspace,
+                  size_t workspace_bytes, void* stream);
+
 int ed_arrow_eigh_workspace(int B, int m, int nwant, size_t* bytes);
 int ed_arrow_eigh(int B, int m, int ka, int nwant, const double* d, const double* s, const double* e,
                   double* evals, double* evecs, void* workspace, size_t workspace_bytes, void* stream);

@@ -55,6 +55,16 @@ def test_argument_validation_is_host_side():
     assert L.ed_cgs_pass(2, 5, 100, 16, 400, 16, 16, 5, None, None) == _lib.ED_ERR_ARG  # batch stride < r*n
     assert L.ed_cgs_pass(2, 5, 100, 8, 500, 16, 16, 5, None, None) == _lib.ED_ERR_ARG  # misaligned V
     assert L.ed_cgs_pass(2, 5, 100, 16, 500, 16, 16, 4, None, None) == _lib.ED_ERR_ARG  # ldh < r
+    nb = ctypes.c_size_t()
+    assert L.ed_lanczos_workspace(6, 6, 6, 2, 16, 40, ctypes.byref(nb)) == _lib.ED_OK and nb.value > 2 * 41 * 648 * 16
+    assert L.ed_lanczos_workspace(6, 6, 6, 2, 16, 16, ctypes.byref(nb)) == _lib.ED_ERR_ARG  # ncv <= Ne
+    st = (ctypes.c_int * 3)()
+    assert L.ed_lanczos_tr(6, 6, 6, 2, None, 16, ctypes.c_double(1e-10), 40, 10, 0, ctypes.c_double(0.0), 256, 256, st,
+                           256, 1 << 30, None) == _lib.ED_ERR_ARG  # null links
+    assert L.ed_lanczos_tr(6, 6, 6, 2, 256, 16, ctypes.c_double(1e-10), 40, 10, 4, ctypes.c_double(0.0), 256, 256, st,
+                           256, 1 << 30, None) == _lib.ED_ERR_ARG  # Chebyshev without a cut
+    assert L.ed_lanczos_tr(6, 6, 6, 2, 256, 16, ctypes.c_double(1e-10), 40, 10, 0, ctypes.c_double(0.0), 256, 256, st,
+                           256, 1024, None) == _lib.ED_ERR_WORKSPACE
 
 
 @pytest.mark.parametrize(
