@@ -1,0 +1,81 @@
+"""Checks at the full benchmark sizes (32^3, Ne = 200), where the CPU oracle
+is too slow, through properties that do not depend on the size:
+
+* the split-precision elemental (f16x3, 13 operators x 27 momenta) against the
+  plain FP64 GPU path on the same timeslice: relative Frobenius error <= 1e-6;
+* E[no derivative, p = 0] = V^H V = identity for orthonormal eigenvectors (up
+  to the complex64 rounding of V the reference applies as well);
+* the plain and the Chebyshev-accelerated eigensolve of the 200 lowest modes:
+  residuals ||L x - lambda x|| < 1e-9, orthonormal vectors, ascending
+  eigenvalues, and the same eigenvalues to 1e-10 relative."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+LATT = [32, 32, 32, 1]
+NE = 200
+
+
+def _inputs(seed=9):
+    from easydistillation_gb300.ops import links_to_soa  # noqa: F401  (loads the library)
+    from easydistillation_gb300.synthetic import gauge_field
+
+    g = gauge_field(LATT, 0.3, seed)  # [1, Lz, Ly, Lx, 4, 3, 3]
+    U = torch.from_numpy(np.ascontiguousarray(g.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0])).cuda()  # [3, Lz, Ly, Lx, 3, 3]
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    n = 3 * LATT[0] * LATT[1] * LATT[2]
+    Z = torch.complex(torch.randn((n, NE), dtype=torch.float64, device="cuda", generator=gen),
+                      torch.randn((n, NE), dtype=torch.float64, device="cuda", generator=gen))
+    V = torch.linalg.qr(Z)[0].T.contiguous()  # [Ne, 3*V3] orthonormal rows
+    return g, U, V
+
+
+def test_elemental_f16x3_vs_fp64_full_size():
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.ops import ElementalPlan
+
+    _, U, V = _inputs()
+    V3 = LATT[0] * LATT[1] * LATT[2]
+    moms = mom_dict_to_list(3)
+    out = {}
+    for mode in ("f16x3", "fp64"):
+        plan = ElementalPlan(LATT, NE, 2, moms, mode, tuning={"f64_tile": 3} if mode == "fp64" else None)
+        o = torch.empty((13, 27, NE, NE), dtype=torch.complex128, device="cuda")
+        plan.run(U, V3 * 9, 9, V, o)
+        if mode != "fp64":
+            assert plan.factorised == (9, 3)
+            plan.check_status()
+        out[mode] = o
+        del plan
+        torch.cuda.empty_cache()
+    err = float(torch.linalg.vector_norm(out["f16x3"] - out["fp64"]) / torch.linalg.vector_norm(out["fp64"]))
+    assert err <= 1e-6, err
+    # no derivative, zero momentum: V^H V = I up to the complex64 rounding of V
+    p0 = moms.index((0, 0, 0))
+    eye = torch.eye(NE, dtype=torch.complex128, device="cuda")
+    for mode in ("f16x3", "fp64"):
+        assert float((out[mode][0, p0] - eye).abs().max()) < 1e-6
+
+
+def test_chebyshev_eigensolve_full_size():
+    from easydistillation_gb300.ops import lanczos_tr, laplacian, links_to_soa
+
+    g, _, _ = _inputs(seed=10)
+    U = torch.from_numpy(np.ascontiguousarray(g.transpose(4, 0, 1, 2, 3, 5, 6))).cuda()
+    L = links_to_soa(U, LATT)
+    ev0, X0, st0 = lanczos_tr(L, LATT, NE, 1e-10)  # plain thick-restart
+    assert st0["converged"]
+    ev, X, st = lanczos_tr(L, LATT, NE, 1e-12, poly_deg=16, lambda_cut=1.15 * float(ev0[0, -1]))
+    assert st["converged"]
+    assert torch.allclose(ev, ev0, rtol=1e-10, atol=0)
+    for lam, Y in ((ev0, X0), (ev, X)):
+        assert bool((lam[:, 1:] >= lam[:, :-1]).all())
+        LY = laplacian(L, Y, LATT)
+        res = torch.linalg.vector_norm((LY - lam[:, :, None, None].to(Y.dtype) * Y).reshape(1, NE, -1), dim=2)
+        assert float(res.max()) < 1e-9
+        Yf = Y.reshape(NE, -1)
+        G = Yf.conj() @ Yf.T
+        assert float((G - torch.eye(NE, dtype=G.dtype, device=G.device)).abs().max()) < 1e-12
