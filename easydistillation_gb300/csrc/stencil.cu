@@ -25,8 +25,7 @@ namespace ed {
 // copy bandwidth against 83 % for the kernel that reads neighbours through
 // L1/L2 (the links, 27 of the 33 complex numbers per site, dominate the
 // traffic, and the per-plane block barrier costs latency hiding).
-static int g_stencil_tma = 0;
-static bool laplacian_tma_enabled() { return g_stencil_tma != 0; }
+static int g_stencil_tma = 2;  // ed_laplacian_config: 0 L1/L2, 1 TMA input planes, 2 TMA strips (default)
 
 template <typename T, int S>
 struct Pack;
@@ -425,6 +424,183 @@ __global__ void __launch_bounds__(LT_THREADS) laplacian_tma_kernel(const __grid_
   }
 }
 
+// ------------------------------------------------------------ strip-staged Laplacian (complex64, TMA links + input)
+// One block owns a strip of R rows x Lx sites of a z slab of one (timeslice,
+// vector) and marches through the slab.  For every plane TMA brings into a
+// shared-memory slot: the 27 link streams of the strip, the U_y links of the
+// row below the strip, the input rows of the strip and the two halo rows
+// above and below (the plane below the slab brings only its U_z links and
+// input rows, the plane above only its input rows).  Three slots: per plane
+// the block first applies the backward z hop (slot of plane z-1), releases
+// that slot to the load of plane z+2, then the x and y hops and the forward
+// z hop.  Every link and input value reaches shared memory by a bulk copy,
+// so the bytes in flight do not depend on registers; one thread per site
+// reads everything from shared memory.  Waits are bounded (status word).
+
+constexpr int LS_SLOTS = 3, LS_MAX_SITES = 128;
+
+struct LsGeom {
+  int links, uyh, fmain, fhlo, fhhi, bytes;  // byte offsets inside a slot, slot size
+};
+__host__ __device__ inline int ls_al(int v) { return (v + 127) / 128 * 128; }
+__host__ __device__ inline LsGeom ls_geom(int RLx, int Lx) {
+  LsGeom g;
+  g.links = 0;
+  g.uyh = g.links + ls_al(27 * RLx * 8);
+  g.fmain = g.uyh + ls_al(9 * Lx * 8);
+  g.fhlo = g.fmain + ls_al(3 * RLx * 8);
+  g.fhhi = g.fhlo + ls_al(3 * Lx * 8);
+  g.bytes = g.fhhi + ls_al(3 * Lx * 8);
+  return g;
+}
+
+__device__ __forceinline__ void ls_tma2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          st_smem(dst)),
+      "l"(map), "r"(st_smem(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ void ls_tma3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::
+          "r"(st_smem(dst)),
+      "l"(map), "r"(st_smem(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ cplx<float> ls_ld(const uint8_t* base, int idx) {
+  const float2 v = reinterpret_cast<const float2*>(base)[idx];
+  return mk(v.x, v.y);
+}
+
+__global__ void __launch_bounds__(LS_MAX_SITES, 2)
+    laplacian_strip_kernel(const __grid_constant__ CUtensorMap mL27, const __grid_constant__ CUtensorMap mL9,
+                           const __grid_constant__ CUtensorMap mLz, const __grid_constant__ CUtensorMap mF,
+                           const __grid_constant__ CUtensorMap mFh, Latt L, int R, int zb,
+                           cplx<float>* __restrict__ out, long long out_tstride, float diag) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  const int Lx = L.Lx, Ly = L.Ly, Lz = L.Lz, V3 = L.V3(), P = Lx * Ly, RLx = R * Lx;
+  const LsGeom g = ls_geom(RLx, Lx);
+  uint64_t* bar = (uint64_t*)(sm + LS_SLOTS * g.bytes);
+  const int nstrip = Ly / R;
+  const int strip = blockIdx.x % nstrip, slab = blockIdx.x / nstrip;
+  const int v = blockIdx.y, t = blockIdx.z;
+  const int y0 = strip * R, ylo = wrap_dec(y0, Ly), yhi = (y0 + R) % Ly;
+  const int z0 = slab * zb, z1 = min(Lz, z0 + zb);
+  const int nplanes = (z1 - z0) + 2;  // plane j holds z = z0 - 1 + j (periodic)
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < LS_SLOTS; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st_smem(&bar[q])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int j) {  // thread 0 only
+    const int z = (z0 - 1 + j + Lz) % Lz;
+    const int q = j % LS_SLOTS;
+    uint8_t* base = sm + q * g.bytes;
+    const bool first = j == 0, last = j == nplanes - 1;
+    uint32_t bytes = 3 * RLx * 8;
+    if (first)
+      bytes += 9 * RLx * 8;
+    else if (!last)
+      bytes += 27 * RLx * 8 + 9 * Lx * 8 + 6 * Lx * 8;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(st_smem(&bar[q])), "r"(bytes)
+                 : "memory");
+    ls_tma3d(base + g.fmain, &mF, &bar[q], z * P + y0 * Lx, v * 3, t);
+    if (first) {
+      ls_tma2d(base + g.links + 18 * RLx * 8, &mLz, &bar[q], z * P + y0 * Lx, t * 27 + 18);
+    } else if (!last) {
+      ls_tma2d(base + g.links, &mL27, &bar[q], z * P + y0 * Lx, t * 27);
+      ls_tma2d(base + g.uyh, &mL9, &bar[q], z * P + ylo * Lx, t * 27 + 9);
+      ls_tma3d(base + g.fhlo, &mFh, &bar[q], z * P + ylo * Lx, v * 3, t);
+      ls_tma3d(base + g.fhhi, &mFh, &bar[q], z * P + yhi * Lx, v * 3, t);
+    }
+  };
+  int issued_hi = -1;  // thread 0 only
+  if (threadIdx.x == 0)
+    for (int j = 0; j < LS_SLOTS && j < nplanes; ++j) {
+      issue(j);
+      issued_hi = j;
+    }
+  const int p = threadIdx.x;  // site of the strip
+  const bool active = p < RLx;
+  const int xx = active ? p % Lx : 0, yy = active ? p / Lx : 0;
+  const int pxm = yy * Lx + wrap_dec(xx, Lx), pxp = yy * Lx + wrap_inc(xx, Lx);
+  cplx<float>* O = out + (long long)t * out_tstride + (long long)v * 3 * V3;
+  bool ok = true, failed = false;
+  for (int z = z0; z < z1; ++z) {
+    const int jc = z - z0 + 1;
+    const uint8_t* Sm = sm + ((jc - 1) % LS_SLOTS) * g.bytes;
+    const uint8_t* Sc = sm + (jc % LS_SLOTS) * g.bytes;
+    const uint8_t* Sp = sm + ((jc + 1) % LS_SLOTS) * g.bytes;
+    ok = ok && st_wait(&bar[(jc - 1) % LS_SLOTS], ((jc - 1) / LS_SLOTS) & 1) &&
+         st_wait(&bar[jc % LS_SLOTS], (jc / LS_SLOTS) & 1);
+    cplx<float> hop[3] = {mk(0.f, 0.f), mk(0.f, 0.f), mk(0.f, 0.f)};
+    if (active && ok) {  // backward z: U_z(z-1)^dag F(z-1)
+      cplx<float> u[9], f[3];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = ls_ld(Sm + g.links, (18 + e) * RLx + p);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = ls_ld(Sm + g.fmain, c * RLx + p);
+      mvd_add(hop, u, f);
+    }
+    failed = __syncthreads_or(!ok) != 0;  // the slot of plane z-1 is free from here on
+    if (failed) break;
+    if (threadIdx.x == 0 && jc + 2 < nplanes) {
+      issue(jc + 2);
+      issued_hi = jc + 2;
+    }
+    ok = st_wait(&bar[(jc + 1) % LS_SLOTS], ((jc + 1) / LS_SLOTS) & 1);
+    if (active && ok) {
+      cplx<float> u[9], f[3], f0[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f0[c] = ls_ld(Sc + g.fmain, c * RLx + p);
+      // x forward: U_x(x) F(x+1); x backward: U_x(x-1)^dag F(x-1)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = ls_ld(Sc + g.links, e * RLx + p);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = ls_ld(Sc + g.fmain, c * RLx + pxp);
+      mv_add(hop, u, f);
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = ls_ld(Sc + g.links, e * RLx + pxm);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = ls_ld(Sc + g.fmain, c * RLx + pxm);
+      mvd_add(hop, u, f);
+      // y forward: U_y(y) F(y+1) (the row above the strip comes from the halo)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = ls_ld(Sc + g.links, (9 + e) * RLx + p);
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        f[c] = yy + 1 < R ? ls_ld(Sc + g.fmain, c * RLx + p + Lx) : ls_ld(Sc + g.fhhi, c * Lx + xx);
+      mv_add(hop, u, f);
+      // y backward: U_y(y-1)^dag F(y-1) (links and input of the row below the strip from the halo)
+#pragma unroll
+      for (int e = 0; e < 9; ++e)
+        u[e] = yy > 0 ? ls_ld(Sc + g.links, (9 + e) * RLx + p - Lx) : ls_ld(Sc + g.uyh, e * Lx + xx);
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        f[c] = yy > 0 ? ls_ld(Sc + g.fmain, c * RLx + p - Lx) : ls_ld(Sc + g.fhlo, c * Lx + xx);
+      mvd_add(hop, u, f);
+      // z forward: U_z(z) F(z+1)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = ls_ld(Sc + g.links, (18 + e) * RLx + p);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = ls_ld(Sp + g.fmain, c * RLx + p);
+      mv_add(hop, u, f);
+      const int site = z * P + (y0 + yy) * Lx + xx;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        O[(long long)c * V3 + site] = mk(diag * f0[c].re - hop[c].re, diag * f0[c].im - hop[c].im);
+    }
+  }
+  if (!failed) failed = __syncthreads_or(!ok) != 0;  // a wait of the last plane's second half
+  if (threadIdx.x == 0 && failed) {
+    atomicExch(&g_stencil_error, 1);
+    for (int j = issued_hi; j >= 0 && j > issued_hi - LS_SLOTS; --j) st_wait(&bar[j % LS_SLOTS], (j / LS_SLOTS) & 1);
+  }
+}
+
 using StEncodeFn = PFN_cuTensorMapEncodeTiled_v12000;
 static StEncodeFn st_encoder() {
   static StEncodeFn fn = nullptr;
@@ -477,14 +653,76 @@ static int launch_laplacian_tma(Latt L, int nt, int nvec, const void* links, con
   return ED_OK;
 }
 
+// The strip-staged path serves complex64 when Lx is even and a strip of whole
+// rows (R rows, R | Ly, R * Lx <= 128 sites) exists; returns -1 otherwise.
+static int launch_laplacian_strip(Latt L, int nt, int nvec, const void* links, const void* in, long long its,
+                                  void* out, long long ots, cudaStream_t stream) {
+  const int Lx = L.Lx, Ly = L.Ly, Lz = L.Lz, V3 = L.V3();
+  if (Lx % 2 || Lx > LS_MAX_SITES || its % 2 || ((uintptr_t)in % 16) || ((uintptr_t)links % 16)) return -1;
+  int R = 0;
+  for (int r = 1; r <= Ly && r * Lx <= LS_MAX_SITES; ++r)
+    if (Ly % r == 0) R = r;
+  // RLx % 8 keeps every TMA destination (the U_z rows start 18 * RLx * 8 bytes into a slot) 128-byte aligned
+  if (R == 0 || (R * Lx) % 8 || (long long)27 * nt >= (1LL << 31) || (long long)3 * nvec >= (1LL << 31)) return -1;
+  StEncodeFn enc = st_encoder();
+  if (!enc) return -1;
+  const int RLx = R * Lx;
+  CUtensorMap mL27, mL9, mLz, mF, mFh;
+  cuuint64_t ldim[2] = {(cuuint64_t)V3, (cuuint64_t)(27LL * nt)};
+  cuuint64_t lstride[1] = {(cuuint64_t)(8LL * V3)};
+  cuuint64_t fdim[3] = {(cuuint64_t)V3, (cuuint64_t)(3LL * nvec), (cuuint64_t)nt};
+  cuuint64_t fstride[2] = {(cuuint64_t)(8LL * V3), (cuuint64_t)(8LL * its)};
+  cuuint32_t es[3] = {1, 1, 1};
+  auto enc2 = [&](CUtensorMap* m, cuuint32_t bx, cuuint32_t by) {
+    cuuint32_t box[2] = {bx, by};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void*>(links), ldim, lstride, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  auto enc3 = [&](CUtensorMap* m, cuuint32_t bx) {
+    cuuint32_t box[3] = {bx, 3, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void*>(in), fdim, fstride, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  };
+  if (!enc2(&mL27, RLx, 27) || !enc2(&mL9, Lx, 9) || !enc2(&mLz, RLx, 9) || !enc3(&mF, RLx) || !enc3(&mFh, Lx))
+    return -1;
+  const LsGeom geo = ls_geom(RLx, Lx);
+  const int smem = LS_SLOTS * geo.bytes + 64;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(laplacian_strip_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024) !=
+        cudaSuccess)
+      return -1;
+    attr = true;
+  }
+  if (smem > 110 * 1024) return -1;
+  // z slabs long enough to amortise their two halo planes, short enough for about four waves of two blocks per SM
+  const int nstrip = Ly / R;
+  const long long want = 8LL * num_sms();
+  const int zb = (int)std::max(2LL, std::min<long long>(Lz, (long long)Lz * nstrip * nvec * nt / want));
+  const int nslab = ceil_div(Lz, zb);
+  if ((long long)nstrip * nslab >= (1LL << 31) || nvec > 65535 || nt > 65535) return -1;
+  dim3 grid(nstrip * nslab, nvec, nt);
+  const int threads = (RLx + 31) / 32 * 32;
+  laplacian_strip_kernel<<<grid, threads, smem, stream>>>(mL27, mL9, mLz, mF, mFh, L, R, zb, (cplx<float>*)out, ots,
+                                                          6.0f);
+  ED_RETURN_LAUNCH("laplacian (strip-staged)");
+  return ED_OK;
+}
+
 // ------------------------------------------------------------ launchers
 
 int launch_laplacian(int prec, Latt L, int nt, int nvec, const void* links, const void* in, long long its,
                      void* out, long long ots, cudaStream_t stream) {
   const int V3 = L.V3();
   const long long lts = 27LL * V3;
-  if (prec == ED_C64 && laplacian_tma_enabled()) {
+  if (prec == ED_C64 && g_stencil_tma == 1) {
     const int rc = launch_laplacian_tma(L, nt, nvec, links, in, its, out, ots, stream);
+    if (rc != -1) return rc;
+  }
+  if (prec == ED_C64 && g_stencil_tma == 2) {
+    const int rc = launch_laplacian_strip(L, nt, nvec, links, in, its, out, ots, stream);
     if (rc != -1) return rc;
   }
   if (prec == ED_C128) {
@@ -558,7 +796,7 @@ extern "C" int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, 
 }
 
 extern "C" int ed_laplacian_config(int use_tma) {
-  ED_CHECK_ARG(use_tma == 0 || use_tma == 1, "ed_laplacian_config: use_tma must be 0 or 1");
+  ED_CHECK_ARG(use_tma >= 0 && use_tma <= 2, "ed_laplacian_config: use_tma must be 0, 1 or 2");
   ed::g_stencil_tma = use_tma;
   return ED_OK;
 }

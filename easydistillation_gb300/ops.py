@@ -120,11 +120,14 @@ def laplacian(links_soa: torch.Tensor, F: torch.Tensor, latt_size: Sequence[int]
     return out
 
 
-def laplacian_config(use_tma: bool = False):
-    """Select the complex64 Laplacian kernel process-wide: the TMA-staged
-    one (used where its shape limits allow) or the default one reading all
-    neighbours through L1/L2 (faster on GB300)."""
-    call("ed_laplacian_config", 1 if use_tma else 0)
+def laplacian_config(use_tma=2):
+    """Select the complex64 Laplacian kernel process-wide: 0 / False = the
+    kernel reading every neighbour through L1/L2; 1 / True = input planes
+    staged by TMA; 2 (the default) = strips whose links and inputs are all
+    staged by TMA.  The staged kernels are used where their shape limits
+    allow."""
+    mode = int(use_tma) if not isinstance(use_tma, bool) else (1 if use_tma else 0)
+    call("ed_laplacian_config", mode)
 
 
 def laplacian_status():

@@ -290,8 +290,8 @@ def tuned_plan(latt_size, Ne, num_nabla, momentum_list, mode="f16x3", device=Non
 
 def tune_laplacian(latt_size, nt: int = 1, nvec: int = 1, device=None, reps: int = 5,
                    cache: Optional[TuningCache] = None, retune: bool = False, apply: bool = True) -> TuneResult:
-    """Choose the complex64 Laplacian kernel (``use_tma`` False/True) for this
-    shape by timing both; ``apply`` sets the winner process-wide
+    """Choose the complex64 Laplacian kernel (``use_tma`` 0 = L1/L2, 1 = input
+    planes staged by TMA, 2 = strips staged by TMA) for this shape by timing them; ``apply`` sets the winner process-wide
     (``ops.laplacian_config``)."""
     from .ops import laplacian, laplacian_config, laplacian_status
 
@@ -315,7 +315,7 @@ def tune_laplacian(latt_size, nt: int = 1, nvec: int = 1, device=None, reps: int
         out = torch.empty_like(F)
 
         def measure(c: Candidate):
-            laplacian_config(bool(c.tuning.get("use_tma", 0)))
+            laplacian_config(int(c.tuning.get("use_tma", 0)))
             try:
                 laplacian(links, F, latt_size, out)
                 ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -330,11 +330,11 @@ def tune_laplacian(latt_size, nt: int = 1, nvec: int = 1, device=None, reps: int
                 times = sorted(a.elapsed_time(b) for a, b in ev)
                 return times[len(times) // 2], out.clone()
             finally:
-                laplacian_config(False)
+                laplacian_config()  # the library default
 
-        stages = [lambda best: [Candidate(True, {"use_tma": 0}), Candidate(True, {"use_tma": 1})]]
+        stages = [lambda best: [Candidate(True, {"use_tma": m}) for m in (0, 1, 2)]]
         res = _run_search(stages, Candidate(True, {"use_tma": 0}), measure, _rel_err, 1e-5)
         cache.put(dev, key, {"best": res.best.as_dict(), "ms": res.ms, "trials": res.trials})
     if apply:
-        laplacian_config(bool(res.best.tuning.get("use_tma", 0)))
+        laplacian_config(int(res.best.tuning.get("use_tma", 0)))
     return res

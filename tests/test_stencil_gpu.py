@@ -125,9 +125,10 @@ def test_momentum_phases_golden():
     assert np.abs(out - g["phase"]).max() < 1e-15 * 8
 
 
+@pytest.mark.parametrize("staged", [1, 2])
 @pytest.mark.parametrize("latt, nvec", [([8, 8, 6, 3], 2), ([16, 16, 16, 2], 1), ([32, 32, 32, 2], 1),
-                                        ([24, 24, 24, 1], 3), ([4, 4, 3, 2], 2)])
-def test_laplacian_tma_matches_plain_and_oracle(latt, nvec):
+                                        ([24, 24, 24, 1], 3), ([4, 4, 3, 2], 2), ([12, 10, 5, 2], 2)])
+def test_laplacian_tma_matches_plain_and_oracle(latt, nvec, staged):
     """complex64: the TMA-staged kernel (input planes z-1, z, z+1 in shared
     memory, several z slabs per (timeslice, vector)) against the plain kernel
     and the FP64 oracle, with a padded timeslice stride."""
@@ -142,13 +143,13 @@ def test_laplacian_tma_matches_plain_and_oracle(latt, nvec):
     big = torch.zeros((Lt, nvec + 1, 3, V3), dtype=torch.complex64, device="cuda")
     big[:, :nvec] = torch.from_numpy(np.stack([_planes(F[t].T, latt) for t in range(Lt)])).to(torch.complex64)
     try:
-        laplacian_config(True)
+        laplacian_config(staged)
         o_tma = laplacian(links, big[:, :nvec], latt).cpu().numpy()
         assert laplacian_status() == 0
-        laplacian_config(False)
+        laplacian_config(0)
         o_plain = laplacian(links, big[:, :nvec], latt).cpu().numpy()
     finally:
-        laplacian_config(False)
+        laplacian_config()
     assert rel_err(o_tma, o_plain) < 1e-6
     for t in range(Lt):
         Ut = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, t]
