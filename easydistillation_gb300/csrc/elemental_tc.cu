@@ -640,7 +640,7 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
 // Tensor map over four k-block-major planes of R rows: dimensions (k within
 // the 64-byte row, row, plane*nkb + k-block); a box is 128 rows of one
 // k-block, 8 KB contiguous in HBM.
-static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, long long R) {
+static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, long long R, int box_rows = TC_BM) {
   EncodeFn enc = get_encode();
   if (!enc) {
     set_error("cuTensorMapEncodeTiled is unavailable from the driver");
@@ -650,7 +650,7 @@ static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, lo
   const long long KB = TC_ROWB / (long long)esz, nkb = K / KB;
   cuuint64_t gdim[3] = {(cuuint64_t)KB, (cuuint64_t)R, (cuuint64_t)(4 * nkb)};
   cuuint64_t gstride[2] = {(cuuint64_t)TC_ROWB, (cuuint64_t)(R * TC_ROWB)};
-  cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)TC_BM, 1};
+  cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)box_rows, 1};
   cuuint32_t estride[3] = {1, 1, 1};
   CUresult cr = enc(map, kind == TC_TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, base,
                     gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
@@ -712,9 +712,10 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
       chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
   ED_RETURN_LAUNCH("variant planes");
 
-  CUtensorMap amap, bmap;
+  CUtensorMap amap, bmap, bmap16;
   if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra))) return rc;
   if ((rc = encode_kmajor(&bmap, KIND, bpl, K, lay.rb))) return rc;
+  if ((rc = encode_kmajor(&bmap16, KIND, bpl, K, lay.rb, 16))) return rc;  // the narrow last column tile
 
   TcFacTable tab;
   tab.njobs = nb * P->jobs_per_t;
@@ -733,9 +734,21 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
     d.g_off = j.g_off;
     d.mt = (int)ceil_div((long long)j.nright * pz * Ne, TC_BM);
     d.nt = (int)ceil_div((long long)pxy * Ne, TC_BN);
-    d.tile0 = tiles;
-    tiles += d.mt * d.nt;
   }
+  // a last column tile of at most 112 valid columns runs narrow (16-row B boxes, smaller MMA N); number the
+  // full tiles first and the narrow ones after them
+  const int last_cols = pxy * Ne - (tab.j[0].nt - 1) * TC_BN;
+  const bool narrow = ((last_cols + 15) & ~15) < TC_BN;
+  int tiles_n = 0;
+  for (int k = 0; k < tab.njobs; ++k) {
+    TcFacJob& d = tab.j[k];
+    d.tile0 = tiles;
+    tiles += d.mt * (d.nt - (narrow ? 1 : 0));
+    d.tile0n = tiles_n;
+    tiles_n += narrow ? d.mt : 0;
+  }
+  tab.nfull = tiles;
+  tiles += tiles_n;
   static bool attr_set[4] = {};
   static int resident[4] = {};
   if (!attr_set[KIND]) {
@@ -768,7 +781,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, tab, Ne, P->V3, sc, DF, tiles, slab_kb);
+  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");
@@ -992,6 +1005,7 @@ static int launch_ozaki(const ed_elemental_plan* P, const cplx<float>* chains, c
     d.tile0 = tiles;
     tiles += d.mt * d.nt;
   }
+  tab.nfull = tiles;  // every tile full-width (the Ozaki kernel numbers its tiles per group)
   static bool attr_set = false;
   if (!attr_set) {
     e = cudaFuncSetAttribute(tc_ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);

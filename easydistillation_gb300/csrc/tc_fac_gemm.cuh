@@ -35,10 +35,12 @@ struct TcFacJob {
   int brow0;   // first B row (left variants of the group's left chain) within a plane
   int nright;  // right chains of the group
   int tile0, mt, nt;
+  int tile0n;  // first of the group's narrow last-column tiles (numbered after every full tile)
   long long g_off;
 };
 struct TcFacTable {
   int njobs, pxy, pz;
+  int nfull;  // tiles below nfull are full-width; the rest are the groups' narrow last-column tiles
   TcFacJob j[kMaxJobs];
   signed char pidx[kMaxFac];  // momentum index of (a, c) = pidx[a*pz + c], -1 if not requested
 };
@@ -116,7 +118,8 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
 template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fac_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
-                       const __grid_constant__ TcFacTable tab, int Ne, int V3, TcScalars* __restrict__ sc,
+                       const __grid_constant__ CUtensorMap bmap16, const __grid_constant__ TcFacTable tab, int Ne,
+                       int V3, TcScalars* __restrict__ sc,
                        float4* __restrict__ DF, int ntiles, int slab_kb) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;   // k elements per stage
@@ -148,13 +151,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   auto step_tile = [&](int q) { return (q % J) * G + cta; };
   auto step_kb0 = [&](int q) { return (q / J) * slab_kb; };
   auto step_kb1 = [&](int q) { return min(nkb, (q / J + 1) * slab_kb); };
+  // Tile numbering: the full-width tiles of every group (column tile fastest), then, when the groups' last
+  // column tile is narrow, those narrow tiles; grouped like this they share lock steps, which then run faster.
+  const bool has_narrow = tab.nfull < ntiles;
   auto decode = [&](int tile, int& jb, int& mtile, int& ntile) {
     jb = 0;
-    while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
-    const int local = tile - tab.j[jb].tile0;
-    mtile = local / tab.j[jb].nt;
-    ntile = local - mtile * tab.j[jb].nt;
+    if (tile < tab.nfull) {
+      while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
+      const int local = tile - tab.j[jb].tile0;
+      const int ntc = tab.j[jb].nt - (has_narrow ? 1 : 0);
+      mtile = local / ntc;
+      ntile = local - mtile * ntc;
+    } else {
+      const int t2 = tile - tab.nfull;
+      while (jb + 1 < tab.njobs && t2 >= tab.j[jb + 1].tile0n) ++jb;
+      mtile = t2 - tab.j[jb].tile0n;
+      ntile = tab.j[jb].nt - 1;
+    }
   };
+  // columns the MMAs of a tile cover: all TC_BN, or for the last column tile of a group its valid columns
+  // rounded up to 16 (e.g. 16 for the 8 left over by 9 x 200 = 1800 = 14 x 128 + 8); its B rows then come in
+  // 16-row boxes and the MMA runs with that N
+  const int Ncols = tab.pxy * Ne;
+  auto tile_cols = [&](int ntile) { return min(TC_BN, (min(TC_BN, Ncols - ntile * TC_BN) + 15) & ~15); };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TCF_STAGES; ++s) {
@@ -205,6 +224,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           decode(tile, jb, mtile, ntile);
           const int ay = tab.j[jb].arow0 + mtile * TC_BM;
           const int by = tab.j[jb].brow0 + ntile * TC_BN;
+          const int ncol = tile_cols(ntile);
           const int kb1 = step_kb1(q);
           for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
             const int s = (int)(g % TCF_STAGES);
@@ -215,10 +235,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             uint8_t* As = smem + s * TCF_STAGE_BYTES;
             uint8_t* Bs = As + TC_A_BYTES;
-            mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+            mbar_arrive_expect_tx(&full[s], TC_A_BYTES + 4 * ncol * TC_ROWB);
             for (int p = 0; p < 4; ++p) {  // k-block-major planes: one contiguous 8 KB box each
               tma_load_3d(As + p * TC_BM * TC_ROWB, &amap, &full[s], 0, ay, p * nkb + kb);
-              tma_load_3d(Bs + p * TC_BN * TC_ROWB, &bmap, &full[s], 0, by, p * nkb + kb);
+              if (ncol == TC_BN) {
+                tma_load_3d(Bs + p * TC_BN * TC_ROWB, &bmap, &full[s], 0, by, p * nkb + kb);
+              } else {
+                for (int r = 0; r < ncol; r += 16)
+                  tma_load_3d(Bs + p * TC_BN * TC_ROWB + r * TC_ROWB, &bmap16, &full[s], 0, by + r, p * nkb + kb);
+              }
             }
             issued_last = g;
           }
@@ -233,7 +258,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         long long g = 0;  // stages consumed == accumulator buffers filled
         bool ok = true;
         for (int q = 0; q < nsteps && ok; ++q) {
-          if (step_tile(q) >= ntiles) continue;
+          const int tile = step_tile(q);
+          if (tile >= ntiles) continue;
+          int jb, mtile, ntile;
+          decode(tile, jb, mtile, ntile);
+          const uint32_t nfield = (uint32_t)(tile_cols(ntile) >> 3) << 17;  // the instruction's N
+          const uint32_t ID = (IDESC & ~(0x3Fu << 17)) | nfield, ID_NEG = (IDESC_NEG & ~(0x3Fu << 17)) | nfield;
           const int kb1 = step_kb1(q);
           for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
             const int s = (int)(g % TCF_STAGES);
@@ -255,24 +285,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               const uint64_t A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB), A3 = umma_desc_sw64(ao + 3 * TC_BM * TC_ROWB);
               const uint64_t B0 = umma_desc_sw64(bo), B1 = umma_desc_sw64(bo + TC_BN * TC_ROWB);
               const uint64_t B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB), B3 = umma_desc_sw64(bo + 3 * TC_BN * TC_ROWB);
-              umma<KIND>(d_re, A0, B1, IDESC, acc);
-              umma<KIND>(d_re, A1, B0, IDESC, 1u);
-              umma<KIND>(d_re, A2, B3, IDESC_NEG, 1u);
-              umma<KIND>(d_re, A3, B2, IDESC_NEG, 1u);
-              umma<KIND>(d_im, A0, B3, IDESC, acc);
-              umma<KIND>(d_im, A1, B2, IDESC, 1u);
-              umma<KIND>(d_im, A2, B1, IDESC, 1u);
-              umma<KIND>(d_im, A3, B0, IDESC, 1u);
+              umma<KIND>(d_re, A0, B1, ID, acc);
+              umma<KIND>(d_re, A1, B0, ID, 1u);
+              umma<KIND>(d_re, A2, B3, ID_NEG, 1u);
+              umma<KIND>(d_re, A3, B2, ID_NEG, 1u);
+              umma<KIND>(d_im, A0, B3, ID, acc);
+              umma<KIND>(d_im, A1, B2, ID, 1u);
+              umma<KIND>(d_im, A2, B1, ID, 1u);
+              umma<KIND>(d_im, A3, B0, ID, 1u);
             }
 #pragma unroll
             for (int ks = 0; ks < KE / KINST; ++ks) {
               const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
               const uint64_t A0 = umma_desc_sw64(ao), A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB);
               const uint64_t B0 = umma_desc_sw64(bo), B2 = umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB);
-              umma<KIND>(d_re, A0, B0, IDESC, 1u);
-              umma<KIND>(d_re, A2, B2, IDESC_NEG, 1u);
-              umma<KIND>(d_im, A0, B2, IDESC, 1u);
-              umma<KIND>(d_im, A2, B0, IDESC, 1u);
+              umma<KIND>(d_re, A0, B0, ID, 1u);
+              umma<KIND>(d_re, A2, B2, ID_NEG, 1u);
+              umma<KIND>(d_im, A0, B2, ID, 1u);
+              umma<KIND>(d_im, A2, B0, ID, 1u);
             }
             umma_commit(&empty[s]);  // frees the stage when these MMAs complete
             umma_commit(&accf[b]);   // the buffer is ready to drain
