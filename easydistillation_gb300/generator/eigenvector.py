@@ -51,8 +51,8 @@ class EigenvectorGenerator:
     def __init__(self, latt_size: List[int], gauge_field, Ne: int, tol: float, *, stencil_precision: str = "fp64",
                  device=None, ncv: int = None, driver: str = "native") -> None:
         """``ncv``: Krylov dimension of the thick-restart Lanczos (default
-        max(3 Ne, Ne + 32), 2 Ne with Chebyshev acceleration, capped by the
-        problem size).  ``driver``: ``"native"`` runs the FP64-stencil
+        max(9 Ne / 4, Ne + 32), 2 Ne with Chebyshev acceleration, capped by
+        the problem size).  ``driver``: ``"native"`` runs the FP64-stencil
         eigensolve in the library (``ed_lanczos_tr``); ``"python"`` drives the
         same kernels from ``lanczos.trlanczos`` (the FP32-stencil mode always
         does)."""

@@ -37,10 +37,20 @@ class LanczosResult:
 
 
 def default_ncv(nev: int, n: int) -> int:
-    """Krylov dimension: three times the wanted pairs (the reference's QUDA path
-    uses two, eigenvector.py:271-272).  Measured at 24^3, Ne = 100, 8 timeslices:
-    2 nev -> 33 restarts, 6.9 s; 3 nev -> 16 restarts, 5.9 s; 1.5 nev -> 69, 7.3 s."""
-    return min(max(3 * nev, nev + 32), n - 1)
+    """Krylov dimension: 9/4 of the wanted pairs (the reference's QUDA path
+    uses two, eigenvector.py:271-272), with ``kept_pairs`` Ritz pairs kept at
+    a restart.  Measured on GB300 (8 timeslices at 24^3, Ne = 100, and 4 at
+    32^3, Ne = 200; (Krylov dimension, kept) -> seconds): (300, 200) 4.05,
+    (300, 150) 3.11, (300, 110) 2.73, (250, 110) 2.58, (200, 110) 2.59;
+    (600, 400) 20.6, (500, 220) 13.2, (450, 220) 12.5.  Keeping few pairs
+    beyond the wanted ones makes each restart cycle longer and the restarts
+    (one FP64 rotation of the basis each) fewer."""
+    return min(max(9 * nev // 4, nev + 32), n - 1)
+
+
+def kept_pairs(nev: int, ncv: int) -> int:
+    """Ritz pairs kept at a thick restart: the wanted ones and a tenth more (at least 8)."""
+    return min(ncv - 1, nev + max(8, nev // 10))
 
 
 def _reorth_once(Vj: torch.Tensor, w: torch.Tensor, kernel: bool = True):
@@ -120,8 +130,7 @@ def trlanczos(
         v = v0.to(device=device, dtype=c128).clone()
     V[:, 0] = v / torch.linalg.vector_norm(v, dim=1, keepdim=True)
     T = torch.zeros((B, ncv, ncv), dtype=f64, device=device)
-    # Ritz pairs kept at a thick restart: the wanted ones plus half the rest
-    kk = min(ncv - 1, nev + max(1, (ncv - nev) // 2))
+    kk = kept_pairs(nev, ncv)  # Ritz pairs kept at a thick restart
 
     def projected_eigh(k):
         if small_eigh == "dense":

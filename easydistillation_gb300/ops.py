@@ -154,7 +154,7 @@ def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int
         raise ValueError("links must be [nt, 27, Lx*Ly*Lz]")
     n = 3 * V3
     if ncv is None:
-        ncv = min(max((2 if poly_deg > 0 else 3) * Ne, Ne + 32), n)
+        ncv = min(max(2 * Ne if poly_deg > 0 else 9 * Ne // 4, Ne + 32), n - 1)
     if max_restarts is None:
         max_restarts = max(30, 10 * n // max(1, ncv - Ne))
     nbytes = ctypes.c_size_t()

@@ -170,8 +170,9 @@ int ed_cgs_pass(int B, int r, long long n, const void* V, long long v_bstride, v
  * [nt][27][V3] (ed_links_to_soa); evecs out: complex128 colour planes
  * [nt][Ne][3][V3], unit norm; evals out: [nt][Ne] ascending; status (host,
  * int[3]): converged (1/0), restarts, operator applications.  ncv: Krylov
- * dimension (Ne < ncv <= 3*V3); the kept Ritz pairs at a restart are
- * min(ncv-1, Ne + max(1, (ncv-Ne)/2)).  Convergence: |beta y_m,i| <= tol
+ * dimension (Ne < ncv <= 3*V3; 9/4 Ne plain and 2 Ne with Chebyshev
+ * acceleration measured best); the kept Ritz pairs at a restart are
+ * min(ncv-1, Ne + max(8, Ne/10)).  Convergence: |beta y_m,i| <= tol
  * |theta_i| for every wanted pair (ARPACK's test).  poly_deg > 0 iterates on
  * the Chebyshev filter of degree poly_deg that maps [lambda_cut, 12] to
  * [-1, 1] and returns Rayleigh quotients as eigenvalues.  Synchronises the

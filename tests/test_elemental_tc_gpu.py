@@ -121,6 +121,15 @@ def test_fac_many_ragged_tiles(mode):
     assert rel_err(E, ref) < TOL[mode]
 
 
+@pytest.mark.parametrize("Ne", [12, 14, 128, 113])
+def test_fac_last_column_tile_widths(Ne):
+    """9*Ne left-variant columns: 108 (one narrow tile, N = 112), 126 (one tile, rounded to 128: not
+    narrow), 1152 (nine full tiles), 1017 (seven full tiles and a last one of 121 valid columns, not narrow)"""
+    gen, E, ref = _run_fac([4, 4, 4, 1], Ne, 1, R.mom_dict_to_list(3), "f16x3", True)
+    assert gen._plan.factorised == (9, 3)
+    assert rel_err(E, ref) < TOL["f16x3"]
+
+
 def test_fac_long_k():
     """K = 3 * 16^3 = 12288"""
     gen, E, ref = _run_fac([16, 16, 16, 1], 24, 1, R.mom_dict_to_list(3), "f16x3", True)
