@@ -446,30 +446,38 @@ extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, 
 
   // From the second restart on every cycle runs the same launches (steps kk .. ncv-1): they are recorded once
   // on a private stream into a CUDA graph and replayed on the caller's stream.
+  // If recording fails (a caller stream that is itself being captured, for instance), the cycles run eagerly.
   struct GraphRes {
     cudaStream_t cs = nullptr;
     cudaGraph_t g = nullptr;
     cudaGraphExec_t x = nullptr;
-    ~GraphRes() {
+    bool unusable = false;
+    void release() {
       if (x) cudaGraphExecDestroy(x);
       if (g) cudaGraphDestroy(g);
       if (cs) cudaStreamDestroy(cs);
+      x = nullptr;
+      g = nullptr;
+      cs = nullptr;
     }
+    ~GraphRes() { release(); }
   } gr;
+  auto record = [&](int k) -> bool {
+    if (cudaStreamCreateWithFlags(&gr.cs, cudaStreamNonBlocking) != cudaSuccess) return false;
+    if (cudaStreamBeginCapture(gr.cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    sr = gr.cs;
+    const int r = cycle(k);
+    sr = st;
+    const bool ended = cudaStreamEndCapture(gr.cs, &gr.g) == cudaSuccess;
+    return r == ED_OK && ended && cudaGraphInstantiate(&gr.x, gr.g, 0) == cudaSuccess;
+  };
   auto cycle_replayed = [&](int k) -> int {
-    if (!gr.x) {
-      int r = lz_chk(cudaStreamCreateWithFlags(&gr.cs, cudaStreamNonBlocking), "Lanczos capture stream");
-      if (r != ED_OK) return r;
-      if ((r = lz_chk(cudaStreamBeginCapture(gr.cs, cudaStreamCaptureModeThreadLocal), "Lanczos capture")) != ED_OK)
-        return r;
-      sr = gr.cs;
-      r = cycle(k);
-      sr = st;
-      const int r2 = lz_chk(cudaStreamEndCapture(gr.cs, &gr.g), "Lanczos capture end");
-      if (r != ED_OK) return r;
-      if (r2 != ED_OK) return r2;
-      if ((r = lz_chk(cudaGraphInstantiate(&gr.x, gr.g, 0), "Lanczos graph instantiation")) != ED_OK) return r;
+    if (!gr.x && !gr.unusable && !record(k)) {
+      gr.release();
+      gr.unusable = true;
+      cudaGetLastError();  // clear the failed recording's error; the eager cycle reports real launch errors
     }
+    if (!gr.x) return cycle(k);
     return lz_chk(cudaGraphLaunch(gr.x, st), "Lanczos graph launch");
   };
 

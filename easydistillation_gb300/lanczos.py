@@ -181,14 +181,22 @@ def trlanczos(
             cycle(k)  # the first restart cycle also warms up everything the capture will record
         else:
             if cycle_graph is None:
-                cycle_graph = torch.cuda.CUDAGraph()
-                cs = torch.cuda.Stream(device)
-                cs.wait_stream(torch.cuda.current_stream(device))
-                with torch.cuda.stream(cs):
-                    with torch.cuda.graph(cycle_graph, stream=cs):
-                        cycle(k)
-                torch.cuda.current_stream(device).wait_stream(cs)
-            cycle_graph.replay()
+                try:
+                    cycle_graph = torch.cuda.CUDAGraph()
+                    cs = torch.cuda.Stream(device)
+                    cs.wait_stream(torch.cuda.current_stream(device))
+                    with torch.cuda.stream(cs):
+                        with torch.cuda.graph(cycle_graph, stream=cs):
+                            cycle(k)
+                    torch.cuda.current_stream(device).wait_stream(cs)
+                except RuntimeError:
+                    # an operator that cannot be recorded: run the cycles eagerly (recording has not
+                    # executed anything, so V and T are untouched)
+                    cycle_graph, use_graph = None, False
+            if cycle_graph is not None:
+                cycle_graph.replay()
+            else:
+                cycle(k)
         if k > 0:
             restart_cycles += 1
         matvecs += ncv - k
