@@ -625,7 +625,7 @@ def run_grad(args):
     anU = float((U1.grad.conj() * dU).real.sum())
     anw = float((w1.grad * dw).sum())
     line = {"metric": "correlator-loss gradient (dL/dw, dL/dU) 24^3x48 Ne=100", "value": 1.0 / min(times[1:]),
-            "unit": "loss+gradient evaluations/s", "seconds": min(times[1:]), "loss": float(L),
+            "unit": "loss+gradient evaluations/s", "seconds": min(times[1:]), "loss": float(L.detach()),
             "fd_check": {"h": h, "dU_directional": [anU, fdU], "dw_directional": [anw, fdw],
                          "rel_err_U": abs(anU - fdU) / max(abs(fdU), 1e-30),
                          "rel_err_w": abs(anw - fdw) / max(abs(fdw), 1e-30)},
