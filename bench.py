@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
     ap.add_argument("--stencil", action="store_true",
                     help="measure only the Laplacian kernels (c64, c64 TMA-staged, c128) at --lattice")
+    ap.add_argument("--secondary", action="store_true",
+                    help="measure the components beside the hot path: stout smearing, displacement elementals, "
+                         "two-point correlators")
     ap.add_argument("--eigen-batch", type=int, default=8)
     ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--eigen-cpu", action="store_true", help="also time the oracle's scipy eigensolve (slow)")
@@ -634,6 +637,109 @@ def run_grad(args):
     print(json.dumps(line), flush=True)
 
 
+# FP64 flops of one stout link update: four staples of two 3x3 complex products, C U^dag, the
+# anti-Hermitian traceless projection and exp(iQ) (Cayley-Hamilton), the final product: about 1.6e3
+STOUT_FLOP_PER_LINK = 1.6e3
+
+
+def run_secondary(args):
+    """Secondary measurement (``--secondary``) of the components beside the
+    hot path, each timed with CUDA events after a warm-up run:
+
+    * stout smearing (``lattice/generator/stout_smear.cu:159-245``), 32^3 x 64
+      spatial links, rho = 0.1: links/s and the FP64 rate from an estimated
+      1.6 kflop per link; the oracle's numpy form on one timeslice as the CPU
+      baseline;
+    * DisplacementElementalGenerator.calc, 24^3, Ne = 100, distance 2, 7
+      momenta, FP64 and f16x3: timeslices/s;
+    * the two-point correlator of ``lattice/correlator/one_particle.py:12-77``
+      at 48 timeslices, Ne = 100, gamma_5, summed over all 48 sources:
+      correlators/s."""
+    import numpy as np
+    import torch
+
+    from easydistillation_gb300 import DisplacementElementalGenerator
+    from easydistillation_gb300.correlator import gamma, twopoint
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.stout import stout_smear_
+
+    dev = torch.device("cuda", 0)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / reps
+
+    out = {}
+    # stout smearing
+    latt = [32, 32, 32, 64]
+    gauge, _ = make_inputs(latt, 1, distinct_t=4)
+    U = links_to_device(gauge, latt, dev)
+    nlinks = 3 * 32 ** 3 * 64
+    sec = timed(lambda: stout_smear_(U, latt, 1, 0.1), 5)
+    stout = {"links_per_s": nlinks / sec, "seconds_per_step": sec,
+             "fp64_tflops_est": nlinks * STOUT_FLOP_PER_LINK / sec / 1e12, "fp64_peak_tflops": FP64_PEAK_TFLOPS,
+             "workload": "32^3 x 64 spatial links, one step, rho 0.1"}
+    if not args.no_cpu:
+        from oracle import restatement as R
+
+        U1 = np.ascontiguousarray(gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, :1])
+        t0 = time.perf_counter()
+        R.stout_smear(U1, 1, 0.1)
+        cdt = time.perf_counter() - t0
+        stout["cpu_baseline"] = {"links_per_s": 3 * 32 ** 3 / cdt, "kind": "port", "cores": 1,
+                                 "sample": "oracle numpy stout step on one 32^3 timeslice"}
+    out["stout"] = stout
+    del U
+    # displacement elementals
+    latt = [24, 24, 24, 8]
+    V3 = 24 ** 3
+    gauge, evecs = make_inputs(latt, 100, distinct_t=4)
+
+    class _D:
+        def __init__(self, a):
+            self.a, self.file = a, "mem"
+
+        def __getitem__(self, k):
+            return self.a[k]
+
+    class _Src:
+        def __init__(self, a, Ne=None):
+            self.d, self.Ne = _D(a), Ne
+
+        def load(self, key):
+            return self.d
+
+    ev = np.stack([evecs[t % len(evecs)].reshape(100, 24, 24, 24, 3) for t in range(latt[3])])
+    disp = {}
+    for prec in ("fp64", "f16x3"):
+        gen = DisplacementElementalGenerator(latt, _Src(gauge), _Src(ev, 100), 2, mom_dict_to_list(3)[:7],
+                                             precision=prec, device=dev)
+        gen.load("bench")
+        sec = timed(lambda: [gen.calc(t) for t in range(4)], 2) / 4
+        disp[prec] = {"timeslices_per_s": 1.0 / sec}
+    out["displacement_elemental"] = dict(disp, workload="24^3, Ne=100, distance 2, 7 momenta")
+    # two-point correlator
+    Lt, Ne = 48, 100
+    g = torch.Generator(device=dev).manual_seed(4005)
+    peram = torch.complex(torch.randn((Lt, Lt, 4, 4, Ne, Ne), generator=g, device=dev, dtype=torch.float64),
+                          torch.randn((Lt, Lt, 4, 4, Ne, Ne), generator=g, device=dev, dtype=torch.float64))
+    el = torch.complex(torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64),
+                       torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64))
+    ops = [(gamma(15, dev)[None], el)]
+    sec = timed(lambda: twopoint(ops, peram, range(Lt), Lt), 2)
+    out["twopoint"] = {"correlators_per_s": 1.0 / sec, "seconds": sec,
+                       "workload": "48 timeslices, Ne=100, gamma_5, all 48 sources"}
+    print(json.dumps({"metric": "secondary components", **out}), flush=True)
+
+
 def run_stencil(args):
     """Secondary measurement (``--stencil``): the HBM roofline of the Laplacian
     kernels alone (the lines ``bench_stencil`` adds to the main JSON line), at
@@ -722,6 +828,9 @@ def main():
         return
     if args.stencil:
         run_stencil(args)
+        return
+    if args.secondary:
+        run_secondary(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
