@@ -588,6 +588,10 @@ extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int val
       ED_CHECK_ARG(value >= 0 && value <= (1 << 20), "ed_elemental_set_tuning: grid of %d CTAs", value);
       plan->tc_grid = value;
       return ED_OK;
+    case ED_TUNE_TC_STAGES:
+      ED_CHECK_ARG(value == 0 || value == 2 || value == 3, "ed_elemental_set_tuning: %d stages (0, 2 or 3)", value);
+      plan->tc_stages = value;
+      return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_set_tuning: unknown key %d", key);
   }
@@ -605,6 +609,9 @@ extern "C" int ed_elemental_get_tuning(const ed_elemental_plan* plan, int key, i
       return ED_OK;
     case ED_TUNE_TC_GRID:
       *value = plan->tc_grid;
+      return ED_OK;
+    case ED_TUNE_TC_STAGES:
+      *value = plan->tc_stages;
       return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_get_tuning: unknown key %d", key);

@@ -752,10 +752,11 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   static bool attr_set[4] = {};
   static int resident[4] = {};
   if (!attr_set[KIND]) {
-    e = cudaFuncSetAttribute(tc_fac_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, TCF_SMEM);
+    e = cudaFuncSetAttribute(tc_fac_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tcf_smem(TCF_MAX_STAGES));
     if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[KIND], tc_fac_gemm_kernel<KIND>, TC_THREADS,
-                                                      TCF_SMEM);
+                                                      tcf_smem(TCF_MAX_STAGES));
     if (e != cudaSuccess) return cuda_status(e, "tc kernel occupancy");
     if (resident[KIND] < 1) {
       set_error("the factorised tensor-core GEMM does not fit on an SM");
@@ -773,7 +774,8 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(TC_THREADS);
-  cfg.dynamicSmemBytes = TCF_SMEM;
+  const int nst = P->tc_stages > 0 ? P->tc_stages : TCF_DEFAULT_STAGES;
+  cfg.dynamicSmemBytes = tcf_smem(nst);
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -781,7 +783,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb);
+  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb, nst);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");

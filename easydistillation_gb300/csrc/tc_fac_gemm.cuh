@@ -22,10 +22,12 @@
 // warpgroups rise to 200 (256*56 + 256*200 = 512*128), enough to keep two
 // 32-column TMEM loads in flight per wait.
 
-constexpr int TCF_STAGES = 3;
+// Operand stages of 64 KB in the shared-memory ring: 2 or 3, a launch setting (ED_TUNE_TC_STAGES).  Measured
+// at 32^3, Ne = 200, 4 timeslices: 2 stages 144-146 ms, 3 stages 152 ms per launch.
+constexpr int TCF_MAX_STAGES = 3, TCF_DEFAULT_STAGES = 2;
 constexpr int TCF_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;  // 64 KB
-constexpr int TCF_SMEM = TCF_STAGES * TCF_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-static_assert(TCF_SMEM <= 232448, "shared memory per block");
+__host__ __device__ constexpr int tcf_smem(int nst) { return nst * TCF_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/; }
+static_assert(tcf_smem(TCF_MAX_STAGES) <= 232448, "shared memory per block");
 constexpr int TCF_REGS_LOW = 56, TCF_REGS_HIGH = 200;
 static_assert(256 * TCF_REGS_LOW + 256 * TCF_REGS_HIGH == TC_THREADS * TC_LAUNCH_REGS, "register split");
 constexpr int kMaxFac = 128;  // Pxy * Pz
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fac_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
                        const __grid_constant__ CUtensorMap bmap16, const __grid_constant__ TcFacTable tab, int Ne,
                        int V3, TcScalars* __restrict__ sc,
-                       float4* __restrict__ DF, int ntiles, int slab_kb) {
+                       float4* __restrict__ DF, int ntiles, int slab_kb, int nst) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;   // k elements per stage
   constexpr int KINST = 32 / ESZ;     // k elements per MMA instruction
@@ -130,9 +132,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + TCF_STAGES * TCF_STAGE_BYTES);
-  uint64_t* empty = full + TCF_STAGES;
-  uint64_t* accf = empty + TCF_STAGES;  // 2: accumulator buffer ready to drain
+  uint64_t* full = (uint64_t*)(smem + nst * TCF_STAGE_BYTES);
+  uint64_t* empty = full + TCF_MAX_STAGES;
+  uint64_t* accf = empty + TCF_MAX_STAGES;  // 2: accumulator buffer ready to drain
   uint64_t* acce = accf + 2;            // 2: accumulator buffer drained
   uint64_t* mma_done = acce + 2;        // every issued MMA has completed
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   auto tile_cols = [&](int ntile) { return min(TC_BN, (min(TC_BN, Ncols - ntile * TC_BN) + 15) & ~15); };
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TCF_STAGES; ++s) {
+    for (int s = 0; s < nst; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -227,9 +229,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const int ncol = tile_cols(ntile);
           const int kb1 = step_kb1(q);
           for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
-            const int s = (int)(g % TCF_STAGES);
-            if (g >= TCF_STAGES &&
-                !mbar_wait(&empty[s], (uint32_t)(((g / TCF_STAGES) + 1) & 1), status, TC_ERR_EMPTY)) {
+            const int s = (int)(g % nst);
+            if (g >= nst &&
+                !mbar_wait(&empty[s], (uint32_t)(((g / nst) + 1) & 1), status, TC_ERR_EMPTY)) {
               ok = false;
               break;
             }
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
         }
         if (issued_last >= 0)  // do not leave while our copies may still land in shared memory
-          mbar_wait(&full[issued_last % TCF_STAGES], (uint32_t)((issued_last / TCF_STAGES) & 1), status,
+          mbar_wait(&full[issued_last % nst], (uint32_t)((issued_last / nst) & 1), status,
                     TC_ERR_FULL, false);
       }
     } else if (warp == 1) {
@@ -266,9 +268,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t ID = (IDESC & ~(0x3Fu << 17)) | nfield, ID_NEG = (IDESC_NEG & ~(0x3Fu << 17)) | nfield;
           const int kb1 = step_kb1(q);
           for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
-            const int s = (int)(g % TCF_STAGES);
+            const int s = (int)(g % nst);
             const int b = (int)(g & 1);
-            if (!mbar_wait(&full[s], (uint32_t)((g / TCF_STAGES) & 1), status, TC_ERR_FULL) ||
+            if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL) ||
                 (g >= 2 && !mbar_wait(&acce[b], (uint32_t)(((g >> 1) + 1) & 1), status, TC_ERR_ACCE))) {
               ok = false;
               break;

@@ -273,7 +273,7 @@ def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
 MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3, "ozaki_i8": 4}
 _FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR = 0x100, 0x200
 #: plan launch settings (ED_TUNE_* keys)
-TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3}
+TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4}
 #: FP64 pair GEMM tile shapes (rows, cols) by ED_TUNE_F64_TILE value
 F64_TILES = {0: (64, 64), 1: (32, 64), 2: (64, 32), 3: (32, 32)}
 
@@ -334,7 +334,7 @@ class ElementalPlan:
     def set_tuning(self, **settings):
         """Launch settings of later runs: ``f64_tile`` (0..3, see ``F64_TILES``),
         ``tc_slab_kb`` (0 or a power of two <= 256), ``tc_grid`` (0 or a CTA
-        bound).  0 restores the built-in default."""
+        bound), ``tc_stages`` (0, 2 or 3).  0 restores the built-in default."""
         for name, value in settings.items():
             if name not in TUNING_KEYS:
                 raise ValueError(f"unknown tuning setting {name!r}; available: {sorted(TUNING_KEYS)}")

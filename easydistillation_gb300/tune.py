@@ -10,7 +10,8 @@ choices whose best value depends on the shape:
   the requested momenta, slower per product);
 * the K-slab length of the persistent factorised GEMM's lock-step schedule
   (shorter slabs keep the CTAs closer together in K, for L2 reuse of the
-  operand rows, at the cost of more result flushes);
+  operand rows, at the cost of more result flushes) and its number of
+  operand stages (2 or 3 of 64 KB);
 * the tile shape of the FP64 pair GEMM (an Ne that is not a multiple of 64
   wastes part of every 64-row tile);
 * the complex64 Laplacian kernel: neighbours read through L1/L2, or input
@@ -271,7 +272,9 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
                                   factorise=best.factorise)
             if probe.factorised is None or mode == "ozaki_i8":
                 return []
-            return [best] + [Candidate(best.factorise, {"tc_slab_kb": s}) for s in SLABS[1:]]
+            return ([best] + [Candidate(best.factorise, {"tc_slab_kb": s}) for s in SLABS[1:]] +
+                    [Candidate(best.factorise, {"tc_stages": 3}),
+                     Candidate(best.factorise, {"tc_stages": 3, "tc_slab_kb": SLABS[1]})])
 
         stages.append(slabs)
     res = _run_search(stages, Candidate(True, {}), measure, _rel_err, TOLERANCE[mode])

@@ -79,6 +79,8 @@ extern "C" {
                               * the FP32 sums. */
 #define ED_TUNE_TC_GRID 3    /* CTAs of the persistent factorised GEMM: 0 (default: every CTA that
                               * fits on the device at once) or an upper bound on that number */
+#define ED_TUNE_TC_STAGES 4  /* 64 KB operand stages in the factorised GEMM's shared-memory ring: 0
+                              * (default, 2), 2 or 3 */
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);

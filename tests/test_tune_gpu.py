@@ -50,14 +50,16 @@ def test_f64_tile_shapes_are_bit_identical():
 
 @pytest.mark.parametrize("mode", ["f16x3", "tf32x3"])
 def test_tc_slab_and_grid_settings(mode):
-    """Lock-step slabs of 64 / 128 k-blocks (several slabs over K = 3*16^3) and
-    a grid of 2 CTAs (several tiles per CTA) against the oracle."""
+    """Lock-step slabs of 64 / 128 k-blocks (several slabs over K = 3*16^3), a
+    grid of 2 CTAs (several tiles per CTA) and 2 / 3 operand stages against
+    the oracle."""
     from easydistillation_gb300.ops import ElementalPlan
 
     latt, Ne, moms = [16, 16, 16, 1], 8, R.mom_dict_to_list(3)
     U, evec = _case(latt, Ne, seed=7)
     ref = R.elemental(evec, U, latt, 1, moms)
-    for tuning in ({}, {"tc_slab_kb": 64}, {"tc_slab_kb": 128}, {"tc_grid": 2}, {"tc_grid": 3, "tc_slab_kb": 32}):
+    for tuning in ({}, {"tc_slab_kb": 64}, {"tc_slab_kb": 128}, {"tc_grid": 2}, {"tc_grid": 3, "tc_slab_kb": 32},
+                   {"tc_stages": 3}, {"tc_stages": 2, "tc_slab_kb": 64}):
         p = ElementalPlan(latt, Ne, 1, moms, mode, tuning=tuning)
         assert p.factorised == (9, 3)
         assert rel_err(_run_plan(p, U, evec, latt, 1, moms), ref) < 1e-6, tuning
