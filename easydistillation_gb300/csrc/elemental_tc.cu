@@ -320,68 +320,96 @@ struct TcFacSlots {
   int lchain[kMaxDeriv];
 };
 
+// Chain elements each thread of the split kernel loads before its first
+// store: four 16-byte loads in flight per thread for the right side (3 pz
+// variants per element, read-heavy); one for the left side, whose 9 (px, py)
+// variants per element make it write-bound (and four would spill).
+constexpr int kSplitUnrollRight = 4, kSplitUnrollLeft = 1;
+
+// Writes the nvar variants of the two complex elements v (k = 2*kp, 2*kp + 1)
+// of chain row (slot, i) into the planes.
+template <int KIND, bool LEFT>
+__device__ __forceinline__ void tc_fac_split_emit(const float4 v, int kp, long long orow0, int Ne, int nvar,
+                                                  const cplx<float>* __restrict__ fac, int V3, long long Rplane,
+                                                  long long K, int K2, void* __restrict__ planes) {
+  const int site = (2 * kp) % V3;  // V3 is even: both elements lie in one colour plane
+  for (int a = 0; a < nvar; ++a) {
+    const float4 f = *reinterpret_cast<const float4*>(fac + (long long)a * V3 + site);
+    const float fr0 = f.x, fi0 = f.y, fr1 = f.z, fi1 = f.w;
+    float re0, im0, re1, im1;
+    if constexpr (LEFT) {  // conj(x) * f
+      re0 = v.x * fr0 + v.y * fi0;
+      im0 = v.x * fi0 - v.y * fr0;
+      re1 = v.z * fr1 + v.w * fi1;
+      im1 = v.z * fi1 - v.w * fr1;
+    } else {  // f * y
+      re0 = fr0 * v.x - fi0 * v.y;
+      im0 = fr0 * v.y + fi0 * v.x;
+      re1 = fr1 * v.z - fi1 * v.w;
+      im1 = fr1 * v.w + fi1 * v.z;
+    }
+    const long long orow = orow0 + (long long)a * Ne;
+    // k-block-major planes: element (row, k) of a plane at ((k / KB) * Rplane + row) * KB + k % KB,
+    // KB = the k elements of one 64-byte TMA row, so each (128-row, k-block) box is contiguous
+    if constexpr (KIND == TC_TF32) {
+      uint32_t* P = (uint32_t*)planes;
+      const long long plane = Rplane * K, e0 = ((2LL * kp / 16) * Rplane + orow) * 16 + (2 * kp) % 16;
+      uint32_t h, l;
+      Split<TC_TF32>::one(re0, h, l);
+      P[e0] = h;
+      P[plane + e0] = l;
+      Split<TC_TF32>::one(re1, h, l);
+      P[e0 + 1] = h;
+      P[plane + e0 + 1] = l;
+      Split<TC_TF32>::one(im0, h, l);
+      P[2 * plane + e0] = h;
+      P[3 * plane + e0] = l;
+      Split<TC_TF32>::one(im1, h, l);
+      P[2 * plane + e0 + 1] = h;
+      P[3 * plane + e0 + 1] = l;
+    } else {
+      uint32_t* P = (uint32_t*)planes;  // 16-bit elements, pairs as words (16 words per 64-byte row)
+      const long long plane = Rplane * K2, w = (((long long)kp / 16) * Rplane + orow) * 16 + kp % 16;
+      uint32_t h, l;
+      Split<KIND>::pair(re0, re1, h, l);
+      P[w] = h;
+      P[plane + w] = l;
+      Split<KIND>::pair(im0, im1, h, l);
+      P[2 * plane + w] = h;
+      P[3 * plane + w] = l;
+    }
+  }
+}
+
 // out row (slot*nvar + a)*Ne + i of the planes <- conj(X_i) f_a   (LEFT)
 //                                              or f_a Y_i         (right)
 // for input row (slot, i) of the chain buffer; f_a = factor table a in
-// complex64, already scaled by 2^e (tc_phase_kernel).
-template <int KIND, bool LEFT>
-__global__ void tc_fac_split_kernel(const cplx<float>* __restrict__ chains, TcFacSlots sl, int nrows, int Ne,
+// complex64, already scaled by 2^e (tc_phase_kernel).  A block covers
+// UNROLL * blockDim.x element pairs of a row; each thread loads its UNROLL
+// pairs (blockDim.x apart) before it writes any variant.
+template <int KIND, bool LEFT, int UNROLL>
+__global__ void __launch_bounds__(256, 3) tc_fac_split_kernel(const cplx<float>* __restrict__ chains, TcFacSlots sl, int nrows, int Ne,
                                     int nvar, const cplx<float>* __restrict__ fac, int V3, long long Rplane,
                                     void* __restrict__ planes) {
   const long long K = 3LL * V3;
   const int K2 = (int)(K / 2);
+  const int span = UNROLL * blockDim.x;
   for (int row = blockIdx.y; row < nrows; row += gridDim.y) {
     const int slot = row / Ne, i = row - (row / Ne) * Ne;
     const int chain = LEFT ? (slot / sl.nl) * sl.nchain + sl.lchain[slot % sl.nl] : slot;
     const float4* src = reinterpret_cast<const float4*>(chains + ((long long)chain * Ne + i) * K);
-    for (int kp = blockIdx.x * blockDim.x + threadIdx.x; kp < K2; kp += gridDim.x * blockDim.x) {
-      const float4 v = src[kp];
-      const int site = (2 * kp) % V3;  // V3 is even: both elements lie in one colour plane
-      for (int a = 0; a < nvar; ++a) {
-        const float4 f = *reinterpret_cast<const float4*>(fac + (long long)a * V3 + site);
-        const float fr0 = f.x, fi0 = f.y, fr1 = f.z, fi1 = f.w;
-        float re0, im0, re1, im1;
-        if constexpr (LEFT) {  // conj(x) * f
-          re0 = v.x * fr0 + v.y * fi0;
-          im0 = v.x * fi0 - v.y * fr0;
-          re1 = v.z * fr1 + v.w * fi1;
-          im1 = v.z * fi1 - v.w * fr1;
-        } else {  // f * y
-          re0 = fr0 * v.x - fi0 * v.y;
-          im0 = fr0 * v.y + fi0 * v.x;
-          re1 = fr1 * v.z - fi1 * v.w;
-          im1 = fr1 * v.w + fi1 * v.z;
-        }
-        const long long orow = ((long long)slot * nvar + a) * Ne + i;
-        // k-block-major planes: element (row, k) of a plane at ((k / KB) * Rplane + row) * KB + k % KB,
-        // KB = the k elements of one 64-byte TMA row, so each (128-row, k-block) box is contiguous
-        if constexpr (KIND == TC_TF32) {
-          uint32_t* P = (uint32_t*)planes;
-          const long long plane = Rplane * K, e0 = ((2LL * kp / 16) * Rplane + orow) * 16 + (2 * kp) % 16;
-          uint32_t h, l;
-          Split<TC_TF32>::one(re0, h, l);
-          P[e0] = h;
-          P[plane + e0] = l;
-          Split<TC_TF32>::one(re1, h, l);
-          P[e0 + 1] = h;
-          P[plane + e0 + 1] = l;
-          Split<TC_TF32>::one(im0, h, l);
-          P[2 * plane + e0] = h;
-          P[3 * plane + e0] = l;
-          Split<TC_TF32>::one(im1, h, l);
-          P[2 * plane + e0 + 1] = h;
-          P[3 * plane + e0 + 1] = l;
-        } else {
-          uint32_t* P = (uint32_t*)planes;  // 16-bit elements, pairs as words (16 words per 64-byte row)
-          const long long plane = Rplane * K2, w = (((long long)kp / 16) * Rplane + orow) * 16 + kp % 16;
-          uint32_t h, l;
-          Split<KIND>::pair(re0, re1, h, l);
-          P[w] = h;
-          P[plane + w] = l;
-          Split<KIND>::pair(im0, im1, h, l);
-          P[2 * plane + w] = h;
-          P[3 * plane + w] = l;
-        }
+    const long long orow0 = (long long)slot * nvar * Ne + i;
+    for (int k0 = blockIdx.x * span + threadIdx.x; k0 < K2; k0 += gridDim.x * span) {
+      float4 v[UNROLL];
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        const int kp = k0 + u * blockDim.x;
+        if (kp < K2) v[u] = src[kp];
+      }
+#pragma unroll
+      for (int u = 0; u < UNROLL; ++u) {
+        const int kp = k0 + u * blockDim.x;
+        if (kp < K2) tc_fac_split_emit<KIND, LEFT>(v[u], kp, orow0, Ne, nvar, fac, V3, Rplane, K, K2, planes);
       }
     }
   }
@@ -704,11 +732,11 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   sl.nl = nl;
   sl.nchain = P->nchain;
   for (int s = 0; s < nl; ++s) sl.lchain[s] = P->fac_lchain[s];
-  const int kx = (int)ceil_div(K / 2, 256);
+  const int kxl = (int)ceil_div(K / 2, 256 * kSplitUnrollLeft), kxr = (int)ceil_div(K / 2, 256 * kSplitUnrollRight);
   const int lrows = nb * nl * Ne, rrows = nb * P->nchain * Ne;
-  tc_fac_split_kernel<KIND, true><<<dim3(kx, std::min(lrows, 65535)), 256, 0, stream>>>(
+  tc_fac_split_kernel<KIND, true, kSplitUnrollLeft><<<dim3(kxl, std::min(lrows, 65535)), 256, 0, stream>>>(
       chains, sl, lrows, Ne, pxy, fxy32, P->V3, lay.rb, bpl);
-  tc_fac_split_kernel<KIND, false><<<dim3(kx, std::min(rrows, 65535)), 256, 0, stream>>>(
+  tc_fac_split_kernel<KIND, false, kSplitUnrollRight><<<dim3(kxr, std::min(rrows, 65535)), 256, 0, stream>>>(
       chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
   ED_RETURN_LAUNCH("variant planes");
 
