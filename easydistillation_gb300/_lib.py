@@ -25,6 +25,7 @@ ED_ERR_TIMEOUT = -5
 
 ED_C128 = 0
 ED_C64 = 1
+ED_BIG_ENDIAN = 0x10
 
 _c = ctypes
 _vp = _c.c_void_p
@@ -36,6 +37,8 @@ _SIGNATURES = {
     "ed_last_error": ([_c.c_char_p, _c.c_size_t], _i),
     "ed_links_to_soa": ([_i, _i, _i, _i, _i, _vp, _ll, _ll, _ll, _vp, _vp], _i),
     "ed_vectors_to_planes": ([_i, _i, _i, _ll, _i, _vp, _vp, _vp], _i),
+    "ed_decode_complex": ([_i, _ll, _vp, _i, _vp, _vp], _i),
+    "ed_decode_links": ([_i, _ll, _vp, _vp, _vp], _i),
     "ed_vectors_from_planes": ([_i, _i, _ll, _i, _vp, _vp, _vp], _i),
     "ed_momentum_phases": ([_i, _i, _i, _c.POINTER(_i), _i, _vp, _vp], _i),
     "ed_laplacian": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _ll, _vp, _ll, _vp], _i),

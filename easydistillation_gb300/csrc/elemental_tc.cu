@@ -287,9 +287,17 @@ __global__ void tc_split_kernel(const cplx<float>* __restrict__ chains, long lon
   }
 }
 
-// double-float pair results -> complex128
+// double-float pair results -> complex128; two 16-byte loads in flight per
+// thread (elements i and i + stride) before the stores
 __global__ void tc_df_to_c128_kernel(const float4* __restrict__ DF, long long n, cplx<double>* __restrict__ G) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    const float4 a = DF[i], b = DF[i + stride];
+    G[i] = mk((double)a.x + (double)a.y, (double)a.z + (double)a.w);
+    G[i + stride] = mk((double)b.x + (double)b.y, (double)b.z + (double)b.w);
+  }
+  if (i < n) {
     const float4 d = DF[i];
     G[i] = mk((double)d.x + (double)d.y, (double)d.z + (double)d.w);
   }
@@ -660,7 +668,7 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
   kern<<<tiles, TC_THREADS, TC_SMEM, stream>>>(amap, tab, P->Ne, P->nmom, P->V3, R, chains, ph32, sc, DF, xr);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   ED_RETURN_LAUNCH("tensor-core pair GEMM");
-  tc_df_to_c128_kernel<<<4 * sms, 256, 0, stream>>>(DF, g_used, G);
+  tc_df_to_c128_kernel<<<8 * sms, 256, 0, stream>>>(DF, g_used, G);
   ED_RETURN_LAUNCH("double-float to complex128");
   return ED_OK;
 }
@@ -815,7 +823,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");
-  tc_df_to_c128_kernel<<<4 * sms, 256, 0, stream>>>(DF, g_used, G);
+  tc_df_to_c128_kernel<<<8 * sms, 256, 0, stream>>>(DF, g_used, G);
   ED_RETURN_LAUNCH("double-float to complex128");
   return ED_OK;
 }

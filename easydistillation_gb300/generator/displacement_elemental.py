@@ -18,7 +18,7 @@ import torch
 
 from ..insertion import MomentumPhase
 from ..ops import PairPlan, links_to_soa, mean_c128, parallel_transport, vectors_to_planes
-from .elemental import ElementalGenerator, links_to_device
+from .elemental import ElementalGenerator, gauge_to_device
 
 NC = 3
 
@@ -47,7 +47,7 @@ class DisplacementElementalGenerator:
         self._reader.device = self.device
 
     def load(self, key: str):
-        self._U = links_to_device(self.gauge_field.load(key)[:], self.latt_size, self.device)
+        self._U = gauge_to_device(self.gauge_field.load(key), self.latt_size, self.device)
         self._links = links_to_soa(self._U, self.latt_size)
         self._eigenvector_data = self.eigenvector.load(key)
 

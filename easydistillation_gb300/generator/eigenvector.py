@@ -23,7 +23,7 @@ import torch
 
 from .. import lanczos as LZ
 from ..ops import lanczos_tr, links_to_soa, laplacian, vectors_from_planes
-from .elemental import links_to_device
+from .elemental import gauge_to_device
 
 NC = 3
 
@@ -73,7 +73,7 @@ class EigenvectorGenerator:
         self.last_stats = None
 
     def load(self, key: str):
-        self._U = links_to_device(self.gauge_field.load(key)[:], self.latt_size, self.device)
+        self._U = gauge_to_device(self.gauge_field.load(key), self.latt_size, self.device)
         self._soa = {}
 
     def project_SU3(self):

@@ -92,6 +92,20 @@ def links_to_device(gauge_data, latt_size, device) -> torch.Tensor:
     return U.permute(4, 0, 1, 2, 3, 5, 6)[: ND - 1].contiguous()
 
 
+def gauge_to_device(gauge_file_data, latt_size, device) -> torch.Tensor:
+    """Spatial links ``[3, Lt, Lz, Ly, Lx, 3, 3]`` complex128 on the device
+    from ``gauge_field.load(key)``.  A reader of this package that offers
+    ``links_to_device`` (ILDG, npy, raw binary with complex values) uploads
+    the stored bytes and converts and transposes them on the device; any other
+    object is read with ``[:]`` (the reference's ``elemental.py:103``) and
+    goes through :func:`links_to_device`."""
+    if hasattr(gauge_file_data, "links_to_device"):
+        U = gauge_file_data.links_to_device(latt_size, device)
+        if U is not None:
+            return U
+    return links_to_device(gauge_file_data[:], latt_size, device)
+
+
 def admit_batch(latt_size, Ne, num_nabla, momentum_list, precision="fp64", device=None, max_batch=8,
                 reserve=0.1, factorise: bool = True) -> int:
     """Largest batch of timeslices whose plan workspace fits the free HBM of
@@ -169,7 +183,7 @@ class ElementalGenerator:
                              self.device, batch=batch, factorise=self.factorise)
 
     def load(self, key: str):
-        self._U = links_to_device(self.gauge_field.load(key)[:], self.latt_size, self.device)
+        self._U = gauge_to_device(self.gauge_field.load(key), self.latt_size, self.device)
         self._eigenvector_data = self.eigenvector.load(key)
 
     def _read_vectors(self, t: int) -> torch.Tensor:
@@ -180,6 +194,10 @@ class ElementalGenerator:
         data = self._eigenvector_data
         if isinstance(data, torch.Tensor):
             return data[t, :Ne].reshape(Ne, Lz * Ly * Lx * NC).to(self.device).contiguous()
+        if hasattr(data, "raw"):
+            dev = self._read_vectors_raw(t, data)
+            if dev is not None:
+                return dev
         if self._stage is None:
             self._stage = torch.empty((Ne, Lz * Ly * Lx * NC), dtype=torch.complex128).pin_memory()
         # the previous host->device copy out of the pinned stage must finish before it is refilled
@@ -203,6 +221,48 @@ class ElementalGenerator:
             self._stage_event = torch.cuda.Event()
         self._stage_event.record()
         return dev
+
+    def _read_vectors_raw(self, t: int, data) -> torch.Tensor:
+        """``eigenvector[t, 0:Ne]`` from a reader of this package: the stored
+        bytes (one memory-mapped block, or one record per e for keyed files
+        such as QDP lazy-disk maps) are copied into a pinned byte stage,
+        uploaded in one copy and converted to complex128 on the device
+        (``ops.decode_complex``).  None when the stored values are not
+        complex numbers, so the caller converts on the host."""
+        from .. import ops
+        from ..preset import pinned_bytes
+
+        Lx, Ly, Lz, Lt = self.latt_size
+        Ne, n = self.Ne, Lz * Ly * Lx * NC
+        views = None
+        try:
+            v = data.raw((t, slice(0, Ne)), copy=False)
+            if np.size(v) == Ne * n:
+                views = [v]
+        except (IndexError, TypeError, ValueError, KeyError):
+            views = None
+        if views is None:
+            views = [data.raw((t, e), copy=False) for e in range(Ne)]
+            if sum(np.size(v) for v in views) != Ne * n:
+                raise ValueError(f"eigenvector data of timeslice {t} do not hold {Ne} vectors of {n} components")
+        dt = np.dtype(views[0].dtype)
+        if dt.kind != "c" or any(np.dtype(v.dtype) != dt for v in views):
+            return None
+        nbytes = Ne * n * dt.itemsize
+        if getattr(self, "_raw_stage", None) is None or self._raw_stage.numel() < nbytes:
+            self._raw_stage = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        # the previous host->device copy out of the pinned stage must finish before it is refilled
+        if getattr(self, "_stage_event", None) is not None:
+            self._stage_event.synchronize()
+        off = 0
+        for v in views:
+            pinned_bytes(v, self._raw_stage[off:])
+            off += v.nbytes
+        raw = self._raw_stage[:nbytes].to(self.device, non_blocking=True)
+        if getattr(self, "_stage_event", None) is None:
+            self._stage_event = torch.cuda.Event()
+        self._stage_event.record()
+        return ops.decode_complex(raw, dt, torch.complex128).reshape(Ne, n)
 
     def _fetch_chunk(self, chunk, slot, stream):
         """Eigenvectors of the timeslices in ``chunk`` into the device input

@@ -7,6 +7,7 @@ torch stream; none has a CPU path.
 from __future__ import annotations
 
 import ctypes
+import sys
 from typing import Sequence
 
 import torch
@@ -15,6 +16,7 @@ from . import _lib
 from ._lib import ED_C64, ED_C128, call, ptr, require_cuda, stream_handle
 
 _PREC = {torch.complex128: ED_C128, torch.complex64: ED_C64}
+_NATIVE_LITTLE = sys.byteorder == "little"
 _DTYPE = {ED_C128: torch.complex128, ED_C64: torch.complex64}
 
 
@@ -47,6 +49,64 @@ def links_to_soa(U: torch.Tensor, latt_size: Sequence[int], dtype=torch.complex1
         raise ValueError(f"unknown link layout {layout!r}")
     out = torch.empty((nt, 27, V3), dtype=dtype, device=U.device)
     call("ed_links_to_soa", _PREC[dtype], Lx, Ly, Lz, nt, ptr(U), ts, ds, ss, ptr(out), stream_handle())
+    return out
+
+
+def file_prec(dtype) -> int:
+    """Source precision code of ``ed_decode_*`` for a stored complex numpy
+    dtype (``">c16"``, ``"<c8"`` ...): ED_C128 / ED_C64, plus ED_BIG_ENDIAN
+    when the bytes are big-endian."""
+    import numpy as np
+
+    dt = np.dtype(dtype)
+    if dt.kind != "c" or dt.itemsize not in (8, 16):
+        raise ValueError(f"not a complex64/complex128 dtype: {dtype!r}")
+    big = dt.byteorder == ">" or (dt.byteorder == "=" and not _NATIVE_LITTLE)
+    return (ED_C128 if dt.itemsize == 16 else ED_C64) | (_lib.ED_BIG_ENDIAN if big else 0)
+
+
+def decode_complex(raw: torch.Tensor, file_dtype, dtype=torch.complex128, out: torch.Tensor = None) -> torch.Tensor:
+    """Complex numbers from a file's byte image on the device.
+
+    ``raw`` holds the stored bytes (any dtype, contiguous, on the device);
+    ``file_dtype`` is their numpy dtype (e.g. ``">c16"`` for ILDG, ``">c8"``
+    for QDP eigenvectors).  Returns (or fills ``out``) a flat ``dtype``
+    tensor: the byte order swapped and the precision converted on the device,
+    bit-identical to numpy's ``astype`` (``lattice/filedata/ildg.py:70``,
+    ``timeslice.py:96``)."""
+    require_cuda(raw, "raw")
+    if not raw.is_contiguous():
+        raise ValueError("raw bytes must be contiguous")
+    src = file_prec(file_dtype)
+    esz = 16 if (src & ~_lib.ED_BIG_ENDIAN) == ED_C128 else 8
+    nbytes = raw.numel() * raw.element_size()
+    if nbytes % esz:
+        raise ValueError(f"{nbytes} bytes is not a whole number of {esz}-byte complex numbers")
+    n = nbytes // esz
+    if out is None:
+        out = torch.empty(n, dtype=dtype, device=raw.device)
+    elif out.numel() != n or out.dtype != dtype or not out.is_contiguous():
+        raise ValueError("out must be a contiguous tensor of the decoded size and dtype")
+    call("ed_decode_complex", src, n, ptr(raw), _PREC[dtype], ptr(out), stream_handle())
+    return out
+
+
+def decode_links(raw: torch.Tensor, file_dtype, latt_size: Sequence[int]) -> torch.Tensor:
+    """Links in the ILDG order ``[Lt, Lz, Ly, Lx, 4, 3, 3]`` (the file's byte
+    image on the device) -> the generators' spatial links
+    ``[3, Lt, Lz, Ly, Lx, 3, 3]`` complex128 (``elemental.py:103``,
+    ``eigenvector.py:50``), in one device pass."""
+    require_cuda(raw, "raw")
+    if not raw.is_contiguous():
+        raise ValueError("raw bytes must be contiguous")
+    Lx, Ly, Lz, Lt = latt_size
+    sites = Lx * Ly * Lz * Lt
+    src = file_prec(file_dtype)
+    esz = 16 if (src & ~_lib.ED_BIG_ENDIAN) == ED_C128 else 8
+    if raw.numel() * raw.element_size() != sites * 36 * esz:
+        raise ValueError("raw bytes do not hold [Lt, Lz, Ly, Lx, 4, 3, 3] complex numbers")
+    out = torch.empty((3, Lt, Lz, Ly, Lx, 3, 3), dtype=torch.complex128, device=raw.device)
+    call("ed_decode_links", src, sites, ptr(raw), ptr(out), stream_handle())
     return out
 
 

@@ -7,8 +7,16 @@ file-data object that is indexed like a numpy array (``[:]``, ``[t]``,
 ``[t, e]``, slices).  Reads are memory-mapped; the result is a host numpy
 array with the reference's dtype conversion (ILDG data up-cast to complex128,
 ``lattice/filedata/ildg.py:70``; QDP lazy-disk-map data down-cast to
-complex64, ``timeslice.py:96``).  ``to_device(key, device)`` uploads an index
-through pinned memory in one copy.
+complex64, ``timeslice.py:96``).
+
+Device side (no counterpart in the reference, whose readers convert on the
+host): ``raw(key)`` gives the stored values without conversion;
+``to_device(key)`` copies the stored bytes of complex data into pinned
+memory, uploads them in one copy and converts them on the device
+(``ops.decode_complex``: byte order and precision, bit-identical to the host
+conversion); ``links_to_device(latt_size)`` does the same for a gauge field in
+the ILDG order and transposes it to the generators' spatial-link layout in the
+same pass (``ops.decode_links``).
 
 Formats:
 * ILDG / LIME (``ildg.py:82-96``): records of an 8-byte magic/version word, a
@@ -52,21 +60,79 @@ class _Data:
     def _convert(self, a):
         return a
 
+    # numpy dtype __getitem__ converts to (None: the stored dtype)
+    _target = None
+
+    def _account(self, start, nbytes):
+        self.time_in_sec += time() - start
+        self.size_in_byte += nbytes
+        self.timeInSec, self.sizeInByte = self.time_in_sec, self.size_in_byte
+
+    def _view(self, key):
+        """The stored values of ``key``, memory-mapped (no copy)."""
+        return self._array()[key]
+
     def __getitem__(self, key):
         s = time()
-        arr = self._array()
-        ret = self._convert(np.array(arr[key], copy=True))
-        self.time_in_sec += time() - s
-        self.size_in_byte += ret.nbytes
-        self.timeInSec, self.sizeInByte = self.time_in_sec, self.size_in_byte
+        ret = self._convert(np.array(self._view(key), copy=True))
+        self._account(s, ret.nbytes)
+        return ret
+
+    def raw(self, key, copy: bool = True):
+        """The stored values of ``key`` without conversion: a host array in
+        the file's own dtype (byte order and precision as on disk); with
+        ``copy=False`` the memory-mapped view."""
+        s = time()
+        v = self._view(key)
+        ret = np.array(v, copy=True) if copy else v
+        self._account(s, ret.nbytes)
         return ret
 
     def to_device(self, key, device=None, dtype=None):
-        a = self[key]
-        t = torch.from_numpy(np.ascontiguousarray(a))
-        if dtype is not None:
-            t = t.to(dtype)
-        return t.pin_memory().to(device or "cuda", non_blocking=True)
+        """``self[key]`` as a device tensor.  Complex data go up as stored and
+        are converted on the device (to ``dtype``, default the reader's own
+        conversion); other data are converted on the host first."""
+        v = self.raw(key, copy=False)
+        if np.dtype(v.dtype).kind != "c":
+            t = torch.from_numpy(np.ascontiguousarray(self._convert(np.array(v, copy=True))))
+            if dtype is not None:
+                t = t.to(dtype)
+            return t.pin_memory().to(device or "cuda", non_blocking=True)
+        from . import ops
+
+        if dtype is None:
+            dtype = torch.complex128 if np.dtype(self._target or v.dtype).itemsize == 16 else torch.complex64
+        raw = pinned_bytes(v).to(device or "cuda", non_blocking=True)
+        return ops.decode_complex(raw, v.dtype, dtype).reshape(np.shape(v))
+
+    def links_to_device(self, latt_size, device=None):
+        """The gauge field of this file (ILDG order ``[Lt, Lz, Ly, Lx, 4, 3,
+        3]``, complex) as the generators' spatial links ``[3, Lt, Lz, Ly, Lx,
+        3, 3]`` complex128 on the device, converted and transposed there; None
+        when the stored values are not complex numbers of that count."""
+        v = self.raw(slice(None), copy=False)
+        Lx, Ly, Lz, Lt = latt_size
+        if np.dtype(v.dtype).kind != "c" or np.size(v) != Lt * Lz * Ly * Lx * 36:
+            return None
+        from . import ops
+
+        raw = pinned_bytes(v).to(device or "cuda", non_blocking=True)
+        return ops.decode_links(raw, v.dtype, latt_size)
+
+
+def pinned_bytes(a, out: torch.Tensor = None) -> torch.Tensor:
+    """The bytes of array ``a`` (a memory-mapped view or any numpy array) in
+    page-locked host memory, copied in one pass: a uint8 tensor of
+    ``a.nbytes`` (or the first ``a.nbytes`` bytes of ``out``, a pinned uint8
+    tensor, when given)."""
+    a = np.asarray(a)
+    if out is None:
+        out = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+    elif out.dtype != torch.uint8 or out.numel() < a.nbytes:
+        raise ValueError("out must be a uint8 tensor of at least a.nbytes bytes")
+    dst = out[: a.nbytes].numpy().view(a.dtype).reshape(a.shape)
+    np.copyto(dst, a, casting="no")
+    return out[: a.nbytes]
 
 
 class NdarrayFileData(_Data):
@@ -134,6 +200,8 @@ class IldgFileData(_Data):
     def _array(self):
         return np.memmap(self.file, dtype=self.dtype, mode="r", offset=self.offset, shape=tuple(self.shape))
 
+    _target = "<c16"
+
     def _convert(self, a):
         return a.astype("<c16")
 
@@ -164,19 +232,22 @@ class QDPLazyDiskMapObjFileData(_Data):
         self.time_in_sec = self.timeInSec = 0.0
         self.size_in_byte = self.sizeInByte = 0
 
-    def __getitem__(self, key):
+    _target = "<c8"
+
+    def _convert(self, a):
+        return a.astype("<c8")
+
+    def links_to_device(self, latt_size, device=None):
+        return None  # records are keyed by (t, mu), not in the ILDG site order
+
+    def _view(self, key):
         if isinstance(key, int):
             key = (key,)
         head = tuple(key[: self.extra])
         if head not in self.offsets:
             raise IndexError(f"index {key} is out of bounds for axes")
-        s = time()
         arr = np.memmap(self.file, dtype=self.dtype, mode="r", offset=self.offsets[head], shape=tuple(self.shape))
-        ret = np.array(arr[tuple(key[self.extra :])], copy=True).astype("<c8")
-        self.time_in_sec += time() - s
-        self.size_in_byte += ret.nbytes
-        self.timeInSec, self.sizeInByte = self.time_in_sec, self.size_in_byte
-        return ret
+        return arr[tuple(key[self.extra :])]
 
 
 class _Preset:

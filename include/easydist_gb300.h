@@ -46,6 +46,7 @@ extern "C" {
 /* ---- storage precisions */
 #define ED_C128 0 /* complex128: double2 */
 #define ED_C64 1  /* complex64:  float2  */
+#define ED_BIG_ENDIAN 0x10 /* flag on a source precision of ed_decode_*: stored big-endian */
 
 /* ---- elemental arithmetic modes */
 #define ED_MODE_FP64 0   /* plain FP64 SIMT contraction (V rounded to c64, all else c128) */
@@ -331,6 +332,23 @@ int ed_elemental_set_profile_events(ed_elemental_plan* plan, void* start, void* 
  * tensor-core kernel gave up (its output is then invalid).  *code receives
  * the raw status word (0 = ok). */
 int ed_elemental_status(const ed_elemental_plan* plan, const void* workspace, int* code, void* stream);
+
+/* ---- on-disk formats (lattice/filedata/ildg.py:70, lattice/filedata/timeslice.py:96,
+ *      lattice/generator/elemental.py:103: the readers' byte-order and precision
+ *      conversion and the generators' link transpose, on the device) */
+
+/* n complex numbers from a file's byte image in device memory (src_prec
+ * ED_C128 or ED_C64, | ED_BIG_ENDIAN when stored big-endian) to native
+ * complex numbers of dst_prec (ED_C128 widens exactly; ED_C64 rounds to
+ * nearest, as numpy's astype).  src aligned to its element size, dst to its;
+ * the two ranges must not overlap.  n = 0 is a no-op. */
+int ed_decode_complex(int src_prec, long long n, const void* src, int dst_prec, void* dst, void* stream);
+
+/* Spatial links from the ILDG site order: src [sites][4][3][3] complex (the
+ * file's byte image, src_prec as above, sites = Lt*Lz*Ly*Lx), dst
+ * [3][sites][3][3] complex128, the generators' [dir][t][z][y][x][3][3]
+ * layout (the time links are dropped).  dst 16-byte aligned, no overlap. */
+int ed_decode_links(int src_prec, long long sites, const void* src, void* dst, void* stream);
 
 #ifdef __cplusplus
 }

@@ -65,6 +65,21 @@ def test_argument_validation_is_host_side():
                            256, 1 << 30, None) == _lib.ED_ERR_ARG  # Chebyshev without a cut
     assert L.ed_lanczos_tr(6, 6, 6, 2, 256, 16, ctypes.c_double(1e-10), 40, 10, 0, ctypes.c_double(0.0), 256, 256, st,
                            256, 1024, None) == _lib.ED_ERR_WORKSPACE
+    # on-disk decoding: precision codes, null / misaligned / overlapping pointers
+    BE = _lib.ED_BIG_ENDIAN
+    assert L.ed_decode_complex(_lib.ED_C128 | BE, 0, None, _lib.ED_C128, None, None) == _lib.ED_OK  # empty
+    assert L.ed_decode_complex(2, 4, 256, _lib.ED_C128, 4096, None) == _lib.ED_ERR_ARG
+    assert L.ed_decode_complex(_lib.ED_C64 | 0x20, 4, 256, _lib.ED_C128, 4096, None) == _lib.ED_ERR_ARG
+    assert L.ed_decode_complex(_lib.ED_C128, 4, 256, 5, 4096, None) == _lib.ED_ERR_ARG
+    assert L.ed_decode_complex(_lib.ED_C128 | BE, 4, None, _lib.ED_C128, 4096, None) == _lib.ED_ERR_ARG
+    assert L.ed_decode_complex(_lib.ED_C128 | BE, 4, 264, _lib.ED_C128, 4096, None) == _lib.ED_ERR_ARG  # src % 16
+    assert "misaligned" in _lib.last_error()
+    assert L.ed_decode_complex(_lib.ED_C64 | BE, 4, 264, _lib.ED_C128, 4104, None) == _lib.ED_ERR_ARG  # dst % 16
+    assert L.ed_decode_complex(_lib.ED_C128 | BE, 4, 256, _lib.ED_C128, 288, None) == _lib.ED_ERR_ARG  # overlap
+    assert "overlap" in _lib.last_error()
+    assert L.ed_decode_links(_lib.ED_C128 | BE, 0, 256, 4096, None) == _lib.ED_ERR_ARG
+    assert L.ed_decode_links(_lib.ED_C128 | BE, 2, 256, 1000, None) == _lib.ED_ERR_ARG  # overlap (2 sites: 1152 B)
+    assert L.ed_decode_links(_lib.ED_C64 | BE, 2, 256, 4104, None) == _lib.ED_ERR_ARG  # dst % 16
 
 
 @pytest.mark.parametrize(

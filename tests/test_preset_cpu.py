@@ -79,3 +79,44 @@ def test_qdp_lazy_disk_map(tmp_path):
         out = d[t, e]
         assert out.dtype == np.complex64
         np.testing.assert_array_equal(out, arr.astype(np.complex64))
+
+
+def test_raw_gives_the_stored_values(tmp_path):
+    """``raw(key)`` returns the file's own dtype (byte order and precision as
+    stored), which the readers' host conversion turns into ``[key]``."""
+    from easydistillation_gb300.preset import EigenvectorTimeSlice, GaugeFieldIldg
+
+    g = golden("ildg_small.npz")
+    Lx, Ly, Lz, Lt = [int(v) for v in g["latt"]]
+    data = GaugeFieldIldg(os.path.join(GOLDEN, "small"), ".lime", [Lt, Lz, Ly, Lx, 4, 3, 3]).load("")
+    r = data.raw(slice(None))
+    assert r.dtype == np.dtype(">c16")
+    np.testing.assert_array_equal(r.astype("<c16"), g["ref_read"])
+    v = data.raw((1, slice(None), 0), copy=False)
+    assert isinstance(v, np.memmap) and v.dtype == np.dtype(">c16")
+    np.testing.assert_array_equal(np.asarray(v).astype("<c16"), g["ref_slice"])
+
+    rng = np.random.default_rng(2)
+    blocks = {(t, e): (rng.standard_normal((6, 3)) + 1j * rng.standard_normal((6, 3))).astype(">c8")
+              for t in range(2) for e in range(3)}
+    _write_qdp(tmp_path / "cfg.mod", blocks)
+    d = EigenvectorTimeSlice(str(tmp_path) + "/", ".mod", [2, 3, 6, 3], 3).load("cfg")
+    for (t, e), arr in blocks.items():
+        r = d.raw((t, e))
+        assert r.dtype == np.dtype(">c8")
+        np.testing.assert_array_equal(r, arr)
+    assert d.links_to_device([1, 1, 1, 1]) is None  # QDP records are not in the ILDG site order
+
+
+def test_file_prec_codes():
+    import pytest
+
+    from easydistillation_gb300 import _lib
+    from easydistillation_gb300.ops import file_prec
+
+    assert file_prec(">c16") == _lib.ED_C128 | _lib.ED_BIG_ENDIAN
+    assert file_prec("<c16") == _lib.ED_C128
+    assert file_prec(">c8") == _lib.ED_C64 | _lib.ED_BIG_ENDIAN
+    assert file_prec(np.complex64) == _lib.ED_C64
+    with pytest.raises(ValueError):
+        file_prec("<f8")
