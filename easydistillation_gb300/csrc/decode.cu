@@ -64,15 +64,16 @@ __global__ void decode_complex_kernel(const void* __restrict__ src, long long n,
 }
 
 // dst [3][sites][9] complex128 <- src [sites][4][9] (the spatial directions
-// of the ILDG site order); one thread per output element, so the writes are
-// contiguous and each warp reads runs of 9 elements.
+// of the ILDG site order).  Threads walk the source order (the 27 spatial
+// elements of a site are contiguous, the 9 time-link elements skipped), so
+// each warp reads one contiguous run and writes three runs of whole sites.
 template <bool SRC16, bool BE>
 __global__ void decode_links_kernel(const void* __restrict__ src, long long sites, double2* __restrict__ dst) {
-  const long long n = 3 * sites * 9;
-  for (long long d = (long long)blockIdx.x * blockDim.x + threadIdx.x; d < n; d += (long long)gridDim.x * blockDim.x) {
-    const long long mu = d / (sites * 9), r = d - mu * sites * 9;
-    const long long site = r / 9, ab = r - site * 9;
-    dst[d] = load_elem<SRC16, BE>(src, (site * 4 + mu) * 9 + ab);
+  const long long n = 27 * sites;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const long long site = e / 27;
+    const int r = (int)(e - site * 27), mu = r / 9, ab = r - 9 * (r / 9);
+    dst[(long long)mu * sites * 9 + site * 9 + ab] = load_elem<SRC16, BE>(src, site * 36 + r);
   }
 }
 

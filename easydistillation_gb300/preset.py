@@ -32,6 +32,7 @@ Formats:
 from __future__ import annotations
 
 import mmap
+import os
 import re
 import struct
 import xml.etree.ElementTree as ET
@@ -120,18 +121,35 @@ class _Data:
         return ops.decode_links(raw, v.dtype, latt_size)
 
 
+_COPY_CHUNK = 64 << 20  # bytes per host thread above which pinned_bytes splits a contiguous copy
+
+
 def pinned_bytes(a, out: torch.Tensor = None) -> torch.Tensor:
     """The bytes of array ``a`` (a memory-mapped view or any numpy array) in
     page-locked host memory, copied in one pass: a uint8 tensor of
     ``a.nbytes`` (or the first ``a.nbytes`` bytes of ``out``, a pinned uint8
-    tensor, when given)."""
+    tensor, when given).  Contiguous arrays above 64 MB are copied by several
+    host threads (the page-cache reads of a memory map and the copy itself
+    scale with cores)."""
     a = np.asarray(a)
     if out is None:
         out = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
     elif out.dtype != torch.uint8 or out.numel() < a.nbytes:
         raise ValueError("out must be a uint8 tensor of at least a.nbytes bytes")
-    dst = out[: a.nbytes].numpy().view(a.dtype).reshape(a.shape)
-    np.copyto(dst, a, casting="no")
+    dst = out[: a.nbytes].numpy()
+    nthreads = min(len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else 1, 16,
+                   a.nbytes // _COPY_CHUNK)
+    if nthreads > 1 and a.flags.c_contiguous:
+        from concurrent.futures import ThreadPoolExecutor
+
+        src = a.reshape(-1).view(np.uint8)
+        bounds = np.linspace(0, a.nbytes, nthreads + 1).astype(np.int64) // 64 * 64
+        bounds[-1] = a.nbytes
+        with ThreadPoolExecutor(nthreads) as ex:
+            list(ex.map(lambda k: np.copyto(dst[bounds[k]: bounds[k + 1]], src[bounds[k]: bounds[k + 1]]),
+                        range(nthreads)))
+    else:
+        np.copyto(dst.view(a.dtype).reshape(a.shape), a, casting="no")
     return out[: a.nbytes]
 
 
