@@ -120,3 +120,28 @@ def test_file_prec_codes():
     assert file_prec(np.complex64) == _lib.ED_C64
     with pytest.raises(ValueError):
         file_prec("<f8")
+
+
+def test_pinned_bytes_split_copy(monkeypatch):
+    """The byte copy behind the device-side readers: contiguous arrays above
+    the per-thread chunk are split across host threads (chunk lowered here so
+    a small array takes that path), other layouts copied in one pass; into a
+    caller's buffer at an offset.  Runs on CPU with an ordinary tensor as
+    ``out`` (page-locked memory needs a GPU)."""
+    import torch
+
+    from easydistillation_gb300 import preset
+
+    monkeypatch.setattr(preset, "_COPY_CHUNK", 1 << 12)
+    rng = np.random.default_rng(3)
+    a = (rng.standard_normal((300, 37)) + 1j * rng.standard_normal((300, 37))).astype(">c16")
+    for src in (a, a[:, ::3], a[7], a[:0]):
+        buf = torch.zeros(src.nbytes + 24, dtype=torch.uint8)
+        out = preset.pinned_bytes(src, buf[8:])
+        assert out.numel() == src.nbytes
+        np.testing.assert_array_equal(out.numpy().view(">c16").reshape(src.shape), src)
+        assert not buf[:8].any() and not buf[8 + src.nbytes:].any()
+    import pytest
+
+    with pytest.raises(ValueError):
+        preset.pinned_bytes(a, torch.zeros(a.nbytes - 1, dtype=torch.uint8))
