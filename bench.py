@@ -64,7 +64,10 @@ def parse():
                     help="measure only the Laplacian kernels (c64, c64 TMA-staged, c128) at --lattice")
     ap.add_argument("--secondary", action="store_true",
                     help="measure the components beside the hot path: stout smearing, displacement elementals, "
-                         "two-point correlators")
+                         "two-point correlators, ILDG gauge-file loading")
+    ap.add_argument("--gauge-load", action="store_true",
+                    help="measure only loading a 32^3 x 64 ILDG gauge file into device links (host conversion "
+                         "vs device decode)")
     ap.add_argument("--eigen-batch", type=int, default=8)
     ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--eigen-cpu", action="store_true", help="also time the oracle's scipy eigensolve (slow)")
@@ -672,18 +675,7 @@ def run_secondary(args):
     from easydistillation_gb300.stout import stout_smear_
 
     dev = torch.device("cuda", 0)
-
-    def timed(fn, reps):
-        fn()
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        for _ in range(reps):
-            fn()
-        b.record()
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / 1e3 / reps
-
+    timed = event_seconds
     out = {}
     # stout smearing
     latt = [32, 32, 32, 64]
@@ -747,6 +739,32 @@ def run_secondary(args):
     # ILDG gauge file -> device links
     out["gauge_load"] = bench_gauge_load(dev, timed)
     print(json.dumps({"metric": "secondary components", **out}), flush=True)
+
+
+def event_seconds(fn, reps):
+    """Seconds per call of ``fn`` by CUDA events on the current stream, after
+    one untimed call, with a synchronize on both sides."""
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3 / reps
+
+
+def run_gauge_load(args):
+    """Secondary measurement (``--gauge-load``): only the ILDG gauge-file line
+    of ``--secondary``."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    print(json.dumps({"metric": "ILDG gauge file -> device links",
+                      "gauge_load": bench_gauge_load(dev, event_seconds)}), flush=True)
 
 
 def bench_gauge_load(dev, timed):
@@ -893,6 +911,9 @@ def main():
         return
     if args.secondary:
         run_secondary(args)
+        return
+    if args.gauge_load:
+        run_gauge_load(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
