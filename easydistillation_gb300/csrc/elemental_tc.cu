@@ -331,9 +331,8 @@ struct TcFacSlots {
 // Chain elements each thread of the split kernel loads before its first
 // store: four 16-byte loads in flight per thread for the right side (3 pz
 // variants per element, read-heavy); one for the left side, whose 9 (px, py)
-// variants per element make it write-bound (two or more would spill).
+// variants per element make it write-bound (and four would spill).
 constexpr int kSplitUnrollRight = 4, kSplitUnrollLeft = 1;
-constexpr int kSplitRows = 8;  // plane rows per block, one warp each
 
 // Writes the nvar variants of the two complex elements v (k = 2*kp, 2*kp + 1)
 // of chain row (slot, i) into the planes.
@@ -394,38 +393,30 @@ __device__ __forceinline__ void tc_fac_split_emit(const float4 v, int kp, long l
 //                                              or f_a Y_i         (right)
 // for input row (slot, i) of the chain buffer; f_a = factor table a in
 // complex64, already scaled by 2^e (tc_phase_kernel).  A block covers
-// kSplitRows consecutive rows (warp w: row 8*g + w) and 32 * UNROLL element
-// pairs of each; every lane loads its UNROLL pairs (32 apart) before it
-// writes any variant.  Row groups run along blockIdx.x, so consecutive
-// blocks fill consecutive 512-byte runs (8 rows x 64 bytes) of the same
-// (128-row, k-block) boxes of every plane: the writes reach DRAM as whole
-// lines of a few boxes at a time.
+// UNROLL * blockDim.x element pairs of a row; each thread loads its UNROLL
+// pairs (blockDim.x apart) before it writes any variant.
 template <int KIND, bool LEFT, int UNROLL>
 __global__ void __launch_bounds__(256, 3) tc_fac_split_kernel(const cplx<float>* __restrict__ chains, TcFacSlots sl, int nrows, int Ne,
                                     int nvar, const cplx<float>* __restrict__ fac, int V3, long long Rplane,
                                     void* __restrict__ planes) {
   const long long K = 3LL * V3;
   const int K2 = (int)(K / 2);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int span = 32 * UNROLL;
-  for (long long g = blockIdx.x; g * kSplitRows < nrows; g += gridDim.x) {
-    const long long rowl = g * kSplitRows + warp;
-    if (rowl >= nrows) continue;  // no block-wide barriers below
-    const int row = (int)rowl;
+  const int span = UNROLL * blockDim.x;
+  for (int row = blockIdx.y; row < nrows; row += gridDim.y) {
     const int slot = row / Ne, i = row - (row / Ne) * Ne;
     const int chain = LEFT ? (slot / sl.nl) * sl.nchain + sl.lchain[slot % sl.nl] : slot;
     const float4* src = reinterpret_cast<const float4*>(chains + ((long long)chain * Ne + i) * K);
     const long long orow0 = (long long)slot * nvar * Ne + i;
-    for (int k0 = blockIdx.y * span + lane; k0 < K2; k0 += gridDim.y * span) {
+    for (int k0 = blockIdx.x * span + threadIdx.x; k0 < K2; k0 += gridDim.x * span) {
       float4 v[UNROLL];
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
-        const int kp = k0 + 32 * u;
+        const int kp = k0 + u * blockDim.x;
         if (kp < K2) v[u] = src[kp];
       }
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
-        const int kp = k0 + 32 * u;
+        const int kp = k0 + u * blockDim.x;
         if (kp < K2) tc_fac_split_emit<KIND, LEFT>(v[u], kp, orow0, Ne, nvar, fac, V3, Rplane, K, K2, planes);
       }
     }
@@ -749,13 +740,11 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   sl.nl = nl;
   sl.nchain = P->nchain;
   for (int s = 0; s < nl; ++s) sl.lchain[s] = P->fac_lchain[s];
-  const int kyl = (int)std::min<long long>(ceil_div(K / 2, 32 * kSplitUnrollLeft), 65535),
-            kyr = (int)std::min<long long>(ceil_div(K / 2, 32 * kSplitUnrollRight), 65535);
+  const int kxl = (int)ceil_div(K / 2, 256 * kSplitUnrollLeft), kxr = (int)ceil_div(K / 2, 256 * kSplitUnrollRight);
   const int lrows = nb * nl * Ne, rrows = nb * P->nchain * Ne;
-  const int gl = (int)ceil_div(lrows, kSplitRows), gr = (int)ceil_div(rrows, kSplitRows);
-  tc_fac_split_kernel<KIND, true, kSplitUnrollLeft><<<dim3(gl, kyl), 32 * kSplitRows, 0, stream>>>(
+  tc_fac_split_kernel<KIND, true, kSplitUnrollLeft><<<dim3(kxl, std::min(lrows, 65535)), 256, 0, stream>>>(
       chains, sl, lrows, Ne, pxy, fxy32, P->V3, lay.rb, bpl);
-  tc_fac_split_kernel<KIND, false, kSplitUnrollRight><<<dim3(gr, kyr), 32 * kSplitRows, 0, stream>>>(
+  tc_fac_split_kernel<KIND, false, kSplitUnrollRight><<<dim3(kxr, std::min(rrows, 65535)), 256, 0, stream>>>(
       chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
   ED_RETURN_LAUNCH("variant planes");
 
