@@ -669,7 +669,7 @@ def run_secondary(args):
     import torch
 
     from easydistillation_gb300 import DisplacementElementalGenerator
-    from easydistillation_gb300.correlator import gamma, twopoint
+    from easydistillation_gb300.correlator import gamma, twopoint_assembled
     from easydistillation_gb300.generator.elemental import links_to_device
     from easydistillation_gb300.insertion import mom_dict_to_list
     from easydistillation_gb300.stout import stout_smear_
@@ -733,7 +733,7 @@ def run_secondary(args):
     el = torch.complex(torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64),
                        torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64))
     ops = [(gamma(15, dev)[None], el)]
-    sec = timed(lambda: twopoint(ops, peram, range(Lt), Lt), 2)
+    sec = timed(lambda: twopoint_assembled(ops, peram, range(Lt), Lt), 2)
     out["twopoint"] = {"correlators_per_s": 1.0 / sec, "seconds": sec,
                        "workload": "48 timeslices, Ne=100, gamma_5, all 48 sources"}
     # ILDG gauge file -> device links

@@ -14,6 +14,7 @@ The arithmetic runs in ``libeasydist_gb300.so`` (C ABI:
 ``python -m easydistillation_gb300.build``.  There is no CPU fallback.
 """
 
+from .backend import get_backend, set_backend
 from .generator import DisplacementElementalGenerator, EigenvectorGenerator, ElementalGenerator
 from .insertion import MomentumPhase, derivative, mom_dict_to_list, num_derivative
 from .preset import (
@@ -38,6 +39,8 @@ __all__ = [
     "MomentumPhase",
     "derivative",
     "mom_dict_to_list",
+    "get_backend",
+    "set_backend",
     "num_derivative",
     "GaugeFieldIldg",
     "GaugeFieldBinary",

@@ -55,6 +55,7 @@ _SIGNATURES = {
     "ed_elemental_status": ([_vp, _vp, _c.POINTER(_i), _vp], _i),
     "ed_elemental_set_profile_events": ([_vp, _vp, _vp], _i),
     "ed_elemental_run_noalloc": ([_vp, _vp, _ll, _ll, _i, _vp, _vp, _vp, _vp], _i),
+    "ed_elemental_status_noalloc": ([_vp, _c.POINTER(_i), _vp], _i),
     "ed_elemental_plan_create_batched": (
         [_c.POINTER(_vp), _i, _i, _i, _i, _i, _c.POINTER(_i), _i, _i, _i],
         _i,

@@ -1,13 +1,39 @@
-"""Meson two-point correlators from elementals and perambulators (GPU, torch).
+"""Meson two-point correlators from elementals and perambulators (GPU).
 
-Mirrors ``lattice/correlator/one_particle.py:12-77`` (``twopoint``) with the
-operator data already assembled (``lattice/data.py:7-33``): an operator is a
-pair ``(gammas [X, 4, 4], elementals [X, Lt, Ne, Ne])`` of X parts.  The
-contraction is the reference's
-``"tijab,xjk,xtbc,tklcd,yli,yad->t"`` with ``tau_bw = g5 tau^dag g5`` and the
-source gamma ``g4 Gamma^* g4``; it runs as a chain of complex GEMMs on the
-device (cuBLAS through torch).  The gamma matrices follow
-``lattice/insertion/gamma.py`` (``gamma(n) = g0^(n&1) g1^(n&2) g2^(n&4) g3^(n&8)``).
+Same interface as ``lattice/correlator/one_particle.py``:
+
+* :class:`InsertionRowMom` and :class:`Operator` build an operator's
+  ``parts`` exactly like ``lattice/insertion/__init__.py:109-145`` (a gamma
+  index, then ``[coefficient, derivative, momentum]`` triples; the
+  coefficient is negated for gamma 5 and 13, the reference's sign
+  convention);
+* :func:`get_elemental_data` assembles, per operator, the gammas of its parts
+  and the coefficient sums of ``elemental[d, p, :, :usedNe, :usedNe]``
+  (``lattice/data.py:7-33``);
+* :func:`twopoint` (``one_particle.py:12-77``) and :func:`twopoint_profile`
+  (``one_particle.py:80-135``) take the operators, the elemental and
+  perambulator file data (anything indexable like
+  ``elemental[d, p, :, :Ne, :Ne]`` / ``perambulator[t_src, ...]``: the
+  reference's ``FileData``, this package's readers, numpy arrays or torch
+  tensors) and return ``C[op, t]`` / ``C[op, t, a, d]`` (``C[op, t, a]``
+  with ``is_diagonal``), averaged over the source timeslices unless
+  ``is_sum_over_source_t`` is False, with the reference's overall minus sign.
+
+Results are complex128 device tensors (host numpy arrays after
+``set_backend("numpy")``).  The gamma matrices follow
+``lattice/insertion/gamma.py`` (``gamma(n) = g0^(n&1) g1^(n&2) g2^(n&4)
+g3^(n&8)``); every one of them is monomial (one non-zero per row), which the
+contraction uses: with ``tau_bw = g5 tau^dag g5`` (``one_particle.py:59-63``)
+and the source gamma ``G = g4 Gamma^dag g4`` (``:66``),
+
+    C(t) = sum_{x,y} Tr[ tau_bw(t) (Gamma_x (x) phi_x(t)) tau(t) (G_y (x) psi_y) ]
+
+is evaluated as one batched product of the 16 spin blocks of ``tau_bw(t)``
+with ``phi_x(t)`` and one of ``tau(t)`` with ``psi_y^T``, after which the
+gammas only permute and scale spin blocks, and a trace over the surviving
+block pairs: 32 Ne x Ne x Ne products per (t, part pair) instead of the
+dense (4 Ne)^3 ones.  Per source timeslice all sink times t and all parts of
+an operator go into one batched GEMM launch.
 """
 
 from __future__ import annotations
@@ -15,7 +41,10 @@ from __future__ import annotations
 from functools import lru_cache
 from typing import Iterable, List, Sequence, Tuple
 
+import numpy as np
 import torch
+
+from .backend import to_backend
 
 _G = {
     0: [[0, 0, 0, 1j], [0, 0, 1j, 0], [0, -1j, 0, 0], [-1j, 0, 0, 0]],
@@ -41,9 +70,249 @@ def gamma(n: int, device=None) -> torch.Tensor:
     return _gamma_cpu(n).to(device or "cpu")
 
 
+# ---------------------------------------------------------------- operators
+
+
+class InsertionRowMom:
+    """One insertion row at one momentum (``lattice/insertion/__init__.py:103-106``):
+    ``row = [gamma, [(coeff, derivative), ...], gamma, [...], ...]`` and the
+    momentum index into the elementals' momentum axis."""
+
+    def __init__(self, row, momentum) -> None:
+        self.row = row
+        self.momentum = momentum
+
+
+class Operator:
+    """An interpolating operator: a sum of insertion rows with coefficients
+    (``lattice/insertion/__init__.py:109-145``).  ``parts`` alternates a gamma
+    index and its elemental terms ``[coefficient * coeff, derivative, momentum]``."""
+
+    def __init__(self, name: str, insertion_rows: List[InsertionRowMom], coefficients: List[float]) -> None:
+        assert len(insertion_rows) == len(coefficients), (
+            f"Unmatched numbers of insertion rows {len(insertion_rows)} and coefficients {len(coefficients)}"
+        )
+        parts = []
+        for ins, coefficient in zip(insertion_rows, coefficients):
+            row, momentum = ins.row, ins.momentum
+            for i in range(len(row) // 2):
+                g = row[2 * i]
+                parts.append(g)
+                # gamma_3 gamma_1 = -gamma(5) and gamma_3 gamma_1 gamma_4 = -gamma(13) in the reference's table
+                sign = -1 if g in (5, 13) else 1
+                parts.append([[coefficient * dc * sign, d, momentum] for dc, d in row[2 * i + 1]])
+        self.name = name
+        self.parts = parts
+
+    def __str__(self) -> str:
+        return f"Operator({self.name!r}, parts={self.parts})"
+
+
+def _fetch(data, key, device) -> torch.Tensor:
+    x = data[key]
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=torch.complex128)
+    if hasattr(x, "get") and not isinstance(x, np.ndarray):  # cupy
+        x = x.get()
+    arr = np.ascontiguousarray(np.asarray(x)).astype(np.complex128, copy=False)
+    return torch.from_numpy(arr).to(device)
+
+
+def _cuda(device) -> torch.device:
+    device = torch.device(device or "cuda")
+    if device.type != "cuda":
+        raise ValueError("the correlator contractions run on a CUDA device (there is no CPU path)")
+    return device
+
+
+def get_elemental_data(operators: Sequence[Operator], elemental, usedNe: int = None, device=None):
+    """Per operator ``(gammas [X, 4, 4], elementals [X, Lt, Ne', Ne'])`` on the
+    device: the gammas of its X parts and the coefficient sums of their
+    elementals ``elemental[d, p, :, :usedNe, :usedNe]``, each (d, p) read once
+    (``lattice/data.py:7-33``)."""
+    device = _cuda(device)
+    cache = {}
+    out = []
+    for op in operators:
+        parts = op.parts
+        gs, es = [], []
+        for i in range(len(parts) // 2):
+            gs.append(gamma(parts[2 * i], device))
+            acc = None
+            for coeff, d, p in parts[2 * i + 1]:
+                key = (d, p)
+                if key not in cache:
+                    cache[key] = _fetch(elemental, (d, p, slice(None), slice(None, usedNe), slice(None, usedNe)),
+                                        device)
+                term = coeff * cache[key]
+                acc = term if acc is None else acc + term
+            es.append(acc)
+        out.append((torch.stack(gs), torch.stack(es)))
+    return out
+
+
+# ---------------------------------------------------------------- contraction
+
+
+@lru_cache(maxsize=None)
+def _monomial(n: int, conj_src: bool) -> Tuple[Tuple[int, ...], Tuple[complex, ...]]:
+    """gamma(n) (or the source form g4 gamma(n)^dag g4 of ``one_particle.py:66``)
+    as (column of the non-zero in each row, its value)."""
+    g = _gamma_cpu(n)
+    if conj_src:
+        g8 = _gamma_cpu(8)
+        g = g8 @ g.conj().T @ g8
+    cols, vals = [], []
+    for r in range(4):
+        nz = [c for c in range(4) if abs(complex(g[r, c])) > 0]
+        if len(nz) != 1:
+            raise AssertionError("gamma matrices of the insertion table are monomial")
+        cols.append(nz[0])
+        vals.append(complex(g[r, nz[0]]))
+    return tuple(cols), tuple(vals)
+
+
+def _gamma_index(g: torch.Tensor) -> int:
+    for n in range(16):
+        if torch.equal(_gamma_cpu(n), g.detach().cpu()):
+            return n
+    raise ValueError("not a gamma matrix of the insertion table")
+
+
+def _backward(tau: torch.Tensor) -> torch.Tensor:
+    """``tau_bw[t, i, j, a, b] = g5_ii conj(tau[t, j, i, b, a]) g5_jj``
+    (``one_particle.py:59-63``; g5 is diagonal)."""
+    d = torch.diagonal(gamma(15, tau.device)).real
+    s = (d[:, None] * d[None, :]).to(tau.dtype)  # [i, j]
+    return s[None, :, :, None, None] * tau.conj().permute(0, 2, 1, 4, 3)
+
+
+def _left_blocks(tau_bw: torch.Tensor, phi: torch.Tensor, gidx: int) -> torch.Tensor:
+    """``tau_bw(t) (Gamma (x) phi(t))`` as spin blocks ``[t, i, k, a, c]``:
+    block (i, k) = Gamma[j, k] tau_bw[t, i, j] phi(t) with j the row whose
+    non-zero sits in column k."""
+    cols, vals = _monomial(gidx, False)
+    prod = torch.matmul(tau_bw, phi[:, None, None])  # [t, i, j, a, c]
+    out = torch.empty_like(prod)
+    for j in range(4):
+        out[:, :, cols[j]] = vals[j] * prod[:, :, j]
+    return out
+
+
+def _right_blocks(tau: torch.Tensor, psi: torch.Tensor, gidx: int) -> torch.Tensor:
+    """``tau(t) (G (x) psi^T)`` with G = g4 Gamma^dag g4 (the source gamma) as spin
+    blocks ``[t, k, i, c, a]``: block (k, i) = G[l, i] tau[t, k, l] psi^T,
+    psi = conj(phi(t_src))."""
+    cols, vals = _monomial(gidx, True)
+    prod = torch.matmul(tau, psi.transpose(-1, -2)[None, None, None])  # [t, k, l, c, a]
+    out = torch.empty_like(prod)
+    for l in range(4):
+        out[:, :, cols[l]] = vals[l] * prod[:, :, l]
+    return out
+
+
+def _source_terms(tau, tau_bw, phis, t_src, dts=None, mode="trace"):
+    """All operators for one source timeslice.  ``tau``/``tau_bw``:
+    ``[T, 4, 4, Ne, Ne]`` at the sink times; ``phis``: per operator
+    ``(gammas, elementals)`` with elementals ``[X, Lt, Ne, Ne]``.
+    mode "trace": ``[Nop, T]``; "profile": ``[Nop, T, Ne, Ne]`` (indices a, d);
+    "diagonal": ``[Nop, T, Ne]``."""
+    out = []
+    for gammas, el in phis:
+        gid = [_gamma_index(g) for g in gammas]
+        sink = torch.roll(el, -t_src, 1)
+        if dts is not None:
+            sink = sink[:, dts]
+        psi = el[:, t_src].conj()
+        if mode == "trace":
+            acc = 0
+            lefts = [_left_blocks(tau_bw, sink[x], gid[x]) for x in range(len(gid))]
+            for y in range(len(gid)):
+                R = _right_blocks(tau, psi[y], gid[y])  # [t, k, i, c, a]
+                for L in lefts:  # [t, i, k, a, c]
+                    acc = acc + torch.einsum("tikac,tkica->t", L, R)
+            out.append(acc)
+        elif mode == "profile":
+            # C[t, a, d] = psi[a, d] sum_{i,l} G[l, i] (left . tau)[t][(i, a), (l, d)]
+            acc = 0
+            for x in range(len(gid)):
+                L = _left_blocks(tau_bw, sink[x], gid[x])  # [t, i, k, a, c]
+                Q = torch.einsum("tikac,tklcd->tilad", L, tau)
+                for y in range(len(gid)):
+                    cols, vals = _monomial(gid[y], True)
+                    for l in range(4):
+                        acc = acc + vals[l] * Q[:, cols[l], l] * el[y, t_src].conj()[None]
+            out.append(acc)
+        else:  # diagonal: C[t, a] = psi[a, a] sum tau_bw[i,j,a,b] Gamma[j,k] phi[b,b] tau[k,l,b,a] G[l,i]
+            acc = 0
+            for x in range(len(gid)):
+                cj, vj = _monomial(gid[x], False)
+                dphi = torch.diagonal(sink[x], dim1=-2, dim2=-1)  # [t, b]
+                for y in range(len(gid)):
+                    cl, vl = _monomial(gid[y], True)
+                    dpsi = torch.diagonal(el[y, t_src].conj())  # [a]
+                    for l in range(4):
+                        i = cl[l]
+                        for j in range(4):
+                            k = cj[j]
+                            term = (tau_bw[:, i, j] * tau[:, k, l].transpose(-1, -2)) @ dphi[..., None]
+                            acc = acc + vj[j] * vl[l] * term[..., 0] * dpsi[None]
+            out.append(acc)
+    return torch.stack(out)
+
+
+def _peram_block(perambulator, t_src, tsel, usedNe, device):
+    key = (t_src, tsel, slice(None), slice(None), slice(None, usedNe), slice(None, usedNe))
+    return _fetch(perambulator, key, device)
+
+
+def twopoint(operators: List[Operator], elemental, perambulator, timeslices: Iterable[int], Lt: int,
+             usedNe: int = None, perambulator_bw=None, is_sum_over_source_t: bool = True, *, device=None):
+    """Two-point functions ``C[op, t]`` (``lattice/correlator/one_particle.py:12-77``):
+    ``-mean over t_src`` of the contraction, or ``[Nop, Nsrc, Lt]`` per source
+    with ``is_sum_over_source_t=False``.  ``perambulator_bw`` replaces the
+    backward quark propagator (``tau_bw = g5 perambulator_bw^dag g5``)."""
+    device = _cuda(device)
+    ts = list(timeslices)
+    phis = get_elemental_data(operators, elemental, usedNe, device)
+    ret = torch.zeros((len(operators), len(ts), Lt), dtype=torch.complex128, device=device)
+    for it, t_src in enumerate(ts):
+        tau = _peram_block(perambulator, t_src, slice(None), usedNe, device)
+        src_bw = tau if perambulator_bw is None else _peram_block(perambulator_bw, t_src, slice(None), usedNe, device)
+        ret[:, it] = _source_terms(tau, _backward(src_bw), phis, t_src)
+    ret = -ret.mean(1) if is_sum_over_source_t else -ret
+    return to_backend(ret)
+
+
+def twopoint_profile(operators: List[Operator], elemental, perambulator, timeslices: Iterable[int],
+                     delta_t_slices: Iterable[int], usedNe: int = None, perambulator_bw=None,
+                     is_sum_over_source_t: bool = True, is_diagonal: bool = False, *, device=None):
+    """Two-point functions at the sink separations ``delta_t_slices``, resolved
+    in the eigenvector indices (``lattice/correlator/one_particle.py:80-135``):
+    ``C[op, dt, a, d]``, or ``C[op, dt, a]`` with ``is_diagonal``.
+    ``perambulator_bw`` is read at the same sink separations (the reference
+    reads it at every sink time, ``:100-101``, which agrees when
+    ``delta_t_slices`` covers all of them and fails otherwise)."""
+    device = _cuda(device)
+    ts, dts = list(timeslices), [int(v) for v in delta_t_slices]
+    phis = get_elemental_data(operators, elemental, usedNe, device)
+    ne = phis[0][1].shape[-1]
+    shape = (len(operators), len(ts), len(dts)) + ((ne,) if is_diagonal else (ne, ne))
+    ret = torch.zeros(shape, dtype=torch.complex128, device=device)
+    for it, t_src in enumerate(ts):
+        tau = _peram_block(perambulator, t_src, dts, usedNe, device)
+        src_bw = tau if perambulator_bw is None else _peram_block(perambulator_bw, t_src, dts, usedNe, device)
+        ret[:, it] = _source_terms(tau, _backward(src_bw), phis, t_src, dts,
+                                   "diagonal" if is_diagonal else "profile")
+    ret = -ret.mean(1) if is_sum_over_source_t else -ret
+    return to_backend(ret)
+
+
 def twopoint_source(tau: torch.Tensor, gammas: torch.Tensor, elementals: torch.Tensor, t_src: int,
                     tau_bw: torch.Tensor = None) -> torch.Tensor:
-    """``ret[t]`` for one source timeslice (before the overall minus sign).
+    """``ret[t]`` of one source timeslice and one assembled operator (before
+    the overall minus sign), differentiable through torch autograd: the form
+    the correlator loss of :mod:`easydistillation_gb300.autograd` uses.
 
     ``tau``: perambulator of this source ``[Lt, 4, 4, Ne, Ne]``; ``gammas``
     ``[X, 4, 4]``; ``elementals`` ``[X, Lt, Ne, Ne]``."""
@@ -54,27 +323,23 @@ def twopoint_source(tau: torch.Tensor, gammas: torch.Tensor, elementals: torch.T
     gamma_src = torch.einsum("ij,xkj,kl->xil", g8, gammas.conj(), g8)
     phi_t = torch.roll(elementals, -t_src, 1)
     phi_src = elementals[:, t_src].conj()
-    # contraction order chosen for GEMM shapes: (tau_bw . Gamma_x . E_x(t)) then (. tau . gsrc_y . E_y(src)^*)
     left = torch.einsum("tijab,xjk,xtbc->tikac", tau_bw, gammas, phi_t)
     right = torch.einsum("tklcd,yli,yad->tkica", tau, gamma_src, phi_src)
     return torch.einsum("tikac,tkica->t", left, right)
 
 
-def twopoint(operators: Sequence[Tuple[torch.Tensor, torch.Tensor]], perambulator, timeslices: Iterable[int],
-             Lt: int, usedNe: int = None, is_sum_over_source_t: bool = True) -> torch.Tensor:
-    """``C[op, t]`` like ``lattice/correlator/one_particle.py:12-77``.
-
-    ``operators``: list of ``(gammas [X,4,4], elementals [X, Lt, Ne, Ne])``;
-    ``perambulator``: indexable as ``[t_src]`` -> ``[Lt, 4, 4, Ne, Ne]``
-    (device tensor or host array)."""
+def twopoint_assembled(phis: Sequence[Tuple[torch.Tensor, torch.Tensor]], perambulator, timeslices: Iterable[int],
+                       Lt: int, usedNe: int = None, is_sum_over_source_t: bool = True) -> torch.Tensor:
+    """``C[op, t]`` from operators already assembled as ``(gammas [X,4,4],
+    elementals [X, Lt, Ne, Ne])`` device tensors (the output of
+    :func:`get_elemental_data`); ``perambulator[t_src]`` -> ``[Lt, 4, 4, Ne, Ne]``."""
     ts = list(timeslices)
-    dev = operators[0][1].device
-    ret = torch.zeros((len(operators), len(ts), Lt), dtype=torch.complex128, device=dev)
+    dev = phis[0][1].device
+    phis = [(g.to(dev), e if usedNe is None else e[..., :usedNe, :usedNe]) for g, e in phis]
+    ret = torch.zeros((len(phis), len(ts), Lt), dtype=torch.complex128, device=dev)
     for it, t_src in enumerate(ts):
         tau = torch.as_tensor(perambulator[t_src]).to(dev)
         if usedNe is not None:
             tau = tau[..., :usedNe, :usedNe]
-        for k, (gm, el) in enumerate(operators):
-            e = el if usedNe is None else el[..., :usedNe, :usedNe]
-            ret[k, it] = twopoint_source(tau, gm.to(dev), e, t_src)
+        ret[:, it] = _source_terms(tau, _backward(tau), phis, t_src)
     return -ret.mean(1) if is_sum_over_source_t else -ret

@@ -13,8 +13,15 @@
 //     workspace is larger are rejected with ED_ERR_WORKSPACE.  Every GPU that
 //     loads the library keeps the array until the process exits;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture on the device;
+//     (cudaGetSymbolAddress, with that device current) and caches it.  With
+//     lazy module loading (CUDA_MODULE_LOADING=LAZY, the default of recent
+//     CUDA releases) that lookup is also what loads the library's module on
+//     the device and commits the 32 MiB there, so the first call does take
+//     device memory: make it at an initialisation point where that is
+//     allowed, and before any stream capture on the device;
+//   * the tensor-core modes report a bounded device wait that gave up in a
+//     status word inside the array; ed_elemental_status_noalloc reads it
+//     (a run whose status is not 0 returned invalid elementals);
 //   * all calls share the one array and a call leaves its contents behind.
 //     Every scratch byte a run reads is written earlier in the same run
 //     (the tensor-core modes clear their accumulators explicitly), so the
@@ -28,6 +35,7 @@
 static __device__ __align__(256) unsigned char g_noalloc_scratch[ED_NOALLOC_SCRATCH_BYTES];
 
 namespace ed {
+int tc_read_status(const ed_elemental_plan* P, const void* workspace, int* status, cudaStream_t stream);
 int elemental_run(const ed_elemental_plan* P, const void* links, long long dir_stride, long long site_stride,
                   int evec_prec, const void* evecs, const double* blend, void* out, void* ws, size_t ws_bytes,
                   cudaStream_t stream);
@@ -78,4 +86,21 @@ extern "C" int ed_elemental_run_noalloc(const ed_elemental_plan* plan, const voi
   if (rc != ED_OK) return rc;
   return ed::elemental_run(plan, links, dir_stride, site_stride, evec_prec, evecs, blend, out, scratch,
                            (size_t)ED_NOALLOC_SCRATCH_BYTES, (cudaStream_t)stream);
+}
+
+extern "C" int ed_elemental_status_noalloc(const ed_elemental_plan* plan, int* code, void* stream) {
+  ED_CHECK_ARG(plan && !plan->custom && code, "ed_elemental_status_noalloc: null pointer or a pair plan");
+  ED_CHECK_ARG(plan->ws_bytes <= (size_t)ED_NOALLOC_SCRATCH_BYTES,
+               "ed_elemental_status_noalloc: this plan cannot run in the built-in scratch array");
+  void* scratch = nullptr;
+  int rc = scratch_address(&scratch);
+  if (rc != ED_OK) return rc;
+  rc = ed::tc_read_status(plan, scratch, code, (cudaStream_t)stream);
+  if (rc != ED_OK) return rc;
+  if (*code != 0) {
+    ed::set_error("elemental (no-allocation entry point): a bounded device wait gave up (code %d); the output of "
+                  "that run is invalid", *code);
+    return ED_ERR_TIMEOUT;
+  }
+  return ED_OK;
 }

@@ -16,6 +16,7 @@ from typing import List, Tuple
 
 import torch
 
+from ..backend import to_backend
 from ..insertion import MomentumPhase
 from ..ops import PairPlan, links_to_soa, mean_c128, parallel_transport, vectors_to_planes
 from .elemental import ElementalGenerator, gauge_to_device
@@ -74,4 +75,4 @@ class DisplacementElementalGenerator:
         src = chains if self.precision == "fp64" else chains.to(torch.complex64)
         G = self._pair.run(src)  # [Nmom, Ne, (D+1)*Ne]
         self._VPV.copy_(G.view(self.num_momentum, Ne, D + 1, Ne).permute(2, 0, 1, 3))
-        return self._VPV
+        return to_backend(self._VPV)

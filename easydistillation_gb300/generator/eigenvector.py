@@ -7,7 +7,8 @@ timeslice ``t`` with the library's stencil kernel inside a GPU thick-restart
 Lanczos (FP64 basis, reorthogonalisation and Rayleigh-Ritz), sorts them
 ascending and applies the reference's renormalisation phase
 (``eigenvector.py:249-257``).  It returns device tensors
-``(evecs [Ne, Lz, Ly, Lx, 3] complex128, evals [Ne] float64)``.
+``(evecs [Ne, Lz, Ly, Lx, 3] complex128, evals [Ne] float64)`` (host numpy
+arrays after ``easydistillation_gb300.set_backend("numpy")``).
 
 ``stencil_precision="fp32"`` runs the Lanczos iteration with the FP32 stencil
 and then refines the result with FP64 operator applications (an FP64
@@ -22,6 +23,7 @@ from typing import List, Sequence
 import torch
 
 from .. import lanczos as LZ
+from ..backend import to_backend
 from ..ops import lanczos_tr, links_to_soa, laplacian, vectors_from_planes
 from .elemental import gauge_to_device
 
@@ -166,4 +168,4 @@ class EigenvectorGenerator:
 
     def calc(self, t: int, apply_renorm_phase: bool = True, polynomial_degree: int = 0, lambda_cut: float = 0.0):
         evecs, evals = self.calc_batch([t], apply_renorm_phase, polynomial_degree, lambda_cut)
-        return evecs[0], evals[0]
+        return to_backend(evecs[0]), to_backend(evals[0])

@@ -5,7 +5,9 @@ Same constructor, ``load(key)`` and ``calc(t)`` as the reference
 the library's CUDA kernels (covariant-derivative chains, pair contractions,
 operator combination).  ``calc`` returns the generator's internal
 ``[Nderiv, Nmom, Ne, Ne]`` complex128 device buffer, which the next call
-overwrites, exactly like the reference's ``self._VPV``.
+overwrites, exactly like the reference's ``self._VPV``; after
+``easydistillation_gb300.set_backend("numpy")`` it returns a host numpy copy
+of it instead (the reference's numpy backend).
 
 Extra keyword-only arguments: ``precision``, ``device``, ``factorise`` and
 ``autotune``.
@@ -32,6 +34,7 @@ from typing import List, Tuple
 import numpy as np
 import torch
 
+from ..backend import to_backend
 from ..insertion import MomentumPhase, derivative, num_derivative
 from ..ops import ElementalPlan
 
@@ -376,7 +379,7 @@ class ElementalGenerator:
                        blend=self.stocastic_coeff)
         if self.precision != "fp64":
             self._plan.check_status()
-        return self._VPV
+        return to_backend(self._VPV)
 
     def project_SU3(self):
         """Iterative projection back onto SU(3) (``elemental.py:107-118``)."""

@@ -2,8 +2,8 @@
 lists and momentum phases.
 
 Mirrors ``lattice/insertion/derivative.py:23-33`` (``derivative``),
-``lattice/insertion/mom_dict.py:5-33,162-175`` (``mom_dict_to_list`` for
-|p|^2 <= 1 and <= 3) and ``lattice/insertion/phase.py:6-53``
+``lattice/insertion/mom_dict.py:5-175`` (``mom_dict_to_list`` for
+|p|^2 <= 1, 3 and 9) and ``lattice/insertion/phase.py:6-53``
 (``MomentumPhase``), whose tables are computed on the GPU in FP64.
 """
 
@@ -41,11 +41,27 @@ def num_derivative(num_nabla: int) -> int:
     return (3 ** (num_nabla + 1) - 1) // 2
 
 
-def mom_dict_to_list(mom: int = 3) -> List[Tuple[int, int, int]]:
+def _sphere_momenta(pmax2: int) -> List[Tuple[int, int, int]]:
+    """Every integer momentum with |p|^2 <= pmax2, ordered by (pz, py, px)
+    ascending: the order of the reference's |p|^2 <= 9 table (123 entries,
+    ``mom_dict.py:35-159``), which is this lexicographic walk."""
+    r = int(pmax2 ** 0.5) + 1
+    pts = [(x, y, z) for z in range(-r, r + 1) for y in range(-r, r + 1) for x in range(-r, r + 1)
+           if x * x + y * y + z * z <= pmax2]
+    return sorted(pts, key=lambda p: (p[2], p[1], p[0]))
+
+
+def mom_dict_to_list(mom: int = 9) -> List[Tuple[int, int, int]]:
+    """Momentum list of the reference (``mom_dict.py:162-175``, same default
+    ``mom=9``): ``mom=1`` the zero momentum, ``mom=3`` the 27 momenta with
+    |p|^2 <= 3 in the reference's table order (its first 7 are |p|^2 <= 1),
+    ``mom=9`` the 123 momenta with |p|^2 <= 9; ValueError otherwise."""
     if mom == 1:
         return [(0, 0, 0)]
     if mom == 3:
         return [tuple(int(v) for v in s.split(" ")) for s in _MOM3]
+    if mom == 9:
+        return _sphere_momenta(9)
     raise ValueError(f"Unknown mom max = {mom}")
 
 

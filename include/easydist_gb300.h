@@ -291,11 +291,23 @@ int ed_pair_run(const ed_elemental_plan* plan, const void* chains, void* G, void
  * (it is an addition of this library).  Plans needing more than
  * ED_NOALLOC_SCRATCH_BYTES are rejected with ED_ERR_WORKSPACE.  The first call
  * on a device resolves the array's address and should precede any stream
- * capture; all calls share the array, so calls that overlap on the GPU race
- * and must be serialised by the caller. */
+ * capture; under lazy module loading (CUDA_MODULE_LOADING=LAZY, the default
+ * of recent CUDA releases) that first call also loads the library's module on
+ * the device and commits the 32 MiB there, so make it where allocating is
+ * still allowed (at initialisation).  All calls share the array, so calls
+ * that overlap on the GPU race and must be serialised by the caller.  In the
+ * tensor-core modes a bounded device wait that gave up leaves a status word in
+ * the array: read it with ed_elemental_status_noalloc. */
 int ed_elemental_run_noalloc(const ed_elemental_plan* plan, const void* links, long long dir_stride,
                              long long site_stride, int evec_prec, const void* evecs, const double* blend, void* out,
                              void* stream);
+
+/* ed_elemental_status for runs of ed_elemental_run_noalloc: synchronise
+ * `stream` and report the status word the last run left in the built-in
+ * scratch array (ED_OK, or ED_ERR_TIMEOUT when a bounded wait inside the
+ * tensor-core kernel gave up; *code receives the raw word, 0 = ok).  No
+ * counterpart in the reference. */
+int ed_elemental_status_noalloc(const ed_elemental_plan* plan, int* code, void* stream);
 
 /* Describe the plan's pair groups: *ngroups groups (one per left chain); for
  * group g, left[g] is its left chain and nright[g] its number of right chains

@@ -45,6 +45,12 @@ __all__ = [
     "gell_mann",
     "stout_smear",
     "random_colour_vectors",
+    "gamma",
+    "twopoint",
+    "operator_parts",
+    "elemental_data",
+    "twopoint_operators",
+    "twopoint_profile_operators",
 ]
 
 
@@ -490,4 +496,89 @@ def twopoint(phis, perambulator, timeslices, Lt, usedNe=None, is_sum_over_source
                 "tijab,xjk,xtbc,tklcd,yli,yad->t", tau_bw, g, np.roll(e, -t_src, 1), tau, gamma_src,
                 e[:, t_src].conj(), optimize=True,
             )
+    return -ret.mean(1) if is_sum_over_source_t else -ret
+
+
+def operator_parts(rows, coefficients):
+    """``Operator(name, insertion_rows, coefficients).parts``
+    (``lattice/insertion/__init__.py:116-145``): ``rows`` is a list of
+    ``(row, momentum)`` with ``row = [gamma, [(coeff, derivative), ...], ...]``;
+    every part becomes ``[gamma, [[coefficient*coeff, derivative, momentum], ...]]``
+    with the coefficient negated for gamma 5 and 13."""
+    parts = []
+    for (row, momentum), c in zip(rows, coefficients):
+        for i in range(len(row) // 2):
+            g = row[2 * i]
+            parts.append(g)
+            sign = -1 if g in (5, 13) else 1
+            parts.append([[c * dc * sign, d, momentum] for dc, d in row[2 * i + 1]])
+    return parts
+
+
+def elemental_data(parts_list, elemental, usedNe):
+    """``get_elemental_data`` (``lattice/data.py:7-33``): per operator the
+    gammas ``[X, 4, 4]`` of its parts and the coefficient sums of its
+    elementals ``elemental[d, p, :, :usedNe, :usedNe]`` (``[X, Lt, Ne', Ne']``)."""
+    out = []
+    for parts in parts_list:
+        gs, es = [], []
+        for i in range(len(parts) // 2):
+            gs.append(gamma(parts[2 * i]))
+            acc = None
+            for coeff, d, p in parts[2 * i + 1]:
+                term = coeff * np.asarray(elemental[d, p, :, :usedNe, :usedNe])
+                acc = term if acc is None else acc + term
+            es.append(acc)
+        out.append((np.array(gs), np.array(es)))
+    return out
+
+
+def twopoint_operators(parts_list, elemental, perambulator, timeslices, Lt, usedNe=None, perambulator_bw=None,
+                       is_sum_over_source_t=True):
+    """``twopoint`` on the reference interface (``lattice/correlator/one_particle.py:12-77``):
+    operators given by their ``parts``, elementals ``[Nderiv, Nmom, Lt, Ne, Ne]``,
+    perambulators ``[Lt_src, Lt, 4, 4, Ne, Ne]``; ``perambulator_bw`` replaces
+    the backward propagator ``g5 tau^dag g5`` by ``g5 tau_bw^dag g5``."""
+    phis = elemental_data(parts_list, elemental, usedNe)
+    ts = list(timeslices)
+    ret = np.zeros((len(phis), len(ts), Lt), np.complex128)
+    g15, g8 = gamma(15), gamma(8)
+    for it, t_src in enumerate(ts):
+        tau = np.asarray(perambulator[t_src, :, :, :, :usedNe, :usedNe])
+        src_bw = tau if perambulator_bw is None else np.asarray(perambulator_bw[t_src, :, :, :, :usedNe, :usedNe])
+        tau_bw = np.einsum("ii,tjiba,jj->tijab", g15, src_bw.conj(), g15)
+        for idx, (g, e) in enumerate(phis):
+            gamma_src = np.einsum("ij,xkj,kl->xil", g8, g.conj(), g8)
+            ret[idx, it] = np.einsum("tijab,xjk,xtbc,tklcd,yli,yad->t", tau_bw, g, np.roll(e, -t_src, 1), tau,
+                                     gamma_src, e[:, t_src].conj(), optimize=True)
+    return -ret.mean(1) if is_sum_over_source_t else -ret
+
+
+def twopoint_profile_operators(parts_list, elemental, perambulator, timeslices, delta_t_slices, usedNe=None,
+                               perambulator_bw=None, is_sum_over_source_t=True, is_diagonal=False):
+    """``twopoint_profile`` (``lattice/correlator/one_particle.py:80-135``): the
+    two-point function at the sink separations ``delta_t_slices`` resolved in
+    the eigenvector indices, ``[Nop, Ndt, Ne', Ne']`` (``[Nop, Ndt, Ne']`` with
+    ``is_diagonal``).  The reference reads the backward propagator at every
+    sink time (``:100-101``), so ``perambulator_bw`` needs ``delta_t_slices``
+    to cover all of them, as there."""
+    phis = elemental_data(parts_list, elemental, usedNe)
+    ts, dts = list(timeslices), list(delta_t_slices)
+    ne = np.asarray(elemental[0, 0, 0, :usedNe, :usedNe]).shape[-1]
+    shape = (len(phis), len(ts), len(dts), ne) if is_diagonal else (len(phis), len(ts), len(dts), ne, ne)
+    ret = np.zeros(shape, np.complex128)
+    g15, g8 = gamma(15), gamma(8)
+    for it, t_src in enumerate(ts):
+        tau = np.asarray(perambulator[t_src, dts, :, :, :usedNe, :usedNe])
+        src_bw = tau if perambulator_bw is None else np.asarray(perambulator_bw[t_src, :, :, :, :usedNe, :usedNe])
+        tau_bw = np.einsum("ii,tjiba,jj->tijab", g15, src_bw.conj(), g15)
+        for idx, (g, e) in enumerate(phis):
+            gamma_src = np.einsum("ij,xkj,kl->xil", g8, g.conj(), g8)
+            sink = np.roll(e, -t_src, 1)[:, dts]
+            if is_diagonal:
+                ret[idx, it] = np.einsum("tijab,xjk,xtbb,tklba,yli,yaa->ta", tau_bw, g, sink, tau, gamma_src,
+                                         e[:, t_src].conj(), optimize=True)
+            else:
+                ret[idx, it] = np.einsum("tijab,xjk,xtbc,tklcd,yli,yad->tad", tau_bw, g, sink, tau, gamma_src,
+                                         e[:, t_src].conj(), optimize=True)
     return -ret.mean(1) if is_sum_over_source_t else -ret

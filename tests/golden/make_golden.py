@@ -86,6 +86,8 @@ def main(ref_root: str):
         os.path.join(HERE, "metadata.npz"),
         derivative=np.array([list(derivative(n)) + [-1] * (2 - len(derivative(n))) for n in range(13)]),
         mom3=np.array(mom_dict_to_list(3)),
+        mom9=np.array(mom_dict_to_list(9)),
+        mom_default=np.array(mom_dict_to_list()),
     )
 
     # --- Laplacian on random vectors (two lattices, incl. an L=2 axis) --
@@ -178,7 +180,80 @@ def make_ildg_fixture(ref_root: str):
                         ref_slice=ref[1, :, 0])
 
 
+def make_config0_chain(ref_root: str):
+    """The reference's own chain at the plain-FP64 CPU configuration: 4^3 x 8,
+    links exp(i 0.1 A) (seed 1000), EigenvectorGenerator (Ne = 20, tol 1e-10,
+    ARPACK) on all 8 timeslices, and its eigenvectors fed to
+    ElementalGenerator(num_nabla = 1, the 7 momenta with |p|^2 <= 1)."""
+    lattice = import_reference(ref_root)
+    from lattice.insertion.mom_dict import mom_dict_to_list
+
+    latt = [4, 4, 4, 8]
+    Ne, tol = 20, 1e-10
+    g = synthetic_gauge(latt, 0.1, 1000)
+    eig = lattice.EigenvectorGenerator(latt, MemGauge(g), Ne, tol)
+    eig.load("mem")
+    evecs, evals = [], []
+    for t in range(latt[3]):
+        v, lam = eig.calc(t)
+        evecs.append(np.asarray(v))
+        evals.append(np.asarray(lam))
+    evecs = np.stack(evecs)
+    moms = mom_dict_to_list(3)[:7]
+    gen = lattice.ElementalGenerator(latt, MemGauge(g), MemEigen(evecs, Ne), 1, moms)
+    gen.load("mem")
+    E = np.stack([gen.calc(t).copy() for t in range(latt[3])])
+    np.savez_compressed(os.path.join(HERE, "config0_chain.npz"), latt=latt, gauge=g, Ne=Ne, tol=tol,
+                        evecs=evecs, evals=np.stack(evals), moms=np.array(moms), E=E)
+
+
+def make_correlator_fixture(ref_root: str):
+    """lattice.correlator.one_particle.twopoint / twopoint_profile on synthetic
+    elementals [Nderiv, Nmom, Lt, Ne, Ne] and perambulators
+    [Lt, Lt, 4, 4, Ne, Ne] (complex Gaussian), for operators built with the
+    reference's own Operator class (several parts, derivative and momentum
+    combinations, and the gamma 5 / 13 sign convention of its constructor)."""
+    import_reference(ref_root)
+    from lattice.correlator.one_particle import twopoint, twopoint_profile
+    from lattice.insertion import InsertionRowMom, Operator
+
+    Lt, Ne, usedNe, nder, nmom = 6, 4, 3, 4, 3
+    rng = np.random.default_rng(61)
+
+    def cgauss(*shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+    elem = cgauss(nder, nmom, Lt, Ne, Ne)
+    peram = cgauss(Lt, Lt, 4, 4, Ne, Ne)
+    peram_bw = cgauss(Lt, Lt, 4, 4, Ne, Ne)
+    ops_spec = [
+        # (name, [(row, momentum index)], coefficients); row = [gamma, [(coeff, derivative), ...], ...]
+        ("g5", [([15, [(1.0, 0)]], 0)], [1.0]),
+        ("nabla", [([1, [(1.0, 1), (-0.5, 2)], 8, [(0.25, 0)]], 1), ([5, [(1.0, 3)]], 2)], [1.0, 0.7]),
+        ("g13_mom", [([13, [(2.0, 2)]], 1)], [-1.5]),
+    ]
+    ops = [Operator(n, [InsertionRowMom(r, m) for r, m in rows], cs) for n, rows, cs in ops_spec]
+    ts = [0, 2, 5]
+    dts = [0, 1, 3, 4]
+    res = {
+        "tp": twopoint(ops, elem, peram, ts, Lt, usedNe),
+        "tp_all_src": twopoint(ops, elem, peram, ts, Lt, usedNe, is_sum_over_source_t=False),
+        "tp_bw": twopoint(ops, elem, peram, ts, Lt, usedNe, perambulator_bw=peram_bw),
+        "tp_fullne": twopoint(ops, elem, peram, ts, Lt, Ne),
+        "prof": twopoint_profile(ops, elem, peram, ts, dts, usedNe),
+        "prof_diag": twopoint_profile(ops, elem, peram, ts, dts, usedNe, is_diagonal=True),
+        "prof_all_src": twopoint_profile(ops, elem, peram, ts, dts, usedNe, is_sum_over_source_t=False),
+        "prof_bw_fullt": twopoint_profile(ops, elem, peram, ts, list(range(Lt)), usedNe, perambulator_bw=peram_bw),
+    }
+    spec = np.array(repr(ops_spec))
+    np.savez_compressed(os.path.join(HERE, "correlator.npz"), Lt=Lt, Ne=Ne, usedNe=usedNe, elem=elem, peram=peram,
+                        peram_bw=peram_bw, ts=np.array(ts), dts=np.array(dts), ops_spec=spec,
+                        parts=np.array(repr([op.parts for op in ops])), **res)
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     main(root)
     make_ildg_fixture(root)
+    make_config0_chain(root)
+    make_correlator_fixture(root)

@@ -100,7 +100,7 @@ def test_correlator_loss_gradients_vs_finite_differences():
 
 
 def test_twopoint_matches_oracle():
-    from easydistillation_gb300.correlator import gamma, twopoint
+    from easydistillation_gb300.correlator import gamma, twopoint_assembled
 
     rng = np.random.default_rng(7)
     Lt, Ne, X = 6, 4, 2
@@ -108,7 +108,7 @@ def test_twopoint_matches_oracle():
     e = rng.standard_normal((X, Lt, Ne, Ne)) + 1j * rng.standard_normal((X, Lt, Ne, Ne))
     peram = rng.standard_normal((Lt, Lt, 4, 4, Ne, Ne)) + 1j * rng.standard_normal((Lt, Lt, 4, 4, Ne, Ne))
     ref = R.twopoint([(g, e)], peram, range(Lt), Lt)
-    out = twopoint([(torch.from_numpy(g).cuda(), torch.from_numpy(e).cuda())], torch.from_numpy(peram).cuda(),
-                   range(Lt), Lt)
+    out = twopoint_assembled([(torch.from_numpy(g).cuda(), torch.from_numpy(e).cuda())],
+                             torch.from_numpy(peram).cuda(), range(Lt), Lt)
     np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-11, atol=1e-11)
     np.testing.assert_allclose(gamma(7).numpy(), R.gamma(7), atol=0)

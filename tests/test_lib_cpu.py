@@ -124,6 +124,59 @@ def test_generator_metadata_matches_reference_scheme():
     assert [num_derivative(k) for k in range(3)] == [1, 4, 13]
 
 
+def test_momentum_lists_match_reference_tables():
+    """mom_dict_to_list for 1, 3, 9 and the reference's default (9) against the
+    reference's own tables; other values raise like the reference."""
+    from easydistillation_gb300 import mom_dict_to_list
+    from tests.conftest import golden
+
+    g = golden("metadata.npz")
+    assert mom_dict_to_list(3) == [tuple(int(v) for v in p) for p in g["mom3"]]
+    assert mom_dict_to_list(9) == [tuple(int(v) for v in p) for p in g["mom9"]]
+    assert mom_dict_to_list() == [tuple(int(v) for v in p) for p in g["mom_default"]]
+    assert len(mom_dict_to_list()) == 123 and mom_dict_to_list(1) == [(0, 0, 0)]
+    assert mom_dict_to_list(3)[:7] == [p for p in mom_dict_to_list(3) if sum(v * v for v in p) <= 1]
+    with pytest.raises(ValueError):
+        mom_dict_to_list(5)
+
+
+def test_backend_switch():
+    """set_backend / get_backend mirror lattice/backend.py: numpy, torch and a
+    module object are accepted, unknown names raise ValueError."""
+    import numpy as np
+    import torch
+
+    import easydistillation_gb300 as ed
+    from easydistillation_gb300 import backend as B
+
+    try:
+        ed.set_backend("numpy")
+        assert ed.get_backend() is np
+        out = B.to_backend(torch.zeros(3, dtype=torch.complex128))
+        assert isinstance(out, np.ndarray) and out.dtype == np.complex128
+        ed.set_backend(np)  # a module, as the reference also accepts
+        assert B.backend_name() == "numpy"
+        with pytest.raises(ValueError):
+            ed.set_backend("jax")
+    finally:
+        ed.set_backend("torch")
+    assert ed.get_backend() is torch
+
+
+def test_operator_parts_match_reference():
+    """Operator(name, [InsertionRowMom(row, mom)], coefficients).parts as the
+    reference builds them (incl. the gamma 5 / 13 sign convention)."""
+    from easydistillation_gb300.correlator import InsertionRowMom, Operator
+    from tests.conftest import golden
+
+    z = golden("correlator.npz")
+    spec = eval(str(z["ops_spec"]))
+    ops = [Operator(n, [InsertionRowMom(r, m) for r, m in rows], cs) for n, rows, cs in spec]
+    assert [op.parts for op in ops] == eval(str(z["parts"]))
+    with pytest.raises(AssertionError):
+        Operator("bad", [InsertionRowMom([15, [(1.0, 0)]], 0)], [1.0, 2.0])
+
+
 @pytest.mark.parametrize(
     "moms, mode, factorise, expect",
     [

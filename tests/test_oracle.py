@@ -17,6 +17,29 @@ def test_derivative_and_momentum_lists():
     assert [R.num_derivative(k) for k in range(3)] == [1, 4, 13]
 
 
+def test_correlators_on_operator_interface():
+    """twopoint / twopoint_profile restated on the reference's Operator + file
+    data interface, against the reference's own outputs."""
+    z = golden("correlator.npz")
+    spec = eval(str(z["ops_spec"]))  # a repr of plain lists, tuples and numbers
+    parts = [R.operator_parts(rows, cs) for _n, rows, cs in spec]
+    assert parts == eval(str(z["parts"]))
+    E, P, PB = z["elem"], z["peram"], z["peram_bw"]
+    ts, dts, Lt, u = list(z["ts"]), list(z["dts"]), int(z["Lt"]), int(z["usedNe"])
+    cases = {
+        "tp": R.twopoint_operators(parts, E, P, ts, Lt, u),
+        "tp_all_src": R.twopoint_operators(parts, E, P, ts, Lt, u, is_sum_over_source_t=False),
+        "tp_bw": R.twopoint_operators(parts, E, P, ts, Lt, u, perambulator_bw=PB),
+        "tp_fullne": R.twopoint_operators(parts, E, P, ts, Lt, int(z["Ne"])),
+        "prof": R.twopoint_profile_operators(parts, E, P, ts, dts, u),
+        "prof_diag": R.twopoint_profile_operators(parts, E, P, ts, dts, u, is_diagonal=True),
+        "prof_all_src": R.twopoint_profile_operators(parts, E, P, ts, dts, u, is_sum_over_source_t=False),
+        "prof_bw_fullt": R.twopoint_profile_operators(parts, E, P, ts, list(range(Lt)), u, perambulator_bw=PB),
+    }
+    for k, v in cases.items():
+        np.testing.assert_allclose(v, z[k], rtol=1e-12, atol=1e-12 * np.abs(z[k]).max(), err_msg=k)
+
+
 def test_momentum_phase_sign_and_values():
     g = golden("phase_462.npz")
     latt = list(g["latt"])

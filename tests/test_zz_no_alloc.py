@@ -19,6 +19,9 @@ from oracle import restatement as R
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12  # the relative tolerance of the FP64 elemental tests
+# the tolerance of the split-precision tests against FP64; the no-allocation run
+# and the workspace run use the same kernels, so they must agree far closer
+TC_TOL = 1e-6
 
 
 def _inputs(latt, Ne, seed):
@@ -70,3 +73,42 @@ def test_noalloc_rejects_plans_larger_than_its_scratch():
                                              None, dummy.data_ptr(), _lib.stream_handle())
     assert rc == _lib.ED_ERR_WORKSPACE
     assert "scratch" in _lib.last_error()
+
+
+@pytest.mark.parametrize("nmom", [7, 27])
+def test_noalloc_tensor_core_modes_on_a_dirty_array(nmom):
+    """f16x3 through the built-in array, twice in a row on different inputs, after
+    the FP64 calls above left their own bytes in it: the tensor-core modes clear
+    their accumulators and status word themselves, so each call must agree with
+    ed_elemental_run on a fresh caller workspace, and the status word read back
+    by ed_elemental_status_noalloc must be clean.  Seven momenta run the GEMM that
+    forms the phase-weighted operand on chip, 27 the factorised-phase GEMM."""
+    from easydistillation_gb300 import _lib
+    from easydistillation_gb300.ops import ElementalPlan
+
+    latt = [4, 4, 4, 2]
+    Lx, Ly, Lz, Lt = latt
+    V3 = Lx * Ly * Lz
+    Ne, moms = 6, R.mom_dict_to_list(3)[:nmom]
+    plan = ElementalPlan(latt, Ne, 2, moms, "f16x3")
+    assert plan.workspace_bytes <= (32 << 20)
+    assert (plan.factorised is not None) == (nmom == 27)
+    stream = _lib.stream_handle()
+    outs = []
+    for seed in (7, 8):
+        U, V = _inputs(latt, Ne, seed)
+        links = U[:, 0]
+        ref = torch.empty((13, nmom, Ne, Ne), dtype=torch.complex128, device="cuda")
+        plan.run(links, Lt * V3 * 9, 9, V, ref)
+        assert plan.check_status() == 0
+        out = torch.full_like(ref, float("nan"))
+        rc = _lib.lib().ed_elemental_run_noalloc(plan._h, links.data_ptr(), Lt * V3 * 9, 9, _lib.ED_C128,
+                                                 V.data_ptr(), None, out.data_ptr(), stream)
+        _lib.check(rc, "ed_elemental_run_noalloc")
+        code = ctypes.c_int(-1)
+        rc = _lib.lib().ed_elemental_status_noalloc(plan._h, ctypes.byref(code), stream)
+        _lib.check(rc, "ed_elemental_status_noalloc")
+        assert code.value == 0
+        assert _rel(out, ref) < TC_TOL
+        outs.append(out)
+    assert _rel(outs[0], outs[1]) > 1e-3
