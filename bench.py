@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--no-factor", action="store_true",
                     help="keep the on-chip phase GEMM although the 27 momenta factorise")
     ap.add_argument("--no-stencil", action="store_true", help="skip the Laplacian bandwidth measurement")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the measurements of the other configurations that the default line carries (other "
+                         "split modes, eigensolve, mixed volumes, gradient)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="build the plans with the built-in defaults instead of the autotuner's choice (which is "
                          "measured before the timed region and cached per device and shape)")
@@ -183,19 +186,44 @@ FP64_PEAK_TFLOPS = 1.25
 FP64_PEAK_SOURCE = "nominal GB300 FP64"
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the baseline lines."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def _oracle_inputs(latt, Ne, seed=2):
+    """Seeded synthetic inputs for the CPU legs, built with the oracle alone
+    (nothing of the GPU package is imported on the reference arm): one
+    timeslice of links exp(i 0.3 A) and Ne orthonormal vectors."""
+    from oracle import restatement as R
+
+    g = R.synthetic_gauge(list(latt[:3]) + [1], 0.3, 1000 + seed)
+    U = g.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
+    V = R.random_colour_vectors(Ne, list(latt[:3]) + [1], seed * 100)
+    return U, V
+
+
 def cpu_reference_sample(latt, Ne, threads, reps=2):
-    """Time the oracle (CPU restatement of the reference numpy path) on a
-    bounded sample at full size: one covariant-derivative hop of all Ne
-    vectors and one momentum-weighted zgemm, each the median of `reps` runs,
-    scaled by the reference's counts per timeslice (78 hops, 43 x 27 zgemm)."""
+    """Bounded CPU sample for the ``cpu_baseline`` key of the GPU line (10-30 s
+    of host work): the oracle's restatement of the reference numpy path at full
+    size, one covariant-derivative hop of all Ne vectors and one phase-weighted
+    zgemm, each the median of ``reps`` runs, scaled by the reference's counts
+    per timeslice (78 hops, 43 x 27 zgemm).  ``--impl reference`` times whole
+    timeslices instead."""
     os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
     import numpy as np
 
     from oracle import restatement as R
 
-    gauge, evecs = make_inputs(latt[:3] + [1], Ne, distinct_t=1)
-    U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
-    V = evecs[0].reshape(Ne, latt[2], latt[1], latt[0], 3).astype(np.complex64).astype(np.complex128)
+    U, V = _oracle_inputs(latt, Ne)
+    V = V.astype(np.complex64).astype(np.complex128)
     ph = R.momentum_phase(latt, (0, 0, 1))
     th, tg = [], []
     for _ in range(reps):
@@ -210,30 +238,80 @@ def cpu_reference_sample(latt, Ne, threads, reps=2):
     hop, gemm = statistics.median(th), statistics.median(tg)
     per_ts = REF_HOPS * hop + REF_SUBSETS * NMOM * gemm
     return per_ts, (f"oracle at {latt[0]}^3, Ne={Ne}: one hop ({hop:.2f} s) and one phase-weighted zgemm "
-                    f"({gemm:.2f} s) timed, scaled by {REF_HOPS} hops + {REF_SUBSETS}x{NMOM} zgemm per timeslice")
+                    f"({gemm:.2f} s) timed, scaled by {REF_HOPS} hops + {REF_SUBSETS}x{NMOM} zgemm per timeslice "
+                    f"(an estimate; --impl reference times whole timeslices)")
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU algorithm for this path, as the
+    oracle restates it (``ElementalGenerator.calc``: per derivative operator and
+    left/right subset, both chains rebuilt and one phase-weighted zgemm per
+    momentum), on the host cores, on the GPU arm's workload (32^3, Ne = 200,
+    13 operators x 27 momenta).  The K timed steps together compute WHOLE
+    timeslices: the 43 (operator, subset) work items of a timeslice, in the
+    reference's loop order, are split into K consecutive groups, step i runs
+    group i (with K > 43 the items continue into further timeslices), and
+    ``value`` = timeslices computed / total time.  Warm-up steps run one
+    momentum's zgemm each.  On the default workload (or with ``--eigen-cpu``)
+    it also times scipy/ARPACK, the reference's eigensolver, on one 24^3,
+    Ne = 100 timeslice.  Rank 0 only."""
     if rank != 0:
         return
     threads = len(os.sched_getaffinity(0))
+    import numpy as np
+
+    from oracle import restatement as R
+
     latt = [int(v) for v in args.lattice.split(",")] if args.lattice else LATT
-    times = []
-    sample = ""
-    for i in range(args.warmup + args.steps):
-        per_ts, sample = cpu_reference_sample(latt, args.ne, threads)
-        if i >= args.warmup:
-            times.append(per_ts)
-    per_ts = statistics.median(times)
-    val = 1.0 / per_ts
+    Ne = args.ne
+    moms = R.mom_dict_to_list(3)[:NMOM]
+    U, V = _oracle_inputs(latt, Ne)
+    Vc = V.astype(np.complex64).astype(np.complex128)  # the reference's complex64 buffer
+    phases = [R.momentum_phase(latt, p) for p in moms]
+    items = R.elemental_items(NUM_NABLA)
+    out = np.zeros((R.num_derivative(NUM_NABLA), NMOM, Ne, Ne), np.complex128)
+    for _ in range(args.warmup):
+        lp = (phases[0][None, :, :, :, None] * Vc.conj()).reshape(Ne, -1)
+        _ = lp @ Vc.reshape(Ne, -1).T
+    K = max(1, args.steps)
+    n_items = -(-K // len(items)) * len(items)  # whole timeslices, at least one item per step
+    bounds = [round(i * n_items / K) for i in range(K + 1)]
+    step_s = []
+    for i in range(K):
+        t0 = time.perf_counter()
+        for q in range(bounds[i], bounds[i + 1]):
+            if q % len(items) == 0:
+                out[...] = 0
+            R.elemental_item_into(out, Vc, U, items[q % len(items)], phases)
+        step_s.append(time.perf_counter() - t0)
+    total = sum(step_s)
+    timeslices = n_items / len(items)
+    val = timeslices / total
+    est, est_sample = cpu_reference_sample(latt, Ne, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "timeslices/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_ts * 1e3, "higher_is_better": True,
+        "steps": K, "warmup": args.warmup, "ms_per_step": total / K * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": f"elemental {latt[0]}^3x{latt[3]}, Ne={args.ne}, 13 ops x 27 momenta (CPU sample)"},
-        "cpu_baseline": {"value": val, "unit": "timeslices/s", "cores": threads, "kind": "port", "sample": sample},
+        "config": {"workload": f"elemental {latt[0]}^3x{latt[3]}, Ne={Ne}, 13 ops x {NMOM} momenta (CPU, "
+                               f"{timeslices:g} whole timeslice(s) over the timed steps)"},
+        "cpu_baseline": {"value": val, "unit": "timeslices/s", "cores": threads, "kind": "port",
+                         "cpu_model": cpu_model(),
+                         "sample": f"{timeslices:g} whole timeslice(s) of the oracle's restatement of "
+                                   f"ElementalGenerator.calc ({len(items)} operator/subset items, each rebuilding "
+                                   f"its chains and running {NMOM} phase-weighted zgemms), split over {K} steps; "
+                                   f"OpenBLAS on {threads} threads",
+                         "seconds_per_timeslice": total / timeslices,
+                         "estimate_from_one_hop_one_zgemm": {"value": 1.0 / est, "sample": est_sample}},
         "e2e": {"value": val, "unit": "timeslices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if args.eigen_cpu or not args.lattice:
+        ulatt = [24, 24, 24, 1]
+        Ue, _ = _oracle_inputs(ulatt, 1, seed=1)
+        t0 = time.perf_counter()
+        R.eigensolve(Ue, ulatt, 100, 1e-10)
+        dt = time.perf_counter() - t0
+        line["eigensolve_cpu"] = {"value": 1.0 / dt, "unit": "timeslices/s", "seconds": dt,
+                                  "workload": "24^3, Ne=100, tol 1e-10, scipy eigsh (ARPACK), one timeslice"}
     print(json.dumps(line), flush=True)
 
 
@@ -415,6 +493,7 @@ def run_ours(args, rank, world):
 
     # the plain FP64 GPU path on the same timeslice: speed and the split-precision error against it
     fp64 = None
+    split_modes = None
     if args.mode != "fp64" and not args.no_fp64:
         t_tune = None
         if args.autotune:
@@ -439,7 +518,13 @@ def run_ours(args, rank, world):
         fp64 = {"value": 1e3 / ms64, "unit": "timeslices/s", "rel_err_vs_fp64": rel,
                 "speedup_split_over_fp64": (value / world) / (1e3 / ms64), "plan_settings": plan64.tuning(),
                 "autotune_seconds": t_tune}
-        del plan64, out64
+        del plan64
+        torch.cuda.empty_cache()
+        if not args.no_extra and rank == 0:
+            # the other split-precision modes on the same workload, each with its error against FP64
+            split_modes = bench_split_modes(args, latt, Ne, moms, U, V, out64, t_ref, dev, stream,
+                                            exclude=args.mode)
+        del out64
         torch.cuda.empty_cache()
 
     stencil = None if args.no_stencil else bench_stencil(U, latt, dev)
@@ -496,7 +581,8 @@ def run_ours(args, rank, world):
     if rank == 0 and not args.no_cpu:
         threads = len(os.sched_getaffinity(0))
         per_ts, sample = cpu_reference_sample(latt, Ne, threads)
-        cpu = {"value": 1.0 / per_ts, "unit": "timeslices/s", "cores": threads, "kind": "port", "sample": sample}
+        cpu = {"value": 1.0 / per_ts, "unit": "timeslices/s", "cores": threads, "kind": "port", "sample": sample,
+               "cpu_model": cpu_model()}
 
     if rank == 0:
         line = {
@@ -512,14 +598,143 @@ def run_ours(args, rank, world):
                        "parallelism": f"replicas x{world}"},
             "gpu_launches": args.steps * launches_per_step(args.mode, B, plan.factorised is not None),
             "clocks": clocks, "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "fp64_gpu": fp64,
-            "stencil_roofline": stencil,
+            "split_modes": split_modes, "stencil_roofline": stencil,
         }
+        if not args.no_extra:
+            # the other configurations' measurements, each timed by itself after the headline measurement
+            del plan, outs, out, V, U
+            torch.cuda.empty_cache()
+            line["eigensolve"] = bench_eigen_default(dev)
+            torch.cuda.empty_cache()
+            line["mixed_volumes"] = measure_mixed(args, dev)
+            torch.cuda.empty_cache()
+            line["gradient"] = measure_grad(args, dev)
         if tuned is not None:
             line["autotune"] = tuned
         print(json.dumps(line), flush=True)
 
 
-def run_mixed(args):
+def bench_split_modes(args, latt, Ne, moms, U, V, out64, t_ref, dev, stream, exclude=None, reps=2):
+    """Every split-precision mode other than the headline one on the headline
+    workload: timeslices/s over ``reps`` batched steps (after one warm-up
+    step, CUDA events; batch 2 for the tensor-core modes, 1 for the Ozaki
+    int8 mode), the pair-GEMM kernel time, and the relative Frobenius error
+    against the FP64 GPU elementals of timeslice ``t_ref``."""
+    import torch
+
+    from easydistillation_gb300.ops import ElementalPlan
+
+    Lx, Ly, Lz, Lt = latt
+    V3 = Lx * Ly * Lz
+    out = {}
+    for mode in ("f16x3", "tf32x3", "bf16x3", "ozaki_i8"):
+        if mode == exclude:
+            continue
+        B = 1 if mode == "ozaki_i8" else 2
+        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, mode, dev, batch=B)
+        outs = [torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev) for _ in range(B)]
+
+        def step(i):
+            ts = [((i * B + k) * 7) % Lt for k in range(B)]
+            plan.run_batch([U[:, t] for t in ts], Lt * V3 * 9, 9, [V[(i * B + k) % RESIDENT_T] for k in range(B)],
+                           outs)
+
+        step(0)
+        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, b in kev:
+            a.record(stream)
+            b.record(stream)
+        a0, b0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a0.record(stream)
+        for i in range(reps):
+            plan.set_profile_events(*kev[i])
+            step(1 + i)
+        b0.record(stream)
+        torch.cuda.synchronize()
+        plan.set_profile_events(None, None)
+        ms = a0.elapsed_time(b0)
+        kms = statistics.mean(a.elapsed_time(b) for a, b in kev)
+        plan.run(U[:, t_ref], Lt * V3 * 9, 9, V[args.warmup % RESIDENT_T], outs[0])
+        plan.check_status()
+        err = float(torch.linalg.vector_norm(outs[0] - out64) / torch.linalg.vector_norm(out64))
+        out[mode] = {"value": reps * B / (ms / 1e3), "unit": "timeslices/s", "kernel_ms_per_step": kms,
+                     "timeslices_per_step": B, "rel_err_vs_fp64": err, "factorised_phases": plan.factorised}
+        del plan, outs
+        torch.cuda.empty_cache()
+    return out
+
+
+def bench_eigen_default(dev, batch=8):
+    """The FP64 eigensolve configuration, 24^3, Ne = 100, tol 1e-10, on a batch
+    of ``batch`` timeslices (links exp(i 0.3 A)): the plain native
+    thick-restart Lanczos, the Chebyshev-accelerated one (degree 16, cut 15 %
+    above the largest eigenvalue of the plain solve), and the mixed solve
+    (complex64 stencil in a loose FP64 iteration, then the FP64 Chebyshev
+    refinement with the cut found automatically).  Each: timeslices/s of one
+    solve after an untimed one, the largest residual ||L x - lambda x|| (FP64
+    stencil), the largest deviation of the Gram matrix from identity and the
+    largest eigenvalue difference to the plain solve."""
+    import torch
+
+    from easydistillation_gb300.ops import lanczos_tr, laplacian, links_to_soa
+    from easydistillation_gb300.generator.elemental import links_to_device
+
+    latt = [24, 24, 24, batch]
+    Ne = 100
+    gauge, _ = make_inputs(latt, 1, distinct_t=batch)
+    U = links_to_device(gauge, latt, dev)
+    L64 = links_to_soa(U, latt)
+    L32 = links_to_soa(U, latt, dtype=torch.complex64)
+
+    def quality(ev, X, ref_ev=None):
+        LY = laplacian(L64, X, latt)
+        res = torch.linalg.vector_norm((LY - ev[:, :, None, None].to(X.dtype) * X).reshape(batch, Ne, -1), dim=2)
+        Xf = X.reshape(batch, Ne, -1)
+        G = Xf.conj() @ Xf.transpose(1, 2)
+        eye = torch.eye(Ne, dtype=G.dtype, device=G.device)
+        q = {"max_residual": float(res.max()), "max_gram_dev": float((G - eye).abs().max())}
+        if ref_ev is not None:
+            q["max_rel_eval_diff_vs_plain"] = float(((ev - ref_ev).abs() / ref_ev.abs()).max())
+        return q
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    out = {"workload": f"24^3, Ne={Ne}, tol 1e-10, {batch} timeslices per solve"}
+    (ev0, X0, st0), dt0 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-10))
+    out["plain_fp64"] = {"value": batch / dt0, "unit": "timeslices/s", "converged": st0["converged"],
+                         "restarts": st0["restarts"], **quality(ev0, X0)}
+    cut = 1.15 * float(ev0[:, -1].max())
+    (ev1, X1, st1), dt1 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-12, poly_deg=16, lambda_cut=cut))
+    out["chebyshev_fp64"] = {"value": batch / dt1, "unit": "timeslices/s", "converged": st1["converged"],
+                             "degree": 16, "lambda_cut": cut, "note": "cut taken from the plain solve",
+                             **quality(ev1, X1, ev0)}
+    (ev2, X2, st2), dt2 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-10, stencil_precision="fp32", links_c64=L32))
+    out["mixed_fp32_stencil"] = {"value": batch / dt2, "unit": "timeslices/s", "converged": st2["converged"],
+                                 "matvecs_fp32": st2["matvecs_fp32"], "matvecs_fp64": st2["matvecs_fp64"],
+                                 "restarts_fp32_phase": st2["restarts_fp32"],
+                                 "note": "complex64 stencil in a loose FP64 iteration, then FP64 Chebyshev "
+                                         "refinement (cut found automatically)", **quality(ev2, X2, ev0)}
+    return out
+
+
+def measure_mixed(args, dev):
+    """The mixed-volume configuration as a dict (see ``run_mixed``)."""
+    return run_mixed(args, emit=False)
+
+
+def measure_grad(args, dev):
+    """The differentiation configuration as a dict (see ``run_grad``)."""
+    return run_grad(args, emit=False)
+
+
+def run_mixed(args, emit=True):
     """Secondary measurement (``--mixed``): 96 timeslices, 32 each of 16^3
     (Ne=64), 24^3 (Ne=128) and 32^3 (Ne=256), links exp(i eps A) with eps
     alternating 0.1 / 0.3 over timeslices, 4 operators x 7 momenta, split
@@ -574,10 +789,13 @@ def run_mixed(args):
             "autotune": args.autotune, "plan_setup_seconds": setup_s,
             "graph_replays_per_sweep": 1, "batched_passes_per_sweep": mv.passes(),
             "data": "synthetic, resident in HBM"}
-    print(json.dumps(line), flush=True)
+    del mv, bindings
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
-def run_grad(args):
+def run_grad(args, emit=True):
     """Secondary measurement (``--grad``): gradient of the correlator
     log-ratio loss (t = 6, 12; operator nabla_x, p = 0; gamma_5) with respect
     to the profile weights w_k and the links at 24^3 x 48, Ne = 100, through
@@ -637,7 +855,9 @@ def run_grad(args):
                          "rel_err_w": abs(anw - fdw) / max(abs(fdw), 1e-30)},
             "data": "synthetic: links exp(i 0.3 A), Gaussian vectors and perambulator [48,4,4,100,100], "
                     "w ~ U(0.5, 1.5), sigma = 1"}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 # FP64 flops of one stout link update: four staples of two 3x3 complex products, C U^dag, the
@@ -918,6 +1138,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
+        n = str(len(os.sched_getaffinity(0)))
+        for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS"):
+            os.environ.setdefault(var, n)
         run_reference(args, rank, world)
         return
     if world > 1:

@@ -82,6 +82,9 @@ _SIGNATURES = {
     "ed_lanczos_workspace": ([_i, _i, _i, _i, _i, _i, _c.POINTER(_c.c_size_t)], _i),
     "ed_lanczos_tr": ([_i, _i, _i, _i, _vp, _i, _c.c_double, _i, _i, _i, _c.c_double, _vp, _vp, _c.POINTER(_i), _vp,
                        _c.c_size_t, _vp], _i),
+    "ed_lanczos_workspace_ex": ([_i, _i, _i, _i, _i, _i, _i, _c.POINTER(_c.c_size_t)], _i),
+    "ed_lanczos_tr_ex": ([_i, _i, _i, _i, _vp, _vp, _i, _i, _c.c_double, _i, _i, _i, _c.c_double, _vp, _vp,
+                          _c.POINTER(_i), _vp, _c.c_size_t, _vp], _i),
     "ed_arrow_eigh": ([_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _c.c_size_t, _vp], _i),
     "ed_elemental_get_tuning": ([_vp, _i, _c.POINTER(_i)], _i),
 }

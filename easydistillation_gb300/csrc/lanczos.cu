@@ -14,6 +14,16 @@
 // the host reads one convergence counter per restart.  Convergence follows
 // ARPACK's rule: Ritz pair i is accepted when |beta_m y_{m,i}| <= tol |theta_i|.
 //
+// ed_lanczos_tr_ex adds a mixed-precision solve: phase 1 runs the same
+// iteration with the complex64 stencil (the FP64 basis vector rounded to
+// complex64, the result widened back; Gram-Schmidt, Rayleigh-Ritz and the
+// convergence test in FP64) to a loose tolerance (1e-4, far above the
+// stencil's ~1e-7 rounding); its Ritz values give the Chebyshev cut (15 %
+// above the largest wanted one) and its Ritz vectors the start vector of
+// phase 2, an FP64-stencil Chebyshev-filtered solve to the requested
+// tolerance.  The final eigenpairs, their residual test and the Rayleigh
+// quotients are FP64.
+//
 // With a Chebyshev degree the iteration runs on -T_deg((2L - (12 + cut)) /
 // (12 - cut)) (sign flipped for even degree so the wanted modes are the
 // smallest), which keeps L's eigenvectors and their order below the cut; the
@@ -33,6 +43,10 @@ namespace ed {
 namespace {
 
 constexpr int LZ_THREADS = 256;
+// Mixed solve (ed_lanczos_tr_ex with the complex64 stencil): phase-1 tolerance (well above the complex64
+// stencil's rounding, ~1e-7 relative) and the default Chebyshev degree of the FP64 phase 2
+constexpr double LZ_MIXED_TOL = 1e-4;
+constexpr int LZ_MIXED_DEG = 16;
 
 // ED_OK, or the library's CUDA error status for a failed call
 inline int lz_chk(cudaError_t e, const char* what) { return e == cudaSuccess ? ED_OK : cuda_status(e, what); }
@@ -241,6 +255,38 @@ __global__ void lz_gather_kernel(int nev, long long n, const double2* __restrict
     o[x] = s[x];
 }
 
+// out[b][x] = complex64 rounding of in[b*ib + x] (the operand of the complex64 stencil)
+__global__ void lz_to_c64_kernel(long long n, const double2* __restrict__ in, long long ib, float2* __restrict__ out) {
+  const int b = blockIdx.y;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    const double2 v = in[(long long)b * ib + x];
+    out[(long long)b * n + x] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+// out[b][x] = in[b][x] widened to complex128
+__global__ void lz_from_c64_kernel(long long n, const float2* __restrict__ in, double2* __restrict__ out) {
+  const int b = blockIdx.y;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    const float2 v = in[(long long)b * n + x];
+    out[(long long)b * n + x] = make_double2((double)v.x, (double)v.y);
+  }
+}
+
+// w[b] = sum of the nvec vectors X[b][0..nvec) (a warm start made of earlier Ritz vectors)
+__global__ void lz_sum_vectors_kernel(long long n, int nvec, const double2* __restrict__ X, double2* __restrict__ w) {
+  const int b = blockIdx.y;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (long long)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int i = 0; i < nvec; ++i) {
+      const double2 v = X[((long long)b * nvec + i) * n + x];
+      re += v.x;
+      im += v.y;
+    }
+    w[(long long)b * n + x] = make_double2(re, im);
+  }
+}
+
 // Workspace carve-up (all offsets 256-byte aligned).
 struct LzLayout {
   size_t V, w, t0, t1, t2, lbuf, rot, hA, hB, part, npart, d, e, s, bl, theta, Y, arrow, nbad, rq, perm, total;
@@ -339,30 +385,53 @@ extern "C" int ed_lanczos_workspace(int Lx, int Ly, int Lz, int nt, int Ne, int 
   return ED_OK;
 }
 
-extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, double tol, int ncv,
-                             int max_restarts, int poly_deg, double lambda_cut, void* evecs, double* evals, int* status,
-                             void* workspace, size_t workspace_bytes, void* stream) {
-  using namespace ed;
-  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr: bad sizes");
+namespace ed {
+namespace {
+
+// One thick-restart Lanczos solve (the body of ed_lanczos_tr and of each phase of ed_lanczos_tr_ex).  The operator
+// applications use the FP64 stencil on `links` (stencil_prec ED_C128), or round the FP64 basis vector to complex64,
+// apply the complex64 stencil on `links32` and widen the result (ED_C64).  Everything else is FP64.  With start_nvec
+// > 0 the start vector of problem b is the sum of the start_nvec vectors start[b][..] (else a pseudo-random one).
+// status: converged, restarts, operator applications.  Argument checks are the callers'.
+struct LzArgs {
+  int Lx, Ly, Lz, nt;
+  const void* links;
+  const void* links32;
+  int stencil_prec;
+  int Ne;
+  double tol;
+  int ncv, max_restarts, poly_deg;
+  double lambda_cut;
+  void* evecs;
+  double* evals;
+  const void* start;
+  int start_nvec;
+  int* status;
+  void* workspace;
+  cudaStream_t stream;
+};
+
+size_t lz_c64_bytes(int B, long long n) { return 2 * al((size_t)B * n * 8); }
+
+int lanczos_solve(const LzArgs& a) {
+  const int Lx = a.Lx, Ly = a.Ly, Lz = a.Lz, nt = a.nt, Ne = a.Ne, ncv = a.ncv, max_restarts = a.max_restarts,
+            poly_deg = a.poly_deg;
+  const void* links = a.links;
+  const double tol = a.tol, lambda_cut = a.lambda_cut;
+  void* evecs = a.evecs;
+  double* evals = a.evals;
+  int* status = a.status;
   const long long n = 3LL * Lx * Ly * Lz;
-  ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr: need Ne < ncv <= 3*Lx*Ly*Lz");
-  ED_CHECK_ARG(tol > 0.0 && max_restarts > 0, "ed_lanczos_tr: need tol > 0 and max_restarts > 0");
-  ED_CHECK_ARG(poly_deg >= 0 && (poly_deg == 0 || (lambda_cut > 0.0 && lambda_cut < 12.0)),
-               "ed_lanczos_tr: a Chebyshev degree needs 0 < lambda_cut < 12");
-  ED_CHECK_ARG(links && evecs && evals && status && workspace, "ed_lanczos_tr: null pointer");
-  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0 && ((uintptr_t)evecs % 16) == 0 && ((uintptr_t)links % 16) == 0,
-               "ed_lanczos_tr: workspace must be 256-byte aligned, links and evecs 16-byte aligned");
   const int B = nt, kk = lz_kept(Ne, ncv);
   // elementwise grids: one element per thread; the Gram-Schmidt update kernel writes its ||w||^2 partials on the
   // same grid (ceil(n / 256) blocks per problem)
   const int nblk = (int)((n + LZ_THREADS - 1) / LZ_THREADS);
   const LzLayout Lw = lz_layout(B, n, ncv, kk, Ne, nblk);
-  if (workspace_bytes < Lw.total) {
-    set_error("ed_lanczos_tr: workspace of %zu bytes is smaller than the %zu needed", workspace_bytes, Lw.total);
-    return ED_ERR_WORKSPACE;
-  }
-  cudaStream_t st = (cudaStream_t)stream;
-  uint8_t* W = (uint8_t*)workspace;
+  uint8_t* const W = (uint8_t*)a.workspace;
+  // complex64 operand and result of the FP32 stencil, after the FP64 layout
+  float2* x32 = (float2*)(W + Lw.total);
+  float2* y32 = (float2*)(W + Lw.total + al((size_t)B * n * 8));
+  cudaStream_t st = a.stream;
   double2* V = (double2*)(W + Lw.V);
   double2* w = (double2*)(W + Lw.w);
   double2* t0 = (double2*)(W + Lw.t0);
@@ -398,8 +467,18 @@ extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, 
   const double sgn = (poly_deg % 2 == 0) ? -1.0 : 1.0;
   long long matvecs = 0;
   cudaStream_t sr = st;  // the stream the Lanczos steps go to (a capture stream while a restart cycle is recorded)
+  // L x for every problem: FP64 stencil, or the complex64 stencil between a rounding and a widening
+  auto stencil = [&](const double2* x, long long xb, double2* out) -> int {
+    if (a.stencil_prec == ED_C128) return ed_laplacian(ED_C128, Lx, Ly, Lz, B, 1, links, x, xb, out, n, sr);
+    lz_to_c64_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, x, xb, x32);
+    int r = lz_chk(cudaGetLastError(), "Lanczos operand rounding");
+    if (r != ED_OK) return r;
+    if ((r = ed_laplacian(ED_C64, Lx, Ly, Lz, B, 1, a.links32, x32, n, y32, n, sr)) != ED_OK) return r;
+    lz_from_c64_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, y32, out);
+    return lz_chk(cudaGetLastError(), "Lanczos result widening");
+  };
   auto apply = [&](const double2* x, long long xb, double2* out) -> int {
-    int r = ed_laplacian(ED_C128, Lx, Ly, Lz, B, 1, links, x, xb, poly_deg ? lbuf : out, n, sr);
+    int r = stencil(x, xb, poly_deg ? lbuf : out);
     if (r != ED_OK || poly_deg == 0) return r;
     // T_0 = x, T_1 = A x, T_{k+1} = 2 A T_k - T_{k-1} with A = a L + c; the last step writes out, signed
     double2* bufs[3] = {t0, t1, t2};
@@ -408,7 +487,7 @@ extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, 
                                                   1.0, poly_deg == 1 ? sgn : 1.0);
     if ((r = lz_chk(cudaGetLastError(), "Chebyshev step")) != ED_OK) return r;
     for (int kd = 2; kd <= poly_deg; ++kd) {
-      if ((r = ed_laplacian(ED_C128, Lx, Ly, Lz, B, 1, links, bufs[ci], n, lbuf, n, sr)) != ED_OK) return r;
+      if ((r = stencil(bufs[ci], n, lbuf)) != ED_OK) return r;
       const int ni = pi < 0 ? (ci + 1) % 3 : 3 - ci - pi;
       const bool last = kd == poly_deg;
       lz_cheb_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, lbuf, bufs[ci], n, pi < 0 ? x : bufs[pi], pi < 0 ? xb : n,
@@ -482,7 +561,10 @@ extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, 
   };
 
   // start vectors
-  lz_random_kernel<<<vgrid, LZ_THREADS, 0, st>>>(B, n, w, 12345u);
+  if (a.start_nvec > 0)
+    lz_sum_vectors_kernel<<<vgrid, LZ_THREADS, 0, st>>>(n, a.start_nvec, (const double2*)a.start, w);
+  else
+    lz_random_kernel<<<vgrid, LZ_THREADS, 0, st>>>(B, n, w, 12345u);
   LZ_LAUNCHED("Lanczos start vector");
   lz_dot_kernel<<<vgrid, LZ_THREADS, 0, st>>>(n, w, n, w, n, part);
   LZ_LAUNCHED("Lanczos start norm");
@@ -552,5 +634,125 @@ extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, 
   status[2] = (int)std::min<long long>(matvecs, 2147483647LL);
 #undef LZ_TRY
 #undef LZ_LAUNCHED
+  return ED_OK;
+}
+
+}  // namespace
+}  // namespace ed
+
+extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, double tol, int ncv,
+                             int max_restarts, int poly_deg, double lambda_cut, void* evecs, double* evals, int* status,
+                             void* workspace, size_t workspace_bytes, void* stream) {
+  using namespace ed;
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr: bad sizes");
+  const long long n = 3LL * Lx * Ly * Lz;
+  ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr: need Ne < ncv <= 3*Lx*Ly*Lz");
+  ED_CHECK_ARG(tol > 0.0 && max_restarts > 0, "ed_lanczos_tr: need tol > 0 and max_restarts > 0");
+  ED_CHECK_ARG(poly_deg >= 0 && (poly_deg == 0 || (lambda_cut > 0.0 && lambda_cut < 12.0)),
+               "ed_lanczos_tr: a Chebyshev degree needs 0 < lambda_cut < 12");
+  ED_CHECK_ARG(links && evecs && evals && status && workspace, "ed_lanczos_tr: null pointer");
+  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0 && ((uintptr_t)evecs % 16) == 0 && ((uintptr_t)links % 16) == 0,
+               "ed_lanczos_tr: workspace must be 256-byte aligned, links and evecs 16-byte aligned");
+  const int nblk = (int)((n + LZ_THREADS - 1) / LZ_THREADS);
+  const size_t need = lz_layout(nt, n, ncv, lz_kept(Ne, ncv), Ne, nblk).total;
+  if (workspace_bytes < need) {
+    set_error("ed_lanczos_tr: workspace of %zu bytes is smaller than the %zu needed", workspace_bytes, need);
+    return ED_ERR_WORKSPACE;
+  }
+  LzArgs a{Lx, Ly, Lz, nt, links, nullptr, ED_C128, Ne, tol, ncv, max_restarts, poly_deg, lambda_cut,
+           evecs, evals, nullptr, 0, status, workspace, (cudaStream_t)stream};
+  return lanczos_solve(a);
+}
+
+namespace ed {
+namespace {
+// Krylov dimension of the FP64 Chebyshev refinement of the mixed solve: 2 Ne, at least Ne + 32 (measured best for
+// the Chebyshev-filtered iteration), at most the problem size
+int lz_refine_ncv(int Ne, long long n) { return (int)std::min<long long>(std::max(2 * Ne, Ne + 32), n); }
+}  // namespace
+}  // namespace ed
+
+extern "C" int ed_lanczos_workspace_ex(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, int stencil_prec,
+                                       size_t* bytes) {
+  ED_CHECK_ARG(bytes, "ed_lanczos_workspace_ex: null pointer");
+  ED_CHECK_ARG(stencil_prec == ED_C128 || stencil_prec == ED_C64, "ed_lanczos_workspace_ex: bad stencil precision");
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_workspace_ex: bad sizes");
+  const long long n = 3LL * Lx * Ly * Lz;
+  ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_workspace_ex: need Ne < ncv <= 3*Lx*Ly*Lz");
+  const int nblk = (int)((n + ed::LZ_THREADS - 1) / ed::LZ_THREADS);
+  size_t need = ed::lz_layout(nt, n, ncv, ed::lz_kept(Ne, ncv), Ne, nblk).total;
+  if (stencil_prec == ED_C64) {
+    const int ncv2 = ed::lz_refine_ncv(Ne, n);
+    if (ncv2 > Ne) need = std::max(need, ed::lz_layout(nt, n, ncv2, ed::lz_kept(Ne, ncv2), Ne, nblk).total);
+    need += ed::lz_c64_bytes(nt, n);
+  }
+  *bytes = need;
+  return ED_OK;
+}
+
+extern "C" int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* links, const void* links_c64,
+                                int stencil_prec, int Ne, double tol, int ncv, int max_restarts, int poly_deg,
+                                double lambda_cut, void* evecs, double* evals, int* status, void* workspace,
+                                size_t workspace_bytes, void* stream) {
+  using namespace ed;
+  ED_CHECK_ARG(stencil_prec == ED_C128 || stencil_prec == ED_C64, "ed_lanczos_tr_ex: bad stencil precision");
+  ED_CHECK_ARG(status, "ed_lanczos_tr_ex: null status");
+  for (int q = 0; q < 6; ++q) status[q] = 0;
+  if (stencil_prec == ED_C128) {
+    const int rc = ed_lanczos_tr(Lx, Ly, Lz, nt, links, Ne, tol, ncv, max_restarts, poly_deg, lambda_cut, evecs, evals,
+                                 status, workspace, workspace_bytes, stream);
+    status[4] = status[2];
+    return rc;
+  }
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr_ex: bad sizes");
+  const long long n = 3LL * Lx * Ly * Lz;
+  ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr_ex: need Ne < ncv <= 3*Lx*Ly*Lz");
+  ED_CHECK_ARG(tol > 0.0 && max_restarts > 0 && poly_deg >= 0, "ed_lanczos_tr_ex: need tol > 0, max_restarts > 0");
+  ED_CHECK_ARG(links && links_c64 && evecs && evals && workspace, "ed_lanczos_tr_ex: null pointer");
+  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0 && ((uintptr_t)evecs % 16) == 0 && ((uintptr_t)links % 16) == 0 &&
+                   ((uintptr_t)links_c64 % 16) == 0,
+               "ed_lanczos_tr_ex: workspace must be 256-byte aligned, links and evecs 16-byte aligned");
+  ED_CHECK_ARG(Lx % 2 == 0, "ed_lanczos_tr_ex: the complex64 stencil needs an even Lx");
+  size_t need = 0;
+  int rc = ed_lanczos_workspace_ex(Lx, Ly, Lz, nt, Ne, ncv, ED_C64, &need);
+  if (rc != ED_OK) return rc;
+  if (workspace_bytes < need) {
+    set_error("ed_lanczos_tr_ex: workspace of %zu bytes is smaller than the %zu needed", workspace_bytes, need);
+    return ED_ERR_WORKSPACE;
+  }
+  const int ncv2 = lz_refine_ncv(Ne, n);
+  cudaStream_t st = (cudaStream_t)stream;
+  // phase 1: complex64 stencil, FP64 basis, Gram-Schmidt and Rayleigh-Ritz, to the loose tolerance LZ_MIXED_TOL
+  int st1[3] = {0, 0, 0};
+  LzArgs a1{Lx, Ly, Lz, nt, links, links_c64, ED_C64, Ne, std::max(tol, LZ_MIXED_TOL), ncv, max_restarts, 0, 0.0,
+            evecs, evals, nullptr, 0, st1, workspace, st};
+  if ((rc = lanczos_solve(a1)) != ED_OK) return rc;
+  int lap_code = 0;  // a bounded wait of the TMA-staged complex64 stencil that gave up invalidates phase 1
+  if ((rc = ed_laplacian_status(&lap_code, st)) != ED_OK) return rc;
+  // the Chebyshev cut: 15 % above the largest wanted phase-1 eigenvalue of any timeslice (a caller's cut wins)
+  double cut = lambda_cut;
+  if (!(cut > 0.0)) {
+    std::vector<double> ev((size_t)nt * Ne);
+    rc = lz_chk(cudaMemcpyAsync(ev.data(), evals, ev.size() * 8, cudaMemcpyDeviceToHost, st), "phase-1 eigenvalues");
+    if (rc == ED_OK) rc = lz_chk(cudaStreamSynchronize(st), "phase-1 synchronise");
+    if (rc != ED_OK) return rc;
+    double top = 0.0;
+    for (int b = 0; b < nt; ++b) top = std::max(top, ev[(size_t)b * Ne + Ne - 1]);
+    cut = 1.15 * top;
+  }
+  // phase 2: FP64 stencil, Chebyshev-filtered, started from the sum of the phase-1 Ritz vectors, which stay in
+  // evecs (the solve reads them into its start vector first and writes evecs only at its end)
+  int st2[3] = {0, 0, 0};
+  const int deg = poly_deg > 0 ? poly_deg : LZ_MIXED_DEG;
+  const bool cheb = cut > 0.0 && cut < 12.0 && ncv2 > Ne;
+  LzArgs a2{Lx, Ly, Lz, nt, links, nullptr, ED_C128, Ne, cheb ? std::max(tol, 1e-12) : tol, cheb ? ncv2 : ncv,
+            max_restarts, cheb ? deg : 0, cheb ? cut : 0.0, evecs, evals, evecs, Ne, st2, workspace, st};
+  if ((rc = lanczos_solve(a2)) != ED_OK) return rc;
+  status[0] = st2[0];
+  status[1] = st1[1] + st2[1];
+  status[2] = (int)std::min<long long>((long long)st1[2] + st2[2], 2147483647LL);
+  status[3] = st1[2];
+  status[4] = st2[2];
+  status[5] = st1[1];
   return ED_OK;
 }

@@ -10,10 +10,14 @@ ascending and applies the reference's renormalisation phase
 ``(evecs [Ne, Lz, Ly, Lx, 3] complex128, evals [Ne] float64)`` (host numpy
 arrays after ``easydistillation_gb300.set_backend("numpy")``).
 
-``stencil_precision="fp32"`` runs the Lanczos iteration with the FP32 stencil
-and then refines the result with FP64 operator applications (an FP64
-Lanczos restarted from the FP32 Ritz vectors); ``"fp64"`` (default) uses the
-FP64 stencil throughout.
+``stencil_precision="fp32"`` (native driver) runs the mixed solve of
+``ed_lanczos_tr_ex``: the complex64 stencil inside the thick-restart
+iteration (FP64 basis, Gram-Schmidt, Rayleigh-Ritz and convergence test) to a
+loose tolerance, then an FP64 Chebyshev-filtered refinement of every pair to
+``tol`` whose cut the first phase supplies; with ``driver="python"`` the
+same idea runs as an FP32-stencil Lanczos followed by an FP64 Lanczos started
+from its Ritz vectors.  ``"fp64"`` (default) uses the FP64 stencil
+throughout.
 """
 
 from __future__ import annotations
@@ -126,13 +130,24 @@ class EigenvectorGenerator:
         n = NC * V3
         ts = list(ts)
         B = len(ts)
-        if self.driver == "native" and self.stencil_precision == "fp64":
+        if self.driver == "native":
+            idx = None if ts == list(range(Lt)) else torch.as_tensor(ts, device=self.device)
             links = self._links(torch.complex128)
-            sel = links if ts == list(range(Lt)) else links.index_select(0, torch.as_tensor(ts, device=self.device))
-            poly = polynomial_degree if (polynomial_degree > 0 and lambda_cut > 0) else 0
-            evals, planes, stats = lanczos_tr(sel, self.latt_size, self.Ne, max(self.tol, 1e-12) if poly else self.tol,
-                                              ncv=self.ncv, poly_deg=poly, lambda_cut=lambda_cut if poly else 0.0)
-            self.last_stats = {k: stats[k] for k in ("restarts", "matvecs", "converged")}
+            sel = links if idx is None else links.index_select(0, idx)
+            if self.stencil_precision == "fp32":
+                # mixed solve: complex64 stencil in a loose FP64 iteration, then the FP64 Chebyshev refinement
+                l32 = self._links(torch.complex64)
+                l32 = l32 if idx is None else l32.index_select(0, idx)
+                evals, planes, stats = lanczos_tr(sel, self.latt_size, self.Ne, self.tol, ncv=self.ncv,
+                                                  poly_deg=polynomial_degree if polynomial_degree > 0 else 0,
+                                                  lambda_cut=lambda_cut if lambda_cut > 0 else 0.0,
+                                                  stencil_precision="fp32", links_c64=l32)
+            else:
+                poly = polynomial_degree if (polynomial_degree > 0 and lambda_cut > 0) else 0
+                evals, planes, stats = lanczos_tr(sel, self.latt_size, self.Ne,
+                                                  max(self.tol, 1e-12) if poly else self.tol, ncv=self.ncv,
+                                                  poly_deg=poly, lambda_cut=lambda_cut if poly else 0.0)
+            self.last_stats = {k: v for k, v in stats.items() if k != "ncv"}
             evecs = planes.reshape(B, self.Ne, n)
             if apply_renorm_phase:
                 LZ.renorm_phase_(evecs)

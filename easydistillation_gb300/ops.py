@@ -199,33 +199,55 @@ def laplacian_status():
 
 
 def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int = None, max_restarts: int = None,
-               poly_deg: int = 0, lambda_cut: float = 0.0):
-    """Native batched thick-restart Lanczos (``ed_lanczos_tr``) for the lowest
-    ``Ne`` eigenpairs of the FP64 Laplacian of every timeslice of
-    ``links_soa`` (complex128 ``[nt, 27, V3]``).  Returns (evals ``[nt, Ne]``
-    float64 ascending, evecs ``[nt, Ne, 3, V3]`` complex128 colour planes,
-    stats ``{"converged", "restarts", "matvecs"}``)."""
+               poly_deg: int = 0, lambda_cut: float = 0.0, stencil_precision: str = "fp64",
+               links_c64: torch.Tensor = None):
+    """Native batched thick-restart Lanczos (``ed_lanczos_tr`` /
+    ``ed_lanczos_tr_ex``) for the lowest ``Ne`` eigenpairs of the FP64
+    Laplacian of every timeslice of ``links_soa`` (complex128 ``[nt, 27, V3]``).
+
+    ``stencil_precision="fp32"`` runs the mixed solve: the complex64 stencil
+    on ``links_c64`` (complex64 SoA of the same links) inside a loose FP64
+    thick-restart iteration, then an FP64 Chebyshev-filtered refinement whose
+    cut comes from it (``poly_deg``: its degree, 0 = 16; ``lambda_cut`` <= 0:
+    automatic).  Returns (evals ``[nt, Ne]`` float64 ascending, evecs
+    ``[nt, Ne, 3, V3]`` complex128 colour planes, stats ``{"converged",
+    "restarts", "matvecs", ...}``)."""
     require_cuda(links_soa, "links")
     if links_soa.dtype != torch.complex128:
         raise ValueError("the native Lanczos works on complex128 links")
+    if stencil_precision not in ("fp64", "fp32"):
+        raise ValueError("stencil_precision must be 'fp64' or 'fp32'")
     Lx, Ly, Lz = (int(v) for v in latt_size[:3])
     nt, V3 = links_soa.shape[0], Lx * Ly * Lz
     if tuple(links_soa.shape[1:]) != (27, V3):
         raise ValueError("links must be [nt, 27, Lx*Ly*Lz]")
     n = 3 * V3
+    mixed = stencil_precision == "fp32"
     if ncv is None:
-        ncv = min(max(2 * Ne if poly_deg > 0 else 9 * Ne // 4, Ne + 32), n - 1)
+        ncv = min(max(2 * Ne if (poly_deg > 0 and not mixed) else 9 * Ne // 4, Ne + 32), n - 1)
     if max_restarts is None:
         max_restarts = max(30, 10 * n // max(1, ncv - Ne))
-    nbytes = ctypes.c_size_t()
-    call("ed_lanczos_workspace", Lx, Ly, Lz, nt, Ne, ncv, ctypes.byref(nbytes))
-    ws = torch.empty(nbytes.value, dtype=torch.uint8, device=links_soa.device)
     evecs = torch.empty((nt, Ne, 3, V3), dtype=torch.complex128, device=links_soa.device)
     evals = torch.empty((nt, Ne), dtype=torch.float64, device=links_soa.device)
-    st = (ctypes.c_int * 3)()
-    call("ed_lanczos_tr", Lx, Ly, Lz, nt, ptr(links_soa), Ne, float(tol), ncv, max_restarts, int(poly_deg),
-         float(lambda_cut), ptr(evecs), ptr(evals), st, ptr(ws), ws.numel(), stream_handle())
-    return evals, evecs, {"converged": bool(st[0]), "restarts": int(st[1]), "matvecs": int(st[2]), "ncv": ncv}
+    nbytes = ctypes.c_size_t()
+    if not mixed:
+        call("ed_lanczos_workspace", Lx, Ly, Lz, nt, Ne, ncv, ctypes.byref(nbytes))
+        ws = torch.empty(nbytes.value, dtype=torch.uint8, device=links_soa.device)
+        st = (ctypes.c_int * 3)()
+        call("ed_lanczos_tr", Lx, Ly, Lz, nt, ptr(links_soa), Ne, float(tol), ncv, max_restarts, int(poly_deg),
+             float(lambda_cut), ptr(evecs), ptr(evals), st, ptr(ws), ws.numel(), stream_handle())
+        return evals, evecs, {"converged": bool(st[0]), "restarts": int(st[1]), "matvecs": int(st[2]), "ncv": ncv}
+    if links_c64 is None or links_c64.dtype != torch.complex64 or tuple(links_c64.shape) != tuple(links_soa.shape):
+        raise ValueError("the fp32 stencil needs links_c64: complex64 SoA links of the same shape")
+    require_cuda(links_c64, "links_c64")
+    call("ed_lanczos_workspace_ex", Lx, Ly, Lz, nt, Ne, ncv, ED_C64, ctypes.byref(nbytes))
+    ws = torch.empty(nbytes.value, dtype=torch.uint8, device=links_soa.device)
+    st = (ctypes.c_int * 6)()
+    call("ed_lanczos_tr_ex", Lx, Ly, Lz, nt, ptr(links_soa), ptr(links_c64), ED_C64, Ne, float(tol), ncv,
+         max_restarts, int(poly_deg), float(lambda_cut), ptr(evecs), ptr(evals), st, ptr(ws), ws.numel(),
+         stream_handle())
+    return evals, evecs, {"converged": bool(st[0]), "restarts": int(st[1]), "matvecs": int(st[2]), "ncv": ncv,
+                          "matvecs_fp32": int(st[3]), "matvecs_fp64": int(st[4]), "restarts_fp32": int(st[5])}
 
 
 def cgs_pass(V: torch.Tensor, r: int, w: torch.Tensor, h: torch.Tensor = None, norm: bool = False):

@@ -186,6 +186,30 @@ int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, dou
                   int poly_deg, double lambda_cut, void* evecs, double* evals, int* status, void* workspace,
                   size_t workspace_bytes, void* stream);
 
+/* ed_lanczos_tr with a choice of stencil precision.  stencil_prec = ED_C128 is
+ * ed_lanczos_tr (links_c64 unused).  ED_C64 is a mixed-precision solve of the
+ * same eigenpairs: phase 1 runs the thick-restart iteration with the complex64
+ * stencil on links_c64 (complex64 SoA [nt][27][V3], ed_links_to_soa) applied
+ * to the FP64 basis vectors (rounded to complex64, the result widened),
+ * while Gram-Schmidt, Rayleigh-Ritz and the convergence test stay FP64, to a
+ * tolerance of max(tol, 1e-4); phase 2 refines every pair in FP64: a
+ * Chebyshev-filtered FP64-stencil solve (degree poly_deg, 16 when 0; Krylov
+ * dimension max(2 Ne, Ne + 32)) whose cut is lambda_cut, or when lambda_cut
+ * <= 0, 1.15 x the largest phase-1 eigenvalue of any timeslice, started from
+ * the sum of the phase-1 Ritz vectors, to tol.  ncv is the Krylov dimension of
+ * phase 1.  The outputs are those of ed_lanczos_tr (FP64 eigenpairs;
+ * eigenvalues are FP64 Rayleigh quotients after phase 2).  status (host,
+ * int[6]): converged, total restarts, total operator applications, phase-1
+ * (complex64) applications, phase-2 (FP64) applications, phase-1 restarts.
+ * Lx must be even for ED_C64.  Synchronises the stream once per restart and
+ * once between the phases.  The reference's eigsh is FP64 throughout
+ * (lattice/generator/eigenvector.py:234-257); the precision split has no
+ * counterpart there.  Needs ed_lanczos_workspace_ex bytes. */
+int ed_lanczos_workspace_ex(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, int stencil_prec, size_t* bytes);
+int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* links, const void* links_c64, int stencil_prec,
+                     int Ne, double tol, int ncv, int max_restarts, int poly_deg, double lambda_cut, void* evecs,
+                     double* evals, int* status, void* workspace, size_t workspace_bytes, void* stream);
+
 int ed_arrow_eigh_workspace(int B, int m, int nwant, size_t* bytes);
 int ed_arrow_eigh(int B, int m, int ka, int nwant, const double* d, const double* s, const double* e,
                   double* evals, double* evecs, void* workspace, size_t workspace_bytes, void* stream);

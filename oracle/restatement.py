@@ -38,6 +38,8 @@ __all__ = [
     "covariant_derivative",
     "elemental",
     "elemental_pair_terms",
+    "elemental_items",
+    "elemental_item_into",
     "blending_coeff",
     "displacement_elemental",
     "eigensolve",
@@ -224,6 +226,34 @@ def blending_coeff(Ne: int, dilution) -> np.ndarray:
     return coeff
 
 
+def elemental_items(num_nabla: int):
+    """The work items of one reference timeslice in its loop order
+    (``lattice/generator/elemental.py:299-321``): one ``(operator, coeff,
+    left_chain, right_chain)`` per derivative operator and left/right subset
+    (43 items for ``num_nabla = 2``)."""
+    return [(di, coeff, left, right) for di in range(num_derivative(num_nabla))
+            for coeff, left, right in elemental_pair_terms(derivative(di))]
+
+
+def elemental_item_into(out, Vc, U_t, item, phases, stocastic_coeff=None):
+    """Add one work item of ``ElementalGenerator.calc`` into ``out``
+    (``lattice/generator/elemental.py:320-337``): build its two chains from the
+    (complex64-rounded, complex128) vectors ``Vc`` as the reference does, then
+    one phase-weighted zgemm per momentum."""
+    di, coeff, left_chain, right_chain = item
+    Ne = Vc.shape[0]
+    right = nD(Vc, U_t, right_chain).reshape(Ne, -1)
+    left = nD(Vc, U_t, left_chain)
+    for pi, ph in enumerate(phases):
+        # opt_einsum evaluates "zyx,ezyxc,fzyxc->ef" as an elementwise
+        # phase * conj(left) followed by a tensordot (zgemm).
+        lp = (coeff * ph[None, :, :, :, None] * left.conj()).reshape(Ne, -1)
+        blk = lp @ right.T
+        if stocastic_coeff is not None:
+            blk = blk * stocastic_coeff
+        out[di, pi] += blk
+
+
 def elemental(
     V: np.ndarray,
     U_t: np.ndarray,
@@ -246,22 +276,11 @@ def elemental(
         V = np.asarray(V).astype(np.complex64)
     Vc = V.astype(np.complex128)
     Ne = V.shape[0]
-    nder = num_derivative(num_nabla)
     nmom = len(momentum_list)
     phases = [momentum_phase(latt_size, p) for p in momentum_list]
-    out = np.zeros((nder, nmom, Ne, Ne), np.complex128)
-    for di in range(nder):
-        for coeff, left_chain, right_chain in elemental_pair_terms(derivative(di)):
-            right = nD(Vc, U_t, right_chain).reshape(Ne, -1)
-            left = nD(Vc, U_t, left_chain)
-            for pi, ph in enumerate(phases):
-                # opt_einsum evaluates "zyx,ezyxc,fzyxc->ef" as an elementwise
-                # phase * conj(left) followed by a tensordot (zgemm).
-                lp = (coeff * ph[None, :, :, :, None] * left.conj()).reshape(Ne, -1)
-                blk = lp @ right.T
-                if stocastic_coeff is not None:
-                    blk = blk * stocastic_coeff
-                out[di, pi] += blk
+    out = np.zeros((num_derivative(num_nabla), nmom, Ne, Ne), np.complex128)
+    for item in elemental_items(num_nabla):
+        elemental_item_into(out, Vc, U_t, item, phases, stocastic_coeff)
     return out
 
 

@@ -82,3 +82,28 @@ def test_config1_elementals():
         res[mode] = o
     err = float(torch.linalg.vector_norm(res["f16x3"] - res["fp64"]) / torch.linalg.vector_norm(res["fp64"]))
     assert err <= 1e-6, err
+
+
+def test_config1_mixed_precision_eigensolve():
+    """The complex64 stencil inside the native thick-restart iteration, then the
+    FP64 Chebyshev refinement (ed_lanczos_tr_ex): the same eigenpairs as ARPACK
+    to check (a)'s tolerances, and fewer FP64 operator applications than the
+    plain FP64 solve needs."""
+    from easydistillation_gb300 import EigenvectorGenerator
+
+    gauge = _gauge()
+    U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
+    gen = EigenvectorGenerator(LATT, MemGauge(gauge), NE, 1e-10, stencil_precision="fp32")
+    gen.load("cfg1")
+    X, lam = (a.cpu().numpy() for a in gen.calc(0))
+    st = gen.last_stats
+    assert st["converged"] and st["matvecs_fp32"] > 0 and st["matvecs_fp64"] > 0
+    rv, re = R.eigensolve(U, LATT, NE, 1e-10)
+    np.testing.assert_allclose(lam, re, rtol=1e-10, atol=0)
+    Xf = X.reshape(NE, -1)
+    res = np.linalg.norm(R.laplacian(Xf.T, U, LATT).T - lam[:, None] * Xf, axis=1)
+    assert res.max() < 1e-9
+    assert np.abs(Xf.conj() @ Xf.T - np.eye(NE)).max() < 1e-12
+    Xt = torch.from_numpy(Xf).cuda()
+    Rt = torch.from_numpy(np.ascontiguousarray(rv.reshape(NE, -1))).cuda()
+    assert float((Xt.T @ Xt.conj() - Rt.T @ Rt.conj()).abs().max()) < 1e-7
