@@ -62,7 +62,117 @@ __global__ void __launch_bounds__(128) link_grad_kernel(Latt L, int d, int nvec,
   }
 }
 
+// Adjoint seeds of the pair contraction G_p(X, Y)[i, j] = sum_k conj(X_i[k]) phase_p(k) Y_j[k]
+// (the GEMM of lattice/generator/elemental.py:324-329).  With the gradient Gbar of a pair,
+//   grad Y_j[k] = sum_p sum_i Gbar_p[i][j] X_i[k] conj(phase_p(k))
+//   grad X_i[k] = sum_p sum_j conj(Gbar_p[i][j]) Y_j[k] phase_p(k).
+// Both are one gather-GEMM  out[a][k] += sum_r M[r][a] * Z_r[k] * psi_r(k)  over rows r, each
+// naming a chain vector Z_r = chains[cx[r]][ir[r]] and a phase psi_r = phase_p (pr[r] = p) or
+// conj(phase_p) (pr[r] = -p - 1); M[r][a] carries Gbar (or its conjugate transpose) and the
+// rows of every (partner chain, momentum) a chain takes part in are stacked into one call.
+// 256 threads as 16 x 16, each owning 4 x 4 complex outputs of a 64 (a) x 64 (k) tile; 8 rows
+// per shared-memory stage.  FP64 arithmetic, the FP64 pipe bounds it like the forward GEMM.
+constexpr int ADJ_BK = 8, ADJ_TM = 4, ADJ_TN = 4, ADJ_BM = 16 * ADJ_TM, ADJ_BN = 16 * ADJ_TN;
+
+__global__ void __launch_bounds__(256) chain_adjoint_kernel(int Ne, int V3, int nchain, int nmom, int R,
+                                                            const cplx<double>* __restrict__ M,
+                                                            const int* __restrict__ cx, const int* __restrict__ ir,
+                                                            const int* __restrict__ pr,
+                                                            const cplx<double>* __restrict__ chains,
+                                                            const cplx<double>* __restrict__ phases,
+                                                            cplx<double>* __restrict__ out) {
+  __shared__ cplx<double> Ms[ADJ_BK][ADJ_BM + 1];
+  __shared__ cplx<double> Zs[ADJ_BK][ADJ_BN + 1];
+  const long long K = 3LL * V3;
+  const int a0 = blockIdx.y * ADJ_BM;
+  const long long k0 = (long long)blockIdx.x * ADJ_BN;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int lr = tid >> 5, lc = tid & 31;  // loader: row lr of the stage, 32 consecutive columns x 2 passes
+  cplx<double> acc[ADJ_TM][ADJ_TN];
+#pragma unroll
+  for (int u = 0; u < ADJ_TM; ++u)
+#pragma unroll
+    for (int v = 0; v < ADJ_TN; ++v) acc[u][v] = mk(0.0, 0.0);
+  for (int r0 = 0; r0 < R; r0 += ADJ_BK) {
+    const int r = r0 + lr;
+    bool rok = r < R;
+    const cplx<double>* zrow = nullptr;
+    int p = 0;
+    bool cj = false;
+    if (rok) {
+      const int c = cx[r], i = ir[r], q = pr[r];
+      cj = q < 0;
+      p = cj ? -q - 1 : q;
+      // a row naming a chain, vector or momentum out of range contributes nothing
+      rok = c >= 0 && c < nchain && i >= 0 && i < Ne && p < nmom;
+      if (rok) zrow = chains + ((long long)c * Ne + i) * K;
+    }
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      const int c = lc + 32 * pass;
+      const int a = a0 + c;
+      Ms[lr][c] = (rok && a < Ne) ? ld(M + (long long)r * Ne + a) : mk(0.0, 0.0);
+      const long long k = k0 + c;
+      cplx<double> z = mk(0.0, 0.0);
+      if (rok && k < K) {
+        const cplx<double> ph = ld(phases + (long long)p * V3 + (k % V3));
+        const cplx<double> x = ld(zrow + k);
+        z = cj ? cmul_conj(ph, x) : x * ph;
+      }
+      Zs[lr][c] = z;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < ADJ_BK; ++kk) {
+      cplx<double> mv[ADJ_TM], zv[ADJ_TN];
+#pragma unroll
+      for (int u = 0; u < ADJ_TM; ++u) mv[u] = Ms[kk][ty + 16 * u];
+#pragma unroll
+      for (int v = 0; v < ADJ_TN; ++v) zv[v] = Zs[kk][tx + 16 * v];
+#pragma unroll
+      for (int u = 0; u < ADJ_TM; ++u)
+#pragma unroll
+        for (int v = 0; v < ADJ_TN; ++v) cfma(acc[u][v], mv[u], zv[v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < ADJ_TM; ++u) {
+    const int a = a0 + ty + 16 * u;
+    if (a >= Ne) continue;
+#pragma unroll
+    for (int v = 0; v < ADJ_TN; ++v) {
+      const long long k = k0 + tx + 16 * v;
+      if (k < K) {
+        cplx<double>* o = out + (long long)a * K + k;
+        *o = *o + acc[u][v];
+      }
+    }
+  }
+}
+
 }  // namespace ed
+
+extern "C" int ed_chain_adjoint(int Lx, int Ly, int Lz, int Ne, int nchain, int nmom, int R, const void* M,
+                                const int* cx, const int* ir, const int* pr, const void* chains, const void* phases,
+                                void* out, void* stream) {
+  ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nchain > 0 && nmom > 0 && R >= 0,
+               "ed_chain_adjoint: sizes must be positive");
+  ED_CHECK_ARG(M && cx && ir && pr && chains && phases && out, "ed_chain_adjoint: null pointer");
+  ED_CHECK_ARG(((uintptr_t)M % 16) == 0 && ((uintptr_t)chains % 16) == 0 && ((uintptr_t)phases % 16) == 0 &&
+                   ((uintptr_t)out % 16) == 0,
+               "ed_chain_adjoint: complex buffers must be 16-byte aligned");
+  if (R == 0) return ED_OK;
+  const long long K = 3LL * Lx * Ly * Lz;
+  ED_CHECK_ARG(K / ed::ADJ_BN + 1 < (1LL << 31) && Ne <= 65535 * ed::ADJ_BM, "ed_chain_adjoint: too large");
+  dim3 grid((unsigned)ed::ceil_div(K, ed::ADJ_BN), (unsigned)ed::ceil_div(Ne, ed::ADJ_BM));
+  ed::chain_adjoint_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(
+      Ne, Lx * Ly * Lz, nchain, nmom, R, (const ed::cplx<double>*)M, cx, ir, pr, (const ed::cplx<double>*)chains,
+      (const ed::cplx<double>*)phases, (ed::cplx<double>*)out);
+  ED_RETURN_LAUNCH("chain adjoint");
+  return ED_OK;
+}
 
 extern "C" int ed_link_grad(int Lx, int Ly, int Lz, int dir, int nvec, double alpha, double beta, const void* wbar,
                             const void* f, void* grad_links, void* stream) {

@@ -262,18 +262,23 @@ __device__ __forceinline__ bool st_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool st_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait: false when the barrier has not flipped within `limit` cycles.  The staged kernels take
+// the limit of their data waits as a launch argument (ed_laplacian_wait_limit, default LT_WAIT_CYCLES);
+// the waits that drain their own copies in flight before a block leaves always use LT_WAIT_CYCLES.
+__device__ __forceinline__ bool st_wait(uint64_t* bar, uint32_t parity, long long limit = LT_WAIT_CYCLES) {
   if (st_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (!st_try_wait(bar, parity))
-    if (clock64() - t0 > LT_WAIT_CYCLES) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
+long long g_stencil_wait_cycles = LT_WAIT_CYCLES;  // host-side launch setting
 
 __global__ void __launch_bounds__(LT_THREADS) laplacian_tma_kernel(const __grid_constant__ CUtensorMap fmap, Latt L,
                                                                    int zb, const cplx<float>* __restrict__ links,
                                                                    long long link_tstride, cplx<float>* __restrict__ out,
-                                                                   long long out_tstride, float diag, int slot_bytes) {
+                                                                   long long out_tstride, float diag, int slot_bytes,
+                                                                   long long wait_cycles) {
   extern __shared__ __align__(128) uint8_t sm[];
   uint64_t* bar = (uint64_t*)(sm + LT_SLOTS * slot_bytes);
   __shared__ int failed;
@@ -313,7 +318,7 @@ __global__ void __launch_bounds__(LT_THREADS) laplacian_tma_kernel(const __grid_
     const int jc = z - z0 + 1;
     if (threadIdx.x == 0)
       for (int j = jc - 1; j <= jc + 1; ++j)
-        if (!st_wait(&bar[j % LT_SLOTS], (j / LT_SLOTS) & 1)) failed = 1;
+        if (!st_wait(&bar[j % LT_SLOTS], (j / LT_SLOTS) & 1, wait_cycles)) failed = 1;
     __syncthreads();
     if (failed) break;
     const float2* Fm = (const float2*)(sm + ((jc - 1) % LT_SLOTS) * slot_bytes);  // [c][y][x]
@@ -478,7 +483,7 @@ __global__ void __launch_bounds__(LS_MAX_SITES, 2)
     laplacian_strip_kernel(const __grid_constant__ CUtensorMap mL27, const __grid_constant__ CUtensorMap mL9,
                            const __grid_constant__ CUtensorMap mLz, const __grid_constant__ CUtensorMap mF,
                            const __grid_constant__ CUtensorMap mFh, Latt L, int R, int zb,
-                           cplx<float>* __restrict__ out, long long out_tstride, float diag) {
+                           cplx<float>* __restrict__ out, long long out_tstride, float diag, long long wait_cycles) {
   extern __shared__ __align__(128) uint8_t sm[];
   const int Lx = L.Lx, Ly = L.Ly, Lz = L.Lz, V3 = L.V3(), P = Lx * Ly, RLx = R * Lx;
   const LsGeom g = ls_geom(RLx, Lx);
@@ -534,8 +539,8 @@ __global__ void __launch_bounds__(LS_MAX_SITES, 2)
     const uint8_t* Sm = sm + ((jc - 1) % LS_SLOTS) * g.bytes;
     const uint8_t* Sc = sm + (jc % LS_SLOTS) * g.bytes;
     const uint8_t* Sp = sm + ((jc + 1) % LS_SLOTS) * g.bytes;
-    ok = ok && st_wait(&bar[(jc - 1) % LS_SLOTS], ((jc - 1) / LS_SLOTS) & 1) &&
-         st_wait(&bar[jc % LS_SLOTS], (jc / LS_SLOTS) & 1);
+    ok = ok && st_wait(&bar[(jc - 1) % LS_SLOTS], ((jc - 1) / LS_SLOTS) & 1, wait_cycles) &&
+         st_wait(&bar[jc % LS_SLOTS], (jc / LS_SLOTS) & 1, wait_cycles);
     cplx<float> hop[3] = {mk(0.f, 0.f), mk(0.f, 0.f), mk(0.f, 0.f)};
     if (active && ok) {  // backward z: U_z(z-1)^dag F(z-1)
       cplx<float> u[9], f[3];
@@ -551,7 +556,7 @@ __global__ void __launch_bounds__(LS_MAX_SITES, 2)
       issue(jc + 2);
       issued_hi = jc + 2;
     }
-    ok = st_wait(&bar[(jc + 1) % LS_SLOTS], ((jc + 1) / LS_SLOTS) & 1);
+    ok = st_wait(&bar[(jc + 1) % LS_SLOTS], ((jc + 1) / LS_SLOTS) & 1, wait_cycles);
     if (active && ok) {
       cplx<float> u[9], f[3], f0[3];
 #pragma unroll
@@ -648,7 +653,8 @@ static int launch_laplacian_tma(Latt L, int nt, int nvec, const void* links, con
   const int nslab = ceil_div(L.Lz, zb);
   dim3 grid(nslab, nvec, nt);
   laplacian_tma_kernel<<<grid, LT_THREADS, smem, stream>>>(map, L, zb, (const cplx<float>*)links, 27LL * L.V3(),
-                                                           (cplx<float>*)out, ots, 6.0f, slot_bytes);
+                                                           (cplx<float>*)out, ots, 6.0f, slot_bytes,
+                                                           g_stencil_wait_cycles);
   ED_RETURN_LAUNCH("laplacian (TMA-staged)");
   return ED_OK;
 }
@@ -706,7 +712,7 @@ static int launch_laplacian_strip(Latt L, int nt, int nvec, const void* links, c
   dim3 grid(nstrip * nslab, nvec, nt);
   const int threads = (RLx + 31) / 32 * 32;
   laplacian_strip_kernel<<<grid, threads, smem, stream>>>(mL27, mL9, mLz, mF, mFh, L, R, zb, (cplx<float>*)out, ots,
-                                                          6.0f);
+                                                          6.0f, g_stencil_wait_cycles);
   ED_RETURN_LAUNCH("laplacian (strip-staged)");
   return ED_OK;
 }
@@ -798,6 +804,12 @@ extern "C" int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, 
 extern "C" int ed_laplacian_config(int use_tma) {
   ED_CHECK_ARG(use_tma >= 0 && use_tma <= 2, "ed_laplacian_config: use_tma must be 0, 1 or 2");
   ed::g_stencil_tma = use_tma;
+  return ED_OK;
+}
+
+extern "C" int ed_laplacian_wait_limit(long long cycles) {
+  ED_CHECK_ARG(cycles >= 0, "ed_laplacian_wait_limit: negative limit");
+  ed::g_stencil_wait_cycles = cycles > 0 ? cycles : ed::LT_WAIT_CYCLES;
   return ED_OK;
 }
 

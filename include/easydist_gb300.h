@@ -134,6 +134,15 @@ int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, const void*
  * falls back to 0.  Process-wide setting.  No counterpart in the reference. */
 int ed_laplacian_config(int use_tma);
 
+/* Cycle limit of the TMA-staged Laplacian kernels' waits for their data
+ * (process-wide launch setting; 0 restores the default of 4e9 cycles, about
+ * 2 s).  A wait that runs out sets the status word of ed_laplacian_status and
+ * the block stops computing; it still waits for its own copies in flight,
+ * with the default limit, before it leaves.  A tiny limit makes the waits run
+ * out on purpose (a test of the timeout path).  No counterpart in the
+ * reference. */
+int ed_laplacian_wait_limit(long long cycles);
+
 /* Status of the TMA-staged Laplacian's bounded waits since the last call
  * (synchronises `stream`): ED_OK, or ED_ERR_TIMEOUT when a wait gave up (the
  * output of that launch is invalid).  The status word is cleared. */
@@ -191,8 +200,9 @@ int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, dou
  * same eigenpairs: phase 1 runs the thick-restart iteration with the complex64
  * stencil on links_c64 (complex64 SoA [nt][27][V3], ed_links_to_soa) applied
  * to the FP64 basis vectors (rounded to complex64, the result widened),
- * while Gram-Schmidt, Rayleigh-Ritz and the convergence test stay FP64, to a
- * tolerance of max(tol, 1e-4); phase 2 refines every pair in FP64: a
+ * while Gram-Schmidt, Rayleigh-Ritz and the convergence test stay FP64, for at
+ * most 3 restarts or to a tolerance of max(tol, 1e-3) (it only has to bound
+ * the wanted spectrum from above); phase 2 refines every pair in FP64: a
  * Chebyshev-filtered FP64-stencil solve (degree poly_deg, 16 when 0; Krylov
  * dimension max(2 Ne, Ne + 32)) whose cut is lambda_cut, or when lambda_cut
  * <= 0, 1.15 x the largest phase-1 eigenvalue of any timeslice, started from
@@ -249,6 +259,20 @@ int ed_mean_c128(int nsrc, long long n, long long src_stride, const void* src, v
  * No counterpart in the reference (it has no gradients). */
 int ed_link_grad(int Lx, int Ly, int Lz, int dir, int nvec, double alpha, double beta, const void* wbar,
                  const void* f, void* grad_links, void* stream);
+
+/* Adjoint seeds of the pair contraction (the backward pass of the GEMM of
+ * lattice/generator/elemental.py:324-329; the reference has no gradients):
+ *   out[a][k] += sum_{r < R} M[r][a] * chains[cx[r]][ir[r]][k] * psi_r(k)
+ * with psi_r = phase_p (pr[r] = p >= 0) or conj(phase_p) (pr[r] = -p-1), and
+ * k = colour*V3 + site.  For G_p(X, Y)[i][j] = sum_k conj(X_i[k]) phase_p(k) Y_j[k]
+ * and a loss gradient Gbar_p: grad Y = rows (X, p, i) with M = Gbar_p[i][.]
+ * and conj phases; grad X = rows (Y, p, j) with M = conj(Gbar_p[.][j]) and
+ * phases.  M: device [R][Ne] complex128; cx, ir, pr: device int[R] (rows
+ * naming anything out of range contribute nothing); chains: colour planes
+ * [nchain][Ne][3][V3] complex128; phases: [nmom][V3] complex128; out:
+ * [Ne][3][V3] complex128, accumulated.  FP64. */
+int ed_chain_adjoint(int Lx, int Ly, int Lz, int Ne, int nchain, int nmom, int R, const void* M, const int* cx,
+                     const int* ir, const int* pr, const void* chains, const void* phases, void* out, void* stream);
 
 /* ---- elementals (ElementalGenerator.calc, lattice/generator/elemental.py:290-338) */
 typedef struct ed_elemental_plan ed_elemental_plan;

@@ -61,6 +61,30 @@ def test_elemental_adjoint_matches_einsum_autograd(d, p):
     assert torch.linalg.vector_norm(g1 - g2) / torch.linalg.vector_norm(g2) < 1e-11
 
 
+def test_all_elementals_adjoint_matches_einsum_autograd():
+    """Every operator of num_nabla = 2 and a momentum list closed under p -> -p
+    (the plan then takes half the pairs from hermiticity): forward through the
+    library's elemental plan, backward through the library's adjoint kernels,
+    against torch autograd of the einsum/roll form of the reference."""
+    from easydistillation_gb300.autograd import elementals
+
+    latt = [4, 6, 4, 1]
+    Ne = 4
+    moms = [(0, 0, 0), (1, 0, -1), (-1, 0, 1), (0, 1, 0), (0, -1, 0)]
+    U = torch.from_numpy(R.synthetic_gauge(latt, 0.3, 13).transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0].copy()).cuda()
+    V = torch.from_numpy(R.random_colour_vectors(Ne, latt, 14)).cuda()
+    Vr = V.to(torch.complex64).to(torch.complex128)
+    G = torch.randn((13, len(moms), Ne, Ne), dtype=torch.complex128, device="cuda")
+    U1 = U.clone().requires_grad_(True)
+    E1 = elementals(U1, V, latt, 2, moms)
+    U2 = U.clone().requires_grad_(True)
+    E2 = torch.stack([torch.stack([_torch_elemental(U2, Vr, latt, d, p) for p in moms]) for d in range(13)])
+    assert torch.linalg.vector_norm(E1 - E2) / torch.linalg.vector_norm(E2) < 1e-12
+    (E1 * G.conj()).real.sum().backward()
+    (E2 * G.conj()).real.sum().backward()
+    assert torch.linalg.vector_norm(U1.grad - U2.grad) / torch.linalg.vector_norm(U2.grad) < 1e-11
+
+
 def test_correlator_loss_gradients_vs_finite_differences():
     from easydistillation_gb300.autograd import correlator_log_ratio
     from easydistillation_gb300.correlator import gamma

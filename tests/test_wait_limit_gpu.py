@@ -1,0 +1,50 @@
+"""Failure detection without a GPU fault: the TMA-staged complex64 Laplacian
+bounds every wait for its data.  With a one-cycle limit (a launch setting)
+the waits run out on purpose: the launch must report ED_ERR_TIMEOUT through
+the status word, leave the context usable (every block still drains its own
+copies in flight before it leaves), and the next launch with the default
+limit must be clean and correct."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import restatement as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("variant", [2, 1])  # 2: strip-staged (default), 1: input planes staged
+def test_staged_laplacian_timeout_is_reported_and_recovers(variant):
+    from easydistillation_gb300 import _lib
+    from easydistillation_gb300.ops import laplacian, laplacian_config, links_to_soa
+
+    latt = [16, 16, 16, 2]
+    V3 = 16 ** 3
+    gauge = R.synthetic_gauge(latt, 0.3, 77)
+    U = torch.from_numpy(np.ascontiguousarray(gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3])).cuda()
+    links = links_to_soa(U, latt, dtype=torch.complex64)
+    F = torch.randn((2, 1, 3, V3), dtype=torch.complex64, device="cuda")
+    code = ctypes.c_int(0)
+    try:
+        laplacian_config(variant)
+        assert _lib.lib().ed_laplacian_status(ctypes.byref(code), _lib.stream_handle()) == _lib.ED_OK  # clean start
+        _lib.check(_lib.lib().ed_laplacian_wait_limit(1), "ed_laplacian_wait_limit")
+        laplacian(links, F, latt)
+        rc = _lib.lib().ed_laplacian_status(ctypes.byref(code), _lib.stream_handle())
+        assert rc == _lib.ED_ERR_TIMEOUT and code.value != 0
+        assert "gave up" in _lib.last_error()
+    finally:
+        _lib.lib().ed_laplacian_wait_limit(0)
+        laplacian_config(2)
+    # the status word was cleared by the read; the context is usable and the next launch is exact
+    out = laplacian(links, F, latt)
+    assert _lib.lib().ed_laplacian_status(ctypes.byref(code), _lib.stream_handle()) == _lib.ED_OK and code.value == 0
+    U64 = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3]
+    for t in range(2):
+        f = F[t, 0].cpu().numpy().astype(np.complex128)  # colour planes [3, V3]
+        ref = R.laplacian(f.T.reshape(-1), U64[:, t], latt).reshape(V3, 3).T
+        got = out[t, 0].cpu().numpy()
+        assert np.abs(got - ref).max() < 2e-5 * np.abs(ref).max()
