@@ -589,8 +589,13 @@ extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int val
       plan->tc_grid = value;
       return ED_OK;
     case ED_TUNE_TC_STAGES:
-      ED_CHECK_ARG(value == 0 || value == 2 || value == 3, "ed_elemental_set_tuning: %d stages (0, 2 or 3)", value);
+      ED_CHECK_ARG(value == 0 || value == 2 || value == 3 || value == 4,
+                   "ed_elemental_set_tuning: %d stages (0, 2, 3 or 4)", value);
       plan->tc_stages = value;
+      return ED_OK;
+    case ED_TUNE_TC_PAIR:
+      ED_CHECK_ARG(value >= 0 && value <= 2, "ed_elemental_set_tuning: SM pairing %d (0, 1 or 2)", value);
+      plan->tc_pair = value;
       return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_set_tuning: unknown key %d", key);
@@ -612,6 +617,9 @@ extern "C" int ed_elemental_get_tuning(const ed_elemental_plan* plan, int key, i
       return ED_OK;
     case ED_TUNE_TC_STAGES:
       *value = plan->tc_stages;
+      return ED_OK;
+    case ED_TUNE_TC_PAIR:
+      *value = plan->tc_pair;
       return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_get_tuning: unknown key %d", key);

@@ -60,7 +60,8 @@ struct ed_elemental_plan {
   int f64_tile = 0;    // FP64 pair GEMM tile, rows x cols: 0 = 64x64, 1 = 32x64, 2 = 64x32, 3 = 32x32
   int tc_slab_kb = 0;  // k-blocks per lock-step slab of the factorised GEMM (0 = TC_FLUSH_KB)
   int tc_grid = 0;     // CTAs of the persistent factorised GEMM (0 = every co-resident CTA)
-  int tc_stages = 0;   // 64 KB operand stages of the factorised GEMM: 2 or 3 (0 = the default, 2)
+  int tc_stages = 0;   // operand stages of the factorised GEMM (0 = the default of the GEMM form)
+  int tc_pair = 0;     // factorised GEMM on single SMs (1) or on SM pairs (2); 0 = the built-in default
 };
 
 namespace ed {

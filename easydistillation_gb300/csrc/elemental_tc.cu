@@ -315,6 +315,7 @@ __global__ void tc_phase_kernel(const cplx<double>* __restrict__ ph, long long n
 
 #include "tc_pair_gemm.cuh"
 #include "tc_fac_gemm.cuh"
+#include "tc_fac2_gemm.cuh"
 #include "tc_ozaki_gemm.cuh"
 
 // ------------------------------------------------------------ factorised-phase operands
@@ -698,6 +699,98 @@ static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, lo
   return ED_OK;
 }
 
+// The factorised-phase GEMM on SM pairs (tc_fac2_gemm_kernel): the same job table with 256-row A tiles, a
+// cooperative launch of two-CTA clusters, every cluster co-resident.
+template <int KIND>
+static int launch_fac_pairs(const ed_elemental_plan* P, const FacLayout& lay, void* apl, void* bpl, TcScalars* sc,
+                            float4* DF, cplx<double>* G, cudaStream_t stream, int nb) {
+  const long long K = 3LL * P->V3;
+  const int pxy = P->fac_pxy, pz = P->fac_pz, Ne = P->Ne, nl = (int)P->fac_lchain.size();
+  int rc;
+  CUtensorMap amap, bmap, bmap16;
+  if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra))) return rc;                 // 128-row A halves
+  if ((rc = encode_kmajor(&bmap, KIND, bpl, K, lay.rb, TC_BN / 2))) return rc;      // 64-row B halves
+  if ((rc = encode_kmajor(&bmap16, KIND, bpl, K, lay.rb, 16))) return rc;          // narrow last column tile
+  TcFacTable tab;
+  tab.njobs = nb * P->jobs_per_t;
+  tab.pxy = pxy;
+  tab.pz = pz;
+  for (int q = 0; q < kMaxFac; ++q) tab.pidx[q] = q < pxy * pz ? P->fac_pidx[q] : (signed char)-1;
+  for (int k = 0; k < tab.njobs; ++k) {
+    const Job& j = P->jobs[k];
+    const int b = k / P->jobs_per_t;
+    const int slot = b * nl + P->fac_lslot[P->jobs[k % P->jobs_per_t].left];
+    TcFacJob& d = tab.j[k];
+    d.arow0 = j.right0 * pz * Ne;
+    d.brow0 = slot * pxy * Ne;
+    d.nright = j.nright;
+    d.g_off = j.g_off;
+    d.mt = (int)ceil_div((long long)j.nright * pz * Ne, TCP_BM);
+    d.nt = (int)ceil_div((long long)pxy * Ne, TC_BN);
+  }
+  // a last column tile of at most 96 valid columns runs narrow (N rounded up to 32, 16-row B boxes)
+  const int last_cols = pxy * Ne - (tab.j[0].nt - 1) * TC_BN;
+  const bool narrow = ((last_cols + 31) & ~31) < TC_BN;
+  int tiles = 0, tiles_n = 0;
+  for (int k = 0; k < tab.njobs; ++k) {
+    TcFacJob& d = tab.j[k];
+    d.tile0 = tiles;
+    tiles += d.mt * (d.nt - (narrow ? 1 : 0));
+    d.tile0n = tiles_n;
+    tiles_n += narrow ? d.mt : 0;
+  }
+  tab.nfull = tiles;
+  tiles += tiles_n;
+  const int nst = P->tc_stages > 0 ? std::min(P->tc_stages, TCP_MAX_STAGES) : TCP_DEFAULT_STAGES;
+  cudaError_t e;
+  static bool attr_set[4] = {};
+  if (!attr_set[KIND]) {
+    e = cudaFuncSetAttribute(tc_fac2_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tcp_smem(TCP_MAX_STAGES));
+    if (e != cudaSuccess) return cuda_status(e, "paired tc kernel smem attribute");
+    attr_set[KIND] = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeCooperative;
+  attr[1].val.cooperative = 1;
+  cfg.blockDim = dim3(TC_THREADS);
+  cfg.dynamicSmemBytes = tcp_smem(nst);
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3(2 * num_sms());
+  int clusters = 0;
+  e = cudaOccupancyMaxActiveClusters(&clusters, tc_fac2_gemm_kernel<KIND>, &cfg);
+  if (e != cudaSuccess) return cuda_status(e, "paired tc kernel cluster occupancy");
+  if (clusters < 1) {
+    set_error("the paired factorised tensor-core GEMM does not fit on the device");
+    return ED_ERR_UNSUPPORTED;
+  }
+  // persistent grid: every cluster co-resident (the step counter of the kernel relies on it)
+  int pairs = std::min(tiles, clusters);
+  if (P->tc_grid > 0) pairs = std::max(1, std::min(pairs, P->tc_grid / 2));
+  cfg.gridDim = dim3(2 * pairs);
+  cfg.numAttrs = 2;
+  const int slab_kb = P->tc_slab_kb > 0 ? P->tc_slab_kb : TC_FLUSH_KB;
+  const long long g_used = (long long)nb * P->g_per_t;
+  e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
+  if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
+  if (P->prof_start) cudaEventRecord(P->prof_start, stream);
+  e = cudaLaunchKernelEx(&cfg, tc_fac2_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb,
+                         nst);
+  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
+  if (e != cudaSuccess) return cuda_status(e, "paired factorised-phase GEMM launch");
+  ED_RETURN_LAUNCH("paired factorised-phase GEMM");
+  tc_df_to_c128_kernel<<<8 * num_sms(), 256, 0, stream>>>(DF, g_used, G);
+  ED_RETURN_LAUNCH("double-float to complex128");
+  return ED_OK;
+}
+
 // Factorised-phase path: factor tables, left/right variant planes, one GEMM
 // launch over all groups of the nb timeslices, double-float -> complex128.
 template <int KIND>
@@ -747,6 +840,8 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   tc_fac_split_kernel<KIND, false, kSplitUnrollRight><<<dim3(kxr, std::min(rrows, 65535)), 256, 0, stream>>>(
       chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
   ED_RETURN_LAUNCH("variant planes");
+
+  if (P->tc_pair == 2) return launch_fac_pairs<KIND>(P, lay, apl, bpl, sc, DF, G, stream, nb);
 
   CUtensorMap amap, bmap, bmap16;
   if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra))) return rc;
@@ -810,7 +905,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(TC_THREADS);
-  const int nst = P->tc_stages > 0 ? P->tc_stages : TCF_DEFAULT_STAGES;
+  const int nst = P->tc_stages > 0 ? std::min(P->tc_stages, TCF_MAX_STAGES) : TCF_DEFAULT_STAGES;
   cfg.dynamicSmemBytes = tcf_smem(nst);
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];

@@ -262,10 +262,29 @@ __device__ __forceinline__ bool st_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ bool st_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(st_smem(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
 // Bounded wait: false when the barrier has not flipped within `limit` cycles.  The staged kernels take
 // the limit of their data waits as a launch argument (ed_laplacian_wait_limit, default LT_WAIT_CYCLES);
 // the waits that drain their own copies in flight before a block leaves always use LT_WAIT_CYCLES.
+// try_wait may suspend the thread until the phase completes (up to a hardware time limit), so a limit
+// below LT_SHORT_WAIT is polled with the non-suspending test_wait: such a limit then runs out whenever
+// the data is not there yet, however close it is.
+constexpr long long LT_SHORT_WAIT = 100000;
 __device__ __forceinline__ bool st_wait(uint64_t* bar, uint32_t parity, long long limit = LT_WAIT_CYCLES) {
+  if (limit < LT_SHORT_WAIT) {
+    const long long t0 = clock64();
+    while (!st_test_wait(bar, parity))
+      if (clock64() - t0 > limit) return false;
+    return true;
+  }
   if (st_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (!st_try_wait(bar, parity))

@@ -80,8 +80,12 @@ extern "C" {
                               * the FP32 sums. */
 #define ED_TUNE_TC_GRID 3    /* CTAs of the persistent factorised GEMM: 0 (default: every CTA that
                               * fits on the device at once) or an upper bound on that number */
-#define ED_TUNE_TC_STAGES 4  /* 64 KB operand stages in the factorised GEMM's shared-memory ring: 0
-                              * (default, 2), 2 or 3 */
+#define ED_TUNE_TC_STAGES 4  /* operand stages in the factorised GEMM's shared-memory ring: 0 (the
+                              * default of the GEMM form), 2 or 3 (64 KB stages on single SMs), up to
+                              * 4 (48 KB stages on SM pairs) */
+#define ED_TUNE_TC_PAIR 5    /* factorised GEMM form: 0 (built-in default), 1 = one CTA per SM with
+                              * 128 x 128 tiles, 2 = two-CTA clusters on SM pairs with 256 x 128
+                              * tiles (tcgen05.mma.cta_group::2) */
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);
