@@ -597,6 +597,11 @@ extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int val
       ED_CHECK_ARG(value >= 0 && value <= 2, "ed_elemental_set_tuning: SM pairing %d (0, 1 or 2)", value);
       plan->tc_pair = value;
       return ED_OK;
+    case ED_TUNE_TC_KPB:
+      ED_CHECK_ARG(value >= 0 && value <= 2, "ed_elemental_set_tuning: %d k-blocks per TMEM buffer (0, 1 or 2)",
+                   value);
+      plan->tc_kpb = value;
+      return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_set_tuning: unknown key %d", key);
   }
@@ -620,6 +625,9 @@ extern "C" int ed_elemental_get_tuning(const ed_elemental_plan* plan, int key, i
       return ED_OK;
     case ED_TUNE_TC_PAIR:
       *value = plan->tc_pair;
+      return ED_OK;
+    case ED_TUNE_TC_KPB:
+      *value = plan->tc_kpb;
       return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_get_tuning: unknown key %d", key);

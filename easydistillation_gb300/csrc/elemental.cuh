@@ -62,6 +62,7 @@ struct ed_elemental_plan {
   int tc_grid = 0;     // CTAs of the persistent factorised GEMM (0 = every co-resident CTA)
   int tc_stages = 0;   // operand stages of the factorised GEMM (0 = the default of the GEMM form)
   int tc_pair = 0;     // factorised GEMM on single SMs (1) or on SM pairs (2); 0 = the built-in default
+  int tc_kpb = 0;      // k-blocks accumulated per TMEM buffer of the factorised GEMM: 1 or 2 (0 = 1)
 };
 
 namespace ed {

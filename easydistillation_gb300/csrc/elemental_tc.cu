@@ -781,8 +781,9 @@ static int launch_fac_pairs(const ed_elemental_plan* P, const FacLayout& lay, vo
   e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
+  const int kpb = P->tc_kpb > 0 ? P->tc_kpb : 1;
   e = cudaLaunchKernelEx(&cfg, tc_fac2_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb,
-                         nst);
+                         nst, kpb);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "paired factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("paired factorised-phase GEMM");
@@ -914,7 +915,9 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb, nst);
+  const int kpb = P->tc_kpb > 0 ? P->tc_kpb : 1;
+  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb, nst,
+                         kpb);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");

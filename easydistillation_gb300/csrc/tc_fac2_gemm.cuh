@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fac2_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
                         const __grid_constant__ CUtensorMap bmap16, const __grid_constant__ TcFacTable tab, int Ne,
                         int V3, TcScalars* __restrict__ sc, float4* __restrict__ DF, int ntiles, int slab_kb,
-                        int nst) {
+                        int nst, int kpb) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;
   constexpr int KINST = 32 / ESZ;
@@ -256,7 +256,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else if (warp == 1) {
       // ===================== MMA issuer (leader CTA only; same product order as the single-SM kernel)
       if (leader && lane == 0) {
-        long long g = 0;
+        long long g = 0;   // stages consumed
+        long long gb = 0;  // TMEM buffers filled (kpb k-blocks each, fewer at the end of a step)
         bool ok = true;
         for (int q = 0; q < nsteps && ok; ++q) {
           const int tile = step_tile(q);
@@ -266,12 +267,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t nfield = (uint32_t)(tile_cols(ntile) >> 3) << 17;
           const uint32_t ID = (IDESC & ~(0x3Fu << 17)) | nfield, ID_NEG = (IDESC_NEG & ~(0x3Fu << 17)) | nfield;
           const int kb1 = step_kb1(q);
-          for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
+          const int kb0s = step_kb0(q);
+          for (int kb = kb0s; kb < kb1; ++kb, ++g) {
             const int s = (int)(g % nst);
-            const int b = (int)(g & 1);
+            const int b = (int)(gb & 1);
+            const bool first = (kb - kb0s) % kpb == 0;  // the first k-block of a TMEM buffer
+            const bool last = (kb - kb0s) % kpb == kpb - 1 || kb == kb1 - 1;
             if (!mbar_wait_cluster(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL) ||
-                (g >= 2 &&
-                 !mbar_wait_cluster(&acce[b], (uint32_t)(((g >> 1) + 1) & 1), status, TC_ERR_ACCE))) {
+                (first && gb >= 2 &&
+                 !mbar_wait_cluster(&acce[b], (uint32_t)(((gb >> 1) + 1) & 1), status, TC_ERR_ACCE))) {
               ok = false;
               break;
             }
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint32_t d_re = tmem + b * 256, d_im = d_re + TC_BN;
 #pragma unroll
             for (int ks = 0; ks < KE / KINST; ++ks) {
-              const uint32_t acc = ks > 0 ? 1u : 0u;
+              const uint32_t acc = (ks > 0 || !first) ? 1u : 0u;
               const uint32_t ao = a0 + ks * 32, bo = b0 + ks * 32;
               const uint64_t A0 = umma_desc_sw64(ao), A1 = umma_desc_sw64(ao + TC_BM * TC_ROWB);
               const uint64_t A2 = umma_desc_sw64(ao + 2 * TC_BM * TC_ROWB),
@@ -309,7 +313,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               umma2<KIND>(d_im, A2, B0, ID, 1u);
             }
             umma2_commit_both(&empty[s]);  // frees the stage in both CTAs when these MMAs complete
-            umma2_commit_both(&accf[b]);   // both CTAs' halves of the buffer are ready to drain
+            if (last) {
+              umma2_commit_both(&accf[b]);  // both CTAs' halves of the buffer are ready to drain
+              ++gb;
+            }
           }
         }
         umma2_commit_both(mma_done);  // arrives in both CTAs once every MMA issued above has completed
@@ -339,7 +346,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
       for (int c = 0; c < 64; ++c) sre[c] = sim[c] = 0.f;
       const int kb1 = step_kb1(q);
-      for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
+      for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one TMEM buffer of kpb k-blocks
         const int b = (int)(g & 1);
         if (!warp_wait(&accf[b], (uint32_t)((g >> 1) & 1), status, TC_ERR_ACC)) {
           ok = false;

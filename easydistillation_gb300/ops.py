@@ -355,7 +355,7 @@ def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
 MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3, "ozaki_i8": 4}
 _FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR = 0x100, 0x200
 #: plan launch settings (ED_TUNE_* keys)
-TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4, "tc_pair": 5}
+TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4, "tc_pair": 5, "tc_kpb": 6}
 #: FP64 pair GEMM tile shapes (rows, cols) by ED_TUNE_F64_TILE value
 F64_TILES = {0: (64, 64), 1: (32, 64), 2: (64, 32), 3: (32, 32)}
 

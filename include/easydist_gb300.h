@@ -86,6 +86,11 @@ extern "C" {
 #define ED_TUNE_TC_PAIR 5    /* factorised GEMM form: 0 (built-in default), 1 = one CTA per SM with
                               * 128 x 128 tiles, 2 = two-CTA clusters on SM pairs with 256 x 128
                               * tiles (tcgen05.mma.cta_group::2) */
+#define ED_TUNE_TC_KPB 6     /* k-blocks the factorised GEMM accumulates in one TMEM buffer before the
+                              * drain warps read it: 0 (default, 1) or 2.  The tensor core's FP32
+                              * accumulation truncates, so longer buffers trade accuracy (measured
+                              * at 32^3, Ne = 200, f16x3: 2.0e-7 -> 5.1e-7 vs FP64) for half the
+                              * buffer hand-overs */
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);

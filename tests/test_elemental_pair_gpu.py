@@ -68,3 +68,40 @@ def test_pair_gemm_long_k_and_slabs():
     assert plan.check_status() == 0
     ref = R.elemental(evec[0], gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0], latt, 2, moms)
     assert rel_err(out.cpu().numpy(), ref) < 1e-6
+
+
+@pytest.mark.parametrize("pair", [1, 2])
+def test_two_kblocks_per_tmem_buffer(pair):
+    """ED_TUNE_TC_KPB = 2: each TMEM buffer accumulates two k-blocks before it
+    is drained; still within 1e-6 of FP64.  K = 3 * 16*16*12 = 9216 is 288
+    f16 k-blocks: lock steps of 256 + 32 (default slab) or 4 x 64 + 32."""
+    from easydistillation_gb300.ops import ElementalPlan
+
+    latt, Ne = [16, 16, 12, 1], 30
+    moms = R.mom_dict_to_list(3)
+    gauge, evec, U, V = _inputs(latt, Ne, 47)
+    V3 = 16 * 16 * 12
+    ref = R.elemental(evec[0], gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0], latt, 2, moms)
+    for slab in (0, 64):
+        out = torch.empty((13, 27, Ne, Ne), dtype=torch.complex128, device="cuda")
+        plan = ElementalPlan(latt, Ne, 2, moms, "f16x3", tuning={"tc_pair": pair, "tc_kpb": 2, "tc_slab_kb": slab})
+        plan.run(U[:, 0], V3 * 9, 9, V[0], out)
+        assert plan.check_status() == 0
+        assert rel_err(out.cpu().numpy(), ref) < 1e-6
+
+
+def test_two_kblocks_per_buffer_odd_block_count():
+    """An odd number of k-blocks per lock step: K = 3 * 4*4*2 = 96 is 3 f16
+    k-blocks, so the step ends with a buffer of one k-block."""
+    from easydistillation_gb300.ops import ElementalPlan
+
+    latt, Ne = [4, 4, 2, 1], 5
+    moms = R.mom_dict_to_list(3)
+    gauge, evec, U, V = _inputs(latt, Ne, 49)
+    ref = R.elemental(evec[0], gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0], latt, 2, moms)
+    for pair in (1, 2):
+        out = torch.empty((13, 27, Ne, Ne), dtype=torch.complex128, device="cuda")
+        plan = ElementalPlan(latt, Ne, 2, moms, "f16x3", tuning={"tc_pair": pair, "tc_kpb": 2})
+        plan.run(U[:, 0], 32 * 9, 9, V[0], out)
+        assert plan.check_status() == 0
+        assert rel_err(out.cpu().numpy(), ref) < 1e-6
