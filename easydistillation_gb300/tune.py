@@ -10,8 +10,11 @@ choices whose best value depends on the shape:
   the requested momenta, slower per product);
 * the K-slab length of the persistent factorised GEMM's lock-step schedule
   (shorter slabs keep the CTAs closer together in K, for L2 reuse of the
-  operand rows, at the cost of more result flushes) and its number of
-  operand stages (2 or 3 of 64 KB);
+  operand rows, at the cost of more result flushes), its number of operand
+  stages, whether it runs on single SMs (128 x 128 tiles) or on SM pairs
+  (two-CTA clusters, 256 x 128 tiles), and how many k-blocks it accumulates
+  in one TMEM buffer (1, or 2: half the buffer hand-overs, a larger FP32
+  accumulation error, gated by the tolerance below);
 * the tile shape of the FP64 pair GEMM (an Ne that is not a multiple of 64
   wastes part of every 64-row tile);
 * the complex64 Laplacian kernel: neighbours read through L1/L2, or input
@@ -267,15 +270,28 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
         forms = factorise_options(latt_size, Ne, num_nabla, moms, mode)
         stages.append(lambda best: [Candidate(f, {}) for f in forms])
 
-        def slabs(best: Candidate) -> List[Candidate]:
+        def factorised(best: Candidate) -> bool:
             probe = ElementalPlan(latt_size, Ne, num_nabla, moms, mode, device="cpu", batch=batch,
                                   factorise=best.factorise)
-            if probe.factorised is None or mode == "ozaki_i8":
-                return []
-            return ([best] + [Candidate(best.factorise, {"tc_slab_kb": s}) for s in SLABS[1:]] +
-                    [Candidate(best.factorise, {"tc_stages": 3}),
-                     Candidate(best.factorise, {"tc_stages": 3, "tc_slab_kb": SLABS[1]})])
+            return probe.factorised is not None and mode != "ozaki_i8"
 
+        def forms_on_sms(best: Candidate) -> List[Candidate]:
+            # the factorised GEMM on single SMs or on SM pairs, each with 1 or 2 k-blocks per TMEM buffer
+            if not factorised(best):
+                return []
+            return [Candidate(best.factorise, dict(t)) for t in
+                    ({}, {"tc_kpb": 2}, {"tc_pair": 2}, {"tc_pair": 2, "tc_kpb": 2})]
+
+        def slabs(best: Candidate) -> List[Candidate]:
+            if not factorised(best):
+                return []
+            base = dict(best.tuning)
+            more_stages = 4 if base.get("tc_pair") == 2 else 3
+            return ([best] + [Candidate(best.factorise, {**base, "tc_slab_kb": s}) for s in SLABS[1:]] +
+                    [Candidate(best.factorise, {**base, "tc_stages": more_stages}),
+                     Candidate(best.factorise, {**base, "tc_stages": more_stages, "tc_slab_kb": SLABS[1]})])
+
+        stages.append(forms_on_sms)
         stages.append(slabs)
     res = _run_search(stages, Candidate(True, {}), measure, _rel_err, TOLERANCE[mode])
     cache.put(dev, key, {"best": res.best.as_dict(), "ms": res.ms, "trials": res.trials,
