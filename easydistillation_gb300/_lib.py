@@ -65,6 +65,7 @@ _SIGNATURES = {
         _i,
     ),
     "ed_link_grad": ([_i, _i, _i, _i, _i, _c.c_double, _c.c_double, _vp, _vp, _vp, _vp], _i),
+    "ed_twopoint_trace": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
     "ed_chain_adjoint": ([_i, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
     "ed_parallel_transport": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
     "ed_mean_c128": ([_i, _ll, _ll, _vp, _vp, _vp], _i),

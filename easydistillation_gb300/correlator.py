@@ -211,12 +211,47 @@ def _right_blocks(tau: torch.Tensor, psi: torch.Tensor, gidx: int) -> torch.Tens
     return out
 
 
-def _source_terms(tau, tau_bw, phis, t_src, dts=None, mode="trace"):
-    """All operators for one source timeslice.  ``tau``/``tau_bw``:
-    ``[T, 4, 4, Ne, Ne]`` at the sink times; ``phis``: per operator
-    ``(gammas, elementals)`` with elementals ``[X, Lt, Ne, Ne]``.
-    mode "trace": ``[Nop, T]``; "profile": ``[Nop, T, Ne, Ne]`` (indices a, d);
-    "diagonal": ``[Nop, T, Ne]``."""
+_G5 = (1.0, 1.0, -1.0, -1.0)  # the diagonal of gamma(15) in the reference's basis
+
+
+def _trace_terms(tau, taub, el, gid, t_src):
+    """``out[t]`` of one operator (parts with gamma indices ``gid``) through
+    ``ed_twopoint_trace``: one term per (sink part x, source part y, spin i,
+    spin k) with j the row of gamma_x holding column k, l the row of the source
+    gamma holding column i, coef = gamma_x[j][k] G_y[l][i] g5[i] g5[j]."""
+    from . import _lib
+
+    T, Ne, Lt = tau.shape[0], tau.shape[-1], el.shape[1]
+    idx, coef = [], []
+    for x, gx in enumerate(gid):
+        cx, vx = _monomial(gx, False)
+        for y, gy in enumerate(gid):
+            cy, vy = _monomial(gy, True)
+            for i in range(4):
+                l = cy.index(i)
+                for k in range(4):
+                    j = cx.index(k)
+                    c = vx[j] * vy[l] * _G5[i] * _G5[j]
+                    idx.append((x, y, i, j, k, l))
+                    coef.append((c.real, c.imag))
+    dev = tau.device
+    idx_t = torch.tensor(idx, dtype=torch.int32, device=dev)
+    coef_t = torch.tensor(coef, dtype=torch.float64, device=dev)
+    out = torch.zeros(T, dtype=torch.complex128, device=dev)
+    tau, taub = tau.contiguous(), taub.contiguous()
+    _lib.call("ed_twopoint_trace", T, Ne, Lt, int(t_src), len(gid), len(idx), _lib.ptr(idx_t), _lib.ptr(coef_t),
+              _lib.ptr(tau), _lib.ptr(taub), _lib.ptr(el), _lib.ptr(out), _lib.stream_handle())
+    return out
+
+
+def _source_terms(tau, taub, phis, t_src, dts=None, mode="trace"):
+    """All operators for one source timeslice.  ``tau``: the source's
+    perambulator ``[T, 4, 4, Ne, Ne]`` at the sink times, ``taub`` the one of
+    the backward propagator (``tau`` itself or ``perambulator_bw``); ``phis``:
+    per operator ``(gammas, elementals)`` with elementals ``[X, Lt, Ne, Ne]``.
+    mode "trace" (the library's ``ed_twopoint_trace``): ``[Nop, T]``;
+    "profile": ``[Nop, T, Ne, Ne]`` (indices a, d); "diagonal": ``[Nop, T, Ne]``."""
+    tau_bw = _backward(taub) if mode != "trace" else None
     out = []
     for gammas, el in phis:
         gid = [_gamma_index(g) for g in gammas]
@@ -225,13 +260,7 @@ def _source_terms(tau, tau_bw, phis, t_src, dts=None, mode="trace"):
             sink = sink[:, dts]
         psi = el[:, t_src].conj()
         if mode == "trace":
-            acc = 0
-            lefts = [_left_blocks(tau_bw, sink[x], gid[x]) for x in range(len(gid))]
-            for y in range(len(gid)):
-                R = _right_blocks(tau, psi[y], gid[y])  # [t, k, i, c, a]
-                for L in lefts:  # [t, i, k, a, c]
-                    acc = acc + torch.einsum("tikac,tkica->t", L, R)
-            out.append(acc)
+            out.append(_trace_terms(tau, taub, el.contiguous(), gid, t_src))
         elif mode == "profile":
             # C[t, a, d] = psi[a, d] sum_{i,l} G[l, i] (left . tau)[t][(i, a), (l, d)]
             acc = 0
@@ -279,7 +308,7 @@ def twopoint(operators: List[Operator], elemental, perambulator, timeslices: Ite
     for it, t_src in enumerate(ts):
         tau = _peram_block(perambulator, t_src, slice(None), usedNe, device)
         src_bw = tau if perambulator_bw is None else _peram_block(perambulator_bw, t_src, slice(None), usedNe, device)
-        ret[:, it] = _source_terms(tau, _backward(src_bw), phis, t_src)
+        ret[:, it] = _source_terms(tau, src_bw, phis, t_src)
     ret = -ret.mean(1) if is_sum_over_source_t else -ret
     return to_backend(ret)
 
@@ -302,8 +331,7 @@ def twopoint_profile(operators: List[Operator], elemental, perambulator, timesli
     for it, t_src in enumerate(ts):
         tau = _peram_block(perambulator, t_src, dts, usedNe, device)
         src_bw = tau if perambulator_bw is None else _peram_block(perambulator_bw, t_src, dts, usedNe, device)
-        ret[:, it] = _source_terms(tau, _backward(src_bw), phis, t_src, dts,
-                                   "diagonal" if is_diagonal else "profile")
+        ret[:, it] = _source_terms(tau, src_bw, phis, t_src, dts, "diagonal" if is_diagonal else "profile")
     ret = -ret.mean(1) if is_sum_over_source_t else -ret
     return to_backend(ret)
 
@@ -341,5 +369,5 @@ def twopoint_assembled(phis: Sequence[Tuple[torch.Tensor, torch.Tensor]], peramb
         tau = torch.as_tensor(perambulator[t_src]).to(dev)
         if usedNe is not None:
             tau = tau[..., :usedNe, :usedNe]
-        ret[:, it] = _source_terms(tau, _backward(tau), phis, t_src)
+        ret[:, it] = _source_terms(tau, tau, phis, t_src)
     return -ret.mean(1) if is_sum_over_source_t else -ret

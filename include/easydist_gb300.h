@@ -283,6 +283,27 @@ int ed_link_grad(int Lx, int Ly, int Lz, int dir, int nvec, double alpha, double
 int ed_chain_adjoint(int Lx, int Ly, int Lz, int Ne, int nchain, int nmom, int R, const void* M, const int* cx,
                      const int* ir, const int* pr, const void* chains, const void* phases, void* out, void* stream);
 
+/* ---- correlators (lattice/correlator/one_particle.py) */
+
+/* One source timeslice of the meson two-point contraction
+ * "tijab,xjk,xtbc,tklcd,yli,yad->t" of lattice/correlator/one_particle.py:64-72,
+ * accumulated into out[t] (complex128, t < T) without the overall minus sign:
+ *   out[t] += sum_terms coef * Tr[ conj(taub[t][j][i])^T E_x(t_src + t mod Lt) tau[t][k][l] conj(E_y(t_src))^T ]
+ * tau, taub: device [T][4][4][Ne][Ne] complex128 (the perambulator of the
+ * source at the sink times, and the one of the backward propagator: tau
+ * itself, or perambulator_bw); el: device [nparts][Lt][Ne][Ne] complex128
+ * (the operator's assembled elementals, lattice/data.py:7-33); term_idx:
+ * device int[nterm][6] = (x, y, i, j, k, l), term_coef: device
+ * [nterm][2] doubles: one term per (part x, part y, spin i, spin k), with j
+ * the row of the sink gamma whose non-zero is in column k, l the row of the
+ * source gamma g4 Gamma^dag g4 whose non-zero is in column i, and coef the
+ * product of those two entries and of g5[i][i] g5[j][j] (every gamma of the
+ * reference's table is monomial).  Terms naming an index out of range
+ * contribute nothing.  FP64. */
+int ed_twopoint_trace(int T, int Ne, int Lt, int t_src, int nparts, int nterm, const int* term_idx,
+                      const double* term_coef, const void* tau, const void* taub, const void* el, void* out,
+                      void* stream);
+
 /* ---- elementals (ElementalGenerator.calc, lattice/generator/elemental.py:290-338) */
 typedef struct ed_elemental_plan ed_elemental_plan;
 
