@@ -121,9 +121,13 @@ class ElementalsFunction(torch.autograd.Function):
         links = links_to_soa(U_t.detach().unsqueeze(1).contiguous(), list(latt[:3]) + [1])[0]
         chains = _chains(links, V_ref, latt, nchain)  # recomputed, not stored by the forward pass
         phases = momentum_phases(latt, moms, dev).reshape(nmom, V3)
-        # loss gradient of every ordered chain pair, summed over the operator terms that use it
+        # loss gradient of every ordered chain pair, summed over the operator terms that use it; operators whose
+        # gradient is zero (a loss built from a few elementals) contribute no pairs
+        live = (Ebar.abs().amax(dim=(1, 2, 3)) > 0).tolist()
         gbar: Dict[Tuple[int, int], torch.Tensor] = {}
         for d in range(nchain):
+            if not live[d]:
+                continue
             for coeff, lseq, rseq in _subset_terms(derivative(d)):
                 key = (_chain_id(lseq), _chain_id(rseq))
                 term = coeff * Ebar[d]
