@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="build the plans with the built-in defaults instead of the autotuner's choice (which is "
                          "measured before the timed region and cached per device and shape)")
+    ap.add_argument("--tuning", default="",
+                    help="explicit plan launch settings for --no-autotune runs, e.g. tc_kpb=2,tc_pair=1 (profiling)")
     ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
     ap.add_argument("--stencil", action="store_true",
                     help="measure only the Laplacian kernels (c64, c64 TMA-staged, c128) at --lattice")
@@ -81,6 +83,15 @@ def parse():
     ap.add_argument("--grad", action="store_true",
                     help="measure the correlator-loss gradient (24^3x48, Ne=100) with a finite-difference check")
     return ap.parse_args()
+
+
+def parse_tuning(text):
+    """``key=value,...`` plan settings (``ElementalPlan.set_tuning`` names) -> dict."""
+    out = {}
+    for item in filter(None, (t.strip() for t in text.split(","))):
+        k, v = item.split("=")
+        out[k.strip()] = int(v)
+    return out
 
 
 def launches_per_step(mode, B=1, factorised=False):
@@ -402,7 +413,8 @@ def run_ours(args, rank, world):
         plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=res.best.factorise,
                              tuning=res.best.tuning)
     else:
-        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=not args.no_factor)
+        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=not args.no_factor,
+                             tuning=parse_tuning(args.tuning))
     outs = [torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev) for _ in range(B)]
     out = outs[0]
     stream = torch.cuda.current_stream()
