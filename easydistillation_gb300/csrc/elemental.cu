@@ -198,7 +198,7 @@ int plan_build(ed_elemental_plan* P) {
   P->off_g = off;
   off = up(off + (size_t)P->g_elems * 16);
   P->off_extra = off;
-  off = up(off + tc_extra_workspace(P));
+  off = up(off + tc_extra_workspace(P) + f64_extra_workspace(P));
   P->ws_bytes = off;
   return ED_OK;
 }
@@ -215,6 +215,9 @@ struct GemmTable {
 };
 
 constexpr int F64_BK = 8;
+constexpr long long F64_MIN_KCHUNK = 1024;  // k per K-split partial, at least
+constexpr long long F64_SPLIT_TARGET = 320;  // CTAs the K split aims at (about two per SM)
+constexpr int F64_KSPLIT_MAX = 16;
 
 // One CTA = a (16*TM) x (16*TN) tile of G_p(X, Y-range) for one (group,
 // momentum).  256 threads as 16x16, each owning TM x TN complex outputs.  The
@@ -226,7 +229,8 @@ template <int TM, int TN>
 __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int Ne, int V3, int nmom,
                                                             const cplx<double>* __restrict__ chains,
                                                             const cplx<double>* __restrict__ phases,
-                                                            cplx<double>* __restrict__ G) {
+                                                            cplx<double>* __restrict__ G, long long kchunk,
+                                                            long long part_stride) {
   constexpr int BM = 16 * TM, BN = 16 * TN;
   __shared__ cplx<double> As[F64_BK][BM + 1];
   __shared__ cplx<double> Bs[F64_BK][BN + 1];
@@ -241,6 +245,9 @@ __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int N
   const int mtile = local / J.nt;
   const int ntile = local - mtile * J.nt;
   const long long K = 3LL * V3;
+  // K split: CTA (tile, blockIdx.y) sums k in [k_begin, k_end) into partial blockIdx.y (one partial: G itself)
+  const long long k_begin = blockIdx.y * kchunk, k_end = min(K, k_begin + kchunk);
+  G += blockIdx.y * part_stride;
   const int M = Ne, N = J.nright * Ne;
   const cplx<double>* Lc = chains + (long long)J.left * Ne * K;
   const cplx<double>* Rc = chains + (long long)J.right0 * Ne * K;
@@ -255,16 +262,16 @@ __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int N
 #pragma unroll
     for (int b = 0; b < TN; ++b) acc[a][b] = mk(0.0, 0.0);
 
-  for (long long k0 = 0; k0 < K; k0 += F64_BK) {
+  for (long long k0 = k_begin; k0 < k_end; k0 += F64_BK) {
     const long long k = k0 + lk;
     cplx<double> phk = mk(0.0, 0.0);
-    if (k < K) phk = ld(ph + (k % V3));
+    if (k < k_end) phk = ld(ph + (k % V3));
 #pragma unroll
     for (int pass = 0; pass < BM / 32; ++pass) {
       const int r = lr + 32 * pass;
       const int gi = mtile * BM + r;
       cplx<double> a = mk(0.0, 0.0);
-      if (gi < M && k < K) a = cmul_conj(ld(Lc + (long long)gi * K + k), phk);
+      if (gi < M && k < k_end) a = cmul_conj(ld(Lc + (long long)gi * K + k), phk);
       As[lk][r] = a;
     }
 #pragma unroll
@@ -272,7 +279,7 @@ __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int N
       const int r = lr + 32 * pass;
       const int gj = ntile * BN + r;
       cplx<double> b = mk(0.0, 0.0);
-      if (gj < N && k < K) b = ld(Rc + (long long)gj * K + k);
+      if (gj < N && k < k_end) b = ld(Rc + (long long)gj * K + k);
       Bs[lk][r] = b;
     }
     __syncthreads();
@@ -351,8 +358,18 @@ __global__ void combine_kernel(const CombineTable tab, const cplx<double>* __res
 
 // ------------------------------------------------------------ run
 
+// G[i] = sum over the K-split partials, in a fixed order (results do not depend on scheduling)
+__global__ void f64_reduce_kernel(const cplx<double>* __restrict__ part, long long stride, int nsplit, long long n,
+                                  cplx<double>* __restrict__ G) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    cplx<double> s = part[i];
+    for (int q = 1; q < nsplit; ++q) s = s + part[q * stride + i];
+    G[i] = s;
+  }
+}
+
 int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains, const cplx<double>* phases,
-                         cplx<double>* G, cudaStream_t stream, int njobs) {
+                         cplx<double>* G, cudaStream_t stream, int njobs, void* extra) {
   // tile shapes of ED_TUNE_F64_TILE: rows x cols = 64x64, 32x64, 64x32, 32x32
   static const int kBM[4] = {64, 32, 64, 32}, kBN[4] = {64, 64, 32, 32};
   const int shape = P->f64_tile;
@@ -375,11 +392,40 @@ int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains,
               : shape == 1 ? pair_gemm_f64_kernel<2, 4>
               : shape == 2 ? pair_gemm_f64_kernel<4, 2>
                            : pair_gemm_f64_kernel<2, 2>;
+  // Few output tiles (few momenta, small Ne) leave most SMs idle over a long K: split K into partials, summed in
+  // a fixed order afterwards, up to the plan's partial buffers and at least F64_MIN_KCHUNK k per part.
+  const long long K = 3LL * P->V3;
+  int nsplit = std::min<long long>(P->f64_ksplit, std::max<long long>(1, K / F64_MIN_KCHUNK));
+  nsplit = std::max(1, std::min(nsplit, ceil_div(2LL * num_sms(), tiles)));
+  const long long kchunk = (ceil_div(K, nsplit) + F64_BK - 1) / F64_BK * F64_BK;
+  nsplit = ceil_div(K, kchunk);
+  const long long g_used = njobs > 0 ? P->jobs[njobs - 1].g_off +
+                                           (long long)P->nmom * P->Ne * P->jobs[njobs - 1].nright * P->Ne
+                                     : 0;
+  cplx<double>* part = nsplit > 1 ? (cplx<double>*)extra : G;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  kern<<<tiles, 256, 0, stream>>>(tab, P->Ne, P->V3, P->nmom, chains, phases, G);
-  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
+  kern<<<dim3(tiles, nsplit), 256, 0, stream>>>(tab, P->Ne, P->V3, P->nmom, chains, phases, part, kchunk, g_used);
   ED_RETURN_LAUNCH("pair GEMM (fp64)");
+  if (nsplit > 1) {
+    const int grid = (int)std::min<long long>(ceil_div(g_used, 256), 4LL * 1024 * num_sms());
+    f64_reduce_kernel<<<grid, 256, 0, stream>>>(part, g_used, nsplit, g_used, G);
+    ED_RETURN_LAUNCH("pair GEMM (fp64) partial sum");
+  }
+  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   return ED_OK;
+}
+
+// K-split partial buffers an FP64 plan reserves: as many as it takes to give about 320 CTAs with the
+// 64 x 64 tiles (the fewest), at most 16, none when the tiles already fill the device.
+size_t f64_extra_workspace(ed_elemental_plan* P) {
+  P->f64_ksplit = 1;
+  if (P->mode != ED_MODE_FP64) return 0;
+  long long tiles = 0;
+  for (size_t k = 0; k < P->jobs.size(); ++k)
+    tiles += (long long)ceil_div(P->Ne, 64) * ceil_div((long long)P->jobs[k].nright * P->Ne, 64) * P->nmom;
+  if (tiles >= F64_SPLIT_TARGET || 3LL * P->V3 < 2 * F64_MIN_KCHUNK) return 0;
+  P->f64_ksplit = (int)std::min<long long>(F64_KSPLIT_MAX, ceil_div(F64_SPLIT_TARGET, std::max(1LL, tiles)));
+  return (size_t)P->f64_ksplit * (size_t)P->g_elems * sizeof(cplx<double>);
 }
 
 int launch_combine(const ed_elemental_plan* P, const cplx<double>* G, const double* blend, cplx<double>* out,
@@ -444,7 +490,8 @@ int elemental_run_batch(const ed_elemental_plan* P, int nb, const void* const* l
   cplx<double>* G = (cplx<double>*)(W + P->off_g);
   const int njobs = nb * P->jobs_per_t;
   if (P->mode == ED_MODE_FP64)
-    rc = launch_pair_gemm_f64(P, (const cplx<double>*)(W + P->off_chain), phases, G, stream, njobs);
+    rc = launch_pair_gemm_f64(P, (const cplx<double>*)(W + P->off_chain), phases, G, stream, njobs,
+                              W + P->off_extra);
   else
     rc = launch_pair_gemm_tc(P, (const cplx<float>*)(W + P->off_chain), phases, G, W + P->off_extra, stream, nb);
   if (rc) return rc;
@@ -693,7 +740,7 @@ extern "C" int ed_pair_plan_create(ed_elemental_plan** plan, int Lx, int Ly, int
   P->moms.assign(moms, moms + 3 * nmom);
   int rc = ed::pair_plan_build(P, left, right0, nright);
   if (rc == ED_OK) rc = ed::tc_plan_check(P);
-  if (rc == ED_OK) P->ws_bytes = P->off_extra + ed::tc_extra_workspace(P);
+  if (rc == ED_OK) P->ws_bytes = P->off_extra + ed::tc_extra_workspace(P) + ed::f64_extra_workspace(P);
   if (rc != ED_OK) {
     delete P;
     return rc;
@@ -718,7 +765,8 @@ extern "C" int ed_pair_run(const ed_elemental_plan* plan, const void* chains, vo
   int rc = ed::launch_phases(ed::Latt{plan->Lx, plan->Ly, plan->Lz}, plan->moms.data(), plan->nmom, phases, s);
   if (rc) return rc;
   if (plan->mode == ED_MODE_FP64)
-    return ed::launch_pair_gemm_f64(plan, (const ed::cplx<double>*)chains, phases, (ed::cplx<double>*)G, s, 1);
+    return ed::launch_pair_gemm_f64(plan, (const ed::cplx<double>*)chains, phases, (ed::cplx<double>*)G, s, 1,
+                                    W + plan->off_extra);
   return ed::launch_pair_gemm_tc(plan, (const ed::cplx<float>*)chains, phases, (ed::cplx<double>*)G,
                                  W + plan->off_extra, s, 1);
 }

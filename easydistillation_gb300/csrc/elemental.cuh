@@ -63,12 +63,14 @@ struct ed_elemental_plan {
   int tc_stages = 0;   // operand stages of the factorised GEMM (0 = the default of the GEMM form)
   int tc_pair = 0;     // factorised GEMM on single SMs (1) or on SM pairs (2); 0 = the built-in default
   int tc_kpb = 0;      // k-blocks accumulated per TMEM buffer of the factorised GEMM: 1 or 2 (0 = 1)
+  int f64_ksplit = 1;  // K-split partial buffers the FP64 pair GEMM may use (sized at plan build)
 };
 
 namespace ed {
 bool mode_supported(int mode);
 void tc_fac_setup(ed_elemental_plan* P);
 size_t tc_extra_workspace(const ed_elemental_plan* P);
+size_t f64_extra_workspace(ed_elemental_plan* P);
 int tc_plan_check(ed_elemental_plan* P);
 int launch_pair_gemm_tc(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
                         cplx<double>* G, void* extra, cudaStream_t stream, int nb);
