@@ -43,6 +43,7 @@ _SIGNATURES = {
     "ed_momentum_phases": ([_i, _i, _i, _c.POINTER(_i), _i, _vp, _vp], _i),
     "ed_laplacian": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _ll, _vp, _ll, _vp], _i),
     "ed_stout_smear_step": ([_i, _i, _i, _i, _c.c_double, _vp, _vp, _vp], _i),
+    "ed_project_su3": ([_ll, _vp, _c.c_double, _i, _vp], _i),
     "ed_covariant_derivative": ([_i, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
     "ed_elemental_plan_create": (
         [_c.POINTER(_vp), _i, _i, _i, _i, _i, _c.POINTER(_i), _i, _i],

@@ -8,7 +8,9 @@
 //   Omega = rho * C * U_mu(x)^dag
 //   Q     = (i/2) (Omega^dag - Omega) - tr(.)/3            (traceless Hermitian)
 //   U'    = exp(iQ) U_mu(x),  exp(iQ) = f0 + f1 Q + f2 Q^2 by Cayley-Hamilton with
-//           the Morningstar-Peardon coefficients (c0 = tr Q^3 / 3, c1 = tr Q^2 / 2).
+//           the coefficients of C. Morningstar and M. Peardon, "Analytic smearing of
+//           SU(3) link variables in lattice QCD", Phys. Rev. D 69, 054501 (2004),
+//           hep-lat/0311018 (c0 = tr Q^3 / 3, c1 = tr Q^2 / 2).
 // The step is out of place (every thread reads the unsmeared field).
 // Layout: the generators' spatial links [3][nt][V3][3][3] complex128.
 #include "common.cuh"
@@ -182,7 +184,64 @@ __global__ void __launch_bounds__(128) stout_step_kernel(Latt L, int nt, double 
   for (int e = 0; e < 9; ++e) o[e] = R.a[e];
 }
 
+// Projection back onto U(3) by the averaged inverse iteration U <- (U + U^-dag) / 2 of
+// lattice/generator/eigenvector.py:55-65 (and elemental.py:107-118), one thread per link, until
+// max |U - U^-dag| and max |U U^dag - 1| are both <= tol for that link (the reference tests the whole
+// field at once; a link that has converged is a fixed point of the iteration up to rounding).
+// U^-dag = conj(cof(U)) / conj(det U) with the cofactor matrix cof.
+__global__ void project_su3_kernel(long long n, C* __restrict__ U, double tol, int max_iter) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  C* p = U + idx * 9;
+  M3 A = ldm(p);
+  for (int it = 0; it < max_iter; ++it) {
+    C cof[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+        cof[i * 3 + j] = A.a[i1 * 3 + j1] * A.a[i2 * 3 + j2] - A.a[i1 * 3 + j2] * A.a[i2 * 3 + j1];
+      }
+    const C det = A.a[0] * cof[0] + A.a[1] * cof[1] + A.a[2] * cof[2];
+    // 1 / conj(det) = det / |det|^2
+    const double n2 = det.re * det.re + det.im * det.im;
+    const C inv = mk(det.re / n2, det.im / n2);
+    double dmax = 0.0, umax = 0.0;
+    M3 Bm;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      Bm.a[e] = mk(cof[e].re, -cof[e].im) * inv;  // U^-dag
+      dmax = fmax(dmax, hypot(A.a[e].re - Bm.a[e].re, A.a[e].im - Bm.a[e].im));
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        C s = mk(0.0, 0.0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) cfma_conj(s, A.a[j * 3 + k], A.a[i * 3 + k]);  // (U U^dag)[i][j]
+        umax = fmax(umax, hypot(s.re - (i == j ? 1.0 : 0.0), s.im));
+      }
+    if (dmax <= tol && umax <= tol) break;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) A.a[e] = mk(0.5 * (A.a[e].re + Bm.a[e].re), 0.5 * (A.a[e].im + Bm.a[e].im));
+  }
+#pragma unroll
+  for (int e = 0; e < 9; ++e) p[e] = A.a[e];
+}
+
 }  // namespace ed
+
+extern "C" int ed_project_su3(long long nlinks, void* U, double tol, int max_iter, void* stream) {
+  ED_CHECK_ARG(nlinks >= 0 && tol >= 0.0 && max_iter > 0, "ed_project_su3: bad arguments");
+  ED_CHECK_ARG(U || nlinks == 0, "ed_project_su3: null pointer");
+  if (nlinks == 0) return ED_OK;
+  ed::project_su3_kernel<<<ed::ceil_div(nlinks, 128), 128, 0, (cudaStream_t)stream>>>(nlinks, (ed::C*)U, tol,
+                                                                                       max_iter);
+  ED_RETURN_LAUNCH("SU(3) projection");
+  return ED_OK;
+}
 
 extern "C" int ed_stout_smear_step(int Lx, int Ly, int Lz, int nt, double rho, const void* U_in, void* U_out,
                                    void* stream) {

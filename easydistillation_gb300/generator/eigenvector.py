@@ -35,15 +35,15 @@ NC = 3
 
 
 def project_su3_(U: torch.Tensor, tol: float = 1e-15, max_iter: int = 100):
-    """In-place projection of links ``[..., 3, 3]`` onto U(3) by the averaged
-    inverse iteration of ``eigenvector.py:55-65`` (``U <- (U + U^-dag)/2``)."""
-    for _ in range(max_iter):
-        Uinv = torch.linalg.inv(U)
-        Uid = Uinv.conj().transpose(-1, -2)
-        eye = torch.eye(3, dtype=U.dtype, device=U.device)
-        if (U - Uid).abs().max() <= tol and (U @ U.conj().transpose(-1, -2) - eye).abs().max() <= tol:
-            break
-        U.copy_(0.5 * (U + Uid))
+    """In-place projection of links ``[..., 3, 3]`` (contiguous complex128 on
+    the device) onto U(3) by the averaged inverse iteration of
+    ``eigenvector.py:55-65`` (``U <- (U + U^-dag)/2``), in the library's
+    ``ed_project_su3`` kernel (one thread per link)."""
+    from .. import _lib
+
+    if U.dtype != torch.complex128 or not U.is_cuda or not U.is_contiguous() or U.shape[-2:] != (3, 3):
+        raise ValueError("links must be a contiguous complex128 CUDA tensor [..., 3, 3]")
+    _lib.call("ed_project_su3", U.numel() // 9, _lib.ptr(U), float(tol), int(max_iter), _lib.stream_handle())
     return U
 
 

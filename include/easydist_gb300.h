@@ -233,6 +233,14 @@ int ed_arrow_eigh_workspace(int B, int m, int nwant, size_t* bytes);
 int ed_arrow_eigh(int B, int m, int ka, int nwant, const double* d, const double* s, const double* e,
                   double* evals, double* evecs, void* workspace, size_t workspace_bytes, void* stream);
 
+/* In-place projection of nlinks 3x3 complex128 links [nlinks][3][3] back onto
+ * U(3) by the averaged inverse iteration U <- (U + U^-dag) / 2 of
+ * lattice/generator/eigenvector.py:55-65 (EigenvectorGenerator.project_SU3)
+ * and elemental.py:107-118, until max|U - U^-dag| and max|U U^dag - 1| are
+ * both <= tol for the link (the reference uses 1e-15 over the whole field),
+ * at most max_iter iterations.  FP64, one thread per link. */
+int ed_project_su3(long long nlinks, void* U, double tol, int max_iter, void* stream);
+
 /* One covariant-derivative hop D_dir on nvec colour-plane vectors:
  * out = U_d(x) in(x+d) - U_d(x-d)^dag in(x-d).
  * Replaces one iteration of ElementalGenerator._nD (elemental.py:282-287).

@@ -53,6 +53,7 @@ __all__ = [
     "elemental_data",
     "twopoint_operators",
     "twopoint_profile_operators",
+    "project_su3",
 ]
 
 
@@ -601,3 +602,16 @@ def twopoint_profile_operators(parts_list, elemental, perambulator, timeslices, 
                 ret[idx, it] = np.einsum("tijab,xjk,xtbc,tklcd,yli,yad->tad", tau_bw, g, sink, tau, gamma_src,
                                          e[:, t_src].conj(), optimize=True)
     return -ret.mean(1) if is_sum_over_source_t else -ret
+
+
+def project_su3(U: np.ndarray, tol: float = 1e-15) -> np.ndarray:
+    """``EigenvectorGenerator.project_SU3`` (``lattice/generator/eigenvector.py:55-65``):
+    ``U <- (U + U^-dag) / 2`` over the whole field until ``max|U - U^-dag|``
+    and ``max|U U^dag - 1|`` are both <= tol.  ``U``: ``[..., 3, 3]``."""
+    U = np.array(U, dtype=np.complex128)
+    eye = np.eye(3)
+    while True:
+        Uid = np.linalg.inv(U).conj().swapaxes(-1, -2)
+        if np.abs(U - Uid).max() <= tol and np.abs(U @ U.conj().swapaxes(-1, -2) - eye).max() <= tol:
+            return U
+        U = 0.5 * (U + Uid)

@@ -251,9 +251,24 @@ def make_correlator_fixture(ref_root: str):
                         parts=np.array(repr([op.parts for op in ops])), **res)
 
 
+def make_project_su3_fixture(ref_root: str):
+    """EigenvectorGenerator.project_SU3 (lattice/generator/eigenvector.py:55-65)
+    on links pushed off SU(3) by 1e-3 Gaussian noise."""
+    lattice = import_reference(ref_root)
+    latt = [4, 4, 2, 2]
+    g = synthetic_gauge(latt, 0.3, 71)
+    rng = np.random.default_rng(72)
+    g = g + 1e-3 * (rng.standard_normal(g.shape) + 1j * rng.standard_normal(g.shape))
+    gen = lattice.EigenvectorGenerator(latt, MemGauge(g), 4, 1e-10)
+    gen.load("mem")
+    gen.project_SU3()
+    np.savez_compressed(os.path.join(HERE, "project_su3.npz"), latt=latt, gauge=g, projected=gen._U[:3].copy())
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     main(root)
     make_ildg_fixture(root)
     make_config0_chain(root)
     make_correlator_fixture(root)
+    make_project_su3_fixture(root)

@@ -103,3 +103,9 @@ def test_eigensolve_and_stout():
     np.testing.assert_allclose(sm, g["smeared"], rtol=0, atol=1e-13)
     evecs1, evals1 = R.eigensolve(sm[:, 1], latt, Ne, 1e-10)
     np.testing.assert_allclose(evals1, g["evals1"], rtol=1e-10, atol=1e-12)
+
+
+def test_project_su3_matches_reference():
+    z = golden("project_su3.npz")
+    U = z["gauge"].transpose(4, 0, 1, 2, 3, 5, 6)[:3]
+    np.testing.assert_allclose(R.project_su3(U), z["projected"], rtol=0, atol=1e-14)

@@ -41,3 +41,26 @@ def test_stout_vs_oracle_nonsymmetric(latt):
     # smeared links stay unitary
     I = np.einsum("...ab,...cb->...ac", out, out.conj())
     assert np.abs(I - np.eye(3)).max() < 1e-13
+
+
+def test_project_su3_matches_reference():
+    """EigenvectorGenerator.project_SU3 on links pushed off SU(3) by 1e-3 noise,
+    against the reference's own result (tests/golden/project_su3.npz).  The
+    kernel stops each link when it has converged, the reference the whole
+    field: the results agree to rounding."""
+    import torch
+
+    from easydistillation_gb300 import EigenvectorGenerator
+    from tests.conftest import golden
+    from tests.helpers import MemGauge
+
+    z = golden("project_su3.npz")
+    latt = [int(v) for v in z["latt"]]
+    gen = EigenvectorGenerator(latt, MemGauge(z["gauge"]), 4, 1e-10)
+    gen.load("k")
+    gen.project_SU3()
+    out = gen._U.cpu().numpy()
+    assert np.abs(out - z["projected"]).max() < 1e-13
+    eye = np.eye(3)
+    assert np.abs(out @ out.conj().swapaxes(-1, -2) - eye).max() < 1e-14
+    torch.cuda.synchronize()
