@@ -79,6 +79,7 @@ _SIGNATURES = {
     "ed_laplacian_config": ([_i], _i),
     "ed_laplacian_status": ([_c.POINTER(_i), _vp], _i),
     "ed_laplacian_wait_limit": ([_c.c_longlong], _i),
+    "ed_laplacian_wait_probe": ([_c.c_int], _i),
     "ed_elemental_factorised": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
     "ed_elemental_set_tuning": ([_vp, _i, _i], _i),
     "ed_arrow_eigh_workspace": ([_i, _i, _i, _c.POINTER(_c.c_size_t)], _i),

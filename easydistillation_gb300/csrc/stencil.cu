@@ -292,12 +292,16 @@ __device__ __forceinline__ bool st_wait(uint64_t* bar, uint32_t parity, long lon
   return true;
 }
 long long g_stencil_wait_cycles = LT_WAIT_CYCLES;  // host-side launch setting
+// Host-side launch setting: when set, every block of the staged kernels first waits, with the data-wait
+// limit, on a barrier of its own that nothing completes, so that the limit runs out whatever the copy
+// latency (the test of the failure path).
+int g_stencil_wait_probe = 0;
 
 __global__ void __launch_bounds__(LT_THREADS) laplacian_tma_kernel(const __grid_constant__ CUtensorMap fmap, Latt L,
                                                                    int zb, const cplx<float>* __restrict__ links,
                                                                    long long link_tstride, cplx<float>* __restrict__ out,
                                                                    long long out_tstride, float diag, int slot_bytes,
-                                                                   long long wait_cycles) {
+                                                                   long long wait_cycles, int probe) {
   extern __shared__ __align__(128) uint8_t sm[];
   uint64_t* bar = (uint64_t*)(sm + LT_SLOTS * slot_bytes);
   __shared__ int failed;
@@ -307,7 +311,7 @@ __global__ void __launch_bounds__(LT_THREADS) laplacian_tma_kernel(const __grid_
   const int nplanes = (z1 - z0) + 2;  // plane j holds z = z0 - 1 + j (periodic)
   if (threadIdx.x == 0) {
     failed = 0;
-    for (int s = 0; s < LT_SLOTS; ++s)
+    for (int s = 0; s <= LT_SLOTS; ++s)  // bar[LT_SLOTS]: the probe barrier, never arrived on
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st_smem(&bar[s])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -331,6 +335,7 @@ __global__ void __launch_bounds__(LT_THREADS) laplacian_tma_kernel(const __grid_
       issue(j);
       issued_hi = j;
     }
+  if (threadIdx.x == 0 && probe && !st_wait(&bar[LT_SLOTS], 0, wait_cycles)) failed = 1;
   const cplx<float>* U = links + (long long)t * link_tstride;
   cplx<float>* O = out + (long long)t * out_tstride + (long long)v * 3 * V3;
   for (int z = z0; z < z1; ++z) {
@@ -502,7 +507,8 @@ __global__ void __launch_bounds__(LS_MAX_SITES, 2)
     laplacian_strip_kernel(const __grid_constant__ CUtensorMap mL27, const __grid_constant__ CUtensorMap mL9,
                            const __grid_constant__ CUtensorMap mLz, const __grid_constant__ CUtensorMap mF,
                            const __grid_constant__ CUtensorMap mFh, Latt L, int R, int zb,
-                           cplx<float>* __restrict__ out, long long out_tstride, float diag, long long wait_cycles) {
+                           cplx<float>* __restrict__ out, long long out_tstride, float diag, long long wait_cycles,
+                           int probe) {
   extern __shared__ __align__(128) uint8_t sm[];
   const int Lx = L.Lx, Ly = L.Ly, Lz = L.Lz, V3 = L.V3(), P = Lx * Ly, RLx = R * Lx;
   const LsGeom g = ls_geom(RLx, Lx);
@@ -514,7 +520,7 @@ __global__ void __launch_bounds__(LS_MAX_SITES, 2)
   const int z0 = slab * zb, z1 = min(Lz, z0 + zb);
   const int nplanes = (z1 - z0) + 2;  // plane j holds z = z0 - 1 + j (periodic)
   if (threadIdx.x == 0) {
-    for (int q = 0; q < LS_SLOTS; ++q)
+    for (int q = 0; q <= LS_SLOTS; ++q)  // bar[LS_SLOTS]: the probe barrier, never arrived on
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(st_smem(&bar[q])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -553,6 +559,7 @@ __global__ void __launch_bounds__(LS_MAX_SITES, 2)
   const int pxm = yy * Lx + wrap_dec(xx, Lx), pxp = yy * Lx + wrap_inc(xx, Lx);
   cplx<float>* O = out + (long long)t * out_tstride + (long long)v * 3 * V3;
   bool ok = true, failed = false;
+  if (threadIdx.x == 0 && probe) ok = st_wait(&bar[LS_SLOTS], 0, wait_cycles);
   for (int z = z0; z < z1; ++z) {
     const int jc = z - z0 + 1;
     const uint8_t* Sm = sm + ((jc - 1) % LS_SLOTS) * g.bytes;
@@ -673,7 +680,7 @@ static int launch_laplacian_tma(Latt L, int nt, int nvec, const void* links, con
   dim3 grid(nslab, nvec, nt);
   laplacian_tma_kernel<<<grid, LT_THREADS, smem, stream>>>(map, L, zb, (const cplx<float>*)links, 27LL * L.V3(),
                                                            (cplx<float>*)out, ots, 6.0f, slot_bytes,
-                                                           g_stencil_wait_cycles);
+                                                           g_stencil_wait_cycles, g_stencil_wait_probe);
   ED_RETURN_LAUNCH("laplacian (TMA-staged)");
   return ED_OK;
 }
@@ -731,7 +738,7 @@ static int launch_laplacian_strip(Latt L, int nt, int nvec, const void* links, c
   dim3 grid(nstrip * nslab, nvec, nt);
   const int threads = (RLx + 31) / 32 * 32;
   laplacian_strip_kernel<<<grid, threads, smem, stream>>>(mL27, mL9, mLz, mF, mFh, L, R, zb, (cplx<float>*)out, ots,
-                                                          6.0f, g_stencil_wait_cycles);
+                                                          6.0f, g_stencil_wait_cycles, g_stencil_wait_probe);
   ED_RETURN_LAUNCH("laplacian (strip-staged)");
   return ED_OK;
 }
@@ -829,6 +836,11 @@ extern "C" int ed_laplacian_config(int use_tma) {
 extern "C" int ed_laplacian_wait_limit(long long cycles) {
   ED_CHECK_ARG(cycles >= 0, "ed_laplacian_wait_limit: negative limit");
   ed::g_stencil_wait_cycles = cycles > 0 ? cycles : ed::LT_WAIT_CYCLES;
+  return ED_OK;
+}
+
+extern "C" int ed_laplacian_wait_probe(int on) {
+  ed::g_stencil_wait_probe = on ? 1 : 0;
   return ED_OK;
 }
 

@@ -87,10 +87,15 @@ extern "C" {
                               * 128 x 128 tiles, 2 = two-CTA clusters on SM pairs with 256 x 128
                               * tiles (tcgen05.mma.cta_group::2) */
 #define ED_TUNE_TC_KPB 6     /* k-blocks the factorised GEMM accumulates in one TMEM buffer before the
-                              * drain warps read it: 0 (default, 1) or 2.  The tensor core's FP32
+                              * drain warps read it: 0 (default, 1), 2 or 4.  The tensor core's FP32
                               * accumulation truncates, so longer buffers trade accuracy (measured
-                              * at 32^3, Ne = 200, f16x3: 2.0e-7 -> 5.1e-7 vs FP64) for half the
+                              * at 32^3, Ne = 200, f16x3: 2.0e-7 -> 5.1e-7 vs FP64 for 2) for fewer
                               * buffer hand-overs */
+#define ED_TUNE_TC_STACK 7   /* single-SM factorised GEMM operand form: 0 (default) = four real
+                              * products per complex one, M = N = 128 MMAs into [re], [im]
+                              * accumulators (double-buffered); 1 = stacked: B = [Br; Bi] in
+                              * shared memory, two M = 128, N = 256 MMAs A_re [Br | Bi] and
+                              * A_im [Br | Bi] into single accumulators, combined by the drain */
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);
@@ -151,6 +156,14 @@ int ed_laplacian_config(int use_tma);
  * out on purpose (a test of the timeout path).  No counterpart in the
  * reference. */
 int ed_laplacian_wait_limit(long long cycles);
+
+/* Test of the failure path (process-wide launch setting, 0 = off): when on,
+ * every block of the TMA-staged Laplacian kernels first waits, with the
+ * data-wait limit, on a barrier of its own that nothing completes, so the
+ * limit runs out whatever the copy latency; the launch then reports
+ * ED_ERR_TIMEOUT through ed_laplacian_status after its blocks have drained
+ * their own copies.  No counterpart in the reference. */
+int ed_laplacian_wait_probe(int on);
 
 /* Status of the TMA-staged Laplacian's bounded waits since the last call
  * (synchronises `stream`): ED_OK, or ED_ERR_TIMEOUT when a wait gave up (the

@@ -1,9 +1,10 @@
 """Failure detection without a GPU fault: the TMA-staged complex64 Laplacian
-bounds every wait for its data.  With a one-cycle limit (a launch setting)
-the waits run out on purpose: the launch must report ED_ERR_TIMEOUT through
-the status word, leave the context usable (every block still drains its own
-copies in flight before it leaves), and the next launch with the default
-limit must be clean and correct."""
+bounds every wait for its data.  With a short limit (a launch setting) and
+the probe setting on, every block first waits on a barrier of its own that
+nothing completes, so the limit runs out whatever the copy latency: the
+launch must report ED_ERR_TIMEOUT through the status word, leave the context
+usable (every block still drains its own copies in flight before it leaves),
+and the next launch with the default settings must be clean and correct."""
 
 import ctypes
 
@@ -31,12 +32,14 @@ def test_staged_laplacian_timeout_is_reported_and_recovers(variant):
     try:
         laplacian_config(variant)
         assert _lib.lib().ed_laplacian_status(ctypes.byref(code), _lib.stream_handle()) == _lib.ED_OK  # clean start
-        _lib.check(_lib.lib().ed_laplacian_wait_limit(1), "ed_laplacian_wait_limit")
+        _lib.check(_lib.lib().ed_laplacian_wait_limit(1000), "ed_laplacian_wait_limit")
+        _lib.check(_lib.lib().ed_laplacian_wait_probe(1), "ed_laplacian_wait_probe")
         laplacian(links, F, latt)
         rc = _lib.lib().ed_laplacian_status(ctypes.byref(code), _lib.stream_handle())
         assert rc == _lib.ED_ERR_TIMEOUT and code.value != 0
         assert "gave up" in _lib.last_error()
     finally:
+        _lib.lib().ed_laplacian_wait_probe(0)
         _lib.lib().ed_laplacian_wait_limit(0)
         laplacian_config(2)
     # the status word was cleared by the read; the context is usable and the next launch is exact
