@@ -777,21 +777,30 @@ def run_mixed(args, emit=True):
                           torch.randn((4, Ne, V3 * 3), generator=gen, device=dev, dtype=torch.float64))
         V /= (2 * V3 * 3) ** 0.5
         bindings.append(VolumeBinding(latt, Ne, U, V, [t % 4 for t in range(Lt)]))
-    t0 = time.perf_counter()
-    mv = MixedVolumeGraph(bindings, 1, moms, mode, max_batch=8, device=dev, autotune=args.autotune)
-    setup_s = time.perf_counter() - t0
-    mv.capture()
-    torch.cuda.synchronize()
     reps = max(1, args.steps)
     n_per = sum(len(b.timeslices) for b in bindings)
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(reps):
-        mv.run()
-    b.record()
-    torch.cuda.synchronize()
-    dt = a.elapsed_time(b) / 1e3
-    mv.check_status()
+
+    def sweep(single_launch):
+        t0 = time.perf_counter()
+        mv = MixedVolumeGraph(bindings, 1, moms, mode, max_batch=8, device=dev, autotune=args.autotune,
+                              single_launch=single_launch)
+        setup_s = time.perf_counter() - t0
+        mv.capture()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            mv.run()
+        b.record()
+        torch.cuda.synchronize()
+        mv.check_status()
+        return mv, a.elapsed_time(b) / 1e3, setup_s
+
+    mv1, dt1, _ = sweep(False)  # one GEMM launch per volume chunk, for comparison
+    launches1 = mv1.gemm_launches
+    del mv1
+    torch.cuda.empty_cache()
+    mv, dt, setup_s = sweep(True)
     line = {"metric": "mixed-volume elemental timeslices/s (96 timeslices: 16^3 Ne=64, 24^3 Ne=128, 32^3 Ne=256; "
                       "4 ops x 7 momenta)", "value": reps * n_per / dt, "unit": "timeslices/s",
             "seconds_per_sweep": dt / reps, "mode": mode,
@@ -799,7 +808,9 @@ def run_mixed(args, emit=True):
             "plan_settings": {f"{v[0][0]}^3": {"factorise": p.factorise, "factorised": p.factorised, **p.tuning()}
                               for v, p in zip(vols, mv.plans)},
             "autotune": args.autotune, "plan_setup_seconds": setup_s,
-            "graph_replays_per_sweep": 1, "batched_passes_per_sweep": mv.passes(),
+            "graph_replays_per_sweep": 1, "gemm_launches_per_sweep": mv.gemm_launches,
+            "per_volume_gemm_launches": {"value": reps * n_per / dt1, "seconds_per_sweep": dt1 / reps,
+                                         "gemm_launches_per_sweep": launches1},
             "data": "synthetic, resident in HBM"}
     del mv, bindings
     if emit:

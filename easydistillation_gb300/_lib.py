@@ -65,6 +65,15 @@ _SIGNATURES = {
         [_vp, _i, _c.POINTER(_vp), _ll, _ll, _i, _c.POINTER(_vp), _vp, _c.POINTER(_vp), _vp, _c.c_size_t, _vp],
         _i,
     ),
+    "ed_elemental_run_batch_begin": (
+        [_vp, _i, _c.POINTER(_vp), _ll, _ll, _i, _c.POINTER(_vp), _vp, _c.c_size_t, _vp],
+        _i,
+    ),
+    "ed_elemental_gemm_multi": (
+        [_i, _c.POINTER(_vp), _c.POINTER(_i), _c.POINTER(_vp), _c.POINTER(_c.c_size_t), _c.POINTER(_i), _vp],
+        _i,
+    ),
+    "ed_elemental_run_batch_end": ([_vp, _i, _vp, _c.POINTER(_vp), _vp, _c.c_size_t, _vp], _i),
     "ed_link_grad": ([_i, _i, _i, _i, _i, _c.c_double, _c.c_double, _vp, _vp, _vp, _vp], _i),
     "ed_twopoint_trace": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
     "ed_chain_adjoint": ([_i, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),

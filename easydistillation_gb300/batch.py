@@ -18,7 +18,7 @@ from typing import Dict, List, Sequence
 import torch
 
 from .insertion import num_derivative
-from .ops import ElementalPlan
+from .ops import ElementalPlan, gemm_multi
 
 
 def admit_batch(latt_size, Ne, num_nabla, momentum_list, precision="fp64", device=None, max_batch=8,
@@ -138,17 +138,24 @@ class MixedVolumeGraph:
     ONE captured CUDA graph.
 
     Each volume gets a batched plan (batch admitted by HBM footprint, the
-    volumes' workspaces held at once, largest volume first); the graph holds,
-    volume by volume, one batched pass per chunk of timeslices, reading the
-    bound input tensors in place and writing the bound outputs, so a replay
-    (``run()``) recomputes everything from the tensors' current contents with
-    one host call.  ``autotune`` builds each plan with the autotuner's choice
+    volumes' workspaces held at once, largest volume first).  The timeslices
+    go in rounds: round r takes the r-th admitted chunk of every volume, builds
+    each chunk's chains, contracts all of them with ONE pair-GEMM launch whose
+    blocks cover the tiles of every volume (``ed_elemental_gemm_multi``; one
+    launch per volume instead when the plans' GEMM forms differ, e.g. a
+    factorised momentum list), and combines each chunk into its bound output.
+    The graph reads the bound input tensors in place, so a replay (``run()``)
+    recomputes everything from their current contents with one host call.
+    ``single_launch=False`` keeps one batched pass (and GEMM launch) per
+    volume chunk.  ``autotune`` builds each plan with the autotuner's choice
     for its shape (``easydistillation_gb300.tune``)."""
 
     def __init__(self, volumes: Sequence[VolumeBinding], num_nabla, momentum_list, precision="f16x3",
-                 max_batch=8, device=None, autotune=False, reserve=0.1):
+                 max_batch=8, device=None, autotune=False, reserve=0.1, single_launch=True):
         self.device = torch.device(device or "cuda")
         self.precision = precision
+        self.single_launch = single_launch
+        self.gemm_launches = None  # GEMM launches per sweep, known after the first run
         self.volumes = list(volumes)
         nd, nm = num_derivative(num_nabla), len(momentum_list)
         self.plans = []
@@ -172,8 +179,10 @@ class MixedVolumeGraph:
             if autotune:
                 from .tune import tuned_plan
 
+                # one GEMM launch per round needs one GEMM form for every volume: the library's default form
+                # for the momentum list (on chip unless it is close to a product set)
                 plan = tuned_plan(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device, batch=b,
-                                  evec_dtype=v.evecs.dtype)
+                                  evec_dtype=v.evecs.dtype, forms=[True] if single_launch else None)
             else:
                 plan = ElementalPlan(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device, batch=b)
             plan.workspace()  # held now, so the next volume's admission sees it
@@ -186,12 +195,29 @@ class MixedVolumeGraph:
         return v.latt_size[0] * v.latt_size[1] * v.latt_size[2]
 
     def _launch(self):
-        for v, plan in zip(self.volumes, self.plans):
-            ts = list(v.timeslices)
-            for s0 in range(0, len(ts), plan.batch):
-                chunk = ts[s0 : s0 + plan.batch]
-                plan.run_batch([v.links[:, t] for t in chunk], v.links.stride(0), 9,
-                               [v.evecs[t] for t in chunk], [v.out[s0 + j] for j in range(len(chunk))])
+        if not self.single_launch:
+            for v, plan in zip(self.volumes, self.plans):
+                ts = list(v.timeslices)
+                for s0 in range(0, len(ts), plan.batch):
+                    chunk = ts[s0 : s0 + plan.batch]
+                    plan.run_batch([v.links[:, t] for t in chunk], v.links.stride(0), 9,
+                                   [v.evecs[t] for t in chunk], [v.out[s0 + j] for j in range(len(chunk))])
+            self.gemm_launches = self.passes()
+            return
+        launches = 0
+        nround = max(-(-len(v.timeslices) // p.batch) for v, p in zip(self.volumes, self.plans))
+        for r in range(nround):
+            members = []  # (volume, plan, first output row, timeslices) of this round
+            for v, plan in zip(self.volumes, self.plans):
+                chunk = list(v.timeslices)[r * plan.batch : (r + 1) * plan.batch]
+                if chunk:
+                    members.append((v, plan, r * plan.batch, chunk))
+            for v, plan, s0, chunk in members:
+                plan.run_batch_begin([v.links[:, t] for t in chunk], v.links.stride(0), 9, [v.evecs[t] for t in chunk])
+            launches += gemm_multi([m[1] for m in members], [len(m[3]) for m in members])
+            for v, plan, s0, chunk in members:
+                plan.run_batch_end([v.out[s0 + j] for j in range(len(chunk))])
+        self.gemm_launches = launches
 
     def capture(self):
         self._launch()  # warm-up outside the capture
@@ -226,7 +252,7 @@ class MixedVolumeGraph:
 
 def run_mixed_volumes(groups: Dict[str, VolumeGroup], links: Dict[str, torch.Tensor],
                       evecs: Dict[str, torch.Tensor], num_nabla, momentum_list, precision="f16x3",
-                      max_batch=8, device=None, autotune=False):
+                      max_batch=8, device=None, autotune=False, single_launch=True):
     """Elementals for several lattice volumes (each with its own Ne), all in
     one graphed pass (:class:`MixedVolumeGraph`).  ``links[name]``:
     ``[3, Lt, Lz, Ly, Lx, 3, 3]``; ``evecs[name]``: ``[Lt, Ne, V3*3]``.
@@ -234,7 +260,8 @@ def run_mixed_volumes(groups: Dict[str, VolumeGroup], links: Dict[str, torch.Ten
     names = list(groups)
     vols = [VolumeBinding(groups[n].latt_size, groups[n].Ne, links[n], evecs[n], list(groups[n].timeslices))
             for n in names]
-    mv = MixedVolumeGraph(vols, num_nabla, momentum_list, precision, max_batch, device, autotune)
+    mv = MixedVolumeGraph(vols, num_nabla, momentum_list, precision, max_batch, device, autotune,
+                          single_launch=single_launch)
     outs = mv.run()
     mv.check_status()
     return dict(zip(names, outs))

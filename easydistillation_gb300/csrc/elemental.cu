@@ -451,9 +451,11 @@ int launch_combine(const ed_elemental_plan* P, const cplx<double>* G, const doub
 }
 
 
-int elemental_run_batch(const ed_elemental_plan* P, int nb, const void* const* links, long long dir_stride,
-                        long long site_stride, int evec_prec, const void* const* evecs, const double* blend,
-                        void* const* outs, void* ws, size_t ws_bytes, cudaStream_t stream) {
+// The three parts of a batched run: the phases and the chains of the nb timeslices (begin), the pair
+// contraction (one launch for the whole batch), and the combine into the caller's outputs (end).
+int elemental_run_batch_begin(const ed_elemental_plan* P, int nb, const void* const* links, long long dir_stride,
+                              long long site_stride, int evec_prec, const void* const* evecs, void* ws,
+                              cudaStream_t stream) {
   char* W = (char*)ws;
   const Latt L{P->Lx, P->Ly, P->Lz};
   int rc;
@@ -487,19 +489,37 @@ int elemental_run_batch(const ed_elemental_plan* P, int nb, const void* const* l
       if (rc) return rc;
     }
   }
+  return ED_OK;
+}
+
+int elemental_run_batch_gemm(const ed_elemental_plan* P, int nb, void* ws, cudaStream_t stream) {
+  char* W = (char*)ws;
+  const cplx<double>* phases = (const cplx<double>*)(W + P->off_phase);
   cplx<double>* G = (cplx<double>*)(W + P->off_g);
-  const int njobs = nb * P->jobs_per_t;
   if (P->mode == ED_MODE_FP64)
-    rc = launch_pair_gemm_f64(P, (const cplx<double>*)(W + P->off_chain), phases, G, stream, njobs,
-                              W + P->off_extra);
-  else
-    rc = launch_pair_gemm_tc(P, (const cplx<float>*)(W + P->off_chain), phases, G, W + P->off_extra, stream, nb);
-  if (rc) return rc;
+    return launch_pair_gemm_f64(P, (const cplx<double>*)(W + P->off_chain), phases, G, stream, nb * P->jobs_per_t,
+                                W + P->off_extra);
+  return launch_pair_gemm_tc(P, (const cplx<float>*)(W + P->off_chain), phases, G, W + P->off_extra, stream, nb);
+}
+
+int elemental_run_batch_end(const ed_elemental_plan* P, int nb, const double* blend, void* const* outs, void* ws,
+                            cudaStream_t stream) {
+  cplx<double>* G = (cplx<double>*)((char*)ws + P->off_g);
   for (int b = 0; b < nb; ++b) {
-    rc = launch_combine(P, G + (size_t)b * P->g_per_t, blend, (cplx<double>*)outs[b], stream);
+    const int rc = launch_combine(P, G + (size_t)b * P->g_per_t, blend, (cplx<double>*)outs[b], stream);
     if (rc) return rc;
   }
   return ED_OK;
+}
+
+int elemental_run_batch(const ed_elemental_plan* P, int nb, const void* const* links, long long dir_stride,
+                        long long site_stride, int evec_prec, const void* const* evecs, const double* blend,
+                        void* const* outs, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  (void)ws_bytes;
+  int rc = elemental_run_batch_begin(P, nb, links, dir_stride, site_stride, evec_prec, evecs, ws, stream);
+  if (rc == ED_OK) rc = elemental_run_batch_gemm(P, nb, ws, stream);
+  if (rc == ED_OK) rc = elemental_run_batch_end(P, nb, blend, outs, ws, stream);
+  return rc;
 }
 
 int elemental_run(const ed_elemental_plan* P, const void* links, long long dir_stride, long long site_stride,
@@ -645,9 +665,13 @@ extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int val
       plan->tc_pair = value;
       return ED_OK;
     case ED_TUNE_TC_KPB:
-      ED_CHECK_ARG(value >= 0 && value <= 2, "ed_elemental_set_tuning: %d k-blocks per TMEM buffer (0, 1 or 2)",
-                   value);
+      ED_CHECK_ARG(value == 0 || value == 1 || value == 2 || value == 4,
+                   "ed_elemental_set_tuning: %d k-blocks per TMEM buffer (0, 1, 2 or 4)", value);
       plan->tc_kpb = value;
+      return ED_OK;
+    case ED_TUNE_TC_STACK:
+      ED_CHECK_ARG(value >= 0 && value <= 2, "ed_elemental_set_tuning: operand form %d (0, 1 or 2)", value);
+      plan->tc_stack = value;
       return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_set_tuning: unknown key %d", key);
@@ -675,6 +699,9 @@ extern "C" int ed_elemental_get_tuning(const ed_elemental_plan* plan, int key, i
       return ED_OK;
     case ED_TUNE_TC_KPB:
       *value = plan->tc_kpb;
+      return ED_OK;
+    case ED_TUNE_TC_STACK:
+      *value = plan->tc_stack;
       return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_get_tuning: unknown key %d", key);

@@ -7,6 +7,7 @@
 
 namespace ed {
 
+enum TcKind { TC_F16 = 1, TC_BF16 = 2, TC_TF32 = 3, TC_OZAKI = 4 };  // ed_elemental_plan::tc_kind
 constexpr int kMaxJobs = 64;   // pair groups (one per left chain and timeslice of a batch)
 constexpr int kMaxTerms = 64;  // subset terms over all operators (43 for num_nabla = 2)
 constexpr int kMaxDeriv = 13;  // operators for num_nabla = 2
@@ -62,7 +63,8 @@ struct ed_elemental_plan {
   int tc_grid = 0;     // CTAs of the persistent factorised GEMM (0 = every co-resident CTA)
   int tc_stages = 0;   // operand stages of the factorised GEMM (0 = the default of the GEMM form)
   int tc_pair = 0;     // factorised GEMM on single SMs (1) or on SM pairs (2); 0 = the built-in default
-  int tc_kpb = 0;      // k-blocks accumulated per TMEM buffer of the factorised GEMM: 1 or 2 (0 = 1)
+  int tc_kpb = 0;      // k-blocks accumulated per TMEM buffer of the factorised GEMM: 1, 2 or 4 (0: the form's default)
+  int tc_stack = 0;    // factorised GEMM on single SMs: 0/1 = stacked [re | im] B operand (N = 256), 2 = four products
   int f64_ksplit = 1;  // K-split partial buffers the FP64 pair GEMM may use (sized at plan build)
 };
 

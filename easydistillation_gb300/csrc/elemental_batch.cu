@@ -14,6 +14,15 @@ int plan_build(ed_elemental_plan* P);
 int elemental_run_batch(const ed_elemental_plan* P, int nb, const void* const* links, long long dir_stride,
                         long long site_stride, int evec_prec, const void* const* evecs, const double* blend,
                         void* const* outs, void* ws, size_t ws_bytes, cudaStream_t stream);
+int elemental_run_batch_begin(const ed_elemental_plan* P, int nb, const void* const* links, long long dir_stride,
+                              long long site_stride, int evec_prec, const void* const* evecs, void* ws,
+                              cudaStream_t stream);
+int elemental_run_batch_gemm(const ed_elemental_plan* P, int nb, void* ws, cudaStream_t stream);
+int elemental_run_batch_end(const ed_elemental_plan* P, int nb, const double* blend, void* const* outs, void* ws,
+                            cudaStream_t stream);
+int launch_pair_gemm_tc_multi(int nplans, const ed_elemental_plan* const* plans, const int* nbs, void* const* ws,
+                              cudaStream_t stream);
+constexpr int kMaxMultiPlans = 4;  // volumes of one multi-volume GEMM launch (kMaxVol of tc_pair_gemm.cuh)
 }  // namespace ed
 
 extern "C" int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne,
@@ -71,4 +80,73 @@ extern "C" int ed_elemental_run_batch(const ed_elemental_plan* plan, int nbatch,
   }
   return ed::elemental_run_batch(plan, nbatch, links, dir_stride, site_stride, evec_prec, evecs, blend, outs,
                                  workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+// ---- several batched plans (lattice volumes with their own Ne) with one pair-contraction launch
+
+static int check_ws(const ed_elemental_plan* plan, const void* workspace, size_t workspace_bytes, const char* fn) {
+  ED_CHECK_ARG(workspace, "%s: null workspace", fn);
+  ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0, "%s: workspace must be 256-byte aligned", fn);
+  if (workspace_bytes < plan->ws_bytes) {
+    ed::set_error("%s: workspace of %zu bytes is smaller than the %zu the plan needs", fn, workspace_bytes,
+                  plan->ws_bytes);
+    return ED_ERR_WORKSPACE;
+  }
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_run_batch_begin(const ed_elemental_plan* plan, int nbatch, const void* const* links,
+                                            long long dir_stride, long long site_stride, int evec_prec,
+                                            const void* const* evecs, void* workspace, size_t workspace_bytes,
+                                            void* stream) {
+  ED_CHECK_ARG(plan && !plan->custom, "ed_elemental_run_batch_begin: needs an elemental plan");
+  ED_CHECK_ARG(nbatch > 0 && nbatch <= plan->nbatch,
+               "ed_elemental_run_batch_begin: batch of %d timeslices, plan holds %d", nbatch, plan->nbatch);
+  ED_CHECK_ARG(links && evecs, "ed_elemental_run_batch_begin: null pointer");
+  for (int b = 0; b < nbatch; ++b)
+    ED_CHECK_ARG(links[b] && evecs[b], "ed_elemental_run_batch_begin: null pointer for timeslice %d", b);
+  ED_CHECK_ARG(evec_prec == ED_C128 || evec_prec == ED_C64, "ed_elemental_run_batch_begin: bad eigenvector precision");
+  ED_CHECK_ARG(dir_stride >= 0 && site_stride >= 0, "ed_elemental_run_batch_begin: negative stride");
+  int rc = check_ws(plan, workspace, workspace_bytes, "ed_elemental_run_batch_begin");
+  if (rc) return rc;
+  return ed::elemental_run_batch_begin(plan, nbatch, links, dir_stride, site_stride, evec_prec, evecs, workspace,
+                                       (cudaStream_t)stream);
+}
+
+extern "C" int ed_elemental_gemm_multi(int nplans, const ed_elemental_plan* const* plans, const int* nbatch,
+                                       void* const* workspaces, const size_t* workspace_bytes, int* launches,
+                                       void* stream) {
+  ED_CHECK_ARG(nplans > 0 && plans && nbatch && workspaces && workspace_bytes,
+               "ed_elemental_gemm_multi: null pointer or no plans");
+  bool one = nplans <= ed::kMaxMultiPlans;
+  for (int v = 0; v < nplans; ++v) {
+    const ed_elemental_plan* P = plans[v];
+    ED_CHECK_ARG(P && !P->custom, "ed_elemental_gemm_multi: plan %d is not an elemental plan", v);
+    ED_CHECK_ARG(nbatch[v] > 0 && nbatch[v] <= P->nbatch,
+                 "ed_elemental_gemm_multi: batch of %d timeslices for plan %d, which holds %d", nbatch[v], v,
+                 P->nbatch);
+    int rc = check_ws(P, workspaces[v], workspace_bytes[v], "ed_elemental_gemm_multi");
+    if (rc) return rc;
+    // one launch needs every plan on the on-chip-phase tensor-core path with the same split kind
+    one = one && P->tc_kind != 0 && P->tc_kind != ed::TC_OZAKI && !P->fac && P->tc_kind == plans[0]->tc_kind;
+  }
+  if (launches) *launches = one ? 1 : nplans;
+  if (one) return ed::launch_pair_gemm_tc_multi(nplans, plans, nbatch, workspaces, (cudaStream_t)stream);
+  for (int v = 0; v < nplans; ++v) {
+    const int rc = ed::elemental_run_batch_gemm(plans[v], nbatch[v], workspaces[v], (cudaStream_t)stream);
+    if (rc) return rc;
+  }
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_run_batch_end(const ed_elemental_plan* plan, int nbatch, const double* blend,
+                                          void* const* outs, void* workspace, size_t workspace_bytes, void* stream) {
+  ED_CHECK_ARG(plan && !plan->custom, "ed_elemental_run_batch_end: needs an elemental plan");
+  ED_CHECK_ARG(nbatch > 0 && nbatch <= plan->nbatch,
+               "ed_elemental_run_batch_end: batch of %d timeslices, plan holds %d", nbatch, plan->nbatch);
+  ED_CHECK_ARG(outs, "ed_elemental_run_batch_end: null pointer");
+  for (int b = 0; b < nbatch; ++b) ED_CHECK_ARG(outs[b], "ed_elemental_run_batch_end: null output %d", b);
+  int rc = check_ws(plan, workspace, workspace_bytes, "ed_elemental_run_batch_end");
+  if (rc) return rc;
+  return ed::elemental_run_batch_end(plan, nbatch, blend, outs, workspace, (cudaStream_t)stream);
 }

@@ -36,7 +36,6 @@ int launch_phases(Latt L, const int* moms, int nmom, cplx<double>* out, cudaStre
 
 #include "tc_config.cuh"
 
-enum TcKind { TC_F16 = 1, TC_BF16 = 2, TC_TF32 = 3, TC_OZAKI = 4 };
 
 struct TcJob {
   int left, right0, nright, tile0, mt, nt;
@@ -596,9 +595,13 @@ static EncodeFn get_encode() {
   return fn;
 }
 
+// The on-chip-phase tensor-core path of one batched plan, in three parts: the operands (scale, split
+// planes, FP32 phases, cleared results) and the description of its GEMM launch (tensor map, job table),
+// the GEMM, and the double-float -> complex128 conversion.  A multi-volume run issues the first and last
+// part per plan and one GEMM launch for all of them.
 template <int KIND>
-static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
-                       cplx<double>* G, void* extra, cudaStream_t stream, int nb) {
+static int tc_onchip_prepare(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
+                             void* extra, cudaStream_t stream, int nb, TcMultiVol* d, bool* staged) {
   constexpr int ESZ = Split<KIND>::ESZ;
   char* X = (char*)extra;
   TcScalars* sc = (TcScalars*)X;
@@ -624,12 +627,11 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
     set_error("cuTensorMapEncodeTiled is unavailable from the driver");
     return ED_ERR_CUDA;
   }
-  CUtensorMap amap;
   cuuint64_t gdim[2] = {(cuuint64_t)K, (cuuint64_t)(4 * R)};
   cuuint64_t gstride[1] = {(cuuint64_t)(K * ESZ)};
   cuuint32_t box[2] = {(cuuint32_t)(TC_ROWB / ESZ), (cuuint32_t)TC_BM};
   cuuint32_t estride[2] = {1, 1};
-  CUresult cr = enc(&amap, KIND == TC_TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2,
+  CUresult cr = enc(&d->amap, KIND == TC_TF32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2,
                     planes, gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS) {
@@ -637,41 +639,132 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
     return ED_ERR_CUDA;
   }
 
-  TcTable tab;
+  TcTable& tab = d->tab;
   tab.njobs = nb * P->jobs_per_t;
   int tiles = 0;
   for (int k = 0; k < tab.njobs; ++k) {
     const Job& j = P->jobs[k];
-    TcJob& d = tab.j[k];
-    d.left = j.left;
-    d.right0 = j.right0;
-    d.nright = j.nright;
-    d.g_off = j.g_off;
-    d.mt = ceil_div((long long)j.nright * P->Ne, TC_BM);
-    d.nt = ceil_div((long long)P->Ne * P->nmom, TC_BN);
-    d.tile0 = tiles;
-    tiles += d.mt * d.nt;
+    TcJob& t = tab.j[k];
+    t.left = j.left;
+    t.right0 = j.right0;
+    t.nright = j.nright;
+    t.g_off = j.g_off;
+    t.mt = ceil_div((long long)j.nright * P->Ne, TC_BM);
+    t.nt = ceil_div((long long)P->Ne * P->nmom, TC_BN);
+    t.tile0 = tiles;
+    tiles += t.mt * t.nt;
   }
   // stage the producers' rows in shared memory when they fit (see tc_pair_gemm.cuh)
-  const int xr = std::min(P->Ne, (TC_BN - 1) / P->nmom + 2);
-  const bool staged = (long long)(xr + P->nmom) * (long long)((TC_ROWB / ESZ) * 8 + TC_XP_PAD) <= TC_XP_BYTES;
-  auto kern = staged ? tc_pair_gemm_kernel<KIND, true> : tc_pair_gemm_kernel<KIND, false>;
-  static bool attr_set[4][2] = {};
-  if (!attr_set[KIND][staged]) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
-    attr_set[KIND][staged] = true;
-  }
+  d->xr = std::min(P->Ne, (TC_BN - 1) / P->nmom + 2);
+  *staged = (long long)(d->xr + P->nmom) * (long long)((TC_ROWB / ESZ) * 8 + TC_XP_PAD) <= TC_XP_BYTES;
+  d->chains = chains;
+  d->phases = ph32;
+  d->sc = sc;
+  d->DF = DF;
+  d->R = R;
+  d->Ne = P->Ne;
+  d->nmom = P->nmom;
+  d->V3 = P->V3;
+  d->tile0 = tiles;  // the caller turns this count into the volume's first block
   const long long g_used = (long long)nb * P->g_per_t;
   e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
-  if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  kern<<<tiles, TC_THREADS, TC_SMEM, stream>>>(amap, tab, P->Ne, P->nmom, P->V3, R, chains, ph32, sc, DF, xr);
-  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
-  ED_RETURN_LAUNCH("tensor-core pair GEMM");
-  tc_df_to_c128_kernel<<<8 * sms, 256, 0, stream>>>(DF, g_used, G);
+  return ED_OK;
+}
+
+static int tc_onchip_finish(const ed_elemental_plan* P, const TcMultiVol& d, cplx<double>* G, cudaStream_t stream,
+                            int nb) {
+  tc_df_to_c128_kernel<<<8 * num_sms(), 256, 0, stream>>>(d.DF, (long long)nb * P->g_per_t, G);
   ED_RETURN_LAUNCH("double-float to complex128");
   return ED_OK;
+}
+
+// the dynamic shared memory attribute of a pair-GEMM kernel, set once per kernel
+static int tc_set_smem(const void* kern) {
+  static const void* done[16] = {};
+  for (const void* k : done)
+    if (k == kern) return ED_OK;
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+  if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
+  for (const void*& k : done)
+    if (!k) {
+      k = kern;
+      break;
+    }
+  return ED_OK;
+}
+
+template <int KIND>
+static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, const cplx<double>* phases,
+                       cplx<double>* G, void* extra, cudaStream_t stream, int nb) {
+  TcMultiVol d;
+  bool staged = false;
+  int rc = tc_onchip_prepare<KIND>(P, chains, phases, extra, stream, nb, &d, &staged);
+  if (rc) return rc;
+  const int tiles = d.tile0;
+  auto kern = staged ? tc_pair_gemm_kernel<KIND, true> : tc_pair_gemm_kernel<KIND, false>;
+  rc = tc_set_smem((const void*)kern);
+  if (rc) return rc;
+  if (P->prof_start) cudaEventRecord(P->prof_start, stream);
+  kern<<<tiles, TC_THREADS, TC_SMEM, stream>>>(d.amap, d.tab, d.Ne, d.nmom, d.V3, d.R, d.chains, d.phases, d.sc,
+                                                d.DF, d.xr);
+  if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
+  ED_RETURN_LAUNCH("tensor-core pair GEMM");
+  return tc_onchip_finish(P, d, G, stream, nb);
+}
+
+template <int KIND>
+static int launch_multi_kind(int nplans, const ed_elemental_plan* const* plans, const int* nbs, void* const* ws,
+                             cudaStream_t stream) {
+  TcMulti M;  // the launch's parameters (about 9 KB, copied by the launch)
+  M.nvol = nplans;
+  bool all_staged = true;
+  long long tiles = 0;
+  for (int v = 0; v < nplans; ++v) {
+    const ed_elemental_plan* P = plans[v];
+    char* W = (char*)ws[v];
+    bool staged = false;
+    const int rc = tc_onchip_prepare<KIND>(P, (const cplx<float>*)(W + P->off_chain),
+                                           (const cplx<double>*)(W + P->off_phase), W + P->off_extra, stream, nbs[v],
+                                           &M.v[v], &staged);
+    if (rc) return rc;
+    all_staged = all_staged && staged;
+    const int n = M.v[v].tile0;
+    M.v[v].tile0 = (int)tiles;
+    tiles += n;
+  }
+  if (tiles >= (1LL << 31)) {
+    set_error("ed_elemental_gemm_multi: too many tiles for one launch");
+    return ED_ERR_UNSUPPORTED;
+  }
+  auto kern = all_staged ? tc_pair_gemm_multi_kernel<KIND, true> : tc_pair_gemm_multi_kernel<KIND, false>;
+  int rc = tc_set_smem((const void*)kern);
+  if (rc) return rc;
+  if (tiles > 0) {
+    kern<<<(unsigned)tiles, TC_THREADS, TC_SMEM, stream>>>(M);
+    ED_RETURN_LAUNCH("tensor-core pair GEMM over several volumes");
+  }
+  for (int v = 0; v < nplans; ++v) {
+    const ed_elemental_plan* P = plans[v];
+    rc = tc_onchip_finish(P, M.v[v], (cplx<double>*)((char*)ws[v] + P->off_g), stream, nbs[v]);
+    if (rc) return rc;
+  }
+  return ED_OK;
+}
+
+int launch_pair_gemm_tc_multi(int nplans, const ed_elemental_plan* const* plans, const int* nbs, void* const* ws,
+                              cudaStream_t stream) {
+  switch (plans[0]->tc_kind) {
+    case TC_F16:
+      return launch_multi_kind<TC_F16>(nplans, plans, nbs, ws, stream);
+    case TC_BF16:
+      return launch_multi_kind<TC_BF16>(nplans, plans, nbs, ws, stream);
+    case TC_TF32:
+      return launch_multi_kind<TC_TF32>(nplans, plans, nbs, ws, stream);
+    default:
+      set_error("ed_elemental_gemm_multi: not a tensor-core split mode");
+      return ED_ERR_UNSUPPORTED;
+  }
 }
 
 // Tensor map over four k-block-major planes of R rows: dimensions (k within
@@ -881,26 +974,27 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   }
   tab.nfull = tiles;
   tiles += tiles_n;
-  static bool attr_set[4] = {};
-  static int resident[4] = {};
-  if (!attr_set[KIND]) {
-    e = cudaFuncSetAttribute(tc_fac_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             tcf_smem(TCF_MAX_STAGES));
+  const int stack = P->tc_stack == 2 ? 0 : 1;  // the stacked form unless the four-product form is asked for
+  auto kern = stack ? tc_fac_gemm_kernel<KIND, true> : tc_fac_gemm_kernel<KIND, false>;
+  static bool attr_set[4][2] = {};
+  static int resident[4][2] = {};
+  if (!attr_set[KIND][stack]) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tcf_smem(TCF_MAX_STAGES));
     if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[KIND], tc_fac_gemm_kernel<KIND>, TC_THREADS,
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[KIND][stack], kern, TC_THREADS,
                                                       tcf_smem(TCF_MAX_STAGES));
     if (e != cudaSuccess) return cuda_status(e, "tc kernel occupancy");
-    if (resident[KIND] < 1) {
+    if (resident[KIND][stack] < 1) {
       set_error("the factorised tensor-core GEMM does not fit on an SM");
       return ED_ERR_UNSUPPORTED;
     }
-    attr_set[KIND] = true;
+    attr_set[KIND][stack] = true;
   }
   const long long g_used = (long long)nb * P->g_per_t;
   e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
   // persistent grid: every CTA co-resident (the step counter of the kernel relies on it)
-  int grid = std::min(tiles, resident[KIND] * sms);
+  int grid = std::min(tiles, resident[KIND][stack] * sms);
   if (P->tc_grid > 0) grid = std::min(grid, P->tc_grid);
   const int slab_kb = P->tc_slab_kb > 0 ? P->tc_slab_kb : TC_FLUSH_KB;
   cudaLaunchConfig_t cfg = {};
@@ -915,9 +1009,8 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  const int kpb = P->tc_kpb > 0 ? P->tc_kpb : 1;
-  e = cudaLaunchKernelEx(&cfg, tc_fac_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb, nst,
-                         kpb);
+  const int kpb = P->tc_kpb > 0 ? P->tc_kpb : (stack ? 2 : 1);
+  e = cudaLaunchKernelEx(&cfg, kern, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb, nst, kpb);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("tensor-core factorised-phase GEMM");

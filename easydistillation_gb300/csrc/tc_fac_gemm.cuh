@@ -30,6 +30,10 @@ __host__ __device__ constexpr int tcf_smem(int nst) { return nst * TCF_STAGE_BYT
 static_assert(tcf_smem(TCF_MAX_STAGES) <= 232448, "shared memory per block");
 constexpr int TCF_REGS_LOW = 56, TCF_REGS_HIGH = 200;
 static_assert(256 * TCF_REGS_LOW + 256 * TCF_REGS_HIGH == TC_THREADS * TC_LAUNCH_REGS, "register split");
+// the stacked form's drain holds the same sums but reads four 64-column slices per k-block group:
+// 48 / 208 compiles without spills (56 / 200 spilled 176 bytes)
+constexpr int TCF_STACK_REGS_LOW = 48, TCF_STACK_REGS_HIGH = 208;
+static_assert(256 * TCF_STACK_REGS_LOW + 256 * TCF_STACK_REGS_HIGH == TC_THREADS * TC_LAUNCH_REGS, "register split");
 constexpr int kMaxFac = 128;  // Pxy * Pz
 
 struct TcFacJob {
@@ -117,7 +121,21 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
 // CTA has started step q - 1 (a bounded wait).  The FP32 register sums are
 // flushed into the double-float results at the end of every step, so a tile
 // is only ever touched by its owner CTA.
-template <int KIND>
+//
+// Stacked form (STACK = true).  The B stage holds the real and imaginary
+// planes of each precision part back to back, [Br_hi; Bi_hi] and
+// [Br_lo; Bi_lo], so one M = 128, N = 2 * ncol MMA computes A * [Br | Bi].
+// Two accumulators of 256 columns fill TMEM: acc1 = Ar [Br | Bi] and
+// acc2 = Ai [Br | Bi], so Re = acc1[:, :ncol] - acc2[:, ncol:] and
+// Im = acc1[:, ncol:] + acc2[:, :ncol], formed by the drain in FP32.  Half as
+// many MMAs, each twice as wide (N = 256 ran at the full per-clock tensor rate
+// in a probe of this part, N = 128 at 78 %), and no negated products; the
+// operand bytes per k-block are unchanged.  Each accumulator is single: in
+// every k-block the acc1 MMAs go first and the acc2 MMAs after them, so the
+// drain reads acc1 while the acc2 MMAs run, and the MMAs of the next TMEM
+// group into acc1 wait only for that read.  Every accumulator column takes
+// 6 accumulating MMAs per k-block (12 in the 4-product form).
+template <int KIND, bool STACK>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fac_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
                        const __grid_constant__ CUtensorMap bmap16, const __grid_constant__ TcFacTable tab, int Ne,
@@ -200,7 +218,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp < 8) {
-    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(TCF_REGS_LOW));
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(STACK ? TCF_STACK_REGS_LOW : TCF_REGS_LOW));
     if (warp == 0) {
       // ===================== TMA of the A and B planes, step by step
       if (lane == 0) {
@@ -240,11 +258,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_arrive_expect_tx(&full[s], TC_A_BYTES + 4 * ncol * TC_ROWB);
             for (int p = 0; p < 4; ++p) {  // k-block-major planes: one contiguous 8 KB box each
               tma_load_3d(As + p * TC_BM * TC_ROWB, &amap, &full[s], 0, ay, p * nkb + kb);
+              // planes re_hi, re_lo, im_hi, im_lo; stacked: [re_hi; im_hi] then [re_lo; im_lo], ncol rows each
+              uint8_t* bd = STACK ? Bs + (p & 1) * 2 * TC_BN * TC_ROWB + (p >> 1) * ncol * TC_ROWB
+                                  : Bs + p * TC_BN * TC_ROWB;
               if (ncol == TC_BN) {
-                tma_load_3d(Bs + p * TC_BN * TC_ROWB, &bmap, &full[s], 0, by, p * nkb + kb);
+                tma_load_3d(bd, &bmap, &full[s], 0, by, p * nkb + kb);
               } else {
                 for (int r = 0; r < ncol; r += 16)
-                  tma_load_3d(Bs + p * TC_BN * TC_ROWB + r * TC_ROWB, &bmap16, &full[s], 0, by + r, p * nkb + kb);
+                  tma_load_3d(bd + r * TC_ROWB, &bmap16, &full[s], 0, by + r, p * nkb + kb);
               }
             }
             issued_last = g;
@@ -265,10 +286,51 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           if (tile >= ntiles) continue;
           int jb, mtile, ntile;
           decode(tile, jb, mtile, ntile);
-          const uint32_t nfield = (uint32_t)(tile_cols(ntile) >> 3) << 17;  // the instruction's N
+          const int ncol = tile_cols(ntile);
+          const uint32_t nfield = (uint32_t)((STACK ? 2 * ncol : ncol) >> 3) << 17;  // the instruction's N
           const uint32_t ID = (IDESC & ~(0x3Fu << 17)) | nfield, ID_NEG = (IDESC_NEG & ~(0x3Fu << 17)) | nfield;
           const int kb1 = step_kb1(q);
           const int kb0s = step_kb0(q);
+          if constexpr (STACK) {
+            for (int kb = kb0s; kb < kb1 && ok; ++kb, ++g) {
+              const int s = (int)(g % nst);
+              const bool first = (kb - kb0s) % kpb == 0;
+              const bool last = (kb - kb0s) % kpb == kpb - 1 || kb == kb1 - 1;
+              if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL)) {
+                ok = false;
+                break;
+              }
+              const uint32_t a0 = smem_u32(smem + s * TCF_STAGE_BYTES);
+              const uint32_t b0 = a0 + TC_A_BYTES;
+#pragma unroll
+              for (int h = 0; h < 2; ++h) {  // acc1 = Ar [Br | Bi], then acc2 = Ai [Br | Bi]
+                if (first && gb >= 1 &&
+                    !mbar_wait(&acce[h], (uint32_t)((gb - 1) & 1), status, TC_ERR_ACCE)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + h * 256;
+#pragma unroll
+                for (int ks = 0; ks < KE / KINST; ++ks) {  // correction products first
+                  const uint32_t acc = (ks > 0 || !first) ? 1u : 0u;
+                  const uint32_t ao = a0 + 2 * h * TC_BM * TC_ROWB + ks * 32, bo = b0 + ks * 32;
+                  umma<KIND>(d, umma_desc_sw64(ao), umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB), ID, acc);
+                  umma<KIND>(d, umma_desc_sw64(ao + TC_BM * TC_ROWB), umma_desc_sw64(bo), ID, 1u);
+                }
+#pragma unroll
+                for (int ks = 0; ks < KE / KINST; ++ks) {
+                  const uint32_t ao = a0 + 2 * h * TC_BM * TC_ROWB + ks * 32, bo = b0 + ks * 32;
+                  umma<KIND>(d, umma_desc_sw64(ao), umma_desc_sw64(bo), ID, 1u);
+                }
+                if (last) umma_commit(&accf[h]);  // this accumulator is ready to drain
+              }
+              if (!ok) break;
+              umma_commit(&empty[s]);  // frees the stage when these MMAs complete
+              if (last) ++gb;
+            }
+            continue;
+          }
           for (int kb = kb0s; kb < kb1; ++kb, ++g) {
             const int s = (int)(g % nst);
             const int b = (int)(gb & 1);
@@ -321,7 +383,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
     }
   } else {
-    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(TCF_REGS_HIGH));
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(STACK ? TCF_STACK_REGS_HIGH : TCF_REGS_HIGH));
     // ===================== drain: TMEM -> FP32 register sums -> double-float result per step
     const int dw = warp - 8;         // 0..7
     const int quarter = warp & 3;    // TMEM lane quarter this warp may access
@@ -343,6 +405,65 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
       for (int c = 0; c < 64; ++c) sre[c] = sim[c] = 0.f;
       const int kb1 = step_kb1(q);
+      if constexpr (STACK) {
+        const int ncol = tile_cols(ntile);
+        for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one group of kpb k-blocks
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            if (!warp_wait(&accf[h], (uint32_t)(g & 1), status, TC_ERR_ACC)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            // acc1: Re += [0, ncol), Im += [ncol, 2 ncol); acc2: Im += [0, ncol), Re -= [ncol, 2 ncol)
+            const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16) + h * 256 + half * 64;
+            {
+              uint32_t r0[32], r1[32];
+              tmem_ld32(tl, r0);
+              tmem_ld32(tl + 32, r1);
+              tmem_wait_ld();
+              if (h == 0) {
+#pragma unroll
+                for (int e = 0; e < 32; ++e) {
+                  sre[e] += __uint_as_float(r0[e]);
+                  sre[32 + e] += __uint_as_float(r1[e]);
+                }
+              } else {
+#pragma unroll
+                for (int e = 0; e < 32; ++e) {
+                  sim[e] += __uint_as_float(r0[e]);
+                  sim[32 + e] += __uint_as_float(r1[e]);
+                }
+              }
+            }
+            {
+              uint32_t r0[32], r1[32];
+              tmem_ld32(tl + ncol, r0);
+              tmem_ld32(tl + ncol + 32, r1);
+              tmem_wait_ld();
+              if (h == 0) {
+#pragma unroll
+                for (int e = 0; e < 32; ++e) {
+                  sim[e] += __uint_as_float(r0[e]);
+                  sim[32 + e] += __uint_as_float(r1[e]);
+                }
+              } else {
+#pragma unroll
+                for (int e = 0; e < 32; ++e) {
+                  sre[e] -= __uint_as_float(r0[e]);
+                  sre[32 + e] -= __uint_as_float(r1[e]);
+                }
+              }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[h]);
+          }
+          if (!ok) break;
+        }
+        if (ok) flush_sums_fac(sre, sim, DF, tab, J, Ne, n0c, m_local, Mrows, inv);
+        continue;
+      }
       for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one TMEM buffer of kpb k-blocks
         const int b = (int)(g & 1);
         if (!warp_wait(&accf[b], (uint32_t)((g >> 1) & 1), status, TC_ERR_ACC)) {

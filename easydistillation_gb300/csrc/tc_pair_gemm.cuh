@@ -81,11 +81,13 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
 // STAGED: the left-chain rows and all phase rows of a k-block fit the staging
 // area (xr + nmom rows); the TMA warp then copies them into shared memory and
 // the producers read them there instead of from global memory.
+// The body of one CTA: tile `tile` of the job table `tab` (the kernels below pass their tensor map and table
+// from the launch's parameter space).
 template <int KIND, bool STAGED>
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_pair_gemm_kernel(const __grid_constant__ CUtensorMap amap, TcTable tab, int Ne, int nmom, int V3, long long R,
-                        const cplx<float>* __restrict__ chains, const cplx<float>* __restrict__ phases,
-                        TcScalars* __restrict__ sc, float4* __restrict__ DF, int xr) {
+__device__ __forceinline__ void tc_pair_gemm_body(const CUtensorMap* amap, const TcTable& tab, int Ne, int nmom,
+                                                  int V3, long long R, const cplx<float>* __restrict__ chains,
+                                                  const cplx<float>* __restrict__ phases, TcScalars* __restrict__ sc,
+                                                  float4* __restrict__ DF, int xr, int tile) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;  // k elements per stage
   constexpr int EPC = 16 / ESZ;      // k elements per 16-byte chunk
@@ -110,7 +112,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   volatile int* status = &sc->status;
 
   // ---- decode the tile: group, n tile (fast), m tile
-  const int tile = blockIdx.x;
   int jb = 0;
   while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
   const TcJob J = tab.j[jb];
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         uint8_t* As = smem + s * TC_STAGE_BYTES;
         mbar_arrive_expect_tx(&full[s], TC_A_BYTES);
         for (int q = 0; q < 4; ++q)
-          tma_load_2d(As + q * TC_BM * TC_ROWB, &amap, &full[s], kb * KE, (int)(q * R + row0));
+          tma_load_2d(As + q * TC_BM * TC_ROWB, amap, &full[s], kb * KE, (int)(q * R + row0));
         issued_last = kb;
       }
       if (issued_last >= 0)  // do not leave while our copies may still land in shared memory
@@ -397,4 +398,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
   }
+}
+
+template <int KIND, bool STAGED>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_pair_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ TcTable tab, int Ne,
+                        int nmom, int V3, long long R, const cplx<float>* __restrict__ chains,
+                        const cplx<float>* __restrict__ phases, TcScalars* __restrict__ sc, float4* __restrict__ DF,
+                        int xr) {
+  tc_pair_gemm_body<KIND, STAGED>(&amap, tab, Ne, nmom, V3, R, chains, phases, sc, DF, xr, (int)blockIdx.x);
+}
+
+// Several lattice volumes (batched plans with their own Ne, V3, chains and results) in ONE launch: the tiles
+// of volume v are blocks tile0[v] .. tile0[v+1]-1, so the small volumes' tiles share the waves of the large
+// ones instead of running as launches of their own.
+constexpr int kMaxVol = 4;
+struct TcMultiVol {
+  CUtensorMap amap;
+  TcTable tab;
+  const cplx<float>* chains;
+  const cplx<float>* phases;
+  TcScalars* sc;
+  float4* DF;
+  long long R;
+  int Ne, nmom, V3, xr, tile0;
+};
+struct TcMulti {
+  TcMultiVol v[kMaxVol];
+  int nvol;
+};
+
+template <int KIND, bool STAGED>
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_pair_gemm_multi_kernel(const __grid_constant__ TcMulti M) {
+  int v = 0;
+  while (v + 1 < M.nvol && (int)blockIdx.x >= M.v[v + 1].tile0) ++v;
+  const TcMultiVol& D = M.v[v];
+  tc_pair_gemm_body<KIND, STAGED>(&D.amap, D.tab, D.Ne, D.nmom, D.V3, D.R, D.chains, D.phases, D.sc, D.DF, D.xr,
+                                  (int)blockIdx.x - D.tile0);
 }

@@ -355,7 +355,8 @@ def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
 MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3, "ozaki_i8": 4}
 _FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR = 0x100, 0x200
 #: plan launch settings (ED_TUNE_* keys)
-TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4, "tc_pair": 5, "tc_kpb": 6}
+TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4, "tc_pair": 5, "tc_kpb": 6,
+               "tc_stack": 7}
 #: FP64 pair GEMM tile shapes (rows, cols) by ED_TUNE_F64_TILE value
 F64_TILES = {0: (64, 64), 1: (32, 64), 2: (64, 32), 3: (32, 32)}
 
@@ -469,6 +470,15 @@ class ElementalPlan:
         """Several timeslices in one pass (one pair-contraction launch).
         ``links``/``evecs``/``outs``: equal-length lists of device tensors, each
         as in :meth:`run`; at most ``batch`` of them."""
+        nb, prec = self._check_batch(links, evecs, outs)
+        ws = self.workspace()
+        P = ctypes.c_void_p * nb
+        call("ed_elemental_run_batch", self._h, nb, P(*[ptr(t) for t in links]), dir_stride, site_stride, prec,
+             P(*[ptr(t) for t in evecs]), None if blend is None else ptr(blend), P(*[ptr(t) for t in outs]),
+             ptr(ws), ws.numel(), stream_handle())
+        return outs
+
+    def _check_batch(self, links, evecs, outs):
         nb = len(links)
         if not (0 < nb <= self.batch) or len(evecs) != nb or len(outs) != nb:
             raise ValueError(f"need 1..{self.batch} timeslices with matching links, evecs and outs")
@@ -479,11 +489,31 @@ class ElementalPlan:
                 raise ValueError("all eigenvector blocks must share a precision")
         for o in outs:
             require_cuda(o, "out")
+        return nb, prec
+
+    def run_batch_begin(self, links, dir_stride: int, site_stride: int, evecs):
+        """First part of :meth:`run_batch` (``ed_elemental_run_batch_begin``):
+        the phases and chains of ``len(links)`` timeslices.  The pair
+        contraction follows in :func:`gemm_multi`, the combine in
+        :meth:`run_batch_end`."""
+        nb, prec = self._check_batch(links, evecs, evecs)
         ws = self.workspace()
         P = ctypes.c_void_p * nb
-        call("ed_elemental_run_batch", self._h, nb, P(*[ptr(t) for t in links]), dir_stride, site_stride, prec,
-             P(*[ptr(t) for t in evecs]), None if blend is None else ptr(blend), P(*[ptr(t) for t in outs]),
-             ptr(ws), ws.numel(), stream_handle())
+        call("ed_elemental_run_batch_begin", self._h, nb, P(*[ptr(t) for t in links]), dir_stride, site_stride, prec,
+             P(*[ptr(t) for t in evecs]), ptr(ws), ws.numel(), stream_handle())
+
+    def run_batch_end(self, outs, blend: torch.Tensor = None):
+        """Last part of :meth:`run_batch` (``ed_elemental_run_batch_end``): the
+        combine of the contracted pairs into ``outs``."""
+        nb = len(outs)
+        if not (0 < nb <= self.batch):
+            raise ValueError(f"need 1..{self.batch} outputs")
+        for o in outs:
+            require_cuda(o, "out")
+        ws = self.workspace()
+        P = ctypes.c_void_p * nb
+        call("ed_elemental_run_batch_end", self._h, nb, None if blend is None else ptr(blend),
+             P(*[ptr(t) for t in outs]), ptr(ws), ws.numel(), stream_handle())
         return outs
 
     def describe(self):
@@ -517,6 +547,23 @@ class ElementalPlan:
             except Exception:
                 pass
             self._h = None
+
+
+def gemm_multi(plans, nbatch) -> int:
+    """The pair contraction of several batched plans (each after its
+    :meth:`ElementalPlan.run_batch_begin`, ``nbatch[v]`` timeslices) in one
+    launch when all take the on-chip-phase tensor-core path with the same
+    split mode, else one launch per plan (``ed_elemental_gemm_multi``).
+    Returns the number of GEMM launches."""
+    n = len(plans)
+    if n == 0 or len(nbatch) != n:
+        raise ValueError("need one batch size per plan")
+    wss = [p.workspace() for p in plans]
+    launches = ctypes.c_int()
+    call("ed_elemental_gemm_multi", n, (ctypes.c_void_p * n)(*[p._h for p in plans]), (ctypes.c_int * n)(*nbatch),
+         (ctypes.c_void_p * n)(*[ptr(w) for w in wss]), (ctypes.c_size_t * n)(*[w.numel() for w in wss]),
+         ctypes.byref(launches), stream_handle())
+    return launches.value
 
 
 class PairPlan:

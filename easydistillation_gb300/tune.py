@@ -214,10 +214,12 @@ FP64_PROXY_EXTENT = 12
 
 def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "f16x3", batch: int = 1,
                    device=None, evec_dtype=torch.complex128, reps: int = 3, cache: Optional[TuningCache] = None,
-                   retune: bool = False) -> TuneResult:
+                   retune: bool = False, forms: Optional[Sequence[object]] = None) -> TuneResult:
     """Best ``Candidate`` (plan form and launch settings) for this elemental
     shape, from the cache or by measurement.  ``batch`` timeslices per run, as
     the caller's plan will have; ``reps`` timed runs per candidate (median).
+    ``forms`` restricts the GEMM forms tried (``factorise`` values, e.g.
+    ``[True]``: the library's default form for the momentum list).
     The FP64 mode is timed on a proxy lattice (``FP64_PROXY_EXTENT``)."""
     if mode not in MODES:
         raise ValueError(f"unknown elemental mode {mode!r}")
@@ -225,6 +227,8 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
     cache = cache or TuningCache()
     dev = device_key(device)
     key = elemental_key(latt_size, Ne, num_nabla, momentum_list, mode, batch, evec_dtype)
+    if forms is not None:
+        key += "|forms=" + ",".join(str(f) for f in forms)
     if not retune:
         hit = cache.get(dev, key)
         if hit is not None:
@@ -267,8 +271,8 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
     if mode == "fp64":
         stages.append(lambda best: [Candidate(True, {"f64_tile": t}) for t in sorted(F64_TILES)])
     else:
-        forms = factorise_options(latt_size, Ne, num_nabla, moms, mode)
-        stages.append(lambda best: [Candidate(f, {}) for f in forms])
+        tried = list(forms) if forms is not None else factorise_options(latt_size, Ne, num_nabla, moms, mode)
+        stages.append(lambda best: [Candidate(f, {}) for f in tried])
 
         def factorised(best: Candidate) -> bool:
             probe = ElementalPlan(latt_size, Ne, num_nabla, moms, mode, device="cpu", batch=batch,
@@ -276,11 +280,12 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
             return probe.factorised is not None and mode != "ozaki_i8"
 
         def forms_on_sms(best: Candidate) -> List[Candidate]:
-            # the factorised GEMM on single SMs or on SM pairs, each with 1 or 2 k-blocks per TMEM buffer
+            # the factorised GEMM on single SMs (stacked operands with 2 or 4 k-blocks per accumulator group,
+            # or the four-product form) or on SM pairs
             if not factorised(best):
                 return []
             return [Candidate(best.factorise, dict(t)) for t in
-                    ({}, {"tc_kpb": 2}, {"tc_pair": 2}, {"tc_pair": 2, "tc_kpb": 2})]
+                    ({}, {"tc_kpb": 4}, {"tc_stack": 2, "tc_kpb": 2}, {"tc_pair": 2, "tc_kpb": 2})]
 
         def slabs(best: Candidate) -> List[Candidate]:
             if not factorised(best):
@@ -293,7 +298,8 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
 
         stages.append(forms_on_sms)
         stages.append(slabs)
-    res = _run_search(stages, Candidate(True, {}), measure, _rel_err, TOLERANCE[mode])
+    start = Candidate(True if forms is None else list(forms)[0], {})
+    res = _run_search(stages, start, measure, _rel_err, TOLERANCE[mode])
     cache.put(dev, key, {"best": res.best.as_dict(), "ms": res.ms, "trials": res.trials,
                          "measured_lattice": meas_latt[:3]})
     return res

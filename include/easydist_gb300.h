@@ -87,15 +87,19 @@ extern "C" {
                               * 128 x 128 tiles, 2 = two-CTA clusters on SM pairs with 256 x 128
                               * tiles (tcgen05.mma.cta_group::2) */
 #define ED_TUNE_TC_KPB 6     /* k-blocks the factorised GEMM accumulates in one TMEM buffer before the
-                              * drain warps read it: 0 (default, 1), 2 or 4.  The tensor core's FP32
-                              * accumulation truncates, so longer buffers trade accuracy (measured
-                              * at 32^3, Ne = 200, f16x3: 2.0e-7 -> 5.1e-7 vs FP64 for 2) for fewer
-                              * buffer hand-overs */
-#define ED_TUNE_TC_STACK 7   /* single-SM factorised GEMM operand form: 0 (default) = four real
-                              * products per complex one, M = N = 128 MMAs into [re], [im]
-                              * accumulators (double-buffered); 1 = stacked: B = [Br; Bi] in
-                              * shared memory, two M = 128, N = 256 MMAs A_re [Br | Bi] and
-                              * A_im [Br | Bi] into single accumulators, combined by the drain */
+                              * drain warps read it: 0 (the form's default: 2 for the stacked form,
+                              * 1 otherwise), 1, 2 or 4.  The tensor core's FP32 accumulation
+                              * truncates, so longer buffers trade accuracy for fewer hand-overs
+                              * (measured at 32^3, Ne = 200, f16x3 vs FP64: four-product form
+                              * 2.0e-7 with 1, 5.1e-7 with 2; stacked form 2.6e-7 with 2) */
+#define ED_TUNE_TC_STACK 7   /* single-SM factorised GEMM operand form: 0 (default) or 1 = stacked:
+                              * B = [Br; Bi] in shared memory, two M = 128, N = 256 MMAs
+                              * A_re [Br | Bi] and A_im [Br | Bi] per split product into single
+                              * 256-column accumulators, re / im formed by the drain (143 ms per
+                              * 4 timeslices at 32^3, Ne = 200, f16x3); 2 = four real products
+                              * per complex one, M = N = 128 MMAs into double-buffered [re], [im]
+                              * accumulators (165-172 ms).  SM pairs (ED_TUNE_TC_PAIR = 2) use the
+                              * four-product form. */
 
 /* Library version as 10000*major + 100*minor + patch. */
 int ed_version(void);
@@ -367,6 +371,29 @@ int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx, int Ly, i
 int ed_elemental_run_batch(const ed_elemental_plan* plan, int nbatch, const void* const* links, long long dir_stride,
                            long long site_stride, int evec_prec, const void* const* evecs, const double* blend,
                            void* const* outs, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ed_elemental_run_batch in three parts, so that several batched plans (lattice
+ * volumes with their own Ne, each with its own workspace) share ONE
+ * pair-contraction launch: for every plan ed_elemental_run_batch_begin (the
+ * phase table and the chains of its nbatch timeslices), then one
+ * ed_elemental_gemm_multi over all plans, then ed_elemental_run_batch_end per
+ * plan (the combine into the outputs).  The three parts of a plan run in
+ * stream order on the same stream and together equal one
+ * ed_elemental_run_batch; they allocate nothing, so the sequence can be
+ * captured in a CUDA graph.  ed_elemental_gemm_multi issues one launch whose
+ * blocks cover the tiles of every plan when all plans (at most 4) take the
+ * on-chip-phase tensor-core path with the same split mode (f16x3, bf16x3 or
+ * tf32x3, a momentum list that is not factorised); otherwise one launch per
+ * plan.  *launches (may be NULL) receives the number of GEMM launches.  The
+ * reference computes each (volume, timeslice) by its own
+ * ElementalGenerator.calc(t) (lattice/generator/elemental.py:290-338). */
+int ed_elemental_run_batch_begin(const ed_elemental_plan* plan, int nbatch, const void* const* links,
+                                 long long dir_stride, long long site_stride, int evec_prec, const void* const* evecs,
+                                 void* workspace, size_t workspace_bytes, void* stream);
+int ed_elemental_gemm_multi(int nplans, const ed_elemental_plan* const* plans, const int* nbatch,
+                            void* const* workspaces, const size_t* workspace_bytes, int* launches, void* stream);
+int ed_elemental_run_batch_end(const ed_elemental_plan* plan, int nbatch, const double* blend, void* const* outs,
+                               void* workspace, size_t workspace_bytes, void* stream);
 
 /* Generic pair contraction on caller-built chains (the GEMM stage of
  * elemental.py:324-329 / displacement_elemental.py:94-95):

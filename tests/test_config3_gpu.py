@@ -1,7 +1,8 @@
-"""Mixed volumes at their real sizes in ONE captured graph: one timeslice
-each of 16^3 (Ne = 64), 24^3 (Ne = 128) and 32^3 (Ne = 256), links
-exp(i eps A) with eps 0.1 / 0.3, 4 operators x 7 momenta, f16x3, against
-the plain FP64 GPU path of each volume: relative Frobenius error <= 1e-6."""
+"""Mixed volumes at their real sizes in ONE captured graph with ONE pair-GEMM
+launch: one timeslice each of 16^3 (Ne = 64), 24^3 (Ne = 128) and 32^3
+(Ne = 256), links exp(i eps A) with eps 0.1 / 0.3, 4 operators x 7 momenta,
+f16x3, against the plain FP64 GPU path of each volume: relative Frobenius
+error <= 1e-6."""
 
 import numpy as np
 import pytest
@@ -34,6 +35,7 @@ def test_mixed_real_volumes_one_graph_vs_fp64():
     outs = [o.clone() for o in mv.run()]
     mv.check_status()
     assert mv.graph is not None
+    assert mv.gemm_launches == 1  # the three volumes' pair contractions share one launch
     for (latt, Ne, eps, seed), v, out in zip(specs, vols, outs):
         V3 = latt[0] * latt[1] * latt[2]
         plan = ElementalPlan(latt, Ne, 1, moms, "fp64", tuning={"f64_tile": 3})

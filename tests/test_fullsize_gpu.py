@@ -80,6 +80,27 @@ def test_elemental_split_modes_vs_fp64_full_size(fp64_full, mode):
     torch.cuda.empty_cache()
 
 
+@pytest.mark.parametrize("tuning", [{"tc_kpb": 4}, {"tc_stack": 2}, {"tc_stack": 2, "tc_kpb": 2},
+                                    {"tc_pair": 2}, {"tc_pair": 2, "tc_kpb": 2}])
+def test_f16x3_gemm_forms_vs_fp64_full_size(fp64_full, tuning):
+    """The other forms of the factorised GEMM the autotuner may pick (stacked
+    operands with 4 k-blocks per accumulator group; the four-product form
+    with 1 or 2; SM pairs) at full size: within 1e-6 of FP64."""
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.ops import ElementalPlan
+
+    U, V, ref = fp64_full
+    V3 = LATT[0] * LATT[1] * LATT[2]
+    plan = ElementalPlan(LATT, NE, 2, mom_dict_to_list(3), "f16x3", tuning=tuning)
+    o = torch.empty((13, 27, NE, NE), dtype=torch.complex128, device="cuda")
+    plan.run(U, V3 * 9, 9, V, o)
+    plan.check_status()
+    err = float(torch.linalg.vector_norm(o - ref) / torch.linalg.vector_norm(ref))
+    assert err <= 1e-6, (tuning, err)
+    del plan
+    torch.cuda.empty_cache()
+
+
 def test_chebyshev_eigensolve_full_size():
     from easydistillation_gb300.ops import lanczos_tr, laplacian, links_to_soa
 

@@ -113,3 +113,38 @@ def test_mixed_volume_graph_one_replay():
         evec *= np.exp(1j * rng.uniform(0, 2 * np.pi, evec.shape[:2]))[..., None, None, None, None]
         v.evecs.copy_(torch.from_numpy(evec.reshape(evec.shape[0], evec.shape[1], -1)))
     check()
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3"])
+def test_mixed_volumes_one_gemm_launch_per_round(mode):
+    """Three volumes with their own Ne on the on-chip-phase tensor-core path
+    (4 operators x 7 momenta): every round of admitted chunks contracts all
+    volumes with ONE pair-GEMM launch (ed_elemental_gemm_multi).  With batches
+    of 2 and 5, 3 and 4 timeslices the three rounds hold 3, 3 and 1 volumes.  Results agree
+    with the oracle and are bit-identical to one GEMM launch per volume chunk
+    (every tile runs the same MMA and flush sequence in either launch)."""
+    from easydistillation_gb300.batch import MixedVolumeGraph, VolumeBinding
+    from easydistillation_gb300.generator.elemental import links_to_device
+
+    moms = R.mom_dict_to_list(3)[:7]
+    specs = [([8, 4, 4, 3], 10, 0.3, 61, [0, 1, 2, 2, 0]), ([4, 4, 4, 2], 6, 0.1, 62, [1, 0, 1]),
+             ([8, 8, 4, 2], 12, 0.3, 63, [0, 1, 1, 0])]
+    vols, host = [], []
+    for latt, Ne, eps, seed, ts in specs:
+        gauge, evec = _inputs(latt, Ne, eps, seed)
+        vols.append(VolumeBinding(latt, Ne, links_to_device(gauge, latt, "cuda"),
+                                  torch.from_numpy(evec.reshape(latt[3], Ne, -1)).cuda(), ts))
+        host.append((gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3], evec))
+    mv = MixedVolumeGraph(vols, 1, moms, mode, max_batch=2)
+    outs = [o.clone() for o in mv.run()]
+    mv.check_status()
+    assert mv.graph is not None and mv.gemm_launches == 3  # one launch per round
+    for (latt, Ne, eps, seed, ts), (Uh, evec), out in zip(specs, host, outs):
+        for k, t in enumerate(ts):
+            assert rel_err(out[k].cpu().numpy(), R.elemental(evec[t], Uh[:, t], latt, 1, moms)) < 1e-6
+    per_volume = MixedVolumeGraph(vols, 1, moms, mode, max_batch=2, single_launch=False)
+    ref = per_volume.run()
+    per_volume.check_status()
+    assert per_volume.gemm_launches == 3 + 2 + 2
+    for a, b in zip(outs, ref):
+        assert torch.equal(a, b)
