@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="build the plans with the built-in defaults instead of the autotuner's choice (which is "
                          "measured before the timed region and cached per device and shape)")
+    ap.add_argument("--gauss", action="store_true",
+                    help="headline plan in the Gauss three-multiplication form (ED_MODE_FLAG_GAUSS; --no-autotune runs)")
     ap.add_argument("--tuning", default="",
                     help="explicit plan launch settings for --no-autotune runs, e.g. tc_kpb=2,tc_pair=1 (profiling)")
     ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
@@ -414,7 +416,7 @@ def run_ours(args, rank, world):
                              tuning=res.best.tuning)
     else:
         plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, args.mode, dev, batch=B, factorise=not args.no_factor,
-                             tuning=parse_tuning(args.tuning))
+                             tuning=parse_tuning(args.tuning), gauss=args.gauss)
     outs = [torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev) for _ in range(B)]
     out = outs[0]
     stream = torch.cuda.current_stream()
@@ -489,7 +491,8 @@ def run_ours(args, rank, world):
         else:
             tiles = sum(-(-(j * Ne) // 128) for j in rights) * (-(-(Ne * NMOM) // 128))
             kname = f"tc_pair_gemm_kernel<{args.mode}>"
-        mma_flop = B * tiles * 128 * 128 * 3 * V3 * 12 * 2.0
+        per_mac = 9 if getattr(plan, "gauss", False) else 12  # real MMAs per complex multiply-add (3 split products)
+        mma_flop = B * tiles * 128 * 128 * 3 * V3 * per_mac * 2.0
         default_workload = (plan.factorised is not None and args.mode == "f16x3" and B == 4 and Ne == NE
                             and list(latt[:3]) == LATT[:3])
         roofline = {"bound": "tensor", "achieved": alg_flop / kms / 1e9, "peak": pk, "unit": "TFLOP/s",
@@ -501,7 +504,8 @@ def run_ours(args, rank, world):
                     "pairs_evaluated_per_momentum": plan.num_pairs, "ref_subsets_per_momentum": REF_SUBSETS,
                     "note": "achieved = algorithmic flops 8*Ne^2*3V3*Nmom*43 per timeslice (the reference's subset "
                             "count); the kernel evaluates 19 distinct chain pairs per momentum and issues 12 "
-                            "fp16/tf32 MMAs per complex multiply-add (3x) plus tile padding (mma_*)"}
+                            "fp16/tf32 MMA products per complex multiply-add (9 in the Gauss form; 3 split "
+                            "products each) plus tile padding (mma_*)"}
 
     # the plain FP64 GPU path on the same timeslice: speed and the split-precision error against it
     fp64 = None
@@ -639,11 +643,12 @@ def bench_split_modes(args, latt, Ne, moms, U, V, out64, t_ref, dev, stream, exc
     Lx, Ly, Lz, Lt = latt
     V3 = Lx * Ly * Lz
     out = {}
-    for mode in ("f16x3", "tf32x3", "bf16x3", "ozaki_i8"):
-        if mode == exclude:
+    for name in ("f16x3", "tf32x3", "bf16x3", "ozaki_i8", "f16x3_gauss3m"):
+        mode, gauss = name.split("_gauss")[0], name.endswith("gauss3m")
+        if name == exclude:
             continue
         B = 1 if mode == "ozaki_i8" else 2
-        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, mode, dev, batch=B)
+        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, mode, dev, batch=B, gauss=gauss)
         outs = [torch.empty((13, NMOM, Ne, Ne), dtype=torch.complex128, device=dev) for _ in range(B)]
 
         def step(i):
@@ -670,8 +675,10 @@ def bench_split_modes(args, latt, Ne, moms, U, V, out64, t_ref, dev, stream, exc
         plan.run(U[:, t_ref], Lt * V3 * 9, 9, V[args.warmup % RESIDENT_T], outs[0])
         plan.check_status()
         err = float(torch.linalg.vector_norm(outs[0] - out64) / torch.linalg.vector_norm(out64))
-        out[mode] = {"value": reps * B / (ms / 1e3), "unit": "timeslices/s", "kernel_ms_per_step": kms,
+        out[name] = {"value": reps * B / (ms / 1e3), "unit": "timeslices/s", "kernel_ms_per_step": kms,
                      "timeslices_per_step": B, "rel_err_vs_fp64": err, "factorised_phases": plan.factorised}
+        if gauss:
+            out[name]["form"] = "Gauss three multiplications (ED_MODE_FLAG_GAUSS), 2 k-blocks per group"
         del plan, outs
         torch.cuda.empty_cache()
     return out

@@ -540,7 +540,7 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0, "ed_elemental_plan_create: sizes must be positive");
   ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create: num_nabla must be 0, 1 or 2");
   ED_CHECK_ARG(moms, "ed_elemental_plan_create: null momentum list");
-  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) == 0 &&
+  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR | ED_MODE_FLAG_GAUSS)) == 0 &&
                    (~mode & (ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) != 0,
                "ed_elemental_plan_create: unknown mode %d", mode);
   ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create: lattice too large");
@@ -554,6 +554,7 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   P->mode = mode & 0xff;
   P->no_factor = (mode & ED_MODE_FLAG_NO_FACTOR) != 0;
   P->force_factor = (mode & ED_MODE_FLAG_FORCE_FACTOR) != 0;
+  P->gauss = (mode & ED_MODE_FLAG_GAUSS) != 0;
   P->use_herm = true;
   P->moms.assign(moms, moms + 3 * nmom);
   int rc = ed::plan_build(P);

@@ -64,6 +64,7 @@ struct ed_elemental_plan {
   int tc_stages = 0;   // operand stages of the factorised GEMM (0 = the default of the GEMM form)
   int tc_pair = 0;     // factorised GEMM on single SMs (1) or on SM pairs (2); 0 = the built-in default
   int tc_kpb = 0;      // k-blocks accumulated per TMEM buffer of the factorised GEMM: 1, 2 or 4 (0: the form's default)
+  bool gauss = false;  // factorised split GEMM in the Gauss three-multiplication form (ED_MODE_FLAG_GAUSS)
   int tc_stack = 0;    // factorised GEMM on single SMs: 0/1 = stacked [re | im] B operand (N = 256), 2 = four products
   int f64_ksplit = 1;  // K-split partial buffers the FP64 pair GEMM may use (sized at plan build)
 };

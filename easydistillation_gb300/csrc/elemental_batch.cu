@@ -33,7 +33,7 @@ extern "C" int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx
                "ed_elemental_plan_create_batched: sizes must be positive");
   ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create_batched: num_nabla must be 0, 1 or 2");
   ED_CHECK_ARG(moms, "ed_elemental_plan_create_batched: null momentum list");
-  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) == 0 &&
+  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR | ED_MODE_FLAG_GAUSS)) == 0 &&
                    (~mode & (ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) != 0,
                "ed_elemental_plan_create_batched: unknown mode %d", mode);
   ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create_batched: lattice too large");
@@ -47,6 +47,7 @@ extern "C" int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx
   P->mode = mode & 0xff;
   P->no_factor = (mode & ED_MODE_FLAG_NO_FACTOR) != 0;
   P->force_factor = (mode & ED_MODE_FLAG_FORCE_FACTOR) != 0;
+  P->gauss = (mode & ED_MODE_FLAG_GAUSS) != 0;
   P->use_herm = true;
   P->nbatch = max_batch;
   P->moms.assign(moms, moms + 3 * nmom);

@@ -336,7 +336,7 @@ constexpr int kSplitUnrollRight = 4, kSplitUnrollLeft = 1;
 
 // Writes the nvar variants of the two complex elements v (k = 2*kp, 2*kp + 1)
 // of chain row (slot, i) into the planes.
-template <int KIND, bool LEFT>
+template <int KIND, bool LEFT, bool SUM>
 __device__ __forceinline__ void tc_fac_split_emit(const float4 v, int kp, long long orow0, int Ne, int nvar,
                                                   const cplx<float>* __restrict__ fac, int V3, long long Rplane,
                                                   long long K, int K2, void* __restrict__ planes) {
@@ -375,6 +375,14 @@ __device__ __forceinline__ void tc_fac_split_emit(const float4 v, int kp, long l
       Split<TC_TF32>::one(im1, h, l);
       P[2 * plane + e0 + 1] = h;
       P[3 * plane + e0 + 1] = l;
+      if constexpr (SUM) {  // planes 4, 5: re + im (Gauss form)
+        Split<TC_TF32>::one(re0 + im0, h, l);
+        P[4 * plane + e0] = h;
+        P[5 * plane + e0] = l;
+        Split<TC_TF32>::one(re1 + im1, h, l);
+        P[4 * plane + e0 + 1] = h;
+        P[5 * plane + e0 + 1] = l;
+      }
     } else {
       uint32_t* P = (uint32_t*)planes;  // 16-bit elements, pairs as words (16 words per 64-byte row)
       const long long plane = Rplane * K2, w = (((long long)kp / 16) * Rplane + orow) * 16 + kp % 16;
@@ -385,6 +393,11 @@ __device__ __forceinline__ void tc_fac_split_emit(const float4 v, int kp, long l
       Split<KIND>::pair(im0, im1, h, l);
       P[2 * plane + w] = h;
       P[3 * plane + w] = l;
+      if constexpr (SUM) {  // planes 4, 5: re + im (Gauss form)
+        Split<KIND>::pair(re0 + im0, re1 + im1, h, l);
+        P[4 * plane + w] = h;
+        P[5 * plane + w] = l;
+      }
     }
   }
 }
@@ -395,7 +408,7 @@ __device__ __forceinline__ void tc_fac_split_emit(const float4 v, int kp, long l
 // complex64, already scaled by 2^e (tc_phase_kernel).  A block covers
 // UNROLL * blockDim.x element pairs of a row; each thread loads its UNROLL
 // pairs (blockDim.x apart) before it writes any variant.
-template <int KIND, bool LEFT, int UNROLL>
+template <int KIND, bool LEFT, int UNROLL, bool SUM>
 __global__ void __launch_bounds__(256, 3) tc_fac_split_kernel(const cplx<float>* __restrict__ chains, TcFacSlots sl, int nrows, int Ne,
                                     int nvar, const cplx<float>* __restrict__ fac, int V3, long long Rplane,
                                     void* __restrict__ planes) {
@@ -417,7 +430,7 @@ __global__ void __launch_bounds__(256, 3) tc_fac_split_kernel(const cplx<float>*
 #pragma unroll
       for (int u = 0; u < UNROLL; ++u) {
         const int kp = k0 + u * blockDim.x;
-        if (kp < K2) tc_fac_split_emit<KIND, LEFT>(v[u], kp, orow0, Ne, nvar, fac, V3, Rplane, K, K2, planes);
+        if (kp < K2) tc_fac_split_emit<KIND, LEFT, SUM>(v[u], kp, orow0, Ne, nvar, fac, V3, Rplane, K, K2, planes);
       }
     }
   }
@@ -511,8 +524,9 @@ static FacLayout fac_layout(const ed_elemental_plan* P) {
   L.fxy32 = L.fz + up256((size_t)P->fac_pz * P->V3 * 16);
   L.fz32 = L.fxy32 + up256((size_t)P->fac_pxy * P->V3 * 8);
   L.bpl = L.fz32 + up256((size_t)P->fac_pz * P->V3 * 8);
-  L.apl = L.bpl + up256(4 * (size_t)L.rb * K * esz);
-  L.df = L.apl + up256(4 * (size_t)L.ra * K * esz);
+  const size_t np = tcf_planes(P->gauss ? TCF_GAUSS : TCF_FOUR);  // re, im (and re + im) x hi, lo
+  L.apl = L.bpl + up256(np * (size_t)L.rb * K * esz);
+  L.df = L.apl + up256(np * (size_t)L.ra * K * esz);
   L.total = L.df + up256((size_t)P->g_elems * sizeof(float4));
   return L;
 }
@@ -555,6 +569,10 @@ size_t tc_extra_workspace(const ed_elemental_plan* P) {
 
 int tc_plan_check(ed_elemental_plan* P) {
   P->tc_kind = tc_kind_of(P->mode);
+  if (P->gauss && (!P->tc_kind || P->tc_kind == TC_OZAKI || !P->fac)) {
+    set_error("the Gauss form (ED_MODE_FLAG_GAUSS) needs f16x3, bf16x3 or tf32x3 with a factorised momentum list");
+    return ED_ERR_UNSUPPORTED;
+  }
   if (!P->tc_kind) return ED_OK;
   if (P->V3 % 32 != 0) {
     set_error("tensor-core elemental modes need Lx*Ly*Lz divisible by 32 (got %d)", P->V3);
@@ -770,7 +788,8 @@ int launch_pair_gemm_tc_multi(int nplans, const ed_elemental_plan* const* plans,
 // Tensor map over four k-block-major planes of R rows: dimensions (k within
 // the 64-byte row, row, plane*nkb + k-block); a box is 128 rows of one
 // k-block, 8 KB contiguous in HBM.
-static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, long long R, int box_rows = TC_BM) {
+static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, long long R, int box_rows = TC_BM,
+                         int nplanes = 4) {
   EncodeFn enc = get_encode();
   if (!enc) {
     set_error("cuTensorMapEncodeTiled is unavailable from the driver");
@@ -778,7 +797,7 @@ static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, lo
   }
   const size_t esz = tc_esz(kind);
   const long long KB = TC_ROWB / (long long)esz, nkb = K / KB;
-  cuuint64_t gdim[3] = {(cuuint64_t)KB, (cuuint64_t)R, (cuuint64_t)(4 * nkb)};
+  cuuint64_t gdim[3] = {(cuuint64_t)KB, (cuuint64_t)R, (cuuint64_t)(nplanes * nkb)};
   cuuint64_t gstride[2] = {(cuuint64_t)TC_ROWB, (cuuint64_t)(R * TC_ROWB)};
   cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)box_rows, 1};
   cuuint32_t estride[3] = {1, 1, 1};
@@ -929,18 +948,27 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   for (int s = 0; s < nl; ++s) sl.lchain[s] = P->fac_lchain[s];
   const int kxl = (int)ceil_div(K / 2, 256 * kSplitUnrollLeft), kxr = (int)ceil_div(K / 2, 256 * kSplitUnrollRight);
   const int lrows = nb * nl * Ne, rrows = nb * P->nchain * Ne;
-  tc_fac_split_kernel<KIND, true, kSplitUnrollLeft><<<dim3(kxl, std::min(lrows, 65535)), 256, 0, stream>>>(
-      chains, sl, lrows, Ne, pxy, fxy32, P->V3, lay.rb, bpl);
-  tc_fac_split_kernel<KIND, false, kSplitUnrollRight><<<dim3(kxr, std::min(rrows, 65535)), 256, 0, stream>>>(
-      chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
+  if (P->gauss) {
+    tc_fac_split_kernel<KIND, true, kSplitUnrollLeft, true><<<dim3(kxl, std::min(lrows, 65535)), 256, 0, stream>>>(
+        chains, sl, lrows, Ne, pxy, fxy32, P->V3, lay.rb, bpl);
+    tc_fac_split_kernel<KIND, false, kSplitUnrollRight, true><<<dim3(kxr, std::min(rrows, 65535)), 256, 0, stream>>>(
+        chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
+  } else {
+    tc_fac_split_kernel<KIND, true, kSplitUnrollLeft, false><<<dim3(kxl, std::min(lrows, 65535)), 256, 0, stream>>>(
+        chains, sl, lrows, Ne, pxy, fxy32, P->V3, lay.rb, bpl);
+    tc_fac_split_kernel<KIND, false, kSplitUnrollRight, false><<<dim3(kxr, std::min(rrows, 65535)), 256, 0, stream>>>(
+        chains, sl, rrows, Ne, pz, fz32, P->V3, lay.ra, apl);
+  }
   ED_RETURN_LAUNCH("variant planes");
 
-  if (P->tc_pair == 2) return launch_fac_pairs<KIND>(P, lay, apl, bpl, sc, DF, G, stream, nb);
+  if (P->tc_pair == 2 && !P->gauss) return launch_fac_pairs<KIND>(P, lay, apl, bpl, sc, DF, G, stream, nb);
 
+  const int form = P->gauss ? TCF_GAUSS : (P->tc_stack == 2 ? TCF_FOUR : TCF_STACKED);
+  const int np = tcf_planes(form);
   CUtensorMap amap, bmap, bmap16;
-  if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra))) return rc;
-  if ((rc = encode_kmajor(&bmap, KIND, bpl, K, lay.rb))) return rc;
-  if ((rc = encode_kmajor(&bmap16, KIND, bpl, K, lay.rb, 16))) return rc;  // the narrow last column tile
+  if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra, TC_BM, np))) return rc;
+  if ((rc = encode_kmajor(&bmap, KIND, bpl, K, lay.rb, TC_BN, np))) return rc;
+  if ((rc = encode_kmajor(&bmap16, KIND, bpl, K, lay.rb, 16, np))) return rc;  // the narrow last column tile
 
   TcFacTable tab;
   tab.njobs = nb * P->jobs_per_t;
@@ -974,34 +1002,36 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   }
   tab.nfull = tiles;
   tiles += tiles_n;
-  const int stack = P->tc_stack == 2 ? 0 : 1;  // the stacked form unless the four-product form is asked for
-  auto kern = stack ? tc_fac_gemm_kernel<KIND, true> : tc_fac_gemm_kernel<KIND, false>;
-  static bool attr_set[4][2] = {};
-  static int resident[4][2] = {};
-  if (!attr_set[KIND][stack]) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tcf_smem(TCF_MAX_STAGES));
+  // the stacked form unless the four-product or the Gauss form is asked for
+  auto kern = form == TCF_GAUSS     ? tc_fac_gemm_kernel<KIND, TCF_GAUSS>
+              : form == TCF_STACKED ? tc_fac_gemm_kernel<KIND, TCF_STACKED>
+                                    : tc_fac_gemm_kernel<KIND, TCF_FOUR>;
+  const int smax = tcf_smem(tcf_max_stages(form), form);
+  static bool attr_set[4][3] = {};
+  static int resident[4][3] = {};
+  if (!attr_set[KIND][form]) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     if (e != cudaSuccess) return cuda_status(e, "tc kernel smem attribute");
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[KIND][stack], kern, TC_THREADS,
-                                                      tcf_smem(TCF_MAX_STAGES));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[KIND][form], kern, TC_THREADS, smax);
     if (e != cudaSuccess) return cuda_status(e, "tc kernel occupancy");
-    if (resident[KIND][stack] < 1) {
+    if (resident[KIND][form] < 1) {
       set_error("the factorised tensor-core GEMM does not fit on an SM");
       return ED_ERR_UNSUPPORTED;
     }
-    attr_set[KIND][stack] = true;
+    attr_set[KIND][form] = true;
   }
   const long long g_used = (long long)nb * P->g_per_t;
   e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
   // persistent grid: every CTA co-resident (the step counter of the kernel relies on it)
-  int grid = std::min(tiles, resident[KIND][stack] * sms);
+  int grid = std::min(tiles, resident[KIND][form] * sms);
   if (P->tc_grid > 0) grid = std::min(grid, P->tc_grid);
   const int slab_kb = P->tc_slab_kb > 0 ? P->tc_slab_kb : TC_FLUSH_KB;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(TC_THREADS);
-  const int nst = P->tc_stages > 0 ? std::min(P->tc_stages, TCF_MAX_STAGES) : TCF_DEFAULT_STAGES;
-  cfg.dynamicSmemBytes = tcf_smem(nst);
+  const int nst = std::min(P->tc_stages > 0 ? P->tc_stages : TCF_DEFAULT_STAGES, tcf_max_stages(form));
+  cfg.dynamicSmemBytes = tcf_smem(nst, form);
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -1009,7 +1039,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  const int kpb = P->tc_kpb > 0 ? P->tc_kpb : (stack ? 2 : 1);
+  const int kpb = P->tc_kpb > 0 ? P->tc_kpb : (form == TCF_FOUR ? 1 : 2);
   e = cudaLaunchKernelEx(&cfg, kern, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb, nst, kpb);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "tensor-core factorised-phase GEMM launch");

@@ -26,8 +26,17 @@
 // at 32^3, Ne = 200, 4 timeslices: 2 stages 144-146 ms, 3 stages 152 ms per launch.
 constexpr int TCF_MAX_STAGES = 3, TCF_DEFAULT_STAGES = 2;
 constexpr int TCF_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;  // 64 KB
-__host__ __device__ constexpr int tcf_smem(int nst) { return nst * TCF_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/; }
+// Forms of the kernel: four real products per complex one (FORM 0), stacked [re | im] B operand (FORM 1),
+// Gauss three multiplications on re, im and re + im planes (FORM 2, six planes per operand: 96 KB stages).
+constexpr int TCF_FOUR = 0, TCF_STACKED = 1, TCF_GAUSS = 2;
+__host__ __device__ constexpr int tcf_planes(int form) { return form == TCF_GAUSS ? 6 : 4; }
+__host__ __device__ constexpr int tcf_stage_bytes(int form) { return tcf_planes(form) * (TC_BM + TC_BN) * TC_ROWB; }
+__host__ __device__ constexpr int tcf_max_stages(int form) { return form == TCF_GAUSS ? 2 : TCF_MAX_STAGES; }
+__host__ __device__ constexpr int tcf_smem(int nst, int form = TCF_FOUR) {
+  return nst * tcf_stage_bytes(form) + 1024 /*align*/ + 256 /*barriers*/;
+}
 static_assert(tcf_smem(TCF_MAX_STAGES) <= 232448, "shared memory per block");
+static_assert(tcf_smem(tcf_max_stages(TCF_GAUSS), TCF_GAUSS) <= 232448, "shared memory per block");
 constexpr int TCF_REGS_LOW = 56, TCF_REGS_HIGH = 200;
 static_assert(256 * TCF_REGS_LOW + 256 * TCF_REGS_HIGH == TC_THREADS * TC_LAUNCH_REGS, "register split");
 // the stacked form's drain holds the same sums but reads four 64-column slices per k-block group:
@@ -122,7 +131,7 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
 // flushed into the double-float results at the end of every step, so a tile
 // is only ever touched by its owner CTA.
 //
-// Stacked form (STACK = true).  The B stage holds the real and imaginary
+// Stacked form (FORM = TCF_STACKED).  The B stage holds the real and imaginary
 // planes of each precision part back to back, [Br_hi; Bi_hi] and
 // [Br_lo; Bi_lo], so one M = 128, N = 2 * ncol MMA computes A * [Br | Bi].
 // Two accumulators of 256 columns fill TMEM: acc1 = Ar [Br | Bi] and
@@ -135,7 +144,16 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
 // drain reads acc1 while the acc2 MMAs run, and the MMAs of the next TMEM
 // group into acc1 wait only for that read.  Every accumulator column takes
 // 6 accumulating MMAs per k-block (12 in the 4-product form).
-template <int KIND, bool STACK>
+//
+// Gauss form (FORM = TCF_GAUSS).  The split also writes the planes of
+// re + im of both operands, so with X = Ar Br, Y = Ai Bi and
+// Z = (Ar + Ai)(Br + Bi), three M = N = 128 accumulators (384 TMEM columns)
+// give re = X - Y and im = Z - X - Y, formed by the drain in FP32: 9 MMAs per
+// split product and K step instead of 12, for 96 KB of operands per k-block
+// instead of 64.  As in the stacked form every accumulator is single and the
+// MMAs of a k-block go accumulator by accumulator, so each one is drained
+// while the next is computed.
+template <int KIND, int FORM>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fac_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap,
                        const __grid_constant__ CUtensorMap bmap16, const __grid_constant__ TcFacTable tab, int Ne,
@@ -147,14 +165,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   constexpr uint32_t FMT = KIND == TC_F16 ? 0u : (KIND == TC_BF16 ? 1u : 2u);
   constexpr uint32_t IDESC = umma_idesc(FMT, false);
   constexpr uint32_t IDESC_NEG = umma_idesc(FMT, true);
+  constexpr bool STACK = FORM == TCF_STACKED, GAUSS = FORM == TCF_GAUSS;
+  constexpr int NPL = tcf_planes(FORM);          // planes per operand
+  constexpr int SB = tcf_stage_bytes(FORM);      // bytes per stage
+  constexpr int AB = NPL * TC_BM * TC_ROWB;      // A bytes per stage
+  constexpr int NACC = GAUSS ? 3 : 2;            // accumulators (buffers) in TMEM
 
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + nst * TCF_STAGE_BYTES);
+  uint64_t* full = (uint64_t*)(smem + nst * SB);
   uint64_t* empty = full + TCF_MAX_STAGES;
-  uint64_t* accf = empty + TCF_MAX_STAGES;  // 2: accumulator buffer ready to drain
-  uint64_t* acce = accf + 2;            // 2: accumulator buffer drained
-  uint64_t* mma_done = acce + 2;        // every issued MMA has completed
+  uint64_t* accf = empty + TCF_MAX_STAGES;  // 3: accumulator (buffer) ready to drain
+  uint64_t* acce = accf + 3;            // 3: accumulator (buffer) drained
+  uint64_t* mma_done = acce + 3;        // every issued MMA has completed
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -200,7 +223,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NACC; ++b) {
       mbar_init(&accf[b], 1);
       mbar_init(&acce[b], TC_DWARPS);
     }
@@ -218,7 +241,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp < 8) {
-    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(STACK ? TCF_STACK_REGS_LOW : TCF_REGS_LOW));
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(FORM != TCF_FOUR ? TCF_STACK_REGS_LOW : TCF_REGS_LOW));
     if (warp == 0) {
       // ===================== TMA of the A and B planes, step by step
       if (lane == 0) {
@@ -253,10 +276,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               ok = false;
               break;
             }
-            uint8_t* As = smem + s * TCF_STAGE_BYTES;
-            uint8_t* Bs = As + TC_A_BYTES;
-            mbar_arrive_expect_tx(&full[s], TC_A_BYTES + 4 * ncol * TC_ROWB);
-            for (int p = 0; p < 4; ++p) {  // k-block-major planes: one contiguous 8 KB box each
+            uint8_t* As = smem + s * SB;
+            uint8_t* Bs = As + AB;
+            mbar_arrive_expect_tx(&full[s], AB + NPL * ncol * TC_ROWB);
+            for (int p = 0; p < NPL; ++p) {  // k-block-major planes: one contiguous 8 KB box each
               tma_load_3d(As + p * TC_BM * TC_ROWB, &amap, &full[s], 0, ay, p * nkb + kb);
               // planes re_hi, re_lo, im_hi, im_lo; stacked: [re_hi; im_hi] then [re_lo; im_lo], ncol rows each
               uint8_t* bd = STACK ? Bs + (p & 1) * 2 * TC_BN * TC_ROWB + (p >> 1) * ncol * TC_ROWB
@@ -300,8 +323,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 ok = false;
                 break;
               }
-              const uint32_t a0 = smem_u32(smem + s * TCF_STAGE_BYTES);
-              const uint32_t b0 = a0 + TC_A_BYTES;
+              const uint32_t a0 = smem_u32(smem + s * SB);
+              const uint32_t b0 = a0 + AB;
 #pragma unroll
               for (int h = 0; h < 2; ++h) {  // acc1 = Ar [Br | Bi], then acc2 = Ai [Br | Bi]
                 if (first && gb >= 1 &&
@@ -331,6 +354,46 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             continue;
           }
+          if constexpr (GAUSS) {
+            for (int kb = kb0s; kb < kb1 && ok; ++kb, ++g) {
+              const int s = (int)(g % nst);
+              const bool first = (kb - kb0s) % kpb == 0;
+              const bool last = (kb - kb0s) % kpb == kpb - 1 || kb == kb1 - 1;
+              if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL)) {
+                ok = false;
+                break;
+              }
+              const uint32_t a0 = smem_u32(smem + s * SB);
+              const uint32_t b0 = a0 + AB;
+#pragma unroll
+              for (int h = 0; h < 3; ++h) {  // X = Ar Br, Y = Ai Bi, Z = (Ar + Ai)(Br + Bi): planes 2h, 2h + 1
+                if (first && gb >= 1 &&
+                    !mbar_wait(&acce[h], (uint32_t)((gb - 1) & 1), status, TC_ERR_ACCE)) {
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + h * TC_BN;
+#pragma unroll
+                for (int ks = 0; ks < KE / KINST; ++ks) {  // correction products first
+                  const uint32_t acc = (ks > 0 || !first) ? 1u : 0u;
+                  const uint32_t ao = a0 + 2 * h * TC_BM * TC_ROWB + ks * 32, bo = b0 + 2 * h * TC_BN * TC_ROWB + ks * 32;
+                  umma<KIND>(d, umma_desc_sw64(ao), umma_desc_sw64(bo + TC_BN * TC_ROWB), ID, acc);
+                  umma<KIND>(d, umma_desc_sw64(ao + TC_BM * TC_ROWB), umma_desc_sw64(bo), ID, 1u);
+                }
+#pragma unroll
+                for (int ks = 0; ks < KE / KINST; ++ks) {
+                  const uint32_t ao = a0 + 2 * h * TC_BM * TC_ROWB + ks * 32, bo = b0 + 2 * h * TC_BN * TC_ROWB + ks * 32;
+                  umma<KIND>(d, umma_desc_sw64(ao), umma_desc_sw64(bo), ID, 1u);
+                }
+                if (last) umma_commit(&accf[h]);  // this accumulator is ready to drain
+              }
+              if (!ok) break;
+              umma_commit(&empty[s]);  // frees the stage when these MMAs complete
+              if (last) ++gb;
+            }
+            continue;
+          }
           for (int kb = kb0s; kb < kb1; ++kb, ++g) {
             const int s = (int)(g % nst);
             const int b = (int)(gb & 1);
@@ -342,8 +405,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               break;
             }
             tc_fence_after();
-            const uint32_t a0 = smem_u32(smem + s * TCF_STAGE_BYTES);
-            const uint32_t b0 = a0 + TC_A_BYTES;
+            const uint32_t a0 = smem_u32(smem + s * SB);
+            const uint32_t b0 = a0 + AB;
             const uint32_t d_re = tmem + b * 256, d_im = d_re + TC_BN;
 #pragma unroll
             for (int ks = 0; ks < KE / KINST; ++ks) {
@@ -383,7 +446,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
     }
   } else {
-    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(STACK ? TCF_STACK_REGS_HIGH : TCF_REGS_HIGH));
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(FORM != TCF_FOUR ? TCF_STACK_REGS_HIGH : TCF_REGS_HIGH));
     // ===================== drain: TMEM -> FP32 register sums -> double-float result per step
     const int dw = warp - 8;         // 0..7
     const int quarter = warp & 3;    // TMEM lane quarter this warp may access
@@ -405,6 +468,54 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
       for (int c = 0; c < 64; ++c) sre[c] = sim[c] = 0.f;
       const int kb1 = step_kb1(q);
+      if constexpr (GAUSS) {
+        for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one group of kpb k-blocks
+#pragma unroll
+          for (int h = 0; h < 3; ++h) {  // X: re += x, im -= x; Y: re -= y, im -= y; Z: im += z
+            if (!warp_wait(&accf[h], (uint32_t)(g & 1), status, TC_ERR_ACC)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16) + h * TC_BN + half * 64;
+            uint32_t r0[32], r1[32];
+            tmem_ld32(tl, r0);
+            tmem_ld32(tl + 32, r1);
+            tmem_wait_ld();
+            if (h == 0) {
+#pragma unroll
+              for (int e = 0; e < 32; ++e) {
+                const float x0 = __uint_as_float(r0[e]), x1 = __uint_as_float(r1[e]);
+                sre[e] += x0;
+                sre[32 + e] += x1;
+                sim[e] -= x0;
+                sim[32 + e] -= x1;
+              }
+            } else if (h == 1) {
+#pragma unroll
+              for (int e = 0; e < 32; ++e) {
+                const float y0 = __uint_as_float(r0[e]), y1 = __uint_as_float(r1[e]);
+                sre[e] -= y0;
+                sre[32 + e] -= y1;
+                sim[e] -= y0;
+                sim[32 + e] -= y1;
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < 32; ++e) {
+                sim[e] += __uint_as_float(r0[e]);
+                sim[32 + e] += __uint_as_float(r1[e]);
+              }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[h]);
+          }
+          if (!ok) break;
+        }
+        if (ok) flush_sums_fac(sre, sim, DF, tab, J, Ne, n0c, m_local, Mrows, inv);
+        continue;
+      }
       if constexpr (STACK) {
         const int ncol = tile_cols(ntile);
         for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one group of kpb k-blocks

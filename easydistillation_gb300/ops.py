@@ -354,6 +354,7 @@ def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
 #: elemental arithmetic modes (ED_MODE_* in include/easydist_gb300.h)
 MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3, "ozaki_i8": 4}
 _FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR = 0x100, 0x200
+_FLAG_GAUSS = 0x400  # ED_MODE_FLAG_GAUSS
 #: plan launch settings (ED_TUNE_* keys)
 TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4, "tc_pair": 5, "tc_kpb": 6,
                "tc_stack": 7}
@@ -365,19 +366,23 @@ class ElementalPlan:
     """Owner of an ``ed_elemental_plan`` and its device workspace."""
 
     def __init__(self, latt_size, Ne: int, num_nabla: int, momentum_list, mode: str = "fp64", device=None,
-                 batch: int = 1, factorise=True, tuning=None):
+                 batch: int = 1, factorise=True, tuning=None, gauss: bool = False):
         """``factorise=False`` keeps the tensor-core GEMM that forms the
         phase-weighted operand inside the kernel even when the momentum list
         factorises (ED_MODE_FLAG_NO_FACTOR); ``factorise="force"`` factorises
         however many (px,py) x pz combinations the list leaves unused
-        (ED_MODE_FLAG_FORCE_FACTOR).  ``tuning``: launch settings
-        ``{"f64_tile", "tc_slab_kb", "tc_grid"}`` (see ``set_tuning``)."""
+        (ED_MODE_FLAG_FORCE_FACTOR).  ``gauss=True`` runs the factorised split
+        GEMM in the Gauss three-multiplication form (ED_MODE_FLAG_GAUSS).
+        ``tuning``: launch settings (``TUNING_KEYS``, see ``set_tuning``)."""
         if mode not in MODES:
             raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES)}")
         if factorise not in (True, False, "force"):
             raise ValueError(f"factorise must be True, False or 'force', not {factorise!r}")
         cmode = MODES[mode] | {True: 0, False: _FLAG_NO_FACTOR, "force": _FLAG_FORCE_FACTOR}[factorise]
+        if gauss:
+            cmode |= _FLAG_GAUSS
         self.factorise = factorise
+        self.gauss = bool(gauss)
         Lx, Ly, Lz = latt_size[0], latt_size[1], latt_size[2]
         self.latt_size = list(latt_size)
         self.Ne = Ne

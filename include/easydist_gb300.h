@@ -69,6 +69,14 @@ extern "C" {
  * (by default at most a quarter may go unused).  Excludes
  * ED_MODE_FLAG_NO_FACTOR.  An autotuner measures both forms. */
 #define ED_MODE_FLAG_FORCE_FACTOR 0x200
+/* Flag OR-ed into f16x3 / bf16x3 / tf32x3 at plan creation: run the
+ * factorised-phase GEMM in the Gauss three-multiplication form (X = Ar Br,
+ * Y = Ai Bi, Z = (Ar + Ai)(Br + Bi); re = X - Y, im = Z - X - Y): 9 MMAs per
+ * split product and K step instead of 12, on six operand planes per side
+ * (re, im, re + im; the split-plane workspace grows by half).  Needs a
+ * factorised plan (ED_ERR_UNSUPPORTED otherwise); runs on single SMs
+ * whatever ED_TUNE_TC_PAIR / ED_TUNE_TC_STACK say. */
+#define ED_MODE_FLAG_GAUSS 0x400
 
 /* ---- launch settings of a plan (ed_elemental_set_tuning keys) */
 #define ED_TUNE_F64_TILE 1   /* FP64 pair GEMM tile, rows x cols: 0 = 64x64 (default), 1 = 32x64,
@@ -91,7 +99,9 @@ extern "C" {
                               * 1 otherwise), 1, 2 or 4.  The tensor core's FP32 accumulation
                               * truncates, so longer buffers trade accuracy for fewer hand-overs
                               * (measured at 32^3, Ne = 200, f16x3 vs FP64: four-product form
-                              * 2.0e-7 with 1, 5.1e-7 with 2; stacked form 2.6e-7 with 2) */
+                              * 2.0e-7 with 1, 5.1e-7 with 2; stacked form 2.6e-7 with 2,
+                              * 5.8e-7 with 4).  4 is meant for the stacked and Gauss forms: the
+                              * four-product form with 4 exceeded 1e-6 at K = 9216. */
 #define ED_TUNE_TC_STACK 7   /* single-SM factorised GEMM operand form: 0 (default) or 1 = stacked:
                               * B = [Br; Bi] in shared memory, two M = 128, N = 256 MMAs
                               * A_re [Br | Bi] and A_im [Br | Bi] per split product into single

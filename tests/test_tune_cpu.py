@@ -141,3 +141,23 @@ def test_tune_elemental_uses_cache_without_measuring(tmp_path, monkeypatch):
     assert res.cached and res.best.tuning == {"tc_slab_kb": 128} and res.ms == 150.0
     with pytest.raises(ValueError):
         tune.tune_elemental([32, 32, 32, 64], 200, 2, moms, "f8", cache=cache)
+
+
+def test_gauss_flag_needs_a_factorised_split_plan():
+    """ED_MODE_FLAG_GAUSS: accepted for f16x3 / bf16x3 / tf32x3 plans that
+    factorise (the split-plane workspace grows by half); rejected for FP64,
+    Ozaki and on-chip-phase plans."""
+    from easydistillation_gb300 import _lib
+
+    base = _plan("all27", "f16x3")
+    g = _plan("all27", "f16x3", gauss=True)
+    assert g.factorised == (9, 3) and g.gauss
+    assert g.workspace_bytes > base.workspace_bytes
+    for mode in ("bf16x3", "tf32x3"):
+        assert _plan("all27", mode, gauss=True).factorised == (9, 3)
+    assert _plan("first7", "f16x3", factorise="force", gauss=True).factorised == (5, 3)
+    for kw in ({"moms": "all27", "mode": "fp64"}, {"moms": "all27", "mode": "ozaki_i8"},
+               {"moms": "first7", "mode": "f16x3"}, {"moms": "all27", "mode": "f16x3", "factorise": False}):
+        with pytest.raises(RuntimeError):
+            _plan(gauss=True, **kw)
+        assert "Gauss form" in _lib.last_error()
