@@ -191,9 +191,9 @@ def make_inputs(latt, Ne, seed=2, distinct_t=RESIDENT_T):
 # total), and one phase-weighted zgemm per subset and momentum.
 REF_HOPS = 78
 REF_SUBSETS = 43
-# DRAM bytes (read + write) of one tc_fac_gemm_kernel<f16x3> launch on the default workload (32^3, Ne = 200,
-# 4 timeslices), from one ncu capture (profiles/tc_fac_gemm_f16x3_32cube_dram.md)
-FAC_TRAFFIC_BYTES = 414.10e9 + 15.97e9
+# DRAM bytes (read + write) of one tc_fac_gemm_kernel<f16x3> launch in the stacked form on the default workload
+# (32^3, Ne = 200, 4 timeslices), from one single-pass ncu capture (profiles/tc_fac_gemm_f16x3_32cube_dram.md)
+FAC_TRAFFIC_BYTES = 190.38e9 + 15.77e9
 # FP64 FMA throughput of this part (register-resident DFMA loop on all SMs)
 FP64_PEAK_TFLOPS = 1.25
 FP64_PEAK_SOURCE = "nominal GB300 FP64"
@@ -493,8 +493,10 @@ def run_ours(args, rank, world):
             kname = f"tc_pair_gemm_kernel<{args.mode}>"
         per_mac = 9 if getattr(plan, "gauss", False) else 12  # real MMAs per complex multiply-add (3 split products)
         mma_flop = B * tiles * 128 * 128 * 3 * V3 * per_mac * 2.0
+        tun = plan.tuning()
         default_workload = (plan.factorised is not None and args.mode == "f16x3" and B == 4 and Ne == NE
-                            and list(latt[:3]) == LATT[:3])
+                            and list(latt[:3]) == LATT[:3] and not getattr(plan, "gauss", False)
+                            and tun.get("tc_stack", 0) != 2 and tun.get("tc_pair", 0) != 2)
         roofline = {"bound": "tensor", "achieved": alg_flop / kms / 1e9, "peak": pk, "unit": "TFLOP/s",
                     "frac": alg_flop / kms / 1e9 / pk,
                     "traffic": FAC_TRAFFIC_BYTES if default_workload else None,
