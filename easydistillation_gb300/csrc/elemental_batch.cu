@@ -128,8 +128,9 @@ extern "C" int ed_elemental_gemm_multi(int nplans, const ed_elemental_plan* cons
                  P->nbatch);
     int rc = check_ws(P, workspaces[v], workspace_bytes[v], "ed_elemental_gemm_multi");
     if (rc) return rc;
-    // one launch needs every plan on the on-chip-phase tensor-core path with the same split kind
-    one = one && P->tc_kind != 0 && P->tc_kind != ed::TC_OZAKI && !P->fac && P->tc_kind == plans[0]->tc_kind;
+    // one launch needs every plan on the on-chip-phase tensor-core path with the same split kind and form
+    one = one && P->tc_kind != 0 && P->tc_kind != ed::TC_OZAKI && !P->fac && P->tc_kind == plans[0]->tc_kind &&
+          (P->tc_stack == 2) == (plans[0]->tc_stack == 2);
   }
   if (launches) *launches = one ? 1 : nplans;
   if (one) return ed::launch_pair_gemm_tc_multi(nplans, plans, nbatch, workspaces, (cudaStream_t)stream);

@@ -684,6 +684,8 @@ static int tc_onchip_prepare(const ed_elemental_plan* P, const cplx<float>* chai
   d->nmom = P->nmom;
   d->V3 = P->V3;
   d->tile0 = tiles;  // the caller turns this count into the volume's first block
+  // stacked form unless the four-product form is asked for; k-blocks per accumulator group (stacked form only)
+  d->kpb = P->tc_stack == 2 ? 1 : (P->tc_kpb > 0 ? P->tc_kpb : 2);
   const long long g_used = (long long)nb * P->g_per_t;
   e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
@@ -720,12 +722,14 @@ static int launch_kind(const ed_elemental_plan* P, const cplx<float>* chains, co
   int rc = tc_onchip_prepare<KIND>(P, chains, phases, extra, stream, nb, &d, &staged);
   if (rc) return rc;
   const int tiles = d.tile0;
-  auto kern = staged ? tc_pair_gemm_kernel<KIND, true> : tc_pair_gemm_kernel<KIND, false>;
+  const bool stack = P->tc_stack != 2;
+  auto kern = staged ? (stack ? tc_pair_gemm_kernel<KIND, true, true> : tc_pair_gemm_kernel<KIND, true, false>)
+                     : (stack ? tc_pair_gemm_kernel<KIND, false, true> : tc_pair_gemm_kernel<KIND, false, false>);
   rc = tc_set_smem((const void*)kern);
   if (rc) return rc;
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
   kern<<<tiles, TC_THREADS, TC_SMEM, stream>>>(d.amap, d.tab, d.Ne, d.nmom, d.V3, d.R, d.chains, d.phases, d.sc,
-                                                d.DF, d.xr);
+                                                d.DF, d.xr, d.kpb);
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   ED_RETURN_LAUNCH("tensor-core pair GEMM");
   return tc_onchip_finish(P, d, G, stream, nb);
@@ -755,7 +759,11 @@ static int launch_multi_kind(int nplans, const ed_elemental_plan* const* plans, 
     set_error("ed_elemental_gemm_multi: too many tiles for one launch");
     return ED_ERR_UNSUPPORTED;
   }
-  auto kern = all_staged ? tc_pair_gemm_multi_kernel<KIND, true> : tc_pair_gemm_multi_kernel<KIND, false>;
+  const bool stack = plans[0]->tc_stack != 2;  // the caller groups plans of one form
+  auto kern = all_staged ? (stack ? tc_pair_gemm_multi_kernel<KIND, true, true>
+                                  : tc_pair_gemm_multi_kernel<KIND, true, false>)
+                         : (stack ? tc_pair_gemm_multi_kernel<KIND, false, true>
+                                  : tc_pair_gemm_multi_kernel<KIND, false, false>);
   int rc = tc_set_smem((const void*)kern);
   if (rc) return rc;
   if (tiles > 0) {

@@ -83,11 +83,19 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
 // the producers read them there instead of from global memory.
 // The body of one CTA: tile `tile` of the job table `tab` (the kernels below pass their tensor map and table
 // from the launch's parameter space).
-template <int KIND, bool STAGED>
+//
+// STACK (the default form): the producers write the B planes of a stage as [re_hi; im_hi], [re_lo; im_lo]
+// (256 rows each), so one M = 128, N = 256 MMA per split product computes A [Br | Bi]: acc1 = A_re [Br | Bi]
+// and acc2 = A_im [Br | Bi] fill the 512 TMEM columns, single, and the drain forms re = acc1[:, :128] -
+// acc2[:, 128:], im = acc1[:, 128:] + acc2[:, :128].  The MMAs of each k-block go accumulator by accumulator
+// and accumulate `kpb` k-blocks per group (the drain reads acc1 while the acc2 MMAs run); the same scheme as
+// the stacked form of tc_fac_gemm.cuh.  Without STACK: four real products into double-buffered [re], [im]
+// buffers, one k-block each.
+template <int KIND, bool STAGED, bool STACK>
 __device__ __forceinline__ void tc_pair_gemm_body(const CUtensorMap* amap, const TcTable& tab, int Ne, int nmom,
                                                   int V3, long long R, const cplx<float>* __restrict__ chains,
                                                   const cplx<float>* __restrict__ phases, TcScalars* __restrict__ sc,
-                                                  float4* __restrict__ DF, int xr, int tile) {
+                                                  float4* __restrict__ DF, int xr, int tile, int kpb) {
   constexpr int ESZ = Split<KIND>::ESZ;
   constexpr int KE = TC_ROWB / ESZ;  // k elements per stage
   constexpr int EPC = 16 / ESZ;      // k elements per 16-byte chunk
@@ -205,7 +213,43 @@ __device__ __forceinline__ void tc_pair_gemm_body(const CUtensorMap* amap, const
     }
   } else if (warp == 1) {
     // ===================== MMA issuer
-    if (lane == 0) {
+    if (lane == 0 && STACK) {
+      constexpr uint32_t ID = (IDESC & ~(0x3Fu << 17)) | ((uint32_t)((2 * TC_BN) >> 3) << 17);  // N = 256
+      bool ok = true;
+      for (int kb = 0; kb < nkb && ok; ++kb) {
+        const int s = kb % TC_STAGES;
+        const int gb = kb / kpb;  // accumulator group
+        const bool first = kb % kpb == 0, last = kb % kpb == kpb - 1 || kb == nkb - 1;
+        if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, status, TC_ERR_FULL)) break;
+        const uint32_t a0 = smem_u32(smem + s * TC_STAGE_BYTES);
+        const uint32_t b0 = a0 + TC_A_BYTES;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {  // acc1 = Ar [Br | Bi], then acc2 = Ai [Br | Bi]
+          if (first && gb >= 1 && !mbar_wait(&acce[h], (uint32_t)((gb - 1) & 1), status, TC_ERR_ACCE)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + h * 256;
+#pragma unroll
+          for (int ks = 0; ks < KE / KINST; ++ks) {  // correction products first
+            const uint32_t acc = (ks > 0 || !first) ? 1u : 0u;
+            const uint32_t ao = a0 + 2 * h * TC_BM * TC_ROWB + ks * 32, bo = b0 + ks * 32;
+            umma<KIND>(d, umma_desc_sw64(ao), umma_desc_sw64(bo + 2 * TC_BN * TC_ROWB), ID, acc);
+            umma<KIND>(d, umma_desc_sw64(ao + TC_BM * TC_ROWB), umma_desc_sw64(bo), ID, 1u);
+          }
+#pragma unroll
+          for (int ks = 0; ks < KE / KINST; ++ks) {
+            const uint32_t ao = a0 + 2 * h * TC_BM * TC_ROWB + ks * 32, bo = b0 + ks * 32;
+            umma<KIND>(d, umma_desc_sw64(ao), umma_desc_sw64(bo), ID, 1u);
+          }
+          if (last) umma_commit(&accf[h]);  // this accumulator is ready to drain
+        }
+        if (!ok) break;
+        umma_commit(&empty[s]);  // frees the stage when these MMAs complete
+      }
+      umma_commit(mma_done);  // arrives once every MMA issued above has completed (also on early exit)
+    } else if (lane == 0) {
       int kb = 0;
       for (; kb < nkb; ++kb) {
         const int s = kb % TC_STAGES;
@@ -334,9 +378,11 @@ __device__ __forceinline__ void tc_pair_gemm_body(const CUtensorMap* amap, const
           for (int e = 0; e < 4; ++e) hre[e] = lre[e] = him[e] = lim[e] = 0u;
         }
         uint8_t* dst = Bs + soff[t];
+        // planes re_hi, re_lo, im_hi, im_lo; stacked: re_hi, im_hi, re_lo, im_lo
+        constexpr int PL = STACK ? 2 : 1, PI = STACK ? 1 : 2;
         *reinterpret_cast<uint4*>(dst + 0 * TC_BN * TC_ROWB) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-        *reinterpret_cast<uint4*>(dst + 1 * TC_BN * TC_ROWB) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
-        *reinterpret_cast<uint4*>(dst + 2 * TC_BN * TC_ROWB) = make_uint4(him[0], him[1], him[2], him[3]);
+        *reinterpret_cast<uint4*>(dst + PL * TC_BN * TC_ROWB) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
+        *reinterpret_cast<uint4*>(dst + PI * TC_BN * TC_ROWB) = make_uint4(him[0], him[1], him[2], him[3]);
         *reinterpret_cast<uint4*>(dst + 3 * TC_BN * TC_ROWB) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
       }
       fence_proxy_async();
@@ -362,7 +408,47 @@ __device__ __forceinline__ void tc_pair_gemm_body(const CUtensorMap* amap, const
 #pragma unroll
     for (int c = 0; c < 64; ++c) sre[c] = sim[c] = 0.f;
     bool ok = true;
-    for (int kb = 0; kb < nkb; ++kb) {
+    if constexpr (STACK) {
+      for (int kb0 = 0, g = 0; kb0 < nkb && ok; kb0 += kpb, ++g) {  // one group of kpb k-blocks
+        const int kbl = min(nkb, kb0 + kpb) - 1;                      // its last k-block
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (!warp_wait(&accf[h], (uint32_t)(g & 1), status, TC_ERR_ACC)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          // acc1: re += [0, 128), im += [128, 256); acc2: im += [0, 128), re -= [128, 256)
+          const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16) + h * 256 + half * 64;
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            float v[16];
+            tmem_ld16(tl + cc * 16, v);
+            if (h == 0) {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) sre[cc * 16 + e] += v[e];
+            } else {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) sim[cc * 16 + e] += v[e];
+            }
+            tmem_ld16(tl + TC_BN + cc * 16, v);
+            if (h == 0) {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) sim[cc * 16 + e] += v[e];
+            } else {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) sre[cc * 16 + e] -= v[e];
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acce[h]);
+        }
+        if (ok && (kb0 / TC_FLUSH_KB != (kbl + 1) / TC_FLUSH_KB || kbl == nkb - 1))
+          flush_sums(sre, sim, DF, J.g_off, N, n0c, Ncols, nmom, Ne, m_local, Mrows, inv);
+      }
+    }
+    for (int kb = 0; kb < (STACK ? 0 : nkb); ++kb) {
       const int b = kb & 1;
       if (!warp_wait(&accf[b], (kb >> 1) & 1, status, TC_ERR_ACC)) {
         ok = false;
@@ -400,13 +486,14 @@ __device__ __forceinline__ void tc_pair_gemm_body(const CUtensorMap* amap, const
   }
 }
 
-template <int KIND, bool STAGED>
+template <int KIND, bool STAGED, bool STACK>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_pair_gemm_kernel(const __grid_constant__ CUtensorMap amap, const __grid_constant__ TcTable tab, int Ne,
                         int nmom, int V3, long long R, const cplx<float>* __restrict__ chains,
                         const cplx<float>* __restrict__ phases, TcScalars* __restrict__ sc, float4* __restrict__ DF,
-                        int xr) {
-  tc_pair_gemm_body<KIND, STAGED>(&amap, tab, Ne, nmom, V3, R, chains, phases, sc, DF, xr, (int)blockIdx.x);
+                        int xr, int kpb) {
+  tc_pair_gemm_body<KIND, STAGED, STACK>(&amap, tab, Ne, nmom, V3, R, chains, phases, sc, DF, xr, (int)blockIdx.x,
+                                         kpb);
 }
 
 // Several lattice volumes (batched plans with their own Ne, V3, chains and results) in ONE launch: the tiles
@@ -421,18 +508,18 @@ struct TcMultiVol {
   TcScalars* sc;
   float4* DF;
   long long R;
-  int Ne, nmom, V3, xr, tile0;
+  int Ne, nmom, V3, xr, tile0, kpb;
 };
 struct TcMulti {
   TcMultiVol v[kMaxVol];
   int nvol;
 };
 
-template <int KIND, bool STAGED>
+template <int KIND, bool STAGED, bool STACK>
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_pair_gemm_multi_kernel(const __grid_constant__ TcMulti M) {
   int v = 0;
   while (v + 1 < M.nvol && (int)blockIdx.x >= M.v[v + 1].tile0) ++v;
   const TcMultiVol& D = M.v[v];
-  tc_pair_gemm_body<KIND, STAGED>(&D.amap, D.tab, D.Ne, D.nmom, D.V3, D.R, D.chains, D.phases, D.sc, D.DF, D.xr,
-                                  (int)blockIdx.x - D.tile0);
+  tc_pair_gemm_body<KIND, STAGED, STACK>(&D.amap, D.tab, D.Ne, D.nmom, D.V3, D.R, D.chains, D.phases, D.sc, D.DF,
+                                         D.xr, (int)blockIdx.x - D.tile0, D.kpb);
 }

@@ -296,7 +296,14 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
                     [Candidate(best.factorise, {**base, "tc_stages": more_stages}),
                      Candidate(best.factorise, {**base, "tc_stages": more_stages, "tc_slab_kb": SLABS[1]})])
 
+        def onchip_forms(best: Candidate) -> List[Candidate]:
+            # the on-chip-phase GEMM: stacked operands with 2 or 4 k-blocks per group, or the four-product form
+            if factorised(best) or mode == "ozaki_i8":
+                return []
+            return [Candidate(best.factorise, dict(t)) for t in ({}, {"tc_kpb": 4}, {"tc_stack": 2})]
+
         stages.append(forms_on_sms)
+        stages.append(onchip_forms)
         stages.append(slabs)
     start = Candidate(True if forms is None else list(forms)[0], {})
     res = _run_search(stages, start, measure, _rel_err, TOLERANCE[mode])

@@ -84,3 +84,41 @@ def test_stacked_gemm_short_group_at_step_end():
         for kpb in (2, 4):
             out = _run(latt, Ne, moms, "f16x3", {"tc_stack": form, "tc_kpb": kpb}, U, V, [0])[0]
             assert rel_err(out, ref) < 1e-6
+
+
+# ---------------------------------------------------------------- on-chip-phase kernel (tc_pair_gemm.cuh)
+def _run_onchip(latt, Ne, num_nabla, moms, mode, tuning, seed):
+    from easydistillation_gb300.ops import ElementalPlan
+
+    gauge, evec, U, V = _inputs(latt, Ne, seed)
+    V3 = latt[0] * latt[1] * latt[2]
+    plan = ElementalPlan(latt, Ne, num_nabla, moms, mode, factorise=False, tuning=tuning)
+    assert plan.factorised is None
+    nd = {0: 1, 1: 4, 2: 13}[num_nabla]
+    out = torch.empty((nd, len(moms), Ne, Ne), dtype=torch.complex128, device="cuda")
+    plan.run(U[:, 0], latt[3] * V3 * 9, 9, V[0], out)
+    assert plan.check_status() == 0
+    ref = R.elemental(evec[0], gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0], latt, num_nabla, moms)
+    return out.cpu().numpy(), ref
+
+
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3", "bf16x3"])
+@pytest.mark.parametrize("tuning", [{}, {"tc_kpb": 1}, {"tc_kpb": 4}, {"tc_stack": 2}])
+def test_onchip_phase_kernel_forms(mode, tuning):
+    """The on-chip-phase GEMM in the stacked form (default, 2 k-blocks per
+    group; 1 and 4) and the four-product form, several ragged M and N tiles,
+    27 momenta kept off the factorised path."""
+    out, ref = _run_onchip([8, 8, 4, 1], 40, 1, R.mom_dict_to_list(3), mode, tuning, 71)
+    assert rel_err(out, ref) < TOL[mode]
+
+
+@pytest.mark.parametrize("kpb", [1, 2, 4])
+def test_onchip_phase_stacked_long_k_and_short_group(kpb):
+    """K = 3 * 16^3 = 12288 (384 k-blocks: flushes after k-block 255 and at
+    the end) with an open momentum list, and K = 3 * 4*4*2 = 96 (3 k-blocks:
+    the last group is short)."""
+    moms = [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (0, 0, 2), (0, 1, 2), (1, 1, 2)]
+    out, ref = _run_onchip([16, 16, 16, 1], 24, 1, moms, "f16x3", {"tc_kpb": kpb}, 73)
+    assert rel_err(out, ref) < 1e-6
+    out, ref = _run_onchip([4, 4, 2, 1], 5, 2, R.mom_dict_to_list(3)[:7], "f16x3", {"tc_kpb": kpb}, 75)
+    assert rel_err(out, ref) < 1e-6
