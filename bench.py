@@ -77,6 +77,8 @@ def parse():
                          "vs device decode)")
     ap.add_argument("--eigen-batch", type=int, default=8)
     ap.add_argument("--eigen-precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--eigen-gs", default="fp64", choices=["fp64", "df"],
+                    help="Gram-Schmidt arithmetic of the eigensolve (df: double-float on the FP32 pipe)")
     ap.add_argument("--eigen-cpu", action="store_true", help="also time the oracle's scipy eigensolve (slow)")
     ap.add_argument("--eigen-poly", type=int, default=0, help="Chebyshev degree for --eigen (0: plain Lanczos)")
     ap.add_argument("--eigen-ncv", type=int, default=None, help="Krylov dimension for --eigen")
@@ -742,6 +744,20 @@ def bench_eigen_default(dev, batch=8):
                                  "restarts_fp32_phase": st2["restarts_fp32"],
                                  "note": "complex64 stencil in a loose FP64 iteration, then FP64 Chebyshev "
                                          "refinement (cut found automatically)", **quality(ev2, X2, ev0)}
+    # the same three solves with the Gram-Schmidt passes in double-float arithmetic on the FP32 pipe
+    df = {}
+    (ev3, X3, st3), dt3 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-10, gs_precision="df"))
+    df["plain"] = {"value": batch / dt3, "converged": st3["converged"], "restarts": st3["restarts"],
+                   **quality(ev3, X3, ev0)}
+    (ev4, X4, st4), dt4 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-12, poly_deg=16, lambda_cut=cut,
+                                                   gs_precision="df"))
+    df["chebyshev"] = {"value": batch / dt4, "converged": st4["converged"], **quality(ev4, X4, ev0)}
+    (ev5, X5, st5), dt5 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-10, stencil_precision="fp32", links_c64=L32,
+                                                   gs_precision="df"))
+    df["mixed_fp32_stencil"] = {"value": batch / dt5, "converged": st5["converged"], **quality(ev5, X5, ev0)}
+    out["double_float_gram_schmidt"] = {"unit": "timeslices/s", **df,
+                                        "note": "gs_precision='df': Gram-Schmidt passes on the FP32 pipe in "
+                                                "double-float arithmetic (~2^-47 products), everything else FP64"}
     return out
 
 
@@ -1115,7 +1131,8 @@ def run_eigen(args):
         def load(self, key):
             return _G(gauge)
 
-    gen = EigenvectorGenerator(latt, _Src(), Ne, 1e-10, stencil_precision=args.eigen_precision, ncv=args.eigen_ncv)
+    gen = EigenvectorGenerator(latt, _Src(), Ne, 1e-10, stencil_precision=args.eigen_precision, ncv=args.eigen_ncv,
+                               gs_precision=args.eigen_gs)
     gen.load("bench")
     ts = list(range(args.eigen_batch))
     kw = {}
@@ -1132,6 +1149,7 @@ def run_eigen(args):
     dt = time.perf_counter() - t0
     line = {"metric": f"eigensolve timeslices/s {latt[0]}^3 Ne={Ne} tol 1e-10", "value": len(ts) / dt,
             "unit": "timeslices/s", "seconds": dt, "batch": len(ts), "stencil_precision": args.eigen_precision,
+            "gs_precision": args.eigen_gs,
             "polynomial_degree": args.eigen_poly, "ncv": gen.ncv,
             "stats": gen.last_stats, "lowest_evals_t0": [float(v) for v in evals[0, :3].cpu()]}
     if args.eigen_cpu:

@@ -25,6 +25,7 @@ ED_ERR_TIMEOUT = -5
 
 ED_C128 = 0
 ED_C64 = 1
+ED_LANCZOS_GS_DF = 0x100  # flag OR-ed into the stencil precision of ed_lanczos_tr_ex
 ED_BIG_ENDIAN = 0x10
 
 _c = ctypes
@@ -93,6 +94,7 @@ _SIGNATURES = {
     "ed_elemental_set_tuning": ([_vp, _i, _i], _i),
     "ed_arrow_eigh_workspace": ([_i, _i, _i, _c.POINTER(_c.c_size_t)], _i),
     "ed_cgs_pass": ([_i, _i, _ll, _vp, _ll, _vp, _vp, _i, _vp, _vp], _i),
+    "ed_cgs_pass_df": ([_i, _i, _ll, _vp, _ll, _vp, _vp, _i, _vp, _vp, _c.c_size_t, _vp], _i),
     "ed_lanczos_workspace": ([_i, _i, _i, _i, _i, _i, _c.POINTER(_c.c_size_t)], _i),
     "ed_lanczos_tr": ([_i, _i, _i, _i, _vp, _i, _c.c_double, _i, _i, _i, _c.c_double, _vp, _vp, _c.POINTER(_i), _vp,
                        _c.c_size_t, _vp], _i),

@@ -41,6 +41,10 @@
 #include "common.cuh"
 
 namespace ed {
+int split_rows(int B, int nrow, long long n, const void* src, long long sb, void* dst, long long db,
+               cudaStream_t st);
+int cgs_pass_df(int B, int r, long long n, const void* Vs, long long vs_bstride, void* w, void* ws, void* h, int ldh,
+                double* norm_part, cudaStream_t st);
 namespace {
 
 constexpr int LZ_THREADS = 256;
@@ -295,13 +299,14 @@ __global__ void lz_sum_vectors_kernel(long long n, int nvec, const double2* __re
 
 // Workspace carve-up (all offsets 256-byte aligned).
 struct LzLayout {
-  size_t V, w, t0, t1, t2, lbuf, rot, hA, hB, part, npart, d, e, s, bl, theta, Y, arrow, nbad, rq, perm, total;
+  size_t V, w, t0, t1, t2, lbuf, rot, hA, hB, part, npart, d, e, s, bl, theta, Y, arrow, nbad, rq, perm, Vs, ws,
+      total;
   size_t arrow_bytes;
 };
 
 size_t al(size_t v) { return (v + 255) / 256 * 256; }
 
-LzLayout lz_layout(int B, long long n, int ncv, int kk, int nev, int nblk) {
+LzLayout lz_layout(int B, long long n, int ncv, int kk, int nev, int nblk, bool gs_df = false) {
   LzLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -334,6 +339,11 @@ LzLayout lz_layout(int B, long long n, int ncv, int kk, int nev, int nblk) {
   L.nbad = take(16);
   L.rq = take((size_t)B * nev * 8);
   L.perm = take((size_t)B * nev * 4);
+  L.Vs = L.ws = 0;
+  if (gs_df) {  // the basis and w in the split form of the double-float Gram-Schmidt pass
+    L.Vs = take((size_t)B * (ncv + 1) * n * 16);
+    L.ws = take(vec);
+  }
   L.total = o;
   return L;
 }
@@ -415,6 +425,7 @@ struct LzArgs {
   int* status;
   void* workspace;
   cudaStream_t stream;
+  bool gs_df = false;  // Gram-Schmidt passes in double-float arithmetic on the FP32 pipe
 };
 
 size_t lz_c64_bytes(int B, long long n) { return 2 * al((size_t)B * n * 8); }
@@ -432,7 +443,10 @@ int lanczos_solve(const LzArgs& a) {
   // elementwise grids: one element per thread; the Gram-Schmidt update kernel writes its ||w||^2 partials on the
   // same grid (ceil(n / 256) blocks per problem)
   const int nblk = (int)((n + LZ_THREADS - 1) / LZ_THREADS);
-  const LzLayout Lw = lz_layout(B, n, ncv, kk, Ne, nblk);
+  const LzLayout Lw = lz_layout(B, n, ncv, kk, Ne, nblk, a.gs_df);
+  float4* const Vs = a.gs_df ? (float4*)((uint8_t*)a.workspace + Lw.Vs) : nullptr;  // split basis rows
+  float4* const wsp = a.gs_df ? (float4*)((uint8_t*)a.workspace + Lw.ws) : nullptr;  // split w
+  const long long vsb = (long long)(ncv + 1) * n;
   uint8_t* const W = (uint8_t*)a.workspace;
   // complex64 operand and result of the FP32 stencil, after the FP64 layout
   float2* x32 = (float2*)(W + Lw.total);
@@ -505,25 +519,39 @@ int lanczos_solve(const LzArgs& a) {
     return ED_OK;
   };
 
+  // one Gram-Schmidt pass of w against rows 0..j: FP64, or double-float on the split rows (split_w: w changed
+  // since the last pass, so its split form is refreshed first)
+  auto gs = [&](int j, double2* h, double* np, bool split_w) -> int {
+    if (!a.gs_df) return ed_cgs_pass(B, j + 1, n, V, vb, w, h, ncv + 1, np, sr);
+    int r = split_w ? split_rows(B, 1, n, w, n, wsp, n, sr) : ED_OK;
+    if (r == ED_OK) r = cgs_pass_df(B, j + 1, n, Vs, vsb, w, wsp, h, ncv + 1, np, sr);
+    return r;
+  };
+  // the split form of basis rows j0 .. j0 + nrow - 1 after they were written
+  auto split_basis = [&](int j0, int nrow, cudaStream_t s2) -> int {
+    return a.gs_df ? split_rows(B, nrow, n, V + (long long)j0 * n, vb, Vs + (long long)j0 * n, vsb, s2) : ED_OK;
+  };
   // Lanczos steps k .. ncv-1 on stream sr
   auto cycle = [&](int k) -> int {
     int r;
     for (int j = k; j < ncv; ++j) {
       if ((r = apply(V + (long long)j * n, vb, w)) != ED_OK) return r;
       if (j == k) {
-        if ((r = ed_cgs_pass(B, j + 1, n, V, vb, w, hA, ncv + 1, nullptr, sr)) != ED_OK) return r;
-        if ((r = ed_cgs_pass(B, j + 1, n, V, vb, w, hB, ncv + 1, npart, sr)) != ED_OK) return r;
+        if ((r = gs(j, hA, nullptr, true)) != ED_OK) return r;
+        if ((r = gs(j, hB, npart, false)) != ED_OK) return r;
         lz_finish_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V, vb, j, w, hA, hB, ncv + 1, npart, nblk, d, e, bl, ncv, 1);
         if ((r = lz_chk(cudaGetLastError(), "Lanczos step end")) != ED_OK) return r;
+        if ((r = split_basis(j + 1, 1, sr)) != ED_OK) return r;
       } else {
         lz_dot_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V + (long long)j * n, vb, w, n, part);
         if ((r = lz_chk(cudaGetLastError(), "Lanczos alpha")) != ED_OK) return r;
         lz_three_term_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V, vb, j, w, part, nblk, d, e, ncv);
         if ((r = lz_chk(cudaGetLastError(), "Lanczos recurrence")) != ED_OK) return r;
-        if ((r = ed_cgs_pass(B, j + 1, n, V, vb, w, hA, ncv + 1, npart, sr)) != ED_OK) return r;
+        if ((r = gs(j, hA, npart, true)) != ED_OK) return r;
         lz_finish_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, V, vb, j, w, hA, nullptr, ncv + 1, npart, nblk, d, e, bl,
                                                         ncv, 0);
         if ((r = lz_chk(cudaGetLastError(), "Lanczos step end")) != ED_OK) return r;
+        if ((r = split_basis(j + 1, 1, sr)) != ED_OK) return r;
       }
     }
     return ED_OK;
@@ -576,6 +604,7 @@ int lanczos_solve(const LzArgs& a) {
   LZ_LAUNCHED("Lanczos start norm");
   lz_normalise_kernel<<<vgrid, LZ_THREADS, 0, st>>>(n, w, part, nblk, V, vb);
   LZ_LAUNCHED("Lanczos start normalise");
+  LZ_TRY(split_basis(0, 1, st));
 
   int k = 0, restarts = 0, converged = 0, restart_cycles = 0;
   for (restarts = 1; restarts <= max_restarts; ++restarts) {
@@ -608,6 +637,7 @@ int lanczos_solve(const LzArgs& a) {
                        "Lanczos residual vector copy"));
     lz_restart_kernel<<<(B * kk + 127) / 128, 128, 0, st>>>(B, ncv, kk, theta, Y, bl, d, s);
     LZ_LAUNCHED("Lanczos restart");
+    LZ_TRY(split_basis(0, kk + 1, st));  // the rotated rows and the moved residual row
     k = kk;
   }
   if (restarts > max_restarts) restarts = max_restarts;
@@ -681,15 +711,17 @@ int lz_refine_ncv(int Ne, long long n) { return (int)std::min<long long>(std::ma
 extern "C" int ed_lanczos_workspace_ex(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, int stencil_prec,
                                        size_t* bytes) {
   ED_CHECK_ARG(bytes, "ed_lanczos_workspace_ex: null pointer");
-  ED_CHECK_ARG(stencil_prec == ED_C128 || stencil_prec == ED_C64, "ed_lanczos_workspace_ex: bad stencil precision");
+  const bool gs_df = (stencil_prec & ED_LANCZOS_GS_DF) != 0;
+  const int sp = stencil_prec & ~ED_LANCZOS_GS_DF;
+  ED_CHECK_ARG(sp == ED_C128 || sp == ED_C64, "ed_lanczos_workspace_ex: bad stencil precision");
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_workspace_ex: bad sizes");
   const long long n = 3LL * Lx * Ly * Lz;
   ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_workspace_ex: need Ne < ncv <= 3*Lx*Ly*Lz");
   const int nblk = (int)((n + ed::LZ_THREADS - 1) / ed::LZ_THREADS);
-  size_t need = ed::lz_layout(nt, n, ncv, ed::lz_kept(Ne, ncv), Ne, nblk).total;
-  if (stencil_prec == ED_C64) {
+  size_t need = ed::lz_layout(nt, n, ncv, ed::lz_kept(Ne, ncv), Ne, nblk, gs_df).total;
+  if (sp == ED_C64) {
     const int ncv2 = ed::lz_refine_ncv(Ne, n);
-    if (ncv2 > Ne) need = std::max(need, ed::lz_layout(nt, n, ncv2, ed::lz_kept(Ne, ncv2), Ne, nblk).total);
+    if (ncv2 > Ne) need = std::max(need, ed::lz_layout(nt, n, ncv2, ed::lz_kept(Ne, ncv2), Ne, nblk, gs_df).total);
     need += ed::lz_c64_bytes(nt, n);
   }
   *bytes = need;
@@ -701,12 +733,37 @@ extern "C" int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* link
                                 double lambda_cut, void* evecs, double* evals, int* status, void* workspace,
                                 size_t workspace_bytes, void* stream) {
   using namespace ed;
-  ED_CHECK_ARG(stencil_prec == ED_C128 || stencil_prec == ED_C64, "ed_lanczos_tr_ex: bad stencil precision");
+  const bool gs_df = (stencil_prec & ED_LANCZOS_GS_DF) != 0;
+  const int sp = stencil_prec & ~ED_LANCZOS_GS_DF;
+  ED_CHECK_ARG(sp == ED_C128 || sp == ED_C64, "ed_lanczos_tr_ex: bad stencil precision");
   ED_CHECK_ARG(status, "ed_lanczos_tr_ex: null status");
   for (int q = 0; q < 6; ++q) status[q] = 0;
-  if (stencil_prec == ED_C128) {
+  if (sp == ED_C128 && !gs_df) {
     const int rc = ed_lanczos_tr(Lx, Ly, Lz, nt, links, Ne, tol, ncv, max_restarts, poly_deg, lambda_cut, evecs, evals,
                                  status, workspace, workspace_bytes, stream);
+    status[4] = status[2];
+    return rc;
+  }
+  if (sp == ED_C128) {  // FP64 stencil, double-float Gram-Schmidt
+    ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr_ex: bad sizes");
+    const long long n = 3LL * Lx * Ly * Lz;
+    ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr_ex: need Ne < ncv <= 3*Lx*Ly*Lz");
+    ED_CHECK_ARG(tol > 0.0 && max_restarts > 0, "ed_lanczos_tr_ex: need tol > 0 and max_restarts > 0");
+    ED_CHECK_ARG(poly_deg >= 0 && (poly_deg == 0 || (lambda_cut > 0.0 && lambda_cut < 12.0)),
+                 "ed_lanczos_tr_ex: a Chebyshev degree needs 0 < lambda_cut < 12");
+    ED_CHECK_ARG(links && evecs && evals && workspace, "ed_lanczos_tr_ex: null pointer");
+    ED_CHECK_ARG(((uintptr_t)workspace % 256) == 0 && ((uintptr_t)evecs % 16) == 0 && ((uintptr_t)links % 16) == 0,
+                 "ed_lanczos_tr_ex: workspace must be 256-byte aligned, links and evecs 16-byte aligned");
+    size_t need = 0;
+    int rc = ed_lanczos_workspace_ex(Lx, Ly, Lz, nt, Ne, ncv, stencil_prec, &need);
+    if (rc != ED_OK) return rc;
+    if (workspace_bytes < need) {
+      set_error("ed_lanczos_tr_ex: workspace of %zu bytes is smaller than the %zu needed", workspace_bytes, need);
+      return ED_ERR_WORKSPACE;
+    }
+    LzArgs a{Lx, Ly, Lz, nt, links, nullptr, ED_C128, Ne, tol, ncv, max_restarts, poly_deg, lambda_cut,
+             evecs, evals, nullptr, 0, status, workspace, (cudaStream_t)stream, true};
+    rc = lanczos_solve(a);
     status[4] = status[2];
     return rc;
   }
@@ -720,7 +777,7 @@ extern "C" int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* link
                "ed_lanczos_tr_ex: workspace must be 256-byte aligned, links and evecs 16-byte aligned");
   ED_CHECK_ARG(Lx % 2 == 0, "ed_lanczos_tr_ex: the complex64 stencil needs an even Lx");
   size_t need = 0;
-  int rc = ed_lanczos_workspace_ex(Lx, Ly, Lz, nt, Ne, ncv, ED_C64, &need);
+  int rc = ed_lanczos_workspace_ex(Lx, Ly, Lz, nt, Ne, ncv, stencil_prec, &need);
   if (rc != ED_OK) return rc;
   if (workspace_bytes < need) {
     set_error("ed_lanczos_tr_ex: workspace of %zu bytes is smaller than the %zu needed", workspace_bytes, need);
@@ -731,7 +788,7 @@ extern "C" int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* link
   // phase 1: complex64 stencil, FP64 basis, Gram-Schmidt and Rayleigh-Ritz, to the loose tolerance LZ_MIXED_TOL
   int st1[3] = {0, 0, 0};
   LzArgs a1{Lx, Ly, Lz, nt, links, links_c64, ED_C64, Ne, std::max(tol, LZ_MIXED_TOL), ncv,
-            std::min(max_restarts, LZ_MIXED_RESTARTS), 0, 0.0, evecs, evals, nullptr, 0, st1, workspace, st};
+            std::min(max_restarts, LZ_MIXED_RESTARTS), 0, 0.0, evecs, evals, nullptr, 0, st1, workspace, st, gs_df};
   if ((rc = lanczos_solve(a1)) != ED_OK) return rc;
   int lap_code = 0;  // a bounded wait of the TMA-staged complex64 stencil that gave up invalidates phase 1
   if ((rc = ed_laplacian_status(&lap_code, st)) != ED_OK) return rc;
@@ -752,7 +809,7 @@ extern "C" int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* link
   const int deg = poly_deg > 0 ? poly_deg : LZ_MIXED_DEG;
   const bool cheb = cut > 0.0 && cut < 12.0 && ncv2 > Ne;
   LzArgs a2{Lx, Ly, Lz, nt, links, nullptr, ED_C128, Ne, cheb ? std::max(tol, 1e-12) : tol, cheb ? ncv2 : ncv,
-            max_restarts, cheb ? deg : 0, cheb ? cut : 0.0, evecs, evals, evecs, Ne, st2, workspace, st};
+            max_restarts, cheb ? deg : 0, cheb ? cut : 0.0, evecs, evals, evecs, Ne, st2, workspace, st, gs_df};
   if ((rc = lanczos_solve(a2)) != ED_OK) return rc;
   status[0] = st2[0];
   status[1] = st1[1] + st2[1];

@@ -55,15 +55,21 @@ def stout_smear_links_(U: torch.Tensor, latt_size, nstep: int, rho: float):
 
 class EigenvectorGenerator:
     def __init__(self, latt_size: List[int], gauge_field, Ne: int, tol: float, *, stencil_precision: str = "fp64",
-                 device=None, ncv: int = None, driver: str = "native") -> None:
+                 device=None, ncv: int = None, driver: str = "native", gs_precision: str = "fp64") -> None:
         """``ncv``: Krylov dimension of the thick-restart Lanczos (default
         max(9 Ne / 4, Ne + 32), 2 Ne with Chebyshev acceleration, capped by
         the problem size).  ``driver``: ``"native"`` runs the FP64-stencil
         eigensolve in the library (``ed_lanczos_tr``); ``"python"`` drives the
         same kernels from ``lanczos.trlanczos`` (the FP32-stencil mode always
-        does)."""
+        does).  ``gs_precision="df"`` (native driver): Gram-Schmidt in
+        double-float arithmetic on the FP32 pipe (``ED_LANCZOS_GS_DF``)."""
         if stencil_precision not in ("fp64", "fp32"):
             raise ValueError("stencil_precision must be 'fp64' or 'fp32'")
+        if gs_precision not in ("fp64", "df"):
+            raise ValueError("gs_precision must be 'fp64' or 'df'")
+        if gs_precision == "df" and driver != "native":
+            raise ValueError("gs_precision='df' needs the native driver")
+        self.gs_precision = gs_precision
         if driver not in ("native", "python"):
             raise ValueError("driver must be 'native' or 'python'")
         self.driver = driver
@@ -141,13 +147,15 @@ class EigenvectorGenerator:
                 evals, planes, stats = lanczos_tr(sel, self.latt_size, self.Ne, self.tol, ncv=self.ncv,
                                                   poly_deg=polynomial_degree if polynomial_degree > 0 else 0,
                                                   lambda_cut=lambda_cut if lambda_cut > 0 else 0.0,
-                                                  stencil_precision="fp32", links_c64=l32)
+                                                  stencil_precision="fp32", links_c64=l32,
+                                                  gs_precision=self.gs_precision)
             else:
                 poly = polynomial_degree if (polynomial_degree > 0 and lambda_cut > 0) else 0
                 evals, planes, stats = lanczos_tr(sel, self.latt_size, self.Ne,
                                                   max(self.tol, 1e-12) if poly else self.tol, ncv=self.ncv,
-                                                  poly_deg=poly, lambda_cut=lambda_cut if poly else 0.0)
-            self.last_stats = {k: v for k, v in stats.items() if k != "ncv"}
+                                                  poly_deg=poly, lambda_cut=lambda_cut if poly else 0.0,
+                                                  gs_precision=self.gs_precision)
+            self.last_stats = {k: v for k, v in stats.items() if k not in ("ncv", "gs_precision")}
             evecs = planes.reshape(B, self.Ne, n)
             if apply_renorm_phase:
                 LZ.renorm_phase_(evecs)

@@ -13,7 +13,7 @@ from typing import Sequence
 import torch
 
 from . import _lib
-from ._lib import ED_C64, ED_C128, call, ptr, require_cuda, stream_handle
+from ._lib import ED_C64, ED_C128, ED_LANCZOS_GS_DF, call, ptr, require_cuda, stream_handle
 
 _PREC = {torch.complex128: ED_C128, torch.complex64: ED_C64}
 _NATIVE_LITTLE = sys.byteorder == "little"
@@ -200,7 +200,7 @@ def laplacian_status():
 
 def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int = None, max_restarts: int = None,
                poly_deg: int = 0, lambda_cut: float = 0.0, stencil_precision: str = "fp64",
-               links_c64: torch.Tensor = None):
+               links_c64: torch.Tensor = None, gs_precision: str = "fp64"):
     """Native batched thick-restart Lanczos (``ed_lanczos_tr`` /
     ``ed_lanczos_tr_ex``) for the lowest ``Ne`` eigenpairs of the FP64
     Laplacian of every timeslice of ``links_soa`` (complex128 ``[nt, 27, V3]``).
@@ -209,7 +209,10 @@ def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int
     on ``links_c64`` (complex64 SoA of the same links) inside a loose FP64
     thick-restart iteration, then an FP64 Chebyshev-filtered refinement whose
     cut comes from it (``poly_deg``: its degree, 0 = 16; ``lambda_cut`` <= 0:
-    automatic).  Returns (evals ``[nt, Ne]`` float64 ascending, evecs
+    automatic).  ``gs_precision="df"`` runs the Gram-Schmidt passes in
+    double-float arithmetic on the FP32 pipe (``ED_LANCZOS_GS_DF``; products
+    to ~2^-47 relative, the basis streamed at HBM speed) instead of FP64.
+    Returns (evals ``[nt, Ne]`` float64 ascending, evecs
     ``[nt, Ne, 3, V3]`` complex128 colour planes, stats ``{"converged",
     "restarts", "matvecs", ...}``)."""
     require_cuda(links_soa, "links")
@@ -217,6 +220,9 @@ def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int
         raise ValueError("the native Lanczos works on complex128 links")
     if stencil_precision not in ("fp64", "fp32"):
         raise ValueError("stencil_precision must be 'fp64' or 'fp32'")
+    if gs_precision not in ("fp64", "df"):
+        raise ValueError("gs_precision must be 'fp64' or 'df'")
+    gs_flag = ED_LANCZOS_GS_DF if gs_precision == "df" else 0
     Lx, Ly, Lz = (int(v) for v in latt_size[:3])
     nt, V3 = links_soa.shape[0], Lx * Ly * Lz
     if tuple(links_soa.shape[1:]) != (27, V3):
@@ -230,6 +236,15 @@ def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int
     evecs = torch.empty((nt, Ne, 3, V3), dtype=torch.complex128, device=links_soa.device)
     evals = torch.empty((nt, Ne), dtype=torch.float64, device=links_soa.device)
     nbytes = ctypes.c_size_t()
+    if not mixed and gs_flag:
+        call("ed_lanczos_workspace_ex", Lx, Ly, Lz, nt, Ne, ncv, ED_C128 | gs_flag, ctypes.byref(nbytes))
+        ws = torch.empty(nbytes.value, dtype=torch.uint8, device=links_soa.device)
+        st = (ctypes.c_int * 6)()
+        call("ed_lanczos_tr_ex", Lx, Ly, Lz, nt, ptr(links_soa), None, ED_C128 | gs_flag, Ne, float(tol), ncv,
+             max_restarts, int(poly_deg), float(lambda_cut), ptr(evecs), ptr(evals), st, ptr(ws), ws.numel(),
+             stream_handle())
+        return evals, evecs, {"converged": bool(st[0]), "restarts": int(st[1]), "matvecs": int(st[2]), "ncv": ncv,
+                              "gs_precision": gs_precision}
     if not mixed:
         call("ed_lanczos_workspace", Lx, Ly, Lz, nt, Ne, ncv, ctypes.byref(nbytes))
         ws = torch.empty(nbytes.value, dtype=torch.uint8, device=links_soa.device)
@@ -240,22 +255,26 @@ def lanczos_tr(links_soa: torch.Tensor, latt_size, Ne: int, tol: float, ncv: int
     if links_c64 is None or links_c64.dtype != torch.complex64 or tuple(links_c64.shape) != tuple(links_soa.shape):
         raise ValueError("the fp32 stencil needs links_c64: complex64 SoA links of the same shape")
     require_cuda(links_c64, "links_c64")
-    call("ed_lanczos_workspace_ex", Lx, Ly, Lz, nt, Ne, ncv, ED_C64, ctypes.byref(nbytes))
+    call("ed_lanczos_workspace_ex", Lx, Ly, Lz, nt, Ne, ncv, ED_C64 | gs_flag, ctypes.byref(nbytes))
     ws = torch.empty(nbytes.value, dtype=torch.uint8, device=links_soa.device)
     st = (ctypes.c_int * 6)()
-    call("ed_lanczos_tr_ex", Lx, Ly, Lz, nt, ptr(links_soa), ptr(links_c64), ED_C64, Ne, float(tol), ncv,
+    call("ed_lanczos_tr_ex", Lx, Ly, Lz, nt, ptr(links_soa), ptr(links_c64), ED_C64 | gs_flag, Ne, float(tol), ncv,
          max_restarts, int(poly_deg), float(lambda_cut), ptr(evecs), ptr(evals), st, ptr(ws), ws.numel(),
          stream_handle())
     return evals, evecs, {"converged": bool(st[0]), "restarts": int(st[1]), "matvecs": int(st[2]), "ncv": ncv,
                           "matvecs_fp32": int(st[3]), "matvecs_fp64": int(st[4]), "restarts_fp32": int(st[5])}
 
 
-def cgs_pass(V: torch.Tensor, r: int, w: torch.Tensor, h: torch.Tensor = None, norm: bool = False):
+def cgs_pass(V: torch.Tensor, r: int, w: torch.Tensor, h: torch.Tensor = None, norm: bool = False,
+             precision: str = "fp64"):
     """One classical Gram-Schmidt pass (``ed_cgs_pass``): ``h = V[:, :r]^H w``,
     ``w -= V[:, :r] h`` in place.  ``V``: complex128 [B, rows, n] with
     contiguous rows (any batch stride), ``w``: contiguous complex128 [B, n].
     Returns ``h`` [B, r], and with ``norm`` also ``||w||`` [B] float64 of the
-    updated w (from the kernel's per-block partial sums)."""
+    updated w (from the kernel's per-block partial sums).  ``precision="df"``:
+    the double-float pass on the FP32 pipe (``ed_cgs_pass_df``)."""
+    if precision not in ("fp64", "df"):
+        raise ValueError("precision must be 'fp64' or 'df'")
     if V.dtype != torch.complex128 or w.dtype != torch.complex128:
         raise ValueError("cgs_pass works on complex128")
     if not (V.is_cuda and w.is_cuda) or not w.is_contiguous():
@@ -266,8 +285,13 @@ def cgs_pass(V: torch.Tensor, r: int, w: torch.Tensor, h: torch.Tensor = None, n
     if h is None:
         h = torch.empty((B, r), dtype=torch.complex128, device=w.device)
     part = torch.empty((B, (n + 255) // 256), dtype=torch.float64, device=w.device) if norm else None
-    call("ed_cgs_pass", B, r, n, ptr(V), V.stride(0), ptr(w), ptr(h), h.stride(0),
-         None if part is None else ptr(part), stream_handle())
+    if precision == "df":
+        ws = torch.empty(B * (r + 1) * n * 16, dtype=torch.uint8, device=w.device)
+        call("ed_cgs_pass_df", B, r, n, ptr(V), V.stride(0), ptr(w), ptr(h), h.stride(0),
+             None if part is None else ptr(part), ptr(ws), ws.numel(), stream_handle())
+    else:
+        call("ed_cgs_pass", B, r, n, ptr(V), V.stride(0), ptr(w), ptr(h), h.stride(0),
+             None if part is None else ptr(part), stream_handle())
     if norm:
         return h, torch.sqrt(part.sum(dim=1))
     return h

@@ -213,6 +213,13 @@ int ed_laplacian_status(int* code, void* stream);
  * per 16-byte element: about 2.5 TB/s at the FP64 peak), not by HBM. */
 int ed_cgs_pass(int B, int r, long long n, const void* V, long long v_bstride, void* w, void* h, int ldh,
                 double* norm_part, void* stream);
+/* ed_cgs_pass in double-float arithmetic on the FP32 pipe (the pass
+ * ED_LANCZOS_GS_DF selects inside the solver): V and w are split into two
+ * complex64 parts each (into `workspace`, at least B*(r+1)*n*16 bytes), the
+ * sums are (hi, lo) FP32 pairs; h, the updated w and the norm partials are
+ * complex128 / double as in ed_cgs_pass.  Product error ~2^-47 relative. */
+int ed_cgs_pass_df(int B, int r, long long n, const void* V, long long v_bstride, void* w, void* h, int ldh,
+                   double* norm_part, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Lowest Ne eigenpairs of the FP64 3D covariant Laplacian of nt timeslices by
  * batched thick-restart Lanczos: the eigsh call of
@@ -253,7 +260,16 @@ int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, dou
  * Lx must be even for ED_C64.  Synchronises the stream once per restart and
  * once between the phases.  The reference's eigsh is FP64 throughout
  * (lattice/generator/eigenvector.py:234-257); the precision split has no
- * counterpart there.  Needs ed_lanczos_workspace_ex bytes. */
+ * counterpart there.  Needs ed_lanczos_workspace_ex bytes.
+ *
+ * ED_LANCZOS_GS_DF OR-ed into stencil_prec (both calls): the Gram-Schmidt
+ * passes run in double-float arithmetic on the FP32 pipe (ed_cgs_pass_df)
+ * instead of FP64: the basis stays FP64 and gets a split copy (two complex64
+ * parts per value; the workspace grows by the basis size), the products err
+ * by ~2^-47 relative instead of 2^-53, and a pass streams the basis at HBM
+ * speed instead of the FP64 pipe's ~2.5 TB/s.  Everything else (recurrence,
+ * Rayleigh-Ritz, convergence test, Ritz vectors) stays FP64. */
+#define ED_LANCZOS_GS_DF 0x100
 int ed_lanczos_workspace_ex(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, int stencil_prec, size_t* bytes);
 int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* links, const void* links_c64, int stencil_prec,
                      int Ne, double tol, int ncv, int max_restarts, int poly_deg, double lambda_cut, void* evecs,

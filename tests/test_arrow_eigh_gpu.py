@@ -121,6 +121,27 @@ def test_cgs_pass_matches_torch(B, rows, r, n):
     assert torch.allclose(nrm, torch.linalg.vector_norm(w2, dim=1), rtol=1e-13, atol=0)
 
 
+@pytest.mark.parametrize("B,rows,r,n", [(3, 9, 7, 1000), (2, 40, 33, 3 * 216), (1, 5, 5, 17), (2, 1500, 1100, 64)])
+def test_cgs_pass_df_matches_torch(B, rows, r, n):
+    """The double-float Gram-Schmidt pass (FP32 pipe, values split into two
+    complex64 parts, (hi, lo) sums) against torch's FP64 GEMVs: products err by
+    ~2^-47 relative, so the pass agrees to ~1e-13 of the scale."""
+    from easydistillation_gb300.ops import cgs_pass
+
+    g = torch.Generator(device="cuda").manual_seed(r + 1)
+    V = torch.randn((B, rows + 1, n), dtype=torch.complex128, device="cuda", generator=g)
+    w = torch.randn((B, n), dtype=torch.complex128, device="cuda", generator=g)
+    Vj = V[:, :r]
+    h_ref = torch.bmm(w.unsqueeze(1).conj(), Vj.transpose(1, 2)).conj().squeeze(1)
+    w_ref = w - torch.bmm(h_ref.unsqueeze(1), Vj).squeeze(1)
+    w2 = w.clone()
+    h, nrm = cgs_pass(Vj, r, w2, norm=True, precision="df")
+    scale = float(torch.linalg.vector_norm(w)) * float(torch.linalg.vector_norm(Vj))
+    assert float(torch.linalg.vector_norm(h - h_ref)) <= 2e-13 * scale
+    assert float(torch.linalg.vector_norm(w2 - w_ref)) <= 2e-13 * scale * r ** 0.5
+    assert torch.allclose(nrm, torch.linalg.vector_norm(w2, dim=1), rtol=1e-13, atol=0)
+
+
 def test_lanczos_gs_kernel_matches_torch_gemv():
     from easydistillation_gb300.lanczos import trlanczos
     from easydistillation_gb300.ops import laplacian, links_to_soa

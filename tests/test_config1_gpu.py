@@ -107,3 +107,27 @@ def test_config1_mixed_precision_eigensolve():
     Xt = torch.from_numpy(Xf).cuda()
     Rt = torch.from_numpy(np.ascontiguousarray(rv.reshape(NE, -1))).cuda()
     assert float((Xt.T @ Xt.conj() - Rt.T @ Rt.conj()).abs().max()) < 1e-7
+
+
+@pytest.mark.parametrize("stencil", ["fp64", "fp32"])
+def test_config1_double_float_gram_schmidt(stencil):
+    """Gram-Schmidt in double-float arithmetic on the FP32 pipe
+    (gs_precision="df", ED_LANCZOS_GS_DF), with the FP64 and the mixed
+    stencil: the same checks against ARPACK as the FP64 passes."""
+    from easydistillation_gb300 import EigenvectorGenerator
+
+    gauge = _gauge()
+    U = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0]
+    gen = EigenvectorGenerator(LATT, MemGauge(gauge), NE, 1e-10, stencil_precision=stencil, gs_precision="df")
+    gen.load("cfg1")
+    X, lam = (a.cpu().numpy() for a in gen.calc(0))
+    assert gen.last_stats["converged"]
+    rv, re = R.eigensolve(U, LATT, NE, 1e-10)
+    np.testing.assert_allclose(lam, re, rtol=1e-10, atol=0)
+    Xf = X.reshape(NE, -1)
+    res = np.linalg.norm(R.laplacian(Xf.T, U, LATT).T - lam[:, None] * Xf, axis=1)
+    assert res.max() < 1e-9
+    assert np.abs(Xf.conj() @ Xf.T - np.eye(NE)).max() < 1e-12
+    Xt = torch.from_numpy(Xf).cuda()
+    Rt = torch.from_numpy(np.ascontiguousarray(rv.reshape(NE, -1))).cuda()
+    assert float((Xt.T @ Xt.conj() - Rt.T @ Rt.conj()).abs().max()) < 1e-7
