@@ -489,7 +489,9 @@ def run_ours(args, rank, world):
         if plan.factorised:
             pxy, pz = plan.factorised
             tiles = sum(-(-(j * pz * Ne) // 128) for j in rights) * (-(-(pxy * Ne) // 128))
-            kname = f"tc_fac_gemm_kernel<{args.mode}>"
+            pair_form = plan.tuning().get("tc_pair", 0)
+            kname = {2: "tc_fac2_gemm_kernel", 3: "tc_fac2s_gemm_kernel"}.get(pair_form, "tc_fac_gemm_kernel")
+            kname = f"{kname}<{args.mode}>"
         else:
             tiles = sum(-(-(j * Ne) // 128) for j in rights) * (-(-(Ne * NMOM) // 128))
             kname = f"tc_pair_gemm_kernel<{args.mode}>"
@@ -498,7 +500,7 @@ def run_ours(args, rank, world):
         tun = plan.tuning()
         default_workload = (plan.factorised is not None and args.mode == "f16x3" and B == 4 and Ne == NE
                             and list(latt[:3]) == LATT[:3] and not getattr(plan, "gauss", False)
-                            and tun.get("tc_stack", 0) != 2 and tun.get("tc_pair", 0) != 2)
+                            and tun.get("tc_stack", 0) != 2 and tun.get("tc_pair", 0) < 2)
         roofline = {"bound": "tensor", "achieved": alg_flop / kms / 1e9, "peak": pk, "unit": "TFLOP/s",
                     "frac": alg_flop / kms / 1e9 / pk,
                     "traffic": FAC_TRAFFIC_BYTES if default_workload else None,

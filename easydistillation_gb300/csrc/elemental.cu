@@ -662,7 +662,7 @@ extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int val
       plan->tc_stages = value;
       return ED_OK;
     case ED_TUNE_TC_PAIR:
-      ED_CHECK_ARG(value >= 0 && value <= 2, "ed_elemental_set_tuning: SM pairing %d (0, 1 or 2)", value);
+      ED_CHECK_ARG(value >= 0 && value <= 3, "ed_elemental_set_tuning: SM pairing %d (0, 1, 2 or 3)", value);
       plan->tc_pair = value;
       return ED_OK;
     case ED_TUNE_TC_KPB:

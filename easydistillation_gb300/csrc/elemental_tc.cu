@@ -302,6 +302,16 @@ __global__ void tc_df_to_c128_kernel(const float4* __restrict__ DF, long long n,
   }
 }
 
+// the same for the two double-float planes of the SM-pair stacked GEMM (plane 1 at DF + plane), added
+__global__ void tc_df2_to_c128_kernel(const float4* __restrict__ DF, long long plane, long long n,
+                                      cplx<double>* __restrict__ G) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 a = DF[i], b = DF[plane + i];
+    G[i] = mk(((double)a.x + (double)a.y) + ((double)b.x + (double)b.y),
+              ((double)a.z + (double)a.w) + ((double)b.z + (double)b.w));
+  }
+}
+
 // FP64 phases -> complex64 phases scaled by 2^e
 __global__ void tc_phase_kernel(const cplx<double>* __restrict__ ph, long long n, const TcScalars* __restrict__ sc,
                                 cplx<float>* __restrict__ out) {
@@ -527,7 +537,8 @@ static FacLayout fac_layout(const ed_elemental_plan* P) {
   const size_t np = tcf_planes(P->gauss ? TCF_GAUSS : TCF_FOUR);  // re, im (and re + im) x hi, lo
   L.apl = L.bpl + up256(np * (size_t)L.rb * K * esz);
   L.df = L.apl + up256(np * (size_t)L.ra * K * esz);
-  L.total = L.df + up256((size_t)P->g_elems * sizeof(float4));
+  // two planes: the SM-pair stacked GEMM (ED_TUNE_TC_PAIR = 3) gives each CTA of a pair its own
+  L.total = L.df + up256(2 * (size_t)P->g_elems * sizeof(float4));
   return L;
 }
 
@@ -819,18 +830,21 @@ static int encode_kmajor(CUtensorMap* map, int kind, void* base, long long K, lo
   return ED_OK;
 }
 
-// The factorised-phase GEMM on SM pairs (tc_fac2_gemm_kernel): the same job table with 256-row A tiles, a
-// cooperative launch of two-CTA clusters, every cluster co-resident.
+// The factorised-phase GEMMs on SM pairs, a cooperative launch of two-CTA clusters, every cluster co-resident:
+// tc_fac2_gemm_kernel (four-product form, 256-row A tiles) or, with `stacked`, tc_fac2s_gemm_kernel (the
+// single-SM tiles with the complex halves of A and B spread over the pair; two double-float planes).
 template <int KIND>
 static int launch_fac_pairs(const ed_elemental_plan* P, const FacLayout& lay, void* apl, void* bpl, TcScalars* sc,
-                            float4* DF, cplx<double>* G, cudaStream_t stream, int nb) {
+                            float4* DF, cplx<double>* G, cudaStream_t stream, int nb, bool stacked) {
   const long long K = 3LL * P->V3;
   const int pxy = P->fac_pxy, pz = P->fac_pz, Ne = P->Ne, nl = (int)P->fac_lchain.size();
   int rc;
   CUtensorMap amap, bmap, bmap16;
-  if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra))) return rc;                 // 128-row A halves
-  if ((rc = encode_kmajor(&bmap, KIND, bpl, K, lay.rb, TC_BN / 2))) return rc;      // 64-row B halves
-  if ((rc = encode_kmajor(&bmap16, KIND, bpl, K, lay.rb, 16))) return rc;          // narrow last column tile
+  if ((rc = encode_kmajor(&amap, KIND, apl, K, lay.ra))) return rc;  // 128-row A boxes
+  // B: 128-row boxes (stacked: a CTA holds every column of one plane) or 64-row halves
+  if ((rc = encode_kmajor(&bmap, KIND, bpl, K, lay.rb, stacked ? TC_BN : TC_BN / 2))) return rc;
+  if ((rc = encode_kmajor(&bmap16, KIND, bpl, K, lay.rb, 16))) return rc;  // narrow last column tile
+  const int tile_rows = stacked ? TC_BM : TCP_BM;
   TcFacTable tab;
   tab.njobs = nb * P->jobs_per_t;
   tab.pxy = pxy;
@@ -845,12 +859,14 @@ static int launch_fac_pairs(const ed_elemental_plan* P, const FacLayout& lay, vo
     d.brow0 = slot * pxy * Ne;
     d.nright = j.nright;
     d.g_off = j.g_off;
-    d.mt = (int)ceil_div((long long)j.nright * pz * Ne, TCP_BM);
+    d.mt = (int)ceil_div((long long)j.nright * pz * Ne, tile_rows);
     d.nt = (int)ceil_div((long long)pxy * Ne, TC_BN);
   }
-  // a last column tile of at most 96 valid columns runs narrow (N rounded up to 32, 16-row B boxes)
+  // a narrow last column tile: N rounded up to 32 (four-product: each CTA then holds N/2 rows of B, a
+  // multiple of the 16-row box) or to 16 (stacked: each CTA holds the tile's columns of one plane)
   const int last_cols = pxy * Ne - (tab.j[0].nt - 1) * TC_BN;
-  const bool narrow = ((last_cols + 31) & ~31) < TC_BN;
+  const int round_to = stacked ? 16 : 32;
+  const bool narrow = ((last_cols + round_to - 1) & ~(round_to - 1)) < TC_BN;
   int tiles = 0, tiles_n = 0;
   for (int k = 0; k < tab.njobs; ++k) {
     TcFacJob& d = tab.j[k];
@@ -861,14 +877,18 @@ static int launch_fac_pairs(const ed_elemental_plan* P, const FacLayout& lay, vo
   }
   tab.nfull = tiles;
   tiles += tiles_n;
-  const int nst = P->tc_stages > 0 ? std::min(P->tc_stages, TCP_MAX_STAGES) : TCP_DEFAULT_STAGES;
+  const int max_st = stacked ? TCS_MAX_STAGES : TCP_MAX_STAGES;
+  const int nst = P->tc_stages > 0 ? std::min(P->tc_stages, max_st) : (stacked ? TCS_DEFAULT_STAGES : TCP_DEFAULT_STAGES);
+  auto kern4 = tc_fac2_gemm_kernel<KIND>;
+  auto kerns = tc_fac2s_gemm_kernel<KIND>;
+  const void* kfn = stacked ? (const void*)kerns : (const void*)kern4;
   cudaError_t e;
-  static bool attr_set[4] = {};
-  if (!attr_set[KIND]) {
-    e = cudaFuncSetAttribute(tc_fac2_gemm_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             tcp_smem(TCP_MAX_STAGES));
+  static bool attr_set[4][2] = {};
+  if (!attr_set[KIND][stacked]) {
+    e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             stacked ? tcs_smem(TCS_MAX_STAGES) : tcp_smem(TCP_MAX_STAGES));
     if (e != cudaSuccess) return cuda_status(e, "paired tc kernel smem attribute");
-    attr_set[KIND] = true;
+    attr_set[KIND][stacked] = true;
   }
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[2];
@@ -879,13 +899,13 @@ static int launch_fac_pairs(const ed_elemental_plan* P, const FacLayout& lay, vo
   attr[1].id = cudaLaunchAttributeCooperative;
   attr[1].val.cooperative = 1;
   cfg.blockDim = dim3(TC_THREADS);
-  cfg.dynamicSmemBytes = tcp_smem(nst);
+  cfg.dynamicSmemBytes = stacked ? tcs_smem(nst) : tcp_smem(nst);
   cfg.stream = stream;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cfg.gridDim = dim3(2 * num_sms());
   int clusters = 0;
-  e = cudaOccupancyMaxActiveClusters(&clusters, tc_fac2_gemm_kernel<KIND>, &cfg);
+  e = cudaOccupancyMaxActiveClusters(&clusters, kfn, &cfg);
   if (e != cudaSuccess) return cuda_status(e, "paired tc kernel cluster occupancy");
   if (clusters < 1) {
     set_error("the paired factorised tensor-core GEMM does not fit on the device");
@@ -898,16 +918,24 @@ static int launch_fac_pairs(const ed_elemental_plan* P, const FacLayout& lay, vo
   cfg.numAttrs = 2;
   const int slab_kb = P->tc_slab_kb > 0 ? P->tc_slab_kb : TC_FLUSH_KB;
   const long long g_used = (long long)nb * P->g_per_t;
-  e = cudaMemsetAsync(DF, 0, (size_t)g_used * sizeof(float4), stream);
+  const int planes = stacked ? 2 : 1;  // the stacked form's CTAs flush into planes of their own
+  e = cudaMemsetAsync(DF, 0, (size_t)planes * g_used * sizeof(float4), stream);
   if (e != cudaSuccess) return cuda_status(e, "clearing the pair results");
   if (P->prof_start) cudaEventRecord(P->prof_start, stream);
-  const int kpb = P->tc_kpb > 0 ? P->tc_kpb : 1;
-  e = cudaLaunchKernelEx(&cfg, tc_fac2_gemm_kernel<KIND>, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb,
-                         nst, kpb);
+  if (stacked) {
+    const int kpb = P->tc_kpb > 0 ? P->tc_kpb : 2;
+    e = cudaLaunchKernelEx(&cfg, kerns, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, g_used, tiles, slab_kb, nst, kpb);
+  } else {
+    const int kpb = P->tc_kpb > 0 ? P->tc_kpb : 1;
+    e = cudaLaunchKernelEx(&cfg, kern4, amap, bmap, bmap16, tab, Ne, P->V3, sc, DF, tiles, slab_kb, nst, kpb);
+  }
   if (P->prof_stop) cudaEventRecord(P->prof_stop, stream);
   if (e != cudaSuccess) return cuda_status(e, "paired factorised-phase GEMM launch");
   ED_RETURN_LAUNCH("paired factorised-phase GEMM");
-  tc_df_to_c128_kernel<<<8 * num_sms(), 256, 0, stream>>>(DF, g_used, G);
+  if (stacked)
+    tc_df2_to_c128_kernel<<<8 * num_sms(), 256, 0, stream>>>(DF, g_used, g_used, G);
+  else
+    tc_df_to_c128_kernel<<<8 * num_sms(), 256, 0, stream>>>(DF, g_used, G);
   ED_RETURN_LAUNCH("double-float to complex128");
   return ED_OK;
 }
@@ -969,7 +997,8 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   }
   ED_RETURN_LAUNCH("variant planes");
 
-  if (P->tc_pair == 2 && !P->gauss) return launch_fac_pairs<KIND>(P, lay, apl, bpl, sc, DF, G, stream, nb);
+  if (P->tc_pair >= 2 && !P->gauss)
+    return launch_fac_pairs<KIND>(P, lay, apl, bpl, sc, DF, G, stream, nb, P->tc_pair == 3);
 
   const int form = P->gauss ? TCF_GAUSS : (P->tc_stack == 2 ? TCF_FOUR : TCF_STACKED);
   const int np = tcf_planes(form);

@@ -73,12 +73,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Add the 64 register sums of one drain thread (row m, columns n0c..n0c+63)
-// into the double-float results and clear them.  The read-modify-writes go
+// into the double-float results and clear them (with `swap`, sre holds the
+// imaginary parts and -sim the real ones).  The read-modify-writes go
 // in groups of 8: all loads of a group are issued before its stores, so a
 // flush waits for 8 memory round trips instead of 64.
 __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64], float4* __restrict__ DF,
                                                const TcFacTable& tab, const TcFacJob& J, int Ne, int n0c,
-                                               int m_local, int Mrows, float inv) {
+                                               int m_local, int Mrows, float inv, bool swap = false) {
   constexpr int G = 8;
   const int Ncols = tab.pxy * Ne;
   const int N = J.nright * Ne;  // row length of G_p[i][.] within the group
@@ -107,8 +108,10 @@ __device__ __forceinline__ void flush_sums_fac(float (&sre)[64], float (&sim)[64
 #pragma unroll
     for (int u = 0; u < G; ++u) {
       if (off[u] >= 0) {
-        df_add(d[u].x, d[u].y, sre[q0 + u] * inv);
-        df_add(d[u].z, d[u].w, sim[q0 + u] * inv);
+        // swap: the sums hold (im, -re) (the second CTA of a pair in tc_fac2s_gemm_kernel)
+        const float re = swap ? -sim[q0 + u] : sre[q0 + u], im = swap ? sre[q0 + u] : sim[q0 + u];
+        df_add(d[u].x, d[u].y, re * inv);
+        df_add(d[u].z, d[u].w, im * inv);
         base[off[u]] = d[u];
       }
       sre[q0 + u] = 0.f;

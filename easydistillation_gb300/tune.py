@@ -281,16 +281,20 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
 
         def forms_on_sms(best: Candidate) -> List[Candidate]:
             # the factorised GEMM on single SMs (stacked operands with 2 or 4 k-blocks per accumulator group,
-            # or the four-product form) or on SM pairs
+            # or the four-product form) or on SM pairs (four-product form, or the stacked operands spread over
+            # the pair with 4 k-blocks per TMEM buffer)
             if not factorised(best):
                 return []
             return [Candidate(best.factorise, dict(t)) for t in
-                    ({}, {"tc_kpb": 4}, {"tc_stack": 2, "tc_kpb": 2}, {"tc_pair": 2, "tc_kpb": 2})]
+                    ({}, {"tc_kpb": 4}, {"tc_stack": 2, "tc_kpb": 2}, {"tc_pair": 2, "tc_kpb": 2},
+                     {"tc_pair": 3, "tc_kpb": 4})]
 
         def slabs(best: Candidate) -> List[Candidate]:
             if not factorised(best):
                 return []
             base = dict(best.tuning)
+            # the other stage count: 4 (of 48 KB) for the four-product SM pairs, 3 otherwise (single SMs: 2 by
+            # default; stacked SM pairs: 4 of 32 KB by default)
             more_stages = 4 if base.get("tc_pair") == 2 else 3
             return ([best] + [Candidate(best.factorise, {**base, "tc_slab_kb": s}) for s in SLABS[1:]] +
                     [Candidate(best.factorise, {**base, "tc_stages": more_stages}),

@@ -90,10 +90,17 @@ extern "C" {
                               * fits on the device at once) or an upper bound on that number */
 #define ED_TUNE_TC_STAGES 4  /* operand stages in the factorised GEMM's shared-memory ring: 0 (the
                               * default of the GEMM form), 2 or 3 (64 KB stages on single SMs), up to
-                              * 4 (48 KB stages on SM pairs) */
+                              * 4 (48 KB stages on SM pairs, 32 KB in the stacked SM-pair form) */
 #define ED_TUNE_TC_PAIR 5    /* factorised GEMM form: 0 (built-in default), 1 = one CTA per SM with
                               * 128 x 128 tiles, 2 = two-CTA clusters on SM pairs with 256 x 128
-                              * tiles (tcgen05.mma.cta_group::2) */
+                              * tiles (tcgen05.mma.cta_group::2, four real products per complex
+                              * one), 3 = two-CTA clusters with the stacked operands spread over
+                              * the pair: 128 x 128 tiles, CTA r holds plane r (re / im) of the
+                              * tile's A and B rows, one M = 256, N = 256 MMA per split product
+                              * and K step computes [Ar; Ai] [Br | Bi], and each CTA keeps two
+                              * 256-column TMEM buffers, so the MMAs of a k-block group never wait
+                              * for the drain of the previous one (ED_TUNE_TC_KPB default 2;
+                              * 2 to 4 operand stages of 32 KB, default 4) */
 #define ED_TUNE_TC_KPB 6     /* k-blocks the factorised GEMM accumulates in one TMEM buffer before the
                               * drain warps read it: 0 (the form's default: 2 for the stacked form,
                               * 1 otherwise), 1, 2 or 4.  The tensor core's FP32 accumulation

@@ -81,12 +81,14 @@ def test_elemental_split_modes_vs_fp64_full_size(fp64_full, mode):
 
 
 @pytest.mark.parametrize("tuning", [{"tc_kpb": 4}, {"tc_stack": 2}, {"tc_stack": 2, "tc_kpb": 2},
-                                    {"tc_pair": 2}, {"tc_pair": 2, "tc_kpb": 2}, {"gauss": True},
+                                    {"tc_pair": 2}, {"tc_pair": 2, "tc_kpb": 2}, {"tc_pair": 3},
+                                    {"tc_pair": 3, "tc_kpb": 4}, {"gauss": True},
                                     {"gauss": True, "tc_kpb": 1}])
 def test_f16x3_gemm_forms_vs_fp64_full_size(fp64_full, tuning):
     """The other forms of the factorised GEMM the autotuner may pick (stacked
     operands with 4 k-blocks per accumulator group; the four-product form
-    with 1 or 2; SM pairs) and the Gauss three-multiplication form at full
+    with 1 or 2; SM pairs in the four-product and the stacked form) and the
+    Gauss three-multiplication form at full
     size: within 1e-6 of FP64."""
     from easydistillation_gb300.insertion import mom_dict_to_list
     from easydistillation_gb300.ops import ElementalPlan

@@ -31,7 +31,7 @@ def test_tuning_settings_round_trip_and_validation():
     p.set_tuning(tc_slab_kb=0)
     assert p.tuning()["tc_slab_kb"] == 0
     for bad in ({"f64_tile": 4}, {"f64_tile": -1}, {"tc_slab_kb": 96}, {"tc_slab_kb": 512}, {"tc_grid": -2},
-                {"tc_stages": 1}, {"tc_stages": 5}, {"tc_pair": 3}, {"tc_pair": -1}, {"tc_kpb": 3},
+                {"tc_stages": 1}, {"tc_stages": 5}, {"tc_pair": 4}, {"tc_pair": -1}, {"tc_kpb": 3},
                 {"tc_kpb": 8}, {"tc_stack": 3}, {"tc_stack": -1}):
         with pytest.raises(ValueError):
             p.set_tuning(**bad)
