@@ -910,9 +910,11 @@ def run_grad(args, emit=True):
     return line
 
 
-# FP64 flops of one stout link update: four staples of two 3x3 complex products, C U^dag, the
-# anti-Hermitian traceless projection and exp(iQ) (Cayley-Hamilton), the final product: about 1.6e3
-STOUT_FLOP_PER_LINK = 1.6e3
+# FP64 flops of one stout link update (a complex multiply-add = 8 flops, a 3x3 complex product 216):
+# four staples of two products (1728) and their sum (72), rho C U^dag (234), the anti-Hermitian
+# traceless projection (~36), Q^2 (216), Re tr Q^3 (72), f0 + f1 Q + f2 Q^2 (132), exp(iQ) U (216):
+# about 2.7e3, not counting the scalar sqrt / acos / sincos of the Cayley-Hamilton coefficients
+STOUT_FLOP_PER_LINK = 2.7e3
 
 
 def run_secondary(args):
@@ -920,9 +922,12 @@ def run_secondary(args):
     hot path, each timed with CUDA events after a warm-up run:
 
     * stout smearing (``lattice/generator/stout_smear.cu:159-245``), 32^3 x 64
-      spatial links, rho = 0.1: links/s and the FP64 rate from an estimated
-      1.6 kflop per link; the oracle's numpy form on one timeslice as the CPU
-      baseline;
+      spatial links, rho = 0.1: links/s and the FP64 rate from the 2.7 kflop
+      per link counted above, beside the reference's own CUDA kernel
+      (compiled unmodified into ``oracle/_ref`` where the reference's sources
+      were present) on the same links and GPU, each with the reference's
+      driver loop around it (copy the field, one out-of-place step); the
+      oracle's numpy form on one timeslice as the CPU baseline;
     * DisplacementElementalGenerator.calc, 24^3, Ne = 100, distance 2, 7
       momenta, FP64 and f16x3: timeslices/s;
     * the two-point correlator of ``lattice/correlator/one_particle.py:12-77``
@@ -956,6 +961,27 @@ def run_secondary(args):
     stout = {"links_per_s": nlinks / sec, "seconds_per_step": sec,
              "fp64_tflops_est": nlinks * STOUT_FLOP_PER_LINK / sec / 1e12, "fp64_peak_tflops": FP64_PEAK_TFLOPS,
              "workload": "32^3 x 64 spatial links, one step, rho 0.1"}
+    from oracle import ref_kernels
+
+    if os.path.exists(ref_kernels.STOUT_CUBIN):
+        # the reference's kernel with its driver loop (lattice/generator/eigenvector.py:197-199):
+        # U_in = U.copy(); kernel(U, U_in, ...)
+        rk = ref_kernels.RefStout()
+        U_in = torch.empty_like(U)
+        stream = torch.cuda.current_stream().cuda_stream
+
+        def ref_step():
+            U_in.copy_(U)
+            rk.step(U, U_in, 0.1, latt, stream)
+
+        rsec = timed(ref_step, 5)
+        stout["reference_cuda_kernel"] = {
+            "links_per_s": nlinks / rsec, "seconds_per_step": rsec, "speedup_of_library": rsec / sec,
+            "what": "lattice/generator/stout_smear.cu compiled unmodified for sm_103a, grid (V3, 3) x block (Lt), "
+                    "with the reference's copy of the field before each step"}
+        del U_in
+    else:
+        stout["reference_cuda_kernel"] = {"unavailable": "oracle/_ref/stout_smear_ref.cubin was not built"}
     if not args.no_cpu:
         from oracle import restatement as R
 

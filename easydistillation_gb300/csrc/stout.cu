@@ -138,8 +138,13 @@ __global__ void __launch_bounds__(128) stout_step_kernel(Latt L, int nt, double 
     Q.a[8] = Q.a[8] - t3;
   }
   const M3 Q2 = mul(Q, Q);
-  const M3 Q3 = mul(Q, Q2);
-  const double c0_signed = (Q3.a[0].re + Q3.a[4].re + Q3.a[8].re) / 3.0;
+  // c0 = Re tr(Q^3) / 3 needs only the diagonal of Q Q^2: sum_ik Re(Q_ik (Q^2)_ki)
+  double tr3 = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) tr3 += Q.a[i * 3 + k].re * Q2.a[k * 3 + i].re - Q.a[i * 3 + k].im * Q2.a[k * 3 + i].im;
+  const double c0_signed = tr3 / 3.0;
   const double c1 = (Q2.a[0].re + Q2.a[4].re + Q2.a[8].re) / 2.0;
   C f0, f1, f2;
   if (c1 <= 1e-300) {  // Q = 0: exp(iQ) = 1
@@ -149,16 +154,20 @@ __global__ void __launch_bounds__(128) stout_step_kernel(Latt L, int nt, double 
   } else {
     const bool parity = c0_signed < 0;
     const double c0 = fabs(c0_signed);
-    const double c0max = 2.0 * pow(c1 / 3.0, 1.5);
+    const double r = sqrt(c1 / 3.0);
+    const double c0max = 2.0 * (c1 / 3.0) * r;
     const double theta = acos(fmin(1.0, c0 / c0max));
-    const double u = sqrt(c1 / 3.0) * cos(theta / 3.0);
-    const double w = sqrt(c1) * sin(theta / 3.0);
+    double st, ct;
+    sincos(theta / 3.0, &st, &ct);
+    const double u = r * ct;
+    const double w = sqrt(c1) * st;
     const double u2 = u * u, w2 = w * w;
-    double su, cu, s2u, c2u;
+    double su, cu, sw, cw;
     sincos(u, &su, &cu);
-    sincos(2.0 * u, &s2u, &c2u);
-    const double cw = cos(w);
-    const double sinc = fabs(w) > 0.05 ? sin(w) / w : 1.0 - w2 / 6.0 * (1.0 - w2 / 20.0 * (1.0 - w2 / 42.0 * (1.0 - w2 / 72.0)));
+    sincos(w, &sw, &cw);
+    // e^{2iu} from e^{iu} (double-angle identities)
+    const double s2u = 2.0 * su * cu, c2u = (cu - su) * (cu + su);
+    const double sinc = fabs(w) > 0.05 ? sw / w : 1.0 - w2 / 6.0 * (1.0 - w2 / 20.0 * (1.0 - w2 / 42.0 * (1.0 - w2 / 72.0)));
     const double den = 1.0 / (9.0 * u2 - w2);
     // e^{-iu} = cu - i su; e^{2iu} = c2u + i s2u
     f0 = mk(((u2 - w2) * c2u + cu * 8.0 * u2 * cw + su * 2.0 * u * (3.0 * u2 + w2) * sinc) * den,
