@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         relink = any(os.path.getmtime(o) > lt for o in objs)
     if relink:
         tmp = LIB + ".tmp"
-        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcublas"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -9,9 +9,11 @@
 // (launch_laplacian), the three-term recurrence and one classical
 // Gram-Schmidt pass per step (two at the first step after a restart) by
 // ed_cgs_pass, the projected arrowhead + tridiagonal matrix diagonalised by
-// ed_arrow_eigh at each restart, the restart rotation Y^T V as one cuBLAS
-// DGEMM on the (re, im) pairs of the basis.  Everything is FP64 on the GPU;
-// the host reads one convergence counter per restart.  Convergence follows
+// ed_arrow_eigh at each restart, the restart rotation Y^T V by the library's
+// own batched kernel (lz_rotate_kernel: FP64, or double-float on the FP32 pipe
+// in the double-float Gram-Schmidt mode).  Everything is FP64 on the GPU
+// unless that mode is chosen; the host reads one convergence counter per
+// restart.  Convergence follows
 // ARPACK's rule: Ritz pair i is accepted when |beta_m y_{m,i}| <= tol |theta_i|.
 //
 // ed_lanczos_tr_ex adds a mixed-precision solve: phase 1 runs the same
@@ -30,15 +32,16 @@
 // smallest), which keeps L's eigenvectors and their order below the cut; the
 // eigenvalues returned are then the Rayleigh quotients x^H L x.
 
-#include <cublas_v2.h>
-
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <mutex>
 #include <vector>
 
+#include <type_traits>
+
 #include "common.cuh"
+#include "df.cuh"
 
 namespace ed {
 int split_rows(int B, int nrow, long long n, const void* src, long long sb, void* dst, long long db,
@@ -353,39 +356,112 @@ LzLayout lz_layout(int B, long long n, int ncv, int kk, int nev, int nblk, bool 
 // restarts instead of 16: longer cycles, fewer FP64 basis rotations).
 int lz_kept(int nev, int ncv) { return std::min(ncv - 1, nev + std::max(8, nev / 10)); }
 
-std::mutex g_blas_mu;
-cublasHandle_t blas_handle(int dev) {
-  static std::vector<cublasHandle_t> handles;
-  std::lock_guard<std::mutex> lk(g_blas_mu);
-  if ((int)handles.size() <= dev) handles.resize(dev + 1, nullptr);
-  if (!handles[dev]) {
-    if (cublasCreate(&handles[dev]) != CUBLAS_STATUS_SUCCESS) handles[dev] = nullptr;
+// The restart rotation and the Ritz vectors: C[b][j] = sum_r Y[b][r][j] V[b][r] for j < nkeep, r < m, with
+// Y real (the Ritz coefficients, row-major [m][ldy]) and V complex128 rows of n elements.  A block computes
+// 32 output rows (j) x 64 elements (x) from stages of 32 basis rows held in shared memory; each thread owns
+// 2 x 4 complex results.  FP64: bound by this part's FP64 pipe (~1.25 TFLOP/s; 4 flops per complex element
+// and Ritz coefficient).  DF (the double-float Gram-Schmidt mode): the basis rows in their split form
+// (df.cuh) and Y split on the fly, double-float sums on the FP32 pipe.
+constexpr int ROT_J = 32, ROT_X = 64, ROT_R = 32, ROT_THREADS = 256;
+
+template <bool DFM>
+__global__ void __launch_bounds__(ROT_THREADS) lz_rotate_kernel(int m, int nkeep, long long n,
+                                                                const double2* __restrict__ V, long long vb,
+                                                                const float4* __restrict__ Vs, long long vsb,
+                                                                const double* __restrict__ Y, int ldy, long long yb,
+                                                                double2* __restrict__ C, long long cb) {
+  using VT = typename std::conditional<DFM, float4, double2>::type;  // a basis element as staged
+  using YT = typename std::conditional<DFM, float2, double>::type;   // a Ritz coefficient as staged
+  __shared__ YT Ys[ROT_R][ROT_J];
+  __shared__ VT Vt[ROT_R][ROT_X];
+  const int b = blockIdx.z;
+  const long long x0 = (long long)blockIdx.x * ROT_X;
+  const int j0 = blockIdx.y * ROT_J;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const double* Yb = Y + (long long)b * yb;
+  double2 acc[2][4];
+  DF are[2][4], aim[2][4];
+#pragma unroll
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      acc[p][q] = make_double2(0.0, 0.0);
+      are[p][q] = DF{0.f, 0.f};
+      aim[p][q] = DF{0.f, 0.f};
+    }
+  for (int r0 = 0; r0 < m; r0 += ROT_R) {
+    // stage Y[r0 .. r0+31][j0 .. j0+31] and the basis rows r0 .. r0+31, elements x0 .. x0+63 (zeros outside)
+#pragma unroll
+    for (int u = 0; u < (ROT_R * ROT_J) / ROT_THREADS; ++u) {
+      const int lin = tid + u * ROT_THREADS, rr = lin / ROT_J, jj = lin % ROT_J;
+      const int r = r0 + rr, j = j0 + jj;
+      const double y = (r < m && j < nkeep) ? Yb[(long long)r * ldy + j] : 0.0;
+      if constexpr (DFM) {
+        const float yh = __double2float_rn(y);
+        Ys[rr][jj] = make_float2(yh, __double2float_rn(y - (double)yh));
+      } else {
+        Ys[rr][jj] = y;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < (ROT_R * ROT_X) / ROT_THREADS; ++u) {
+      const int lin = tid + u * ROT_THREADS, rr = lin / ROT_X, xx = lin % ROT_X;
+      const int r = r0 + rr;
+      const long long x = x0 + xx;
+      if constexpr (DFM) {
+        Vt[rr][xx] = (r < m && x < n) ? Vs[(long long)b * vsb + (long long)r * n + x] : make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
+        Vt[rr][xx] = (r < m && x < n) ? V[(long long)b * vb + (long long)r * n + x] : make_double2(0.0, 0.0);
+      }
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < ROT_R; ++rr) {
+      YT y[2];
+      VT v[4];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) y[p] = Ys[rr][ty + 16 * p];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = Vt[rr][tx + 16 * q];
+#pragma unroll
+      for (int p = 0; p < 2; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if constexpr (DFM) {
+            df_acc(are[p][q], y[p].x, y[p].y, v[q].x, v[q].z);
+            df_acc(aim[p][q], y[p].x, y[p].y, v[q].y, v[q].w);
+          } else {
+            acc[p][q].x = fma(y[p], v[q].x, acc[p][q].x);
+            acc[p][q].y = fma(y[p], v[q].y, acc[p][q].y);
+          }
+        }
+    }
+    __syncthreads();
   }
-  return handles[dev];
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const int j = j0 + ty + 16 * p;
+    if (j >= nkeep) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long x = x0 + tx + 16 * q;
+      if (x >= n) continue;
+      C[(long long)b * cb + (long long)j * n + x] =
+          DFM ? make_double2(df_value(are[p][q]), df_value(aim[p][q])) : acc[p][q];
+    }
+  }
 }
 
-// C[b] (2n x nkeep, column-major, ldc 2n) = Vr[b] (2n x m) * Y[b]^T-slice: the first nkeep columns of the
-// row-major [m][ldy] Ritz coefficients.  Vr[b] = the first m basis vectors as 2n doubles each.
-int lz_rotate(cudaStream_t st, int B, long long n, int m, int nkeep, const double* V, long long vb,
-              const double* Y, int ldy, long long yb, double* C, long long cb) {
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cublasHandle_t h = blas_handle(dev);
-  if (!h) {
-    set_error("ed_lanczos_tr: cuBLAS handle creation failed");
-    return ED_ERR_CUDA;
-  }
-  std::lock_guard<std::mutex> lk(g_blas_mu);
-  cublasSetStream(h, st);
-  const double one = 1.0, zero = 0.0;
-  const cublasStatus_t s =
-      cublasDgemmStridedBatched(h, CUBLAS_OP_N, CUBLAS_OP_T, (int)(2 * n), nkeep, m, &one, V, (int)(2 * n), 2 * vb, Y,
-                                ldy, yb, &zero, C, (int)(2 * n), 2 * cb, B);
-  if (s != CUBLAS_STATUS_SUCCESS) {
-    set_error("ed_lanczos_tr: cuBLAS DGEMM failed (status %d)", (int)s);
-    return ED_ERR_CUDA;
-  }
-  return ED_OK;
+// C[b] (nkeep rows of n complex128, batch stride cb) = the first nkeep Ritz combinations of the first m
+// basis rows; Vs (the split rows, batch stride vsb) selects the double-float kernel.
+int lz_rotate(cudaStream_t st, int B, long long n, int m, int nkeep, const double2* V, long long vb,
+              const float4* Vs, long long vsb, const double* Y, int ldy, long long yb, double2* C, long long cb) {
+  const dim3 grid((unsigned)((n + ROT_X - 1) / ROT_X), (unsigned)((nkeep + ROT_J - 1) / ROT_J), (unsigned)B);
+  if (Vs)
+    lz_rotate_kernel<true><<<grid, ROT_THREADS, 0, st>>>(m, nkeep, n, V, vb, Vs, vsb, Y, ldy, yb, C, cb);
+  else
+    lz_rotate_kernel<false><<<grid, ROT_THREADS, 0, st>>>(m, nkeep, n, V, vb, Vs, vsb, Y, ldy, yb, C, cb);
+  return lz_chk(cudaGetLastError(), "Lanczos restart rotation");
 }
 
 }  // namespace
@@ -627,8 +703,7 @@ int lanczos_solve(const LzArgs& a) {
     }
     if (restarts == max_restarts) break;
     // thick restart: V[:, :kk] = Y[:, :kk]^T V[:, :ncv], V[:, kk] = V[:, ncv]
-    LZ_TRY(lz_rotate(st, B, n, ncv, kk, (const double*)V, vb, Y, kk, (long long)ncv * kk, (double*)rot,
-                     (long long)kk * n));
+    LZ_TRY(lz_rotate(st, B, n, ncv, kk, V, vb, Vs, vsb, Y, kk, (long long)ncv * kk, rot, (long long)kk * n));
     LZ_TRY(lz_chk(cudaMemcpy2DAsync(V, vb * 16, rot, (size_t)kk * n * 16, (size_t)kk * n * 16, B,
                                          cudaMemcpyDeviceToDevice, st),
                        "Lanczos restart copy"));
@@ -642,8 +717,7 @@ int lanczos_solve(const LzArgs& a) {
   }
   if (restarts > max_restarts) restarts = max_restarts;
   // Ritz vectors X = Y[:, :Ne]^T V and values
-  LZ_TRY(lz_rotate(st, B, n, ncv, Ne, (const double*)V, vb, Y, kk, (long long)ncv * kk, (double*)evecs,
-                   (long long)Ne * n));
+  LZ_TRY(lz_rotate(st, B, n, ncv, Ne, V, vb, Vs, vsb, Y, kk, (long long)ncv * kk, (double2*)evecs, (long long)Ne * n));
   if (poly_deg == 0) {
     LZ_TRY(lz_chk(cudaMemcpy2DAsync(evals, (size_t)Ne * 8, theta, (size_t)kk * 8, (size_t)Ne * 8, B,
                                          cudaMemcpyDeviceToDevice, st),

@@ -18,6 +18,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "df.cuh"
 
 namespace ed {
 namespace {
@@ -138,35 +139,10 @@ __global__ void __launch_bounds__(GS_THREADS) cgs_update_kernel(int r, long long
 }
 
 // ---------------------------------------------------------------- double-float pass on the FP32 pipe
-// The same pass with every complex128 value of V and w carried as two complex64 parts, x = hi + lo
-// (hi = x rounded to FP32, lo = the rest rounded to FP32: 48 significand bits), the basis rows stored
-// once in that form (Vs: float4 {re_hi, im_hi, re_lo, im_lo} per element, written when a row is made),
-// and the sums kept as (hi, lo) FP32 pairs: each real product a*b is ah*bh split exactly into p + e by
-// one FMA, plus the cross terms ah*bl + al*bh; p goes into the pair by Knuth's two-sum, e and the cross
-// terms into its low part.  Relative error of a product ~2^-47 instead of 2^-53; every operation runs on
-// the FP32 pipe, so a pass streams its 16 bytes per element at HBM speed instead of the FP64 pipe's
-// ~2.5 TB/s.
-
-struct DF {
-  float hi, lo;
-};
-__device__ __forceinline__ void df_acc(DF& s, float ah, float al, float bh, float bl) {
-  const float p = ah * bh;
-  const float e = fmaf(ah, bh, -p);
-  const float c = fmaf(ah, bl, fmaf(al, bh, e));
-  const float t = s.hi + p;
-  const float bb = t - s.hi;
-  const float err = (s.hi - (t - bb)) + (p - bb);
-  s.hi = t;
-  s.lo += err + c;
-}
-// s -= a*b
-__device__ __forceinline__ void df_sub(DF& s, float ah, float al, float bh, float bl) { df_acc(s, -ah, -al, bh, bl); }
-
-__device__ __forceinline__ float4 split_c128(double2 v) {
-  const float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
-  return make_float4(rh, ih, __double2float_rn(v.x - (double)rh), __double2float_rn(v.y - (double)ih));
-}
+// The same pass with every complex128 value of V and w carried in the split form of df.cuh, the basis
+// rows stored once in that form (Vs, written when a row is made) and the sums kept as (hi, lo) FP32 pairs:
+// every operation runs on the FP32 pipe, so a pass streams its 16 bytes per element at HBM speed instead
+// of the FP64 pipe's ~2.5 TB/s.
 
 // dst rows (stride db elements per problem) <- split of src rows (stride sb); nrow rows of n elements
 __global__ void split_rows_kernel(long long n, int nrow, const double2* __restrict__ src, long long sb,
