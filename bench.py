@@ -1032,6 +1032,17 @@ def run_secondary(args):
     sec = timed(lambda: twopoint_assembled(ops, peram, range(Lt), Lt), 2)
     out["twopoint"] = {"correlators_per_s": 1.0 / sec, "seconds": sec,
                        "workload": "48 timeslices, Ne=100, gamma_5, all 48 sources"}
+    # the eigenvector-resolved profile of one source at every sink time (ed_twopoint_profile) and its diagonal
+    from easydistillation_gb300.correlator import _source_terms
+
+    tau0 = peram[0].contiguous()
+    psec = timed(lambda: _source_terms(tau0, tau0, ops, 0, list(range(Lt)), "profile"), 3)
+    dsec = timed(lambda: _source_terms(tau0, tau0, ops, 0, list(range(Lt)), "diagonal"), 3)
+    # gamma_5: 16 left blocks and 4 right blocks of 4 Ne^3 complex multiply-adds per sink time
+    pflop = Lt * (16 + 16) * Ne ** 3 * 8.0
+    out["twopoint_profile"] = {"seconds_per_source": psec, "fp64_tflops": pflop / psec / 1e12,
+                               "diagonal_seconds_per_source": dsec,
+                               "workload": "one source, 48 sink times, Ne=100, gamma_5, [48, Ne, Ne] out"}
     # ILDG gauge file -> device links
     out["gauge_load"] = bench_gauge_load(dev, timed)
     print(json.dumps({"metric": "secondary components", **out}), flush=True)

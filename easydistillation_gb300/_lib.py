@@ -77,6 +77,8 @@ _SIGNATURES = {
     "ed_elemental_run_batch_end": ([_vp, _i, _vp, _c.POINTER(_vp), _vp, _c.c_size_t, _vp], _i),
     "ed_link_grad": ([_i, _i, _i, _i, _i, _c.c_double, _c.c_double, _vp, _vp, _vp, _vp], _i),
     "ed_twopoint_trace": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
+    "ed_twopoint_profile": ([_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
+    "ed_twopoint_profile_diag": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
     "ed_chain_adjoint": ([_i, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _i),
     "ed_parallel_transport": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
     "ed_mean_c128": ([_i, _ll, _ll, _vp, _vp, _vp], _i),
@@ -90,6 +92,8 @@ _SIGNATURES = {
     "ed_laplacian_status": ([_c.POINTER(_i), _vp], _i),
     "ed_laplacian_wait_limit": ([_c.c_longlong], _i),
     "ed_laplacian_wait_probe": ([_c.c_int], _i),
+    "ed_elemental_wait_limit": ([_c.c_longlong], _i),
+    "ed_elemental_wait_probe": ([_c.c_int], _i),
     "ed_elemental_factorised": ([_vp, _c.POINTER(_i), _c.POINTER(_i), _c.POINTER(_i)], _i),
     "ed_elemental_set_tuning": ([_vp, _i, _i], _i),
     "ed_arrow_eigh_workspace": ([_i, _i, _i, _c.POINTER(_c.c_size_t)], _i),

@@ -28,12 +28,13 @@ and the source gamma ``G = g4 Gamma^dag g4`` (``:66``),
 
     C(t) = sum_{x,y} Tr[ tau_bw(t) (Gamma_x (x) phi_x(t)) tau(t) (G_y (x) psi_y) ]
 
-is evaluated as one batched product of the 16 spin blocks of ``tau_bw(t)``
-with ``phi_x(t)`` and one of ``tau(t)`` with ``psi_y^T``, after which the
-gammas only permute and scale spin blocks, and a trace over the surviving
-block pairs: 32 Ne x Ne x Ne products per (t, part pair) instead of the
-dense (4 Ne)^3 ones.  Per source timeslice all sink times t and all parts of
-an operator go into one batched GEMM launch.
+is a sum of terms coef Tr[A phi_x(t) B psi_y^T] with A, B single Ne x Ne spin
+blocks of tau_bw(t) and tau(t) (one per part pair and spin pair, j and l fixed
+by the gammas): ``twopoint`` evaluates them in the library's
+``ed_twopoint_trace`` (both products per 32 x 32 tile in shared memory, never
+written to HBM); ``twopoint_profile`` in ``ed_twopoint_profile`` (the 16 left
+blocks L[i][k] = sum_x c A phi_x, then sum_k L[i][k] B weighted by psi_y, the
+output tile kept in registers) or ``ed_twopoint_profile_diag``.  All FP64.
 """
 
 from __future__ import annotations
@@ -179,49 +180,14 @@ def _gamma_index(g: torch.Tensor) -> int:
     raise ValueError("not a gamma matrix of the insertion table")
 
 
-def _backward(tau: torch.Tensor) -> torch.Tensor:
-    """``tau_bw[t, i, j, a, b] = g5_ii conj(tau[t, j, i, b, a]) g5_jj``
-    (``one_particle.py:59-63``; g5 is diagonal)."""
-    d = torch.diagonal(gamma(15, tau.device)).real
-    s = (d[:, None] * d[None, :]).to(tau.dtype)  # [i, j]
-    return s[None, :, :, None, None] * tau.conj().permute(0, 2, 1, 4, 3)
-
-
-def _left_blocks(tau_bw: torch.Tensor, phi: torch.Tensor, gidx: int) -> torch.Tensor:
-    """``tau_bw(t) (Gamma (x) phi(t))`` as spin blocks ``[t, i, k, a, c]``:
-    block (i, k) = Gamma[j, k] tau_bw[t, i, j] phi(t) with j the row whose
-    non-zero sits in column k."""
-    cols, vals = _monomial(gidx, False)
-    prod = torch.matmul(tau_bw, phi[:, None, None])  # [t, i, j, a, c]
-    out = torch.empty_like(prod)
-    for j in range(4):
-        out[:, :, cols[j]] = vals[j] * prod[:, :, j]
-    return out
-
-
-def _right_blocks(tau: torch.Tensor, psi: torch.Tensor, gidx: int) -> torch.Tensor:
-    """``tau(t) (G (x) psi^T)`` with G = g4 Gamma^dag g4 (the source gamma) as spin
-    blocks ``[t, k, i, c, a]``: block (k, i) = G[l, i] tau[t, k, l] psi^T,
-    psi = conj(phi(t_src))."""
-    cols, vals = _monomial(gidx, True)
-    prod = torch.matmul(tau, psi.transpose(-1, -2)[None, None, None])  # [t, k, l, c, a]
-    out = torch.empty_like(prod)
-    for l in range(4):
-        out[:, :, cols[l]] = vals[l] * prod[:, :, l]
-    return out
-
-
 _G5 = (1.0, 1.0, -1.0, -1.0)  # the diagonal of gamma(15) in the reference's basis
 
 
-def _trace_terms(tau, taub, el, gid, t_src):
-    """``out[t]`` of one operator (parts with gamma indices ``gid``) through
-    ``ed_twopoint_trace``: one term per (sink part x, source part y, spin i,
-    spin k) with j the row of gamma_x holding column k, l the row of the source
-    gamma holding column i, coef = gamma_x[j][k] G_y[l][i] g5[i] g5[j]."""
-    from . import _lib
-
-    T, Ne, Lt = tau.shape[0], tau.shape[-1], el.shape[1]
+def _term_table(gid):
+    """The terms of one operator (parts with gamma indices ``gid``): one per
+    (sink part x, source part y, spin i, spin k) with j the row of gamma_x
+    holding column k, l the row of the source gamma holding column i, coef =
+    gamma_x[j][k] G_y[l][i] g5[i] g5[j]."""
     idx, coef = [], []
     for x, gx in enumerate(gid):
         cx, vx = _monomial(gx, False)
@@ -234,6 +200,15 @@ def _trace_terms(tau, taub, el, gid, t_src):
                     c = vx[j] * vy[l] * _G5[i] * _G5[j]
                     idx.append((x, y, i, j, k, l))
                     coef.append((c.real, c.imag))
+    return idx, coef
+
+
+def _trace_terms(tau, taub, el, gid, t_src):
+    """``out[t]`` of one operator through ``ed_twopoint_trace``."""
+    from . import _lib
+
+    T, Ne, Lt = tau.shape[0], tau.shape[-1], el.shape[1]
+    idx, coef = _term_table(gid)
     dev = tau.device
     idx_t = torch.tensor(idx, dtype=torch.int32, device=dev)
     coef_t = torch.tensor(coef, dtype=torch.float64, device=dev)
@@ -244,6 +219,52 @@ def _trace_terms(tau, taub, el, gid, t_src):
     return out
 
 
+def _profile_terms(tau, taub, el, gid, t_src, sink_t, diagonal):
+    """``out[t, a, d]`` (or ``out[t, a]`` with ``diagonal``) of one operator
+    through ``ed_twopoint_profile`` / ``ed_twopoint_profile_diag``; the
+    coefficient of a term factorises into gamma_x[j][k] g5[j] (sink part x,
+    spin k) times G_y[l][i] g5[i] (source part y, spin i)."""
+    from . import _lib
+
+    T, Ne, Lt, X = tau.shape[0], tau.shape[-1], el.shape[1], len(gid)
+    dev = tau.device
+    tau, taub, el = tau.contiguous(), taub.contiguous(), el.contiguous()
+    st = torch.tensor(sink_t, dtype=torch.int32, device=dev)
+    if diagonal:
+        idx, coef = _term_table(gid)
+        idx_t = torch.tensor(idx, dtype=torch.int32, device=dev)
+        coef_t = torch.tensor(coef, dtype=torch.float64, device=dev)
+        out = torch.empty((T, Ne), dtype=torch.complex128, device=dev)
+        _lib.call("ed_twopoint_profile_diag", T, Ne, Lt, int(t_src), X, len(idx), _lib.ptr(st), _lib.ptr(idx_t),
+                  _lib.ptr(coef_t), _lib.ptr(tau), _lib.ptr(taub), _lib.ptr(el), _lib.ptr(out), _lib.stream_handle())
+        return out
+    ltab, lcoef, rtab, rcoef = [], [], [], []
+    for k in range(4):
+        for x in range(X):
+            cx, vx = _monomial(gid[x], False)
+            j = cx.index(k)
+            c = vx[j] * _G5[j]
+            ltab.append(j)
+            lcoef.append((c.real, c.imag))
+    for i in range(4):
+        for y in range(X):
+            cy, vy = _monomial(gid[y], True)
+            l = cy.index(i)
+            c = vy[l] * _G5[i]
+            rtab.append(l)
+            rcoef.append((c.real, c.imag))
+    lt = torch.tensor(ltab, dtype=torch.int32, device=dev)
+    lc = torch.tensor(lcoef, dtype=torch.float64, device=dev)
+    rt = torch.tensor(rtab, dtype=torch.int32, device=dev)
+    rc = torch.tensor(rcoef, dtype=torch.float64, device=dev)
+    work = torch.empty((T, 16, Ne, Ne), dtype=torch.complex128, device=dev)
+    out = torch.empty((T, Ne, Ne), dtype=torch.complex128, device=dev)
+    _lib.call("ed_twopoint_profile", T, Ne, Lt, int(t_src), X, _lib.ptr(st), _lib.ptr(lt), _lib.ptr(lc), _lib.ptr(rt),
+              _lib.ptr(rc), _lib.ptr(tau), _lib.ptr(taub), _lib.ptr(el), _lib.ptr(work), _lib.ptr(out),
+              _lib.stream_handle())
+    return out
+
+
 def _source_terms(tau, taub, phis, t_src, dts=None, mode="trace"):
     """All operators for one source timeslice.  ``tau``: the source's
     perambulator ``[T, 4, 4, Ne, Ne]`` at the sink times, ``taub`` the one of
@@ -251,42 +272,15 @@ def _source_terms(tau, taub, phis, t_src, dts=None, mode="trace"):
     per operator ``(gammas, elementals)`` with elementals ``[X, Lt, Ne, Ne]``.
     mode "trace" (the library's ``ed_twopoint_trace``): ``[Nop, T]``;
     "profile": ``[Nop, T, Ne, Ne]`` (indices a, d); "diagonal": ``[Nop, T, Ne]``."""
-    tau_bw = _backward(taub) if mode != "trace" else None
     out = []
+    Lt = phis[0][1].shape[1]
+    sink_t = [(t_src + int(dt)) % Lt for dt in (dts if dts is not None else range(tau.shape[0]))]
     for gammas, el in phis:
         gid = [_gamma_index(g) for g in gammas]
-        sink = torch.roll(el, -t_src, 1)
-        if dts is not None:
-            sink = sink[:, dts]
-        psi = el[:, t_src].conj()
         if mode == "trace":
             out.append(_trace_terms(tau, taub, el.contiguous(), gid, t_src))
-        elif mode == "profile":
-            # C[t, a, d] = psi[a, d] sum_{i,l} G[l, i] (left . tau)[t][(i, a), (l, d)]
-            acc = 0
-            for x in range(len(gid)):
-                L = _left_blocks(tau_bw, sink[x], gid[x])  # [t, i, k, a, c]
-                Q = torch.einsum("tikac,tklcd->tilad", L, tau)
-                for y in range(len(gid)):
-                    cols, vals = _monomial(gid[y], True)
-                    for l in range(4):
-                        acc = acc + vals[l] * Q[:, cols[l], l] * el[y, t_src].conj()[None]
-            out.append(acc)
-        else:  # diagonal: C[t, a] = psi[a, a] sum tau_bw[i,j,a,b] Gamma[j,k] phi[b,b] tau[k,l,b,a] G[l,i]
-            acc = 0
-            for x in range(len(gid)):
-                cj, vj = _monomial(gid[x], False)
-                dphi = torch.diagonal(sink[x], dim1=-2, dim2=-1)  # [t, b]
-                for y in range(len(gid)):
-                    cl, vl = _monomial(gid[y], True)
-                    dpsi = torch.diagonal(el[y, t_src].conj())  # [a]
-                    for l in range(4):
-                        i = cl[l]
-                        for j in range(4):
-                            k = cj[j]
-                            term = (tau_bw[:, i, j] * tau[:, k, l].transpose(-1, -2)) @ dphi[..., None]
-                            acc = acc + vj[j] * vl[l] * term[..., 0] * dpsi[None]
-            out.append(acc)
+        else:
+            out.append(_profile_terms(tau, taub, el, gid, t_src, sink_t, mode == "diagonal"))
     return torch.stack(out)
 
 
