@@ -51,8 +51,17 @@ struct TcScalars {
   unsigned int absmax_bits;  // max |re|,|im| over all chains (float bits)
   int scale_exp;             // e: operands are multiplied by 2^e before splitting
   int status;                // 0 = ok, else TC_ERR_*
-  int pad[61];
+  unsigned int progress;     // steps started (the lock step of the persistent factorised GEMMs)
+  long long wait_limit;      // cycles a bounded wait of the single-SM factorised GEMM may take (0: TC_WAIT_CYCLES)
+  int probe;                 // nonzero: that GEMM's TMA role issues no copy (the failure-detection test hook)
+  int pad[57];
 };
+static_assert(sizeof(TcScalars) == 256, "device scalars");
+
+// Process-wide settings of the single-SM factorised GEMM's bounded waits (ed_elemental_wait_limit /
+// ed_elemental_wait_probe), written into the device scalars of every run by tc_scale_kernel.
+long long g_tc_wait_cycles = 0;
+int g_tc_wait_probe = 0;
 
 // ------------------------------------------------------------ PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -78,17 +87,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false if the barrier did not flip within TC_WAIT_CYCLES, or,
-// when abort_on_error, as soon as another role has reported an error.
+// Bounded wait: false if the barrier did not flip within `limit` cycles
+// (TC_WAIT_CYCLES unless the kernel passes its run's setting), or, when
+// abort_on_error, as soon as another role has reported an error.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* status, int code,
-                                          bool abort_on_error = true) {
+                                          bool abort_on_error = true, long long limit = TC_WAIT_CYCLES) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 0) {
       if (abort_on_error && *status != 0) return false;
-      if (clock64() - t0 > TC_WAIT_CYCLES) {
+      if (clock64() - t0 > limit) {
         atomicCAS((int*)status, 0, code);
         return false;
       }
@@ -98,9 +108,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
 
 // Warp-uniform bounded wait: lane 0 polls, the outcome is broadcast.
 __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, volatile int* status, int code,
-                                          bool abort_on_error = true) {
+                                          bool abort_on_error = true, long long limit = TC_WAIT_CYCLES) {
   int ok = 0;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, status, code, abort_on_error) ? 1 : 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, status, code, abort_on_error, limit) ? 1 : 0;
   return __shfl_sync(0xffffffffu, ok, 0) != 0;
 }
 
@@ -231,8 +241,10 @@ __global__ void tc_absmax_kernel(const float* __restrict__ x, long long n, TcSca
 
 // e = floor(log2(2^13 / absmax)): split operands of magnitude <= 2^13 (and
 // phase-rotated ones <= 2^13.5) stay well inside the fp16 range.
-__global__ void tc_scale_kernel(TcScalars* sc, int kind) {
+__global__ void tc_scale_kernel(TcScalars* sc, int kind, long long wait_limit, int probe) {
   if (threadIdx.x == 0) {
+    sc->wait_limit = wait_limit;
+    sc->probe = probe;
     int e = 0;
     const float m = __uint_as_float(sc->absmax_bits);
     if (kind == TC_F16 && m > 0.f && isfinite(m)) {
@@ -646,7 +658,7 @@ static int tc_onchip_prepare(const ed_elemental_plan* P, const cplx<float>* chai
   if (e != cudaSuccess) return cuda_status(e, "tc scalars reset");
   const int sms = num_sms();
   tc_absmax_kernel<<<4 * sms, 256, 0, stream>>>((const float*)chains, 2 * R_used * K, sc);
-  tc_scale_kernel<<<1, 32, 0, stream>>>(sc, KIND);
+  tc_scale_kernel<<<1, 32, 0, stream>>>(sc, KIND, g_tc_wait_cycles, g_tc_wait_probe);
   tc_split_kernel<KIND><<<8 * sms, 256, 0, stream>>>(chains, R_used, R, K, sc, planes);
   tc_phase_kernel<<<2 * sms, 256, 0, stream>>>(phases, (long long)P->nmom * P->V3, sc, ph32);
   ED_RETURN_LAUNCH("tensor-core operand preparation");
@@ -964,7 +976,7 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   const int sms = num_sms();
   const long long R_used = (long long)P->nchain * nb * Ne;
   tc_absmax_kernel<<<4 * sms, 256, 0, stream>>>((const float*)chains, 2 * R_used * K, sc);
-  tc_scale_kernel<<<1, 32, 0, stream>>>(sc, KIND);
+  tc_scale_kernel<<<1, 32, 0, stream>>>(sc, KIND, g_tc_wait_cycles, g_tc_wait_probe);
   ED_RETURN_LAUNCH("tensor-core operand scale");
   std::vector<int> m3;
   for (int a = 0; a < pxy; ++a) m3.insert(m3.end(), {P->fac_xy[2 * a], P->fac_xy[2 * a + 1], 0});
@@ -1355,3 +1367,14 @@ int tc_read_status(const ed_elemental_plan* P, const void* workspace, int* statu
 }
 
 }  // namespace ed
+
+extern "C" int ed_elemental_wait_limit(long long cycles) {
+  ED_CHECK_ARG(cycles >= 0, "ed_elemental_wait_limit: negative limit");
+  ed::g_tc_wait_cycles = cycles;
+  return ED_OK;
+}
+
+extern "C" int ed_elemental_wait_probe(int on) {
+  ed::g_tc_wait_probe = on ? 1 : 0;
+  return ED_OK;
+}

@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
   volatile int* status = &sc->status;
-  unsigned int* progress = reinterpret_cast<unsigned int*>(&sc->pad[0]);
+  unsigned int* progress = &sc->progress;
 
   const int G = gridDim.x, cta = blockIdx.x;
   const int pair = cta >> 1, npairs = G >> 1;
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
   volatile int* status = &sc->status;
-  unsigned int* progress = reinterpret_cast<unsigned int*>(&sc->pad[0]);
+  unsigned int* progress = &sc->progress;
 
   const int G = gridDim.x, cta = blockIdx.x;
   const int pair = cta >> 1, npairs = G >> 1;

@@ -185,7 +185,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int* status = &sc->status;
-  unsigned int* progress = reinterpret_cast<unsigned int*>(&sc->pad[0]);  // zeroed with the scalars
+  unsigned int* progress = &sc->progress;  // zeroed with the scalars
+  // the limit of every bounded wait of this run, and the test hook that makes the TMA role issue nothing (so the
+  // first stage wait runs out whatever the copy latency): both set per run by tc_scale_kernel
+  const long long wl = sc->wait_limit > 0 ? sc->wait_limit : TC_WAIT_CYCLES;
+  const bool probe = sc->probe != 0;
 
   const int G = gridDim.x, cta = blockIdx.x;
   const int J = (ntiles + G - 1) / G;  // tiles per CTA (steps per slab)
@@ -247,7 +251,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(FORM != TCF_FOUR ? TCF_STACK_REGS_LOW : TCF_REGS_LOW));
     if (warp == 0) {
       // ===================== TMA of the A and B planes, step by step
-      if (lane == 0) {
+      if (lane == 0 && !probe) {
         long long g = 0, issued_last = -1;
         bool ok = true;
         for (int q = 0; q < nsteps && ok; ++q) {
@@ -256,7 +260,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const unsigned int need = (unsigned int)q * (unsigned int)G;
             const long long t0 = clock64();
             while (*(volatile unsigned int*)progress < need) {
-              if (*status != 0 || clock64() - t0 > TC_WAIT_CYCLES) {
+              if (*status != 0 || clock64() - t0 > wl) {
                 atomicCAS((int*)status, 0, TC_ERR_SYNC);
                 ok = false;
                 break;
@@ -275,7 +279,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           for (int kb = step_kb0(q); kb < kb1; ++kb, ++g) {
             const int s = (int)(g % nst);
             if (g >= nst &&
-                !mbar_wait(&empty[s], (uint32_t)(((g / nst) + 1) & 1), status, TC_ERR_EMPTY)) {
+                !mbar_wait(&empty[s], (uint32_t)(((g / nst) + 1) & 1), status, TC_ERR_EMPTY, true, wl)) {
               ok = false;
               break;
             }
@@ -299,7 +303,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         if (issued_last >= 0)  // do not leave while our copies may still land in shared memory
           mbar_wait(&full[issued_last % nst], (uint32_t)((issued_last / nst) & 1), status,
-                    TC_ERR_FULL, false);
+                    TC_ERR_FULL, false, wl);
       }
     } else if (warp == 1) {
       // ===================== MMA issuer (same product order as tc_pair_gemm_kernel)
@@ -322,7 +326,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               const int s = (int)(g % nst);
               const bool first = (kb - kb0s) % kpb == 0;
               const bool last = (kb - kb0s) % kpb == kpb - 1 || kb == kb1 - 1;
-              if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL)) {
+              if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL, true, wl)) {
                 ok = false;
                 break;
               }
@@ -331,7 +335,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
               for (int h = 0; h < 2; ++h) {  // acc1 = Ar [Br | Bi], then acc2 = Ai [Br | Bi]
                 if (first && gb >= 1 &&
-                    !mbar_wait(&acce[h], (uint32_t)((gb - 1) & 1), status, TC_ERR_ACCE)) {
+                    !mbar_wait(&acce[h], (uint32_t)((gb - 1) & 1), status, TC_ERR_ACCE, true, wl)) {
                   ok = false;
                   break;
                 }
@@ -362,7 +366,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               const int s = (int)(g % nst);
               const bool first = (kb - kb0s) % kpb == 0;
               const bool last = (kb - kb0s) % kpb == kpb - 1 || kb == kb1 - 1;
-              if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL)) {
+              if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL, true, wl)) {
                 ok = false;
                 break;
               }
@@ -371,7 +375,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
               for (int h = 0; h < 3; ++h) {  // X = Ar Br, Y = Ai Bi, Z = (Ar + Ai)(Br + Bi): planes 2h, 2h + 1
                 if (first && gb >= 1 &&
-                    !mbar_wait(&acce[h], (uint32_t)((gb - 1) & 1), status, TC_ERR_ACCE)) {
+                    !mbar_wait(&acce[h], (uint32_t)((gb - 1) & 1), status, TC_ERR_ACCE, true, wl)) {
                   ok = false;
                   break;
                 }
@@ -402,8 +406,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int b = (int)(gb & 1);
             const bool first = (kb - kb0s) % kpb == 0;  // the first k-block of a TMEM buffer
             const bool last = (kb - kb0s) % kpb == kpb - 1 || kb == kb1 - 1;
-            if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL) ||
-                (first && gb >= 2 && !mbar_wait(&acce[b], (uint32_t)(((gb >> 1) + 1) & 1), status, TC_ERR_ACCE))) {
+            if (!mbar_wait(&full[s], (uint32_t)((g / nst) & 1), status, TC_ERR_FULL, true, wl) ||
+                (first && gb >= 2 && !mbar_wait(&acce[b], (uint32_t)(((gb >> 1) + 1) & 1), status, TC_ERR_ACCE, true, wl))) {
               ok = false;
               break;
             }
@@ -475,7 +479,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one group of kpb k-blocks
 #pragma unroll
           for (int h = 0; h < 3; ++h) {  // X: re += x, im -= x; Y: re -= y, im -= y; Z: im += z
-            if (!warp_wait(&accf[h], (uint32_t)(g & 1), status, TC_ERR_ACC)) {
+            if (!warp_wait(&accf[h], (uint32_t)(g & 1), status, TC_ERR_ACC, true, wl)) {
               ok = false;
               break;
             }
@@ -524,7 +528,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one group of kpb k-blocks
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
-            if (!warp_wait(&accf[h], (uint32_t)(g & 1), status, TC_ERR_ACC)) {
+            if (!warp_wait(&accf[h], (uint32_t)(g & 1), status, TC_ERR_ACC, true, wl)) {
               ok = false;
               break;
             }
@@ -580,7 +584,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       for (int kb = step_kb0(q); kb < kb1; kb += kpb, ++g) {  // one TMEM buffer of kpb k-blocks
         const int b = (int)(g & 1);
-        if (!warp_wait(&accf[b], (uint32_t)((g >> 1) & 1), status, TC_ERR_ACC)) {
+        if (!warp_wait(&accf[b], (uint32_t)((g >> 1) & 1), status, TC_ERR_ACC, true, wl)) {
           ok = false;
           break;
         }
@@ -617,7 +621,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (!ok) {
       // wait (without aborting on the error flag) until every issued MMA is
       // done before the block releases TMEM
-      warp_wait(mma_done, 0, status, TC_ERR_ACC, false);
+      warp_wait(mma_done, 0, status, TC_ERR_ACC, false, wl);
     }
   }
   tc_fence_before();

@@ -189,6 +189,24 @@ int ed_laplacian_wait_limit(long long cycles);
  * their own copies.  No counterpart in the reference. */
 int ed_laplacian_wait_probe(int on);
 
+/* Cycle limit of every bounded wait of the single-SM factorised tensor-core
+ * GEMM (tc_fac_gemm_kernel, the default GEMM of the split modes for product
+ * momentum lists; process-wide, read at each run; 0 restores the default of
+ * 4e9 cycles, about 2 s).  A wait that runs out sets the plan's status word
+ * (ed_elemental_status: ED_ERR_TIMEOUT) and every role of the kernel stops:
+ * the MMA issuer after the MMAs it has issued, the copy issuer after waiting
+ * for its copies in flight, the drain warps after waiting for every issued
+ * MMA, before TMEM is released.  No counterpart in the reference. */
+int ed_elemental_wait_limit(long long cycles);
+
+/* Test of that failure path (process-wide, 0 = off): when on, the copy issuer
+ * of tc_fac_gemm_kernel issues no copy at all, so the first operand-stage
+ * wait of the MMA issuer (and the drain warps' first wait) runs out after the
+ * limit of ed_elemental_wait_limit, no MMA is issued, and the run reports
+ * ED_ERR_TIMEOUT.  Other GEMM kernels ignore it.  No counterpart in the
+ * reference. */
+int ed_elemental_wait_probe(int on);
+
 /* Status of the TMA-staged Laplacian's bounded waits since the last call
  * (synchronises `stream`): ED_OK, or ED_ERR_TIMEOUT when a wait gave up (the
  * output of that launch is invalid).  The status word is cleared. */
@@ -364,6 +382,31 @@ int ed_chain_adjoint(int Lx, int Ly, int Lz, int Ne, int nchain, int nmom, int R
 int ed_twopoint_trace(int T, int Ne, int Lt, int t_src, int nparts, int nterm, const int* term_idx,
                       const double* term_coef, const void* tau, const void* taub, const void* el, void* out,
                       void* stream);
+
+/* Eigenvector-resolved two-point function of one source timeslice and one
+ * operator: the contraction "tijab,xjk,xtbc,tklcd,yli,yad->tad" of
+ * twopoint_profile (lattice/correlator/one_particle.py:80-135, :122-130):
+ *   out[t][a][d] = sum_terms coef (conj(taub[t][j][i])^T E_x(sink_t[t]) tau[t][k][l])[a][d] conj(E_y(t_src))[a][d]
+ * over the terms of ed_twopoint_trace, given in factorised form: for the
+ * sink part x and spin k, ltab[k][x] = j and lcoef[k][x] = gamma_x[j][k]
+ * g5[j][j] (device int[4][nparts], double[4][nparts][2]); for the source part
+ * y and spin i, rtab[i][y] = l and rcoef[i][y] = G_y[l][i] g5[i][i].
+ * sink_t: device int[T], the elemental timeslice of each sink time; tau, taub:
+ * [T][4][4][Ne][Ne] at those sink times; el as for ed_twopoint_trace; work:
+ * device scratch of T*16*Ne*Ne complex128; out: device [T][Ne][Ne]
+ * complex128, overwritten.  FP64, written once per element (no atomics). */
+int ed_twopoint_profile(int T, int Ne, int Lt, int t_src, int nparts, const int* sink_t, const int* ltab,
+                        const double* lcoef, const int* rtab, const double* rcoef, const void* tau, const void* taub,
+                        const void* el, void* work, void* out, void* stream);
+
+/* The diagonal form (is_diagonal: "tijab,xjk,xtbb,tklba,yli,yaa->ta",
+ * one_particle.py:113-121): out[t][a] = sum_terms coef conj(E_y(t_src))[a][a]
+ * sum_b conj(taub[t][j][i][b][a]) E_x(sink_t[t])[b][b] tau[t][k][l][b][a], the
+ * terms and arguments as for ed_twopoint_trace plus sink_t; out: device
+ * [T][Ne] complex128, overwritten.  FP64. */
+int ed_twopoint_profile_diag(int T, int Ne, int Lt, int t_src, int nparts, int nterm, const int* sink_t,
+                             const int* term_idx, const double* term_coef, const void* tau, const void* taub,
+                             const void* el, void* out, void* stream);
 
 /* ---- elementals (ElementalGenerator.calc, lattice/generator/elemental.py:290-338) */
 typedef struct ed_elemental_plan ed_elemental_plan;

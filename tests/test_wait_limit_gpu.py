@@ -51,3 +51,42 @@ def test_staged_laplacian_timeout_is_reported_and_recovers(variant):
         ref = R.laplacian(f.T.reshape(-1), U64[:, t], latt).reshape(V3, 3).T
         got = out[t, 0].cpu().numpy()
         assert np.abs(got - ref).max() < 2e-5 * np.abs(ref).max()
+
+
+def test_factorised_tensor_core_gemm_timeout_is_reported_and_recovers():
+    """The same for the single-SM factorised tcgen05 GEMM (f16x3, the 27
+    momenta with |p|^2 <= 3): a short wait limit and the probe (its copy
+    issuer issues nothing) make the first operand-stage wait run out before any
+    MMA is issued; the run must report ED_ERR_TIMEOUT, every role must leave
+    (the drain warps after the MMA issuer's final commit, TMEM released), and
+    the next run with the default settings must be clean and within 1e-6 of
+    the oracle."""
+    from easydistillation_gb300 import _lib
+    from easydistillation_gb300.ops import ElementalPlan
+
+    latt, Ne = [8, 4, 4, 1], 6
+    V3 = 8 * 4 * 4
+    moms = R.mom_dict_to_list(3)
+    gauge = R.synthetic_gauge(latt, 0.3, 79)
+    evec = R.random_colour_vectors(Ne, latt, 80)
+    U = torch.from_numpy(np.ascontiguousarray(gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3])).cuda()
+    V = torch.from_numpy(evec.reshape(Ne, -1)).cuda()
+    plan = ElementalPlan(latt, Ne, 2, moms, "f16x3", tuning={"tc_pair": 1})
+    assert plan.factorised is not None
+    out = torch.empty((13, 27, Ne, Ne), dtype=torch.complex128, device="cuda")
+    try:
+        _lib.check(_lib.lib().ed_elemental_wait_limit(20000), "ed_elemental_wait_limit")
+        _lib.check(_lib.lib().ed_elemental_wait_probe(1), "ed_elemental_wait_probe")
+        plan.run(U[:, 0], V3 * 9, 9, V, out)
+        with pytest.raises(_lib.EDError) as exc:
+            plan.check_status()
+        assert exc.value.code == _lib.ED_ERR_TIMEOUT and "gave up" in str(exc.value)
+    finally:
+        _lib.lib().ed_elemental_wait_probe(0)
+        _lib.lib().ed_elemental_wait_limit(0)
+    # every run clears its status word: the context is usable and the next run is correct
+    plan.run(U[:, 0], V3 * 9, 9, V, out)
+    assert plan.check_status() == 0
+    ref = R.elemental(evec, gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, 0], latt, 2, moms)
+    err = np.linalg.norm(out.cpu().numpy() - ref) / np.linalg.norm(ref)
+    assert err < 1e-6
