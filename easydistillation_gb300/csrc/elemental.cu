@@ -664,6 +664,9 @@ extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int val
     case ED_TUNE_TC_PAIR:
       ED_CHECK_ARG(value >= 0 && value <= 3, "ed_elemental_set_tuning: SM pairing %d (0, 1, 2 or 3)", value);
       plan->tc_pair = value;
+      // the stacked SM-pair form keeps a second double-float plane: the workspace size follows the setting
+      // (query it again; a run with a smaller workspace is refused with ED_ERR_WORKSPACE)
+      plan->ws_bytes = plan->off_extra + ed::tc_extra_workspace(plan) + ed::f64_extra_workspace(plan);
       return ED_OK;
     case ED_TUNE_TC_KPB:
       ED_CHECK_ARG(value == 0 || value == 1 || value == 2 || value == 4,

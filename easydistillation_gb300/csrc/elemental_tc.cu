@@ -549,8 +549,8 @@ static FacLayout fac_layout(const ed_elemental_plan* P) {
   const size_t np = tcf_planes(P->gauss ? TCF_GAUSS : TCF_FOUR);  // re, im (and re + im) x hi, lo
   L.apl = L.bpl + up256(np * (size_t)L.rb * K * esz);
   L.df = L.apl + up256(np * (size_t)L.ra * K * esz);
-  // two planes: the SM-pair stacked GEMM (ED_TUNE_TC_PAIR = 3) gives each CTA of a pair its own
-  L.total = L.df + up256(2 * (size_t)P->g_elems * sizeof(float4));
+  // the SM-pair stacked GEMM (ED_TUNE_TC_PAIR = 3) gives each CTA of a pair a plane of its own
+  L.total = L.df + up256((P->tc_pair == 3 ? 2 : 1) * (size_t)P->g_elems * sizeof(float4));
   return L;
 }
 

@@ -451,6 +451,12 @@ class ElementalPlan:
             if name not in TUNING_KEYS:
                 raise ValueError(f"unknown tuning setting {name!r}; available: {sorted(TUNING_KEYS)}")
             call("ed_elemental_set_tuning", self._h, TUNING_KEYS[name], int(value))
+        # some settings change the workspace the plan needs (the stacked SM-pair GEMM's second result plane)
+        nbytes = ctypes.c_size_t()
+        call("ed_elemental_workspace_size", self._h, ctypes.byref(nbytes))
+        if nbytes.value != self.workspace_bytes:
+            self.workspace_bytes = nbytes.value
+            self._ws = None
 
     def tuning(self) -> dict:
         out = {}
