@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--eigen", action="store_true", help="measure the batched GPU eigensolve instead")
     ap.add_argument("--stencil", action="store_true",
                     help="measure only the Laplacian kernels (c64, c64 TMA-staged, c128) at --lattice")
+    ap.add_argument("--stout", action="store_true",
+                    help="measure only one stout smearing step at --lattice (default 32^3 x 64), the library's kernel "
+                         "beside the reference's own CUDA kernel")
     ap.add_argument("--secondary", action="store_true",
                     help="measure the components beside the hot path: stout smearing, displacement elementals, "
                          "two-point correlators, ILDG gauge-file loading")
@@ -917,6 +920,58 @@ def run_grad(args, emit=True):
 STOUT_FLOP_PER_LINK = 2.7e3
 
 
+def bench_stout(latt, dev, timed, no_cpu):
+    """One stout smearing step (rho = 0.1) of the spatial links of ``latt``: the
+    library's kernel, the reference's own CUDA kernel on the same links (when
+    ``oracle/_ref`` holds it), and the oracle's numpy form on one timeslice."""
+    import numpy as np
+    import torch
+
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.stout import stout_smear_
+
+    gauge, _ = make_inputs(latt, 1, distinct_t=4)
+    U = links_to_device(gauge, latt, dev)
+    Lx, Ly, Lz, Lt = latt
+    nlinks = 3 * Lx * Ly * Lz * Lt
+    sec = timed(lambda: stout_smear_(U, latt, 1, 0.1), 5)
+    stout = {"links_per_s": nlinks / sec, "seconds_per_step": sec,
+             "fp64_tflops_est": nlinks * STOUT_FLOP_PER_LINK / sec / 1e12, "fp64_peak_tflops": FP64_PEAK_TFLOPS,
+             "workload": f"{Lx}x{Ly}x{Lz} x {Lt} spatial links, one step, rho 0.1"}
+    from oracle import ref_kernels
+
+    if os.path.exists(ref_kernels.STOUT_CUBIN):
+        # the reference's kernel with its driver loop (lattice/generator/eigenvector.py:197-199):
+        # U_in = U.copy(); kernel(U, U_in, ...)
+        rk = ref_kernels.RefStout()
+        U_in = torch.empty_like(U)
+        stream = torch.cuda.current_stream().cuda_stream
+
+        def ref_step():
+            U_in.copy_(U)
+            rk.step(U, U_in, 0.1, latt, stream)
+
+        rsec = timed(ref_step, 5)
+        stout["reference_cuda_kernel"] = {
+            "links_per_s": nlinks / rsec, "seconds_per_step": rsec, "speedup_of_library": rsec / sec,
+            "what": "lattice/generator/stout_smear.cu compiled unmodified for sm_103a, grid (V3, 3) x block (Lt), "
+                    "with the reference's copy of the field before each step"}
+        del U_in
+    else:
+        stout["reference_cuda_kernel"] = {"unavailable": "oracle/_ref/stout_smear_ref.cubin was not built"}
+    if not no_cpu:
+        from oracle import restatement as R
+
+        U1 = np.ascontiguousarray(gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, :1])
+        t0 = time.perf_counter()
+        R.stout_smear(U1, 1, 0.1)
+        cdt = time.perf_counter() - t0
+        stout["cpu_baseline"] = {"links_per_s": 3 * Lx * Ly * Lz / cdt, "kind": "port", "cores": 1,
+                                 "sample": "oracle numpy stout step on one timeslice"}
+    del U
+    return stout
+
+
 def run_secondary(args):
     """Secondary measurement (``--secondary``) of the components beside the
     hot path, each timed with CUDA events after a warm-up run:
@@ -953,46 +1008,7 @@ def run_secondary(args):
     timed = event_seconds
     out = {}
     # stout smearing
-    latt = [32, 32, 32, 64]
-    gauge, _ = make_inputs(latt, 1, distinct_t=4)
-    U = links_to_device(gauge, latt, dev)
-    nlinks = 3 * 32 ** 3 * 64
-    sec = timed(lambda: stout_smear_(U, latt, 1, 0.1), 5)
-    stout = {"links_per_s": nlinks / sec, "seconds_per_step": sec,
-             "fp64_tflops_est": nlinks * STOUT_FLOP_PER_LINK / sec / 1e12, "fp64_peak_tflops": FP64_PEAK_TFLOPS,
-             "workload": "32^3 x 64 spatial links, one step, rho 0.1"}
-    from oracle import ref_kernels
-
-    if os.path.exists(ref_kernels.STOUT_CUBIN):
-        # the reference's kernel with its driver loop (lattice/generator/eigenvector.py:197-199):
-        # U_in = U.copy(); kernel(U, U_in, ...)
-        rk = ref_kernels.RefStout()
-        U_in = torch.empty_like(U)
-        stream = torch.cuda.current_stream().cuda_stream
-
-        def ref_step():
-            U_in.copy_(U)
-            rk.step(U, U_in, 0.1, latt, stream)
-
-        rsec = timed(ref_step, 5)
-        stout["reference_cuda_kernel"] = {
-            "links_per_s": nlinks / rsec, "seconds_per_step": rsec, "speedup_of_library": rsec / sec,
-            "what": "lattice/generator/stout_smear.cu compiled unmodified for sm_103a, grid (V3, 3) x block (Lt), "
-                    "with the reference's copy of the field before each step"}
-        del U_in
-    else:
-        stout["reference_cuda_kernel"] = {"unavailable": "oracle/_ref/stout_smear_ref.cubin was not built"}
-    if not args.no_cpu:
-        from oracle import restatement as R
-
-        U1 = np.ascontiguousarray(gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, :1])
-        t0 = time.perf_counter()
-        R.stout_smear(U1, 1, 0.1)
-        cdt = time.perf_counter() - t0
-        stout["cpu_baseline"] = {"links_per_s": 3 * 32 ** 3 / cdt, "kind": "port", "cores": 1,
-                                 "sample": "oracle numpy stout step on one 32^3 timeslice"}
-    out["stout"] = stout
-    del U
+    out["stout"] = bench_stout([32, 32, 32, 64], dev, timed, args.no_cpu)
     # displacement elementals
     latt = [24, 24, 24, 8]
     V3 = 24 ** 3
@@ -1220,6 +1236,14 @@ def main():
         return
     if args.secondary:
         run_secondary(args)
+        return
+    if args.stout:
+        import torch
+
+        latt = [int(v) for v in args.lattice.split(",")] if args.lattice else LATT
+        line = {"metric": "stout smearing links/s",
+                **bench_stout(latt, torch.device("cuda", 0), event_seconds, args.no_cpu)}
+        print(json.dumps(line), flush=True)
         return
     if args.gauge_load:
         run_gauge_load(args)
