@@ -341,7 +341,8 @@ def bench_stencil(U, latt, dev, reps=20):
     them from HBM."""
     import torch
 
-    from easydistillation_gb300.ops import laplacian, laplacian_config, laplacian_status, links_to_soa
+    from easydistillation_gb300.ops import (laplacian, laplacian_config, laplacian_df, laplacian_status, links_to_soa,
+                                            split_c128)
 
     Lx, Ly, Lz, Lt = latt
     V3 = Lx * Ly * Lz
@@ -351,22 +352,28 @@ def bench_stencil(U, latt, dev, reps=20):
     variants = (("c64", torch.complex64, 8, 2, "laplacian_strip_kernel (default: links and input staged by TMA)"),
                 ("c64_l1", torch.complex64, 8, 0, "laplacian_kernel<float,2> (neighbours through L1/L2)"),
                 ("c64_tma_planes", torch.complex64, 8, 1, "laplacian_tma_kernel (input planes staged by TMA)"),
-                ("c128", torch.complex128, 16, 0, "laplacian_kernel<double,1>"))
+                ("c128", torch.complex128, 16, 0, "laplacian_kernel<double,1>"),
+                ("c128_df", torch.complex128, 16, -1, "laplacian_df_kernel (double-float on the FP32 pipe)"))
     for name, dt, s, tma, kname in variants:
-        laplacian_config(tma)
+        laplacian_config(max(tma, 0))
         links = links_to_soa(U, latt, dtype=dt)
+        if tma < 0:  # the double-float kernel: links split once, complex128 vectors
+            links = split_c128(links)
+            lap = lambda L_, X_, latt_, out: laplacian_df(L_, X_, latt_, out=out)  # noqa: E731
+        else:
+            lap = laplacian
         F = torch.randn((Lt, 1, 3, V3), dtype=dt, device=dev)
         G = torch.empty_like(F)
         for _ in range(3):
-            laplacian(links, F, latt, out=G)
+            lap(links, F, latt, out=G)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         a.record()
         for r in range(reps):
             if r % 2 == 0:
-                laplacian(links, F, latt, out=G)
+                lap(links, F, latt, out=G)
             else:
-                laplacian(links, G, latt, out=F)
+                lap(links, G, latt, out=F)
         b.record()
         torch.cuda.synchronize()
         laplacian_status()
@@ -376,7 +383,7 @@ def bench_stencil(U, latt, dev, reps=20):
         out[name] = {"bound": "hbm", "achieved": gbs, "peak": pk, "unit": "GB/s", "frac": gbs / pk,
                      "peak_source": src, "traffic": None, "bytes_per_launch": nbytes, "kernel_ms": ms,
                      "kernel": kname, "workload": f"{Lx}^3 x {Lt} timeslices x 1 vector"}
-        if s == 16:
+        if s == 16 and tma >= 0:
             # FP64 arithmetic, not HBM, bounds the complex128 stencil on this part: 444 flops per site
             fl = 444.0 * V3 * Lt / ms / 1e9
             out[name].update({"bound": "fp64", "fp64_tflops": fl, "fp64_peak_tflops": FP64_PEAK_TFLOPS,

@@ -25,6 +25,7 @@ ED_ERR_TIMEOUT = -5
 
 ED_C128 = 0
 ED_C64 = 1
+ED_DF = 2  # ed_laplacian: double-float links (ed_split_c128), complex128 vectors
 ED_LANCZOS_GS_DF = 0x100  # flag OR-ed into the stencil precision of ed_lanczos_tr_ex
 ED_BIG_ENDIAN = 0x10
 
@@ -43,6 +44,7 @@ _SIGNATURES = {
     "ed_vectors_from_planes": ([_i, _i, _ll, _i, _vp, _vp, _vp], _i),
     "ed_momentum_phases": ([_i, _i, _i, _c.POINTER(_i), _i, _vp, _vp], _i),
     "ed_laplacian": ([_i, _i, _i, _i, _i, _i, _vp, _vp, _ll, _vp, _ll, _vp], _i),
+    "ed_split_c128": ([_ll, _vp, _vp, _vp], _i),
     "ed_stout_smear_step": ([_i, _i, _i, _i, _c.c_double, _vp, _vp, _vp], _i),
     "ed_project_su3": ([_ll, _vp, _c.c_double, _i, _vp], _i),
     "ed_covariant_derivative": ([_i, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),

@@ -302,7 +302,7 @@ __global__ void lz_sum_vectors_kernel(long long n, int nvec, const double2* __re
 
 // Workspace carve-up (all offsets 256-byte aligned).
 struct LzLayout {
-  size_t V, w, t0, t1, t2, lbuf, rot, hA, hB, part, npart, d, e, s, bl, theta, Y, arrow, nbad, rq, perm, Vs, ws,
+  size_t V, w, t0, t1, t2, lbuf, rot, hA, hB, part, npart, d, e, s, bl, theta, Y, arrow, nbad, rq, perm, Vs, ws, Ls,
       total;
   size_t arrow_bytes;
 };
@@ -342,10 +342,11 @@ LzLayout lz_layout(int B, long long n, int ncv, int kk, int nev, int nblk, bool 
   L.nbad = take(16);
   L.rq = take((size_t)B * nev * 8);
   L.perm = take((size_t)B * nev * 4);
-  L.Vs = L.ws = 0;
-  if (gs_df) {  // the basis and w in the split form of the double-float Gram-Schmidt pass
+  L.Vs = L.ws = L.Ls = 0;
+  if (gs_df) {  // the basis and w in the split form of the double-float Gram-Schmidt pass, and the split links
     L.Vs = take((size_t)B * (ncv + 1) * n * 16);
     L.ws = take(vec);
+    L.Ls = take((size_t)B * 9 * n * 16);  // [B][27][V3] float4 (n = 3 V3)
   }
   L.total = o;
   return L;
@@ -522,6 +523,8 @@ int lanczos_solve(const LzArgs& a) {
   const LzLayout Lw = lz_layout(B, n, ncv, kk, Ne, nblk, a.gs_df);
   float4* const Vs = a.gs_df ? (float4*)((uint8_t*)a.workspace + Lw.Vs) : nullptr;  // split basis rows
   float4* const wsp = a.gs_df ? (float4*)((uint8_t*)a.workspace + Lw.ws) : nullptr;  // split w
+  // the links in split form: the double-float mode applies its FP64-class stencil as ED_DF on the FP32 pipe
+  float4* const Ls = (a.gs_df && a.stencil_prec == ED_C128) ? (float4*)((uint8_t*)a.workspace + Lw.Ls) : nullptr;
   const long long vsb = (long long)(ncv + 1) * n;
   uint8_t* const W = (uint8_t*)a.workspace;
   // complex64 operand and result of the FP32 stencil, after the FP64 layout
@@ -557,6 +560,7 @@ int lanczos_solve(const LzArgs& a) {
     if (rc != ED_OK) return rc;    \
   } while (0)
 #define LZ_LAUNCHED(what) LZ_TRY(lz_chk(cudaGetLastError(), what))
+  if (Ls) LZ_TRY(ed_split_c128((long long)B * 9 * n, links, Ls, st));
 
   // the operator: L, or -(+)T_deg of the spectrum map [cut, 12] -> [-1, 1]
   const double ca = poly_deg ? 2.0 / (12.0 - lambda_cut) : 0.0, cc = poly_deg ? -(12.0 + lambda_cut) / (12.0 - lambda_cut) : 0.0;
@@ -565,7 +569,9 @@ int lanczos_solve(const LzArgs& a) {
   cudaStream_t sr = st;  // the stream the Lanczos steps go to (a capture stream while a restart cycle is recorded)
   // L x for every problem: FP64 stencil, or the complex64 stencil between a rounding and a widening
   auto stencil = [&](const double2* x, long long xb, double2* out) -> int {
-    if (a.stencil_prec == ED_C128) return ed_laplacian(ED_C128, Lx, Ly, Lz, B, 1, links, x, xb, out, n, sr);
+    if (a.stencil_prec == ED_C128)
+      return Ls ? ed_laplacian(ED_DF, Lx, Ly, Lz, B, 1, Ls, x, xb, out, n, sr)
+                : ed_laplacian(ED_C128, Lx, Ly, Lz, B, 1, links, x, xb, out, n, sr);
     lz_to_c64_kernel<<<vgrid, LZ_THREADS, 0, sr>>>(n, x, xb, x32);
     int r = lz_chk(cudaGetLastError(), "Lanczos operand rounding");
     if (r != ED_OK) return r;

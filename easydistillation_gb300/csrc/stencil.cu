@@ -17,6 +17,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "df.cuh"
 
 namespace ed {
 
@@ -743,6 +744,96 @@ static int launch_laplacian_strip(Latt L, int nt, int nvec, const void* links, c
   return ED_OK;
 }
 
+// ------------------------------------------------------------ double-float Laplacian
+// The FP64 operator at FP32-pipe speed (this part's FP64 pipe bounds the FP64 kernel above at ~1.2 TFLOP/s,
+// about a fifth of what HBM would allow): links in the split form of df.cuh ([t][dir][row][col][V3] float4
+// {re_hi, im_hi, re_lo, im_lo}, 16 bytes per complex like complex128, split once per solve), colour planes in
+// and out as complex128, each input value split by integer operations on its bits (split_bits), every product
+// an exact FP32 product split plus the cross terms, summed in (hi, lo) pairs; ~2^-47 relative per product.
+// One site per thread.
+
+// y += U x and y += U^dag x on split operands (re, im sums kept apart)
+__device__ __forceinline__ void cmac_df(DF& re, DF& im, float4 u, float4 f) {
+  df_acc(re, u.x, u.z, f.x, f.z);
+  df_sub(re, u.y, u.w, f.y, f.w);
+  df_acc(im, u.x, u.z, f.y, f.w);
+  df_acc(im, u.y, u.w, f.x, f.z);
+}
+__device__ __forceinline__ void cmac_conj_df(DF& re, DF& im, float4 u, float4 f) {
+  df_acc(re, u.x, u.z, f.x, f.z);
+  df_acc(re, u.y, u.w, f.y, f.w);
+  df_acc(im, u.x, u.z, f.y, f.w);
+  df_sub(im, u.y, u.w, f.x, f.z);
+}
+
+__global__ void __launch_bounds__(128) laplacian_df_kernel(Latt L, const float4* __restrict__ links,
+                                                           const double2* __restrict__ in, double2* __restrict__ out,
+                                                           long long link_tstride, long long in_tstride,
+                                                           long long out_tstride) {
+  const int V3 = L.V3();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V3) return;
+  const int t = blockIdx.z;
+  const float4* U = links + (long long)t * link_tstride;
+  const long long voff = (long long)blockIdx.y * 3 * V3;
+  const double2* F = in + (long long)t * in_tstride + voff;
+  double2* O = out + (long long)t * out_tstride + voff;
+  const int x = s % L.Lx, yz = s / L.Lx, y = yz % L.Ly, z = yz / L.Ly;
+  DF hre[3], him[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) hre[c] = him[c] = DF{0.f, 0.f};
+#pragma unroll
+  for (int mu = 0; mu < 3; ++mu) {
+    int sp, sm;
+    if (mu == 0) {
+      sp = s - x + wrap_inc(x, L.Lx);
+      sm = s - x + wrap_dec(x, L.Lx);
+    } else if (mu == 1) {
+      sp = s + (wrap_inc(y, L.Ly) - y) * L.Lx;
+      sm = s + (wrap_dec(y, L.Ly) - y) * L.Lx;
+    } else {
+      sp = s + (wrap_inc(z, L.Lz) - z) * L.Lx * L.Ly;
+      sm = s + (wrap_dec(z, L.Lz) - z) * L.Lx * L.Ly;
+    }
+    {  // U_mu(x) F(x + mu)
+      float4 u[9], f[3];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = __ldg(U + (long long)(mu * 9 + e) * V3 + s);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = split_c128_bits(__ldg(F + (long long)c * V3 + sp));
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) cmac_df(hre[a], him[a], u[a * 3 + b], f[b]);
+    }
+    {  // U_mu(x - mu)^dag F(x - mu)
+      float4 u[9], f[3];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = __ldg(U + (long long)(mu * 9 + e) * V3 + sm);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = split_c128_bits(__ldg(F + (long long)c * V3 + sm));
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) cmac_conj_df(hre[a], him[a], u[b * 3 + a], f[b]);
+    }
+  }
+  // out = 6 F(x) - hop, formed in double-float and widened once
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float4 f = split_c128_bits(__ldg(F + (long long)c * V3 + s));
+    DF ore{-hre[c].hi, -hre[c].lo}, oim{-him[c].hi, -him[c].lo};
+    df_acc(ore, 6.f, 0.f, f.x, f.z);
+    df_acc(oim, 6.f, 0.f, f.y, f.w);
+    O[(long long)c * V3 + s] = make_double2(f2d_bits(ore.hi) + f2d_bits(ore.lo), f2d_bits(oim.hi) + f2d_bits(oim.lo));
+  }
+}
+
+__global__ void split_c128_kernel(long long n, const double2* __restrict__ src, float4* __restrict__ dst) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = split_c128(src[i]);
+}
+
 // ------------------------------------------------------------ launchers
 
 int launch_laplacian(int prec, Latt L, int nt, int nvec, const void* links, const void* in, long long its,
@@ -757,7 +848,11 @@ int launch_laplacian(int prec, Latt L, int nt, int nvec, const void* links, cons
     const int rc = launch_laplacian_strip(L, nt, nvec, links, in, its, out, ots, stream);
     if (rc != -1) return rc;
   }
-  if (prec == ED_C128) {
+  if (prec == ED_DF) {
+    dim3 grid(ceil_div(V3, 128), nvec, nt);
+    laplacian_df_kernel<<<grid, 128, 0, stream>>>(L, (const float4*)links, (const double2*)in, (double2*)out, lts, its,
+                                                   ots);
+  } else if (prec == ED_C128) {
     dim3 grid(ceil_div(V3, 128), nvec, nt);
     laplacian_kernel<double, 1><<<grid, 128, 0, stream>>>(L, (const cplx<double>*)links, (const cplx<double>*)in,
                                                            (cplx<double>*)out, lts, its, ots, 6.0);
@@ -809,9 +904,9 @@ int launch_hop_f32(Latt L, int d, int nvec, const void* links_c64, const void* i
 
 extern "C" int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, const void* links, const void* in,
                             long long in_tstride, void* out, long long out_tstride, void* stream) {
-  ED_CHECK_ARG(prec == ED_C128 || prec == ED_C64, "ed_laplacian: prec must be ED_C128 or ED_C64");
+  ED_CHECK_ARG(prec == ED_C128 || prec == ED_C64 || prec == ED_DF, "ed_laplacian: prec must be ED_C128, ED_C64 or ED_DF");
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nvec > 0, "ed_laplacian: sizes must be positive");
-  ED_CHECK_ARG(prec == ED_C128 || Lx % 2 == 0, "ed_laplacian: c64 path needs an even Lx");
+  ED_CHECK_ARG(prec != ED_C64 || Lx % 2 == 0, "ed_laplacian: c64 path needs an even Lx");
   ED_CHECK_ARG(nvec <= 65535 && nt <= 65535, "ed_laplacian: nvec and nt must be <= 65535");
   ED_CHECK_ARG(links && in && out, "ed_laplacian: null pointer");
   ED_CHECK_ARG(in != out, "ed_laplacian: in and out must not alias");
@@ -821,10 +916,21 @@ extern "C" int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, 
   const long long dflt = 3LL * Lx * Ly * Lz * nvec;
   if (in_tstride == 0) in_tstride = dflt;
   if (out_tstride == 0) out_tstride = dflt;
-  ED_CHECK_ARG(prec == ED_C128 || (in_tstride % 2 == 0 && out_tstride % 2 == 0),
+  ED_CHECK_ARG(prec != ED_C64 || (in_tstride % 2 == 0 && out_tstride % 2 == 0),
                "ed_laplacian: c64 strides must keep 16-byte alignment");
   return ed::launch_laplacian(prec, ed::Latt{Lx, Ly, Lz}, nt, nvec, links, in, in_tstride, out, out_tstride,
                               (cudaStream_t)stream);
+}
+
+extern "C" int ed_split_c128(long long n, const void* src, void* dst, void* stream) {
+  ED_CHECK_ARG(n >= 0, "ed_split_c128: negative size");
+  ED_CHECK_ARG((src && dst) || n == 0, "ed_split_c128: null pointer");
+  ED_CHECK_ARG(((uintptr_t)src % 16) == 0 && ((uintptr_t)dst % 16) == 0, "ed_split_c128: 16-byte alignment");
+  if (n == 0) return ED_OK;
+  const int grid = (int)std::min<long long>(ed::ceil_div(n, 256), 8LL * 1024);
+  ed::split_c128_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(n, (const double2*)src, (float4*)dst);
+  ED_RETURN_LAUNCH("double-float split");
+  return ED_OK;
 }
 
 extern "C" int ed_laplacian_config(int use_tma) {

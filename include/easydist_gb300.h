@@ -46,6 +46,8 @@ extern "C" {
 /* ---- storage precisions */
 #define ED_C128 0 /* complex128: double2 */
 #define ED_C64 1  /* complex64:  float2  */
+#define ED_DF 2   /* double-float (ed_laplacian only): links in the split form of ed_split_c128, vectors
+                   * complex128; FP64-class results (~2^-47 per product) computed on the FP32 pipe */
 #define ED_BIG_ENDIAN 0x10 /* flag on a source precision of ed_decode_*: stored big-endian */
 
 /* ---- elemental arithmetic modes */
@@ -157,9 +159,17 @@ int ed_momentum_phases(int Lx, int Ly, int Lz, const int* moms, int nmom, void* 
  * links: SoA [nt][27][V3] (prec); in/out: colour planes, vector v of
  * timeslice t at base + t*tstride + v*3*V3 (complex units; a stride of 0
  * means the packed 3*V3*nvec).  ED_C64 needs an even Lx and even strides.
- * in and out must not alias. */
+ * ED_DF: links split by ed_split_c128 (same layout, 16 bytes per complex),
+ * in/out complex128; the products and sums run in double-float arithmetic on
+ * the FP32 pipe.  in and out must not alias. */
 int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, const void* links, const void* in,
                  long long in_tstride, void* out, long long out_tstride, void* stream);
+
+/* Split n complex128 values into double-float form: dst[i] = float4 {re_hi,
+ * im_hi, re_lo, im_lo} with hi the value rounded to FP32 and lo the rest
+ * rounded to FP32 (48 significant bits); for the links of ed_laplacian's
+ * ED_DF mode.  No counterpart in the reference. */
+int ed_split_c128(long long n, const void* src, void* dst, void* stream);
 
 /* Choose the complex64 Laplacian kernel: use_tma = 1 stages the input colour
  * planes of z-1, z, z+1 through TMA into shared memory (when 4 planes fit, Lx
@@ -288,12 +298,15 @@ int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, int Ne, dou
  * counterpart there.  Needs ed_lanczos_workspace_ex bytes.
  *
  * ED_LANCZOS_GS_DF OR-ed into stencil_prec (both calls): the Gram-Schmidt
- * passes run in double-float arithmetic on the FP32 pipe (ed_cgs_pass_df)
- * instead of FP64: the basis stays FP64 and gets a split copy (two complex64
- * parts per value; the workspace grows by the basis size), the products err
- * by ~2^-47 relative instead of 2^-53, and a pass streams the basis at HBM
- * speed instead of the FP64 pipe's ~2.5 TB/s.  Everything else (recurrence,
- * Rayleigh-Ritz, convergence test, Ritz vectors) stays FP64. */
+ * passes, the restart rotation and the FP64-class stencil applications run in
+ * double-float arithmetic on the FP32 pipe (ed_cgs_pass_df, the rotation
+ * kernel, ed_laplacian's ED_DF on links split once per solve) instead of
+ * FP64: the basis stays FP64 and gets a split copy (two complex64 parts per
+ * value; the workspace grows by the basis and the links), the products err by
+ * ~2^-47 relative instead of 2^-53, and a pass streams the basis at HBM speed
+ * instead of the FP64 pipe's ~2.5 TB/s.  The recurrence, the projected
+ * eigenproblem, the convergence test and the final Rayleigh quotients stay
+ * FP64. */
 #define ED_LANCZOS_GS_DF 0x100
 int ed_lanczos_workspace_ex(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, int stencil_prec, size_t* bytes);
 int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* links, const void* links_c64, int stencil_prec,

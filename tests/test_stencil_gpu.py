@@ -155,3 +155,41 @@ def test_laplacian_tma_matches_plain_and_oracle(latt, nvec, staged):
         Ut = gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, t]
         ref = _planes(R.laplacian(F[t].T, Ut, latt), latt)
         assert rel_err(o_tma[t], ref) < 3e-6
+
+
+@pytest.mark.parametrize("tag", ["443", "642"])
+def test_laplacian_double_float_golden(tag):
+    """ED_DF (the double-float Laplacian of the df eigensolve mode) against the
+    reference's own Laplacian output, to 1e-13 relative to the largest output
+    (measured 2.6e-14: ~2^-47 per product where FP64 gives 2^-53)."""
+    from easydistillation_gb300.ops import laplacian_df, split_c128
+
+    g = golden(f"laplacian_{tag}.npz")
+    latt = list(g["latt"])
+    links = split_c128(_soa(g["gauge"], latt)[:1].contiguous())
+    F = torch.from_numpy(_planes(g["F"], latt)).cuda().unsqueeze(0)
+    out = laplacian_df(links, F, latt)[0].cpu().numpy()
+    ref = _planes(g["LF"], latt)
+    assert np.abs(out - ref).max() < 1e-13 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("latt", [[6, 4, 8, 3], [16, 16, 16, 2], [24, 24, 24, 1]])
+def test_laplacian_double_float_matches_fp64(latt):
+    """Several timeslices and vectors, odd and even extents, values spanning
+    several orders of magnitude (the split works on the bits of every input):
+    the double-float result is the FP64 kernel's to 1e-13 relative."""
+    from easydistillation_gb300.ops import laplacian, laplacian_df, links_to_soa, split_c128
+
+    Lx, Ly, Lz, Lt = latt
+    V3 = Lx * Ly * Lz
+    gauge = R.synthetic_gauge(latt, 0.3, 31)
+    U = torch.from_numpy(np.ascontiguousarray(gauge.transpose(4, 0, 1, 2, 3, 5, 6))).cuda()
+    links = links_to_soa(U, latt)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    F = torch.complex(torch.randn((Lt, 2, 3, V3), generator=g, device="cuda", dtype=torch.float64),
+                      torch.randn((Lt, 2, 3, V3), generator=g, device="cuda", dtype=torch.float64))
+    F = F * torch.exp(8 * torch.randn((Lt, 2, 3, V3), generator=g, device="cuda", dtype=torch.float64))
+    ref = laplacian(links, F, latt)
+    out = laplacian_df(split_c128(links), F, latt)
+    err = float((out - ref).abs().max() / ref.abs().max())
+    assert err < 1e-13, err
