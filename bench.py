@@ -756,7 +756,7 @@ def bench_eigen_default(dev, batch=8):
                                  "restarts_fp32_phase": st2["restarts_fp32"],
                                  "note": "complex64 stencil in a loose FP64 iteration, then FP64 Chebyshev "
                                          "refinement (cut found automatically)", **quality(ev2, X2, ev0)}
-    # the same three solves with the Gram-Schmidt passes in double-float arithmetic on the FP32 pipe
+    # the same three solves in the double-float mode (Gram-Schmidt, rotation and FP64-class stencil on the FP32 pipe)
     df = {}
     (ev3, X3, st3), dt3 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-10, gs_precision="df"))
     df["plain"] = {"value": batch / dt3, "converged": st3["converged"], "restarts": st3["restarts"],
@@ -768,8 +768,10 @@ def bench_eigen_default(dev, batch=8):
                                                    gs_precision="df"))
     df["mixed_fp32_stencil"] = {"value": batch / dt5, "converged": st5["converged"], **quality(ev5, X5, ev0)}
     out["double_float_gram_schmidt"] = {"unit": "timeslices/s", **df,
-                                        "note": "gs_precision='df': Gram-Schmidt passes on the FP32 pipe in "
-                                                "double-float arithmetic (~2^-47 products), everything else FP64"}
+                                        "note": "gs_precision='df': Gram-Schmidt passes, restart rotations and the "
+                                                "FP64-class stencil on the FP32 pipe in double-float arithmetic "
+                                                "(~2^-47 products); recurrence, projected eigenproblem, "
+                                                "convergence test and final Rayleigh quotients FP64"}
     return out
 
 
