@@ -60,6 +60,15 @@ class RefStout:
         self._check(self._cuda.cuModuleGetFunction(ctypes.byref(self._fn), self._mod, b"ed_ref_stout_smear_f64"),
                     "cuModuleGetFunction")
 
+    def __del__(self):
+        mod = getattr(self, "_mod", None)
+        if mod is not None and mod.value:
+            try:
+                self._cuda.cuModuleUnload(mod)
+            except Exception:
+                pass
+            self._mod = None
+
     @staticmethod
     def _check(rc, what):
         if rc != 0:
