@@ -366,17 +366,25 @@ def bench_stencil(U, latt, dev, reps=20):
         G = torch.empty_like(F)
         for _ in range(3):
             lap(links, F, latt, out=G)
+        torch.cuda.synchronize()
+        # the reps launches replayed from a CUDA graph, so that host-side launch time cannot leave gaps between
+        # these ~0.1 ms kernels (a Python loop of launches measured 0.57 of HBM instead of 0.86 in a busy process)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            for r in range(reps):
+                if r % 2 == 0:
+                    lap(links, F, latt, out=G)
+                else:
+                    lap(links, G, latt, out=F)
+        graph.replay()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         a.record()
-        for r in range(reps):
-            if r % 2 == 0:
-                lap(links, F, latt, out=G)
-            else:
-                lap(links, G, latt, out=F)
+        graph.replay()
         b.record()
         torch.cuda.synchronize()
         laplacian_status()
+        del graph
         ms = a.elapsed_time(b) / reps
         nbytes = V3 * Lt * (27 * s + 6 * s)
         gbs = nbytes / ms / 1e6
@@ -523,6 +531,9 @@ def run_ours(args, rank, world):
                             "fp16/tf32 MMA products per complex multiply-add (9 in the Gauss form; 3 split "
                             "products each) plus tile padding (mma_*)"}
 
+    # the Laplacian's HBM roofline (kernel launches replayed from a CUDA graph)
+    stencil = None if args.no_stencil else bench_stencil(U, latt, dev)
+
     # the plain FP64 GPU path on the same timeslice: speed and the split-precision error against it
     fp64 = None
     split_modes = None
@@ -558,8 +569,6 @@ def run_ours(args, rank, world):
                                             exclude=args.mode)
         del out64
         torch.cuda.empty_cache()
-
-    stencil = None if args.no_stencil else bench_stencil(U, latt, dev)
 
     # end to end through the public generator: host eigenvectors in, host elementals out
     e2e = None
@@ -634,7 +643,12 @@ def run_ours(args, rank, world):
         }
         if not args.no_extra:
             # the other configurations' measurements, each timed by itself after the headline measurement
-            del plan, outs, out, V, U
+            del plan, outs, out, V
+            torch.cuda.empty_cache()
+            line["stout"] = bench_stout(latt, dev, event_seconds, True, U=U)
+            del U
+            torch.cuda.empty_cache()
+            line["correlators"] = bench_correlators(dev, event_seconds)
             torch.cuda.empty_cache()
             line["eigensolve"] = bench_eigen_default(dev)
             torch.cuda.empty_cache()
@@ -929,18 +943,24 @@ def run_grad(args, emit=True):
 STOUT_FLOP_PER_LINK = 2.7e3
 
 
-def bench_stout(latt, dev, timed, no_cpu):
+def bench_stout(latt, dev, timed, no_cpu, U=None):
     """One stout smearing step (rho = 0.1) of the spatial links of ``latt``: the
     library's kernel, the reference's own CUDA kernel on the same links (when
-    ``oracle/_ref`` holds it), and the oracle's numpy form on one timeslice."""
+    ``oracle/_ref`` holds it), and the oracle's numpy form on one timeslice.
+    ``U``: device links [3, Lt, Lz, Ly, Lx, 3, 3] to smear (a copy is taken;
+    synthetic ones otherwise)."""
     import numpy as np
     import torch
 
     from easydistillation_gb300.generator.elemental import links_to_device
     from easydistillation_gb300.stout import stout_smear_
 
-    gauge, _ = make_inputs(latt, 1, distinct_t=4)
-    U = links_to_device(gauge, latt, dev)
+    if U is None:
+        gauge, _ = make_inputs(latt, 1, distinct_t=4)
+        U = links_to_device(gauge, latt, dev)
+    else:
+        gauge = None
+        U = U[:3].clone()
     Lx, Ly, Lz, Lt = latt
     nlinks = 3 * Lx * Ly * Lz * Lt
     sec = timed(lambda: stout_smear_(U, latt, 1, 0.1), 5)
@@ -968,7 +988,7 @@ def bench_stout(latt, dev, timed, no_cpu):
         del U_in
     else:
         stout["reference_cuda_kernel"] = {"unavailable": "oracle/_ref/stout_smear_ref.cubin was not built"}
-    if not no_cpu:
+    if not no_cpu and gauge is not None:
         from oracle import restatement as R
 
         U1 = np.ascontiguousarray(gauge.transpose(4, 0, 1, 2, 3, 5, 6)[:3, :1])
@@ -979,6 +999,41 @@ def bench_stout(latt, dev, timed, no_cpu):
                                  "sample": "oracle numpy stout step on one timeslice"}
     del U
     return stout
+
+
+def bench_correlators(dev, timed):
+    """The two-point correlator of ``lattice/correlator/one_particle.py:12-77``
+    at 48 timeslices, Ne = 100, gamma_5 (every source), and its
+    eigenvector-resolved profile (``:80-135``, one source, every sink time)
+    with its diagonal, on the library's kernels; synthetic complex Gaussian
+    perambulator and elementals."""
+    import torch
+
+    from easydistillation_gb300.correlator import _source_terms, gamma, twopoint_assembled
+
+    out = {}
+    Lt, Ne = 48, 100
+    g = torch.Generator(device=dev).manual_seed(4005)
+    peram = torch.complex(torch.randn((Lt, Lt, 4, 4, Ne, Ne), generator=g, device=dev, dtype=torch.float64),
+                          torch.randn((Lt, Lt, 4, 4, Ne, Ne), generator=g, device=dev, dtype=torch.float64))
+    el = torch.complex(torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64),
+                       torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64))
+    ops = [(gamma(15, dev)[None], el)]
+    sec = timed(lambda: twopoint_assembled(ops, peram, range(Lt), Lt), 2)
+    out["twopoint"] = {"correlators_per_s": 1.0 / sec, "seconds": sec,
+                       "workload": "48 timeslices, Ne=100, gamma_5, all 48 sources"}
+    # the eigenvector-resolved profile of one source at every sink time (ed_twopoint_profile) and its diagonal
+    tau0 = peram[0].contiguous()
+    psec = timed(lambda: _source_terms(tau0, tau0, ops, 0, list(range(Lt)), "profile"), 3)
+    dsec = timed(lambda: _source_terms(tau0, tau0, ops, 0, list(range(Lt)), "diagonal"), 3)
+    # gamma_5: 16 left blocks and 4 right blocks of 4 Ne^3 complex multiply-adds per sink time
+    pflop = Lt * (16 + 16) * Ne ** 3 * 8.0
+    out["twopoint_profile"] = {"seconds_per_source": psec, "fp64_tflops": pflop / psec / 1e12,
+                               "diagonal_seconds_per_source": dsec,
+                               "workload": "one source, 48 sink times, Ne=100, gamma_5, [48, Ne, Ne] out"}
+    del peram, el
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_secondary(args):
@@ -1046,28 +1101,7 @@ def run_secondary(args):
         sec = timed(lambda: [gen.calc(t) for t in range(4)], 2) / 4
         disp[prec] = {"timeslices_per_s": 1.0 / sec}
     out["displacement_elemental"] = dict(disp, workload="24^3, Ne=100, distance 2, 7 momenta")
-    # two-point correlator
-    Lt, Ne = 48, 100
-    g = torch.Generator(device=dev).manual_seed(4005)
-    peram = torch.complex(torch.randn((Lt, Lt, 4, 4, Ne, Ne), generator=g, device=dev, dtype=torch.float64),
-                          torch.randn((Lt, Lt, 4, 4, Ne, Ne), generator=g, device=dev, dtype=torch.float64))
-    el = torch.complex(torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64),
-                       torch.randn((1, Lt, Ne, Ne), generator=g, device=dev, dtype=torch.float64))
-    ops = [(gamma(15, dev)[None], el)]
-    sec = timed(lambda: twopoint_assembled(ops, peram, range(Lt), Lt), 2)
-    out["twopoint"] = {"correlators_per_s": 1.0 / sec, "seconds": sec,
-                       "workload": "48 timeslices, Ne=100, gamma_5, all 48 sources"}
-    # the eigenvector-resolved profile of one source at every sink time (ed_twopoint_profile) and its diagonal
-    from easydistillation_gb300.correlator import _source_terms
-
-    tau0 = peram[0].contiguous()
-    psec = timed(lambda: _source_terms(tau0, tau0, ops, 0, list(range(Lt)), "profile"), 3)
-    dsec = timed(lambda: _source_terms(tau0, tau0, ops, 0, list(range(Lt)), "diagonal"), 3)
-    # gamma_5: 16 left blocks and 4 right blocks of 4 Ne^3 complex multiply-adds per sink time
-    pflop = Lt * (16 + 16) * Ne ** 3 * 8.0
-    out["twopoint_profile"] = {"seconds_per_source": psec, "fp64_tflops": pflop / psec / 1e12,
-                               "diagonal_seconds_per_source": dsec,
-                               "workload": "one source, 48 sink times, Ne=100, gamma_5, [48, Ne, Ne] out"}
+    out.update(bench_correlators(dev, timed))
     # ILDG gauge file -> device links
     out["gauge_load"] = bench_gauge_load(dev, timed)
     print(json.dumps({"metric": "secondary components", **out}), flush=True)
