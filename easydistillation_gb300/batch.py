@@ -22,10 +22,11 @@ from .ops import ElementalPlan, gemm_multi
 
 
 def admit_batch(latt_size, Ne, num_nabla, momentum_list, precision="fp64", device=None, max_batch=8,
-                reserve=0.1, static_buffers=True) -> int:
+                reserve=0.1, static_buffers=True, forms=(True,)) -> int:
     """Largest batch (1..max_batch) whose plan workspace, plus the static
     input/output buffers of a graphed batch, fits the free HBM of ``device``
-    while keeping a ``reserve`` fraction free."""
+    while keeping a ``reserve`` fraction free; with several GEMM ``forms``
+    (``factorise`` values) the largest of their workspaces."""
     device = torch.device(device or "cuda")
     free, _total = torch.cuda.mem_get_info(device)
     budget = free * (1.0 - reserve)
@@ -35,7 +36,13 @@ def admit_batch(latt_size, Ne, num_nabla, momentum_list, precision="fp64", devic
                     num_derivative(num_nabla) * len(momentum_list) * Ne * Ne * 16) if static_buffers else 0
     best = 1
     for b in range(1, max_batch + 1):
-        need = ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, device, batch=b).workspace_bytes
+        need = 0
+        for f in forms:
+            try:
+                need = max(need, ElementalPlan(latt_size, Ne, num_nabla, momentum_list, precision, device, batch=b,
+                                               factorise=f).workspace_bytes)
+            except ValueError:  # a form this mode does not take
+                pass
         if need + b * per_t_static <= budget:
             best = b
         else:
@@ -175,14 +182,20 @@ class MixedVolumeGraph:
                                     device=self.device)
             n = len(v.timeslices)
             b = min(max_batch, n, admit_batch(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device,
-                                              max_batch=max_batch, reserve=reserve, static_buffers=False))
+                                              max_batch=max_batch, reserve=reserve, static_buffers=False,
+                                              forms=(True, "left") if autotune else (True,)))
             if autotune:
-                from .tune import tuned_plan
+                from .tune import factorise_options, tuned_plan
 
-                # one GEMM launch per round needs one GEMM form for every volume: the library's default form
-                # for the momentum list (on chip unless it is close to a product set)
+                # one GEMM launch per round takes the volumes on the library's default GEMM form for the momentum
+                # list (on chip unless it is close to a product set); the factorisation with every phase on the
+                # left (short lists) runs a launch of its own and is measured against it
+                forms = None
+                if single_launch:
+                    forms = [f for f in factorise_options(v.latt_size, v.Ne, num_nabla, momentum_list, precision)
+                             if f in (True, "left")]
                 plan = tuned_plan(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device, batch=b,
-                                  evec_dtype=v.evecs.dtype, forms=[True] if single_launch else None)
+                                  evec_dtype=v.evecs.dtype, forms=forms)
             else:
                 plan = ElementalPlan(v.latt_size, v.Ne, num_nabla, momentum_list, precision, self.device, batch=b)
             plan.workspace()  # held now, so the next volume's admission sees it

@@ -533,6 +533,23 @@ int elemental_run(const ed_elemental_plan* P, const void* links, long long dir_s
 
 // ------------------------------------------------------------ C ABI
 
+namespace ed {
+// an arithmetic mode with at most one of the GEMM-form flags (no / forced / left factorisation) and the Gauss flag
+bool mode_flags_valid(int mode) {
+  const int form = mode & (ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR | ED_MODE_FLAG_LEFT_FACTOR);
+  return mode_supported(mode & 0xff) &&
+         (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR | ED_MODE_FLAG_GAUSS |
+                   ED_MODE_FLAG_LEFT_FACTOR)) == 0 &&
+         (form & (form - 1)) == 0;
+}
+void set_mode_flags(ed_elemental_plan* P, int mode) {
+  P->no_factor = (mode & ED_MODE_FLAG_NO_FACTOR) != 0;
+  P->force_factor = (mode & ED_MODE_FLAG_FORCE_FACTOR) != 0;
+  P->left_factor = (mode & ED_MODE_FLAG_LEFT_FACTOR) != 0;
+  P->gauss = (mode & ED_MODE_FLAG_GAUSS) != 0;
+}
+}  // namespace ed
+
 extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly, int Lz, int Ne, int num_nabla,
                                         const int* moms, int nmom, int mode) {
   ED_CHECK_ARG(plan, "ed_elemental_plan_create: null plan pointer");
@@ -540,9 +557,7 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0, "ed_elemental_plan_create: sizes must be positive");
   ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create: num_nabla must be 0, 1 or 2");
   ED_CHECK_ARG(moms, "ed_elemental_plan_create: null momentum list");
-  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR | ED_MODE_FLAG_GAUSS)) == 0 &&
-                   (~mode & (ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) != 0,
-               "ed_elemental_plan_create: unknown mode %d", mode);
+  ED_CHECK_ARG(ed::mode_flags_valid(mode), "ed_elemental_plan_create: unknown mode %d", mode);
   ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create: lattice too large");
   auto* P = new ed_elemental_plan();
   P->Lx = Lx;
@@ -552,9 +567,7 @@ extern "C" int ed_elemental_plan_create(ed_elemental_plan** plan, int Lx, int Ly
   P->num_nabla = num_nabla;
   P->nmom = nmom;
   P->mode = mode & 0xff;
-  P->no_factor = (mode & ED_MODE_FLAG_NO_FACTOR) != 0;
-  P->force_factor = (mode & ED_MODE_FLAG_FORCE_FACTOR) != 0;
-  P->gauss = (mode & ED_MODE_FLAG_GAUSS) != 0;
+  ed::set_mode_flags(P, mode);
   P->use_herm = true;
   P->moms.assign(moms, moms + 3 * nmom);
   int rc = ed::plan_build(P);

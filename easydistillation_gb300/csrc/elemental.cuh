@@ -47,12 +47,14 @@ struct ed_elemental_plan {
   int tc_kind;        // 0 = none
   int tc_scale_exp;   // power-of-two scale applied before fp16 splitting
   size_t tc_bytes;    // extra workspace
-  // factorised phases: momenta = {(px,py)} x {pz} up to a few unused combinations
+  // factorised phases: momenta = {(px,py)} x {pz} up to a few unused combinations, or every momentum's phase
+  // on the left side (ED_MODE_FLAG_LEFT_FACTOR: left factors = the momenta, one right factor = 1)
   bool no_factor = false;       // ED_MODE_FLAG_NO_FACTOR given at creation
   bool force_factor = false;    // ED_MODE_FLAG_FORCE_FACTOR: factorise however many combinations go unused
+  bool left_factor = false;     // ED_MODE_FLAG_LEFT_FACTOR
   bool fac = false;             // the factorised-phase GEMM serves this plan
-  int fac_pxy = 0, fac_pz = 0;  // distinct (px, py) pairs and pz values
-  std::vector<int> fac_xy, fac_z;       // their values: fac_xy[2a], fac_xy[2a+1]; fac_z[c]
+  int fac_pxy = 0, fac_pz = 0;  // left factors (distinct (px, py) pairs) and right factors (distinct pz)
+  std::vector<int> fac_l, fac_r;  // their momenta, 3 ints each: phase_p = phase_{fac_l[a]} phase_{fac_r[c]}
   std::vector<signed char> fac_pidx;    // momentum index of (a, c), -1 if not in the list
   std::vector<int> fac_lchain;          // left-chain slots of one timeslice -> chain index
   std::vector<int> fac_lslot;           // chain index -> left-chain slot (-1 if never a left chain)
@@ -71,6 +73,8 @@ struct ed_elemental_plan {
 
 namespace ed {
 bool mode_supported(int mode);
+bool mode_flags_valid(int mode);
+void set_mode_flags(ed_elemental_plan* P, int mode);
 void tc_fac_setup(ed_elemental_plan* P);
 size_t tc_extra_workspace(const ed_elemental_plan* P);
 size_t f64_extra_workspace(ed_elemental_plan* P);

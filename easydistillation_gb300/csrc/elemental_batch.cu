@@ -7,6 +7,8 @@
 // partial last wave a single timeslice leaves (1376 tiles = 9.05 waves of 152
 // CTAs at 32^3, Ne = 200, 27 momenta).  All launches are stream-ordered and
 // allocation-free, so the whole batch can be captured in a CUDA graph.
+#include <vector>
+
 #include "elemental.cuh"
 
 namespace ed {
@@ -33,9 +35,7 @@ extern "C" int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx
                "ed_elemental_plan_create_batched: sizes must be positive");
   ED_CHECK_ARG(num_nabla >= 0 && num_nabla <= 2, "ed_elemental_plan_create_batched: num_nabla must be 0, 1 or 2");
   ED_CHECK_ARG(moms, "ed_elemental_plan_create_batched: null momentum list");
-  ED_CHECK_ARG(ed::mode_supported(mode & 0xff) && (mode & ~(0xff | ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR | ED_MODE_FLAG_GAUSS)) == 0 &&
-                   (~mode & (ED_MODE_FLAG_NO_FACTOR | ED_MODE_FLAG_FORCE_FACTOR)) != 0,
-               "ed_elemental_plan_create_batched: unknown mode %d", mode);
+  ED_CHECK_ARG(ed::mode_flags_valid(mode), "ed_elemental_plan_create_batched: unknown mode %d", mode);
   ED_CHECK_ARG((long long)Lx * Ly * Lz <= (1LL << 26), "ed_elemental_plan_create_batched: lattice too large");
   auto* P = new ed_elemental_plan();
   P->Lx = Lx;
@@ -45,9 +45,7 @@ extern "C" int ed_elemental_plan_create_batched(ed_elemental_plan** plan, int Lx
   P->num_nabla = num_nabla;
   P->nmom = nmom;
   P->mode = mode & 0xff;
-  P->no_factor = (mode & ED_MODE_FLAG_NO_FACTOR) != 0;
-  P->force_factor = (mode & ED_MODE_FLAG_FORCE_FACTOR) != 0;
-  P->gauss = (mode & ED_MODE_FLAG_GAUSS) != 0;
+  ed::set_mode_flags(P, mode);
   P->use_herm = true;
   P->nbatch = max_batch;
   P->moms.assign(moms, moms + 3 * nmom);
@@ -119,7 +117,13 @@ extern "C" int ed_elemental_gemm_multi(int nplans, const ed_elemental_plan* cons
                                        void* stream) {
   ED_CHECK_ARG(nplans > 0 && plans && nbatch && workspaces && workspace_bytes,
                "ed_elemental_gemm_multi: null pointer or no plans");
-  bool one = nplans <= ed::kMaxMultiPlans;
+  // the plans on the on-chip-phase tensor-core path with the split kind and form of the first such plan share
+  // one launch (up to kMaxMultiPlans of them); every other plan (factorised, FP64, another kind) gets its own
+  std::vector<const ed_elemental_plan*> mp;
+  std::vector<int> mb, mi;
+  std::vector<void*> mw;
+  std::vector<int> single;
+  const ed_elemental_plan* first = nullptr;
   for (int v = 0; v < nplans; ++v) {
     const ed_elemental_plan* P = plans[v];
     ED_CHECK_ARG(P && !P->custom, "ed_elemental_gemm_multi: plan %d is not an elemental plan", v);
@@ -128,13 +132,28 @@ extern "C" int ed_elemental_gemm_multi(int nplans, const ed_elemental_plan* cons
                  P->nbatch);
     int rc = check_ws(P, workspaces[v], workspace_bytes[v], "ed_elemental_gemm_multi");
     if (rc) return rc;
-    // one launch needs every plan on the on-chip-phase tensor-core path with the same split kind and form
-    one = one && P->tc_kind != 0 && P->tc_kind != ed::TC_OZAKI && !P->fac && P->tc_kind == plans[0]->tc_kind &&
-          (P->tc_stack == 2) == (plans[0]->tc_stack == 2);
+    const bool onchip = P->tc_kind != 0 && P->tc_kind != ed::TC_OZAKI && !P->fac;
+    if (onchip && !first) first = P;
+    if (onchip && (int)mp.size() < ed::kMaxMultiPlans && P->tc_kind == first->tc_kind &&
+        (P->tc_stack == 2) == (first->tc_stack == 2)) {
+      mp.push_back(P);
+      mb.push_back(nbatch[v]);
+      mw.push_back(workspaces[v]);
+      mi.push_back(v);
+    } else {
+      single.push_back(v);
+    }
   }
-  if (launches) *launches = one ? 1 : nplans;
-  if (one) return ed::launch_pair_gemm_tc_multi(nplans, plans, nbatch, workspaces, (cudaStream_t)stream);
-  for (int v = 0; v < nplans; ++v) {
+  if (mp.size() == 1) {  // a lone on-chip plan runs its own batched GEMM
+    single.push_back(mi[0]);
+    mp.clear();
+  }
+  if (launches) *launches = (mp.empty() ? 0 : 1) + (int)single.size();
+  if (!mp.empty()) {
+    const int rc = ed::launch_pair_gemm_tc_multi((int)mp.size(), mp.data(), mb.data(), mw.data(), (cudaStream_t)stream);
+    if (rc) return rc;
+  }
+  for (int v : single) {
     const int rc = ed::elemental_run_batch_gemm(plans[v], nbatch[v], workspaces[v], (cudaStream_t)stream);
     if (rc) return rc;
   }

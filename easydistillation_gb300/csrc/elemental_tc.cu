@@ -483,23 +483,29 @@ static size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 
 // Decide whether the factorised-phase GEMM serves the plan: every momentum
 // is a distinct (px, py) x pz combination and at most a quarter of the
-// Pxy * Pz combinations the GEMM forms are not requested.
+// Pxy * Pz combinations the GEMM forms are not requested.  With
+// ED_MODE_FLAG_LEFT_FACTOR every momentum's whole phase is a left factor and
+// the one right factor is 1 (Pxy = Nmom, Pz = 1): nothing formed goes unused,
+// for any list of distinct momenta, at the price of Nmom left variants per
+// left chain.
 void tc_fac_setup(ed_elemental_plan* P) {
   P->fac = false;
   const bool ozaki = tc_kind_of(P->mode) == TC_OZAKI;  // runs on factorised operands only
   if (!tc_kind_of(P->mode) || P->custom || (P->no_factor && !ozaki) || P->nmom > 127) return;
-  std::vector<int> xy, z, ai(P->nmom), ci(P->nmom);
+  std::vector<int> lm, rm, ai(P->nmom), ci(P->nmom);  // left / right factor momenta, 3 ints each
   for (int m = 0; m < P->nmom; ++m) {
     const int px = P->moms[3 * m], py = P->moms[3 * m + 1], pz = P->moms[3 * m + 2];
+    // (px, py, 0) x (0, 0, pz), or (px, py, pz) x (0, 0, 0)
+    const int l[3] = {px, py, P->left_factor ? pz : 0}, r[3] = {0, 0, P->left_factor ? 0 : pz};
     int a = 0, c = 0;
-    while (a < (int)xy.size() / 2 && !(xy[2 * a] == px && xy[2 * a + 1] == py)) ++a;
-    if (a == (int)xy.size() / 2) xy.insert(xy.end(), {px, py});
-    while (c < (int)z.size() && z[c] != pz) ++c;
-    if (c == (int)z.size()) z.push_back(pz);
+    while (a < (int)lm.size() / 3 && !(lm[3 * a] == l[0] && lm[3 * a + 1] == l[1] && lm[3 * a + 2] == l[2])) ++a;
+    if (a == (int)lm.size() / 3) lm.insert(lm.end(), {l[0], l[1], l[2]});
+    while (c < (int)rm.size() / 3 && !(rm[3 * c] == r[0] && rm[3 * c + 1] == r[1] && rm[3 * c + 2] == r[2])) ++c;
+    if (c == (int)rm.size() / 3) rm.insert(rm.end(), {r[0], r[1], r[2]});
     ai[m] = a;
     ci[m] = c;
   }
-  const int pxy = (int)xy.size() / 2, pz = (int)z.size();
+  const int pxy = (int)lm.size() / 3, pz = (int)rm.size() / 3;
   if (pxy * pz > kMaxFac || (!ozaki && !P->force_factor && 4 * pxy * pz > 5 * P->nmom)) return;
   if (ozaki && (pxy > OZ_MAX_VAR || pz > OZ_MAX_VAR)) return;  // the row-maximum kernel keeps <= 16 per row
   std::vector<signed char> pidx(pxy * pz, -1);
@@ -522,8 +528,8 @@ void tc_fac_setup(ed_elemental_plan* P) {
   P->fac = true;
   P->fac_pxy = pxy;
   P->fac_pz = pz;
-  P->fac_xy = xy;
-  P->fac_z = z;
+  P->fac_l = lm;
+  P->fac_r = rm;
   P->fac_pidx = pidx;
   P->fac_lchain = lchain;
   P->fac_lslot = lslot;
@@ -979,11 +985,11 @@ static int launch_fac(const ed_elemental_plan* P, const cplx<float>* chains, cpl
   tc_scale_kernel<<<1, 32, 0, stream>>>(sc, KIND, g_tc_wait_cycles, g_tc_wait_probe);
   ED_RETURN_LAUNCH("tensor-core operand scale");
   std::vector<int> m3;
-  for (int a = 0; a < pxy; ++a) m3.insert(m3.end(), {P->fac_xy[2 * a], P->fac_xy[2 * a + 1], 0});
+  m3.assign(P->fac_l.begin(), P->fac_l.begin() + 3 * pxy);
   int rc = launch_phases(L, m3.data(), pxy, fxy, stream);
   if (rc) return rc;
   m3.clear();
-  for (int c = 0; c < pz; ++c) m3.insert(m3.end(), {0, 0, P->fac_z[c]});
+  m3.assign(P->fac_r.begin(), P->fac_r.begin() + 3 * pz);
   rc = launch_phases(L, m3.data(), pz, fz, stream);
   if (rc) return rc;
   tc_phase_kernel<<<sms, 256, 0, stream>>>(fxy, (long long)pxy * P->V3, sc, fxy32);
@@ -1264,11 +1270,11 @@ static int launch_ozaki(const ed_elemental_plan* P, const cplx<float>* chains, c
   if (e != cudaSuccess) return cuda_status(e, "tc scalars reset");
   const int sms = num_sms();
   std::vector<int> m3;
-  for (int a = 0; a < pxy; ++a) m3.insert(m3.end(), {P->fac_xy[2 * a], P->fac_xy[2 * a + 1], 0});
+  m3.assign(P->fac_l.begin(), P->fac_l.begin() + 3 * pxy);
   int rc = launch_phases(L, m3.data(), pxy, fxy, stream);
   if (rc) return rc;
   m3.clear();
-  for (int c = 0; c < pz; ++c) m3.insert(m3.end(), {0, 0, P->fac_z[c]});
+  m3.assign(P->fac_r.begin(), P->fac_r.begin() + 3 * pz);
   rc = launch_phases(L, m3.data(), pz, fz, stream);
   if (rc) return rc;
   tc_phase_kernel<<<sms, 256, 0, stream>>>(fxy, (long long)pxy * P->V3, sc, fxy32);

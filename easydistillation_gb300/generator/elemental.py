@@ -20,7 +20,9 @@ is a product set {(px, py)} x {pz} (e.g. all 27 momenta with |p|^2 <= 3),
 those GEMMs use the factorised phase exp(2 pi i p.x / L) = f(px, py) g(pz)
 with both operands prepared in HBM; ``factorise=False`` keeps the kernel
 that forms the phase-weighted operand on chip, ``factorise="force"``
-factorises however many (px, py) x pz combinations go unused.
+factorises however many (px, py) x pz combinations go unused, and
+``factorise="left"`` puts every momentum's whole phase on the left operand
+(any short momentum list, none of the GEMM's work unused).
 ``autotune=True`` replaces ``factorise``: each plan (one per batch size) takes
 the GEMM form and launch settings that the autotuner
 (``easydistillation_gb300.tune``) measured fastest for its shape on this
@@ -305,7 +307,7 @@ class ElementalGenerator:
         host_out = out.device.type == "cpu"
         if batch is None:
             # with autotune the GEMM form is chosen per batch size: admit what every form fits
-            forms = (True, False, "force") if self.autotune else (self.factorise,)
+            forms = (True, False, "force", "left") if self.autotune else (self.factorise,)
             batch = min(admit_batch(self.latt_size, self.Ne, self._num_nabla, self.momentum_list, self.precision,
                                     self.device, max_batch=min(8, len(ts)), factorise=f) for f in forms)
         plan = getattr(self, "_bplan", None)

@@ -414,7 +414,7 @@ def mean_c128(stack: torch.Tensor, out: torch.Tensor = None):
 
 #: elemental arithmetic modes (ED_MODE_* in include/easydist_gb300.h)
 MODES = {"fp64": 0, "f16x3": 1, "bf16x3": 2, "tf32x3": 3, "ozaki_i8": 4}
-_FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR = 0x100, 0x200
+_FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR, _FLAG_LEFT_FACTOR = 0x100, 0x200, 0x800
 _FLAG_GAUSS = 0x400  # ED_MODE_FLAG_GAUSS
 #: plan launch settings (ED_TUNE_* keys)
 TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4, "tc_pair": 5, "tc_kpb": 6,
@@ -432,14 +432,19 @@ class ElementalPlan:
         phase-weighted operand inside the kernel even when the momentum list
         factorises (ED_MODE_FLAG_NO_FACTOR); ``factorise="force"`` factorises
         however many (px,py) x pz combinations the list leaves unused
-        (ED_MODE_FLAG_FORCE_FACTOR).  ``gauss=True`` runs the factorised split
+        (ED_MODE_FLAG_FORCE_FACTOR); ``factorise="left"`` factorises with every
+        momentum's whole phase on the left operand and none on the right
+        (ED_MODE_FLAG_LEFT_FACTOR: Nmom left variants per left chain, no
+        unused combinations, for any list of at most 127 distinct momenta).
+        ``gauss=True`` runs the factorised split
         GEMM in the Gauss three-multiplication form (ED_MODE_FLAG_GAUSS).
         ``tuning``: launch settings (``TUNING_KEYS``, see ``set_tuning``)."""
         if mode not in MODES:
             raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES)}")
-        if factorise not in (True, False, "force"):
-            raise ValueError(f"factorise must be True, False or 'force', not {factorise!r}")
-        cmode = MODES[mode] | {True: 0, False: _FLAG_NO_FACTOR, "force": _FLAG_FORCE_FACTOR}[factorise]
+        if factorise not in (True, False, "force", "left"):
+            raise ValueError(f"factorise must be True, False, 'force' or 'left', not {factorise!r}")
+        cmode = MODES[mode] | {True: 0, False: _FLAG_NO_FACTOR, "force": _FLAG_FORCE_FACTOR,
+                               "left": _FLAG_LEFT_FACTOR}[factorise]
         if gauss:
             cmode |= _FLAG_GAUSS
         self.factorise = factorise

@@ -132,11 +132,18 @@ class TuneResult:
     cached: bool = False
 
 
+# momentum lists up to this length also try the factorisation with every phase on the left operand
+LEFT_FACTOR_MAX_MOM = 16
+
+
 def factorise_options(latt_size, Ne, num_nabla, momentum_list, mode) -> List[object]:
     """The distinct GEMM forms a tensor-core plan can take for this momentum
     list: ``True`` (factorised when at most a quarter of the combinations go
-    unused, else on chip), ``"force"`` when it differs from ``True``, and
-    ``False`` (on chip) when ``True`` factorises.  Host-side plans only."""
+    unused, else on chip), ``"force"`` when it differs from ``True``,
+    ``"left"`` (every phase on the left operand) for lists that are not close
+    to a product set and have at most ``LEFT_FACTOR_MAX_MOM`` momenta (its
+    left operand grows with the momentum count), and ``False`` (on chip) when
+    ``True`` factorises.  Host-side plans only."""
     if mode == "fp64":
         return [True]
     if mode == "ozaki_i8":
@@ -153,6 +160,8 @@ def factorise_options(latt_size, Ne, num_nabla, momentum_list, mode) -> List[obj
     if default is None:
         if fac("force") is not None:
             opts.append("force")
+        if len(momentum_list) <= LEFT_FACTOR_MAX_MOM and fac("left") is not None:
+            opts.append("left")
     else:
         opts.append(False)
     return opts

@@ -79,6 +79,14 @@ extern "C" {
  * factorised plan (ED_ERR_UNSUPPORTED otherwise); runs on single SMs
  * whatever ED_TUNE_TC_PAIR / ED_TUNE_TC_STACK say. */
 #define ED_MODE_FLAG_GAUSS 0x400
+/* Flag OR-ed into a tensor-core mode at plan creation: factorise with every
+ * momentum's whole phase on the left operand, phase_p = phase_p * 1 (Pxy =
+ * Nmom left factors of three components, Pz = 1): the factorised GEMM then
+ * forms exactly the requested momenta, for any list of at most 127 distinct
+ * momenta, at the price of Nmom left variants per left chain in the split
+ * planes (e.g. the 7 momenta with |p|^2 <= 1, which as a (px,py) x pz set
+ * would leave 8 of 15 combinations unused).  Excludes the two flags above. */
+#define ED_MODE_FLAG_LEFT_FACTOR 0x800
 
 /* ---- launch settings of a plan (ed_elemental_set_tuning keys) */
 #define ED_TUNE_F64_TILE 1   /* FP64 pair GEMM tile, rows x cols: 0 = 64x64 (default), 1 = 32x64,
@@ -473,10 +481,11 @@ int ed_elemental_run_batch(const ed_elemental_plan* plan, int nbatch, const void
  * stream order on the same stream and together equal one
  * ed_elemental_run_batch; they allocate nothing, so the sequence can be
  * captured in a CUDA graph.  ed_elemental_gemm_multi issues one launch whose
- * blocks cover the tiles of every plan when all plans (at most 4) take the
- * on-chip-phase tensor-core path with the same split mode (f16x3, bf16x3 or
- * tf32x3, a momentum list that is not factorised); otherwise one launch per
- * plan.  *launches (may be NULL) receives the number of GEMM launches.  The
+ * blocks cover the tiles of the plans (up to 4) that take the on-chip-phase
+ * tensor-core path with the split mode and form of the first such plan
+ * (f16x3, bf16x3 or tf32x3, a momentum list that is not factorised), and one
+ * launch for each other plan (factorised, FP64, another mode).  *launches
+ * (may be NULL) receives the number of GEMM launches.  The
  * reference computes each (volume, timeslice) by its own
  * ElementalGenerator.calc(t) (lattice/generator/elemental.py:290-338). */
 int ed_elemental_run_batch_begin(const ed_elemental_plan* plan, int nbatch, const void* const* links,

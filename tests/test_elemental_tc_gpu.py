@@ -137,6 +137,33 @@ def test_fac_long_k():
     assert rel_err(E, ref) < TOL["f16x3"]
 
 
+@pytest.mark.parametrize("mode", ["f16x3", "tf32x3"])
+@pytest.mark.parametrize("moms", ["first7", "open", "all27"])
+def test_fac_every_phase_on_the_left(mode, moms):
+    """factorise="left" (ED_MODE_FLAG_LEFT_FACTOR): each momentum's whole phase
+    on the left variants and one right factor: the 7 momenta with |p|^2 <= 1
+    (hermitian list, 5 x 3 as a product set), a list not closed under p -> -p,
+    and the 27 momenta (27 left variants); every operator up to num_nabla = 2"""
+    m = {"first7": R.mom_dict_to_list(3)[:7], "all27": R.mom_dict_to_list(3),
+         "open": [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 1), (0, 0, 2), (0, 1, 2), (1, 1, 2)]}[moms]
+    gen, E, ref = _run_fac([8, 4, 4, 2], 20, 2, m, mode, "left", t=1)
+    assert gen._plan.factorised == (len(m), 1)
+    assert rel_err(E, ref) < TOL[mode]
+
+
+def test_fac_left_many_tiles_long_k():
+    """7 left variants x Ne = 150 columns, ragged tiles; K = 3 * 16^3 = 12288"""
+    gen, E, ref = _run_fac([16, 16, 16, 1], 150, 1, R.mom_dict_to_list(3)[:7], "f16x3", "left")
+    assert gen._plan.factorised == (7, 1)
+    assert rel_err(E, ref) < TOL["f16x3"]
+
+
+def test_ozaki_every_phase_on_the_left():
+    gen, E, ref = _run_fac([4, 4, 4, 2], 6, 1, R.mom_dict_to_list(3)[:7], "ozaki_i8", "left", t=1)
+    assert gen._plan.factorised == (7, 1)
+    assert rel_err(E, ref) < TOL_OZAKI
+
+
 # ---------------------------------------------------------------- Ozaki int8 slices
 @pytest.mark.parametrize("num_nabla, moms", [(2, "all27"), (1, "first7")])
 def test_ozaki_small(num_nabla, moms):

@@ -76,10 +76,31 @@ def test_factorise_options():
 
     m27, m7 = mom_dict_to_list(3), mom_dict_to_list(3)[:7]
     assert factorise_options([8, 8, 4, 2], 10, 2, m27, "f16x3") == [True, False]
-    assert factorise_options([8, 8, 4, 2], 10, 2, m7, "f16x3") == [True, "force"]
-    assert factorise_options([8, 8, 4, 2], 10, 2, [(0, 0, 0), (1, 2, 3)], "tf32x3") == [True, "force"]
+    assert factorise_options([8, 8, 4, 2], 10, 2, m7, "f16x3") == [True, "force", "left"]
+    assert factorise_options([8, 8, 4, 2], 10, 2, [(0, 0, 0), (1, 2, 3)], "tf32x3") == [True, "force", "left"]
     assert factorise_options([8, 8, 4, 2], 10, 2, m27, "fp64") == [True]
     assert factorise_options([8, 8, 4, 2], 10, 2, m7, "ozaki_i8") == [True]
+    assert factorise_options([8, 8, 4, 2], 10, 2, mom_dict_to_list(9), "f16x3") == [True]  # 123 momenta: too long
+
+
+def test_left_factorisation_plans():
+    """ED_MODE_FLAG_LEFT_FACTOR: every momentum a left factor, one right factor;
+    the flags that choose the GEMM form exclude one another."""
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.ops import ElementalPlan
+
+    m7 = mom_dict_to_list(3)[:7]
+    assert ElementalPlan([8, 8, 4, 2], 10, 1, m7, "f16x3", device="cpu", factorise="left").factorised == (7, 1)
+    assert ElementalPlan([8, 8, 4, 2], 10, 1, m7, "f16x3", device="cpu").factorised is None
+    assert ElementalPlan([8, 8, 4, 2], 10, 1, m7, "f16x3", device="cpu", factorise="force").factorised == (5, 3)
+    assert ElementalPlan([8, 8, 4, 2], 10, 1, m7, "fp64", device="cpu", factorise="left").factorised is None
+    from easydistillation_gb300 import _lib
+
+    h = ctypes.c_void_p()
+    arr = (ctypes.c_int * 21)(*[c for p in m7 for c in p])
+    for flags in (0x100 | 0x800, 0x200 | 0x800):
+        rc = _lib.lib().ed_elemental_plan_create(ctypes.byref(h), 8, 8, 4, 10, 1, arr, 7, 1 | flags)
+        assert rc == _lib.ED_ERR_ARG
 
 
 def test_coordinate_search_picks_fastest_accurate_candidate():
