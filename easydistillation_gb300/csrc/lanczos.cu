@@ -35,10 +35,8 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
-#include <mutex>
-#include <vector>
-
 #include <type_traits>
+#include <vector>
 
 #include "common.cuh"
 #include "df.cuh"
