@@ -652,6 +652,8 @@ def run_ours(args, rank, world):
             torch.cuda.empty_cache()
             line["eigensolve"] = bench_eigen_default(dev)
             torch.cuda.empty_cache()
+            line["eigensolve_32cube"] = bench_eigen_32(dev)
+            torch.cuda.empty_cache()
             line["mixed_volumes"] = measure_mixed(args, dev)
             torch.cuda.empty_cache()
             line["gradient"] = measure_grad(args, dev)
@@ -786,6 +788,58 @@ def bench_eigen_default(dev, batch=8):
                                                 "FP64-class stencil on the FP32 pipe in double-float arithmetic "
                                                 "(~2^-47 products); recurrence, projected eigenproblem, "
                                                 "convergence test and final Rayleigh quotients FP64"}
+    return out
+
+
+def bench_eigen_32(dev, batch=2):
+    """The mixed-precision configuration's eigensolve, 32^3, Ne = 200, tol
+    1e-10, ``batch`` timeslices per solve: the plain FP64 solve, the mixed
+    solve (complex64 stencil inside the loose FP64 iteration, then the FP64
+    Chebyshev refinement; FP64 Gram-Schmidt and Rayleigh-Ritz) and the same in
+    the double-float mode; timeslices/s of one solve after an untimed one, the
+    largest residual (FP64 stencil) and eigenvalue difference to the plain
+    solve."""
+    import torch
+
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.ops import lanczos_tr, laplacian, links_to_soa
+
+    latt = [32, 32, 32, batch]
+    Ne = 200
+    gauge, _ = make_inputs(latt, 1, distinct_t=batch)
+    U = links_to_device(gauge, latt, dev)
+    L64 = links_to_soa(U, latt)
+    L32 = links_to_soa(U, latt, dtype=torch.complex64)
+    del U
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    def max_res(ev, X):
+        LY = laplacian(L64, X, latt)
+        return float(torch.linalg.vector_norm((LY - ev[:, :, None, None].to(X.dtype) * X).reshape(batch, Ne, -1),
+                                              dim=2).max())
+
+    out = {"workload": f"32^3, Ne={Ne}, tol 1e-10, {batch} timeslices per solve"}
+    (ev0, X0, st0), dt0 = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-10))
+    out["plain_fp64"] = {"value": batch / dt0, "unit": "timeslices/s", "converged": st0["converged"],
+                         "max_residual": max_res(ev0, X0)}
+    del X0
+    for name, gs in (("mixed_fp32_stencil", "fp64"), ("mixed_fp32_stencil_df", "df")):
+        (ev, X, st), dt = timed(lambda: lanczos_tr(L64, latt, Ne, 1e-10, stencil_precision="fp32", links_c64=L32,
+                                                   gs_precision=gs))
+        out[name] = {"value": batch / dt, "unit": "timeslices/s", "converged": st["converged"],
+                     "max_residual": max_res(ev, X),
+                     "max_rel_eval_diff_vs_plain": float(((ev - ev0).abs() / ev0.abs()).max()),
+                     "matvecs_fp32": st["matvecs_fp32"], "matvecs_fp64": st["matvecs_fp64"]}
+        del X
+    out["note"] = ("mixed: complex64 stencil inside the loose FP64 iteration, then the FP64 Chebyshev refinement "
+                   "(cut found automatically); _df: Gram-Schmidt, rotations and FP64-class stencil in double-float")
     return out
 
 
