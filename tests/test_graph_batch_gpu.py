@@ -148,3 +148,39 @@ def test_mixed_volumes_one_gemm_launch_per_round(mode):
     assert per_volume.gemm_launches == 3 + 2 + 2
     for a, b in zip(outs, ref):
         assert torch.equal(a, b)
+
+
+def test_gemm_multi_groups_onchip_plans_and_runs_factorised_alone():
+    """ed_elemental_gemm_multi over two on-chip-phase plans and one plan on the
+    left-only factorised GEMM (4 operators x 7 momenta): the two on-chip plans
+    share one launch, the factorised one runs alone (2 launches), and every
+    result is bit-identical to the plan's own run_batch."""
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.ops import ElementalPlan, gemm_multi
+
+    moms = R.mom_dict_to_list(3)[:7]
+    specs = [([8, 4, 4, 2], 10, True), ([4, 4, 4, 2], 6, True), ([8, 8, 4, 2], 12, "left")]
+    plans, ins, outs, refs = [], [], [], []
+    for k, (latt, Ne, fac) in enumerate(specs):
+        gauge, evec = _inputs(latt, Ne, 0.3, 70 + k)
+        U = links_to_device(gauge, latt, "cuda")
+        V = torch.from_numpy(evec.reshape(latt[3], Ne, -1)).cuda()
+        plan = ElementalPlan(latt, Ne, 1, moms, "f16x3", batch=2, factorise=fac)
+        assert (plan.factorised is not None) == (fac == "left")
+        Lt, V3 = latt[3], latt[0] * latt[1] * latt[2]
+        links, evs = [U[:, t] for t in range(2)], [V[t] for t in range(2)]
+        ref = [torch.empty((4, 7, Ne, Ne), dtype=torch.complex128, device="cuda") for _ in range(2)]
+        plan.run_batch(links, Lt * V3 * 9, 9, evs, ref)
+        plans.append(plan)
+        ins.append((links, Lt * V3 * 9, evs))
+        outs.append([torch.full_like(r, float("nan")) for r in ref])
+        refs.append(ref)
+    for plan, (links, ds, evs) in zip(plans, ins):
+        plan.run_batch_begin(links, ds, 9, evs)
+    assert gemm_multi(plans, [2, 2, 2]) == 2
+    for plan, out in zip(plans, outs):
+        plan.run_batch_end(out)
+    for plan, out, ref in zip(plans, outs, refs):
+        assert plan.check_status() == 0
+        for a, b in zip(out, ref):
+            assert torch.equal(a, b)
