@@ -125,8 +125,9 @@ extern "C" {
                               * 256-column accumulators, re / im formed by the drain (143 ms per
                               * 4 timeslices at 32^3, Ne = 200, f16x3); 2 = four real products
                               * per complex one, M = N = 128 MMAs into double-buffered [re], [im]
-                              * accumulators (165-172 ms).  SM pairs (ED_TUNE_TC_PAIR = 2) use the
-                              * four-product form.  The on-chip-phase GEMM (lists that do not
+                              * accumulators (165-172 ms).  SM pairs take their form from
+                              * ED_TUNE_TC_PAIR (2: four products, 3: stacked).  The on-chip-phase
+                              * GEMM (lists that do not
                               * factorise) takes the same two forms: stacked with ED_TUNE_TC_KPB
                               * k-blocks per group (default 2), or four products, one k-block per
                               * double-buffered TMEM buffer. */
