@@ -618,6 +618,10 @@ extern "C" int ed_elemental_status(const ed_elemental_plan* plan, const void* wo
   ED_CHECK_ARG(plan && workspace && code, "ed_elemental_status: null pointer");
   int rc = ed::tc_read_status(plan, workspace, code, (cudaStream_t)stream);
   if (rc != ED_OK) return rc;
+  if (*code == 7) {  // TC_ERR_CLUSTER: an SM-pair GEMM ran without its two-CTA cluster and stopped at once
+    ed::set_error("elemental: the SM-pair GEMM was launched without its two-CTA cluster; the output is invalid");
+    return ED_ERR_CUDA;
+  }
   if (*code != 0) {
     ed::set_error("elemental: a bounded device wait gave up (code %d); the output of that run is invalid", *code);
     return ED_ERR_TIMEOUT;

@@ -31,4 +31,4 @@ constexpr long long TC_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
 // status codes written by the kernel
 constexpr int TC_ERR_FULL = 1, TC_ERR_EMPTY = 2, TC_ERR_ACC = 3, TC_ERR_ACCE = 4, TC_ERR_XFULL = 5,
-              TC_ERR_SYNC = 6;
+              TC_ERR_SYNC = 6, TC_ERR_CLUSTER = 7;

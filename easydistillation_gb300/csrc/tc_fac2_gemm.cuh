@@ -33,6 +33,11 @@ constexpr int TCP_MAX_STAGES = 4, TCP_DEFAULT_STAGES = 3;
 __host__ __device__ constexpr int tcp_smem(int nst) { return nst * TCP_STAGE_BYTES + 1024 + 256; }
 static_assert(tcp_smem(TCP_MAX_STAGES) <= 232448, "shared memory per block");
 
+__device__ __forceinline__ uint32_t cluster_nctarank() {
+  uint32_t n;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+  return n;
+}
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -134,6 +139,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // every CTA must sit in a two-CTA cluster: the pair's MMAs, multicast commits and remote arrivals address the
+  // peer CTA.  A launch without that cluster shape (for instance by a tool that replays the kernel) stops here,
+  // before any barrier, TMEM allocation or cluster access, and reports TC_ERR_CLUSTER.
+  if (cluster_nctarank() != 2 || (gridDim.x & 1u) != 0u) {
+    if (threadIdx.x == 0) atomicCAS(&sc->status, 0, TC_ERR_CLUSTER);
+    return;
+  }
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
   volatile int* status = &sc->status;
@@ -446,6 +458,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // every CTA must sit in a two-CTA cluster: the pair's MMAs, multicast commits and remote arrivals address the
+  // peer CTA.  A launch without that cluster shape (for instance by a tool that replays the kernel) stops here,
+  // before any barrier, TMEM allocation or cluster access, and reports TC_ERR_CLUSTER.
+  if (cluster_nctarank() != 2 || (gridDim.x & 1u) != 0u) {
+    if (threadIdx.x == 0) atomicCAS(&sc->status, 0, TC_ERR_CLUSTER);
+    return;
+  }
   const uint32_t rank = cluster_ctarank();
   const bool leader = rank == 0;
   volatile int* status = &sc->status;
