@@ -27,6 +27,13 @@ __device__ __forceinline__ void df_acc(DF& s, float ah, float al, float bh, floa
 }
 // s -= a*b
 __device__ __forceinline__ void df_sub(DF& s, float ah, float al, float bh, float bl) { df_acc(s, -ah, -al, bh, bl); }
+// Fold the low part back into the high one (fast two-sum, |lo| <= |hi|): long sums renormalise every few terms so
+// that the low part's own rounding stays at 2^-48 of the sum instead of growing with the number of terms.
+__device__ __forceinline__ void df_renorm(DF& s) {
+  const float t = s.hi + s.lo;
+  s.lo -= t - s.hi;
+  s.hi = t;
+}
 
 __device__ __forceinline__ float4 split_c128(double2 v) {
   const float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "df.cuh"
 #include "elemental.cuh"
 #include "tc_config.cuh"
 
@@ -310,6 +311,127 @@ __global__ void __launch_bounds__(256) pair_gemm_f64_kernel(GemmTable tab, int N
   }
 }
 
+// The same pair GEMM in double-float arithmetic on the FP32 pipe (ED_TUNE_F64_DF): the staged operands are
+// float4 {re_hi, im_hi, re_lo, im_lo} (df.cuh), split from the complex128 chains and phases by integer
+// operations on their bits; the left operand conj(X_i) phase_p is formed in double-float while staged; every
+// complex multiply-add is four exact FP32 product splits with cross terms and two-sum accumulation (~2^-47 per
+// product); results are written as complex128.  On this part the FP32 pipe runs ~60x the FP64 rate.
+__device__ __forceinline__ float4 df_cmul_conj(float4 x, float4 p) {  // conj(x) * p
+  DF re{0.f, 0.f}, im{0.f, 0.f};
+  df_acc(re, x.x, x.z, p.x, p.z);
+  df_acc(re, x.y, x.w, p.y, p.w);
+  df_acc(im, x.x, x.z, p.y, p.w);
+  df_sub(im, x.y, x.w, p.x, p.z);
+  return make_float4(re.hi, im.hi, re.lo, im.lo);
+}
+
+template <int TM, int TN>
+__global__ void __launch_bounds__(256) pair_gemm_df_kernel(GemmTable tab, int Ne, int V3, int nmom,
+                                                           const cplx<double>* __restrict__ chains,
+                                                           const cplx<double>* __restrict__ phases,
+                                                           cplx<double>* __restrict__ G, long long kchunk,
+                                                           long long part_stride) {
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  __shared__ float4 As[F64_BK][BM + 1];
+  __shared__ float4 Bs[F64_BK][BN + 1];
+  int tile = blockIdx.x;
+  int jb = 0;
+  while (jb + 1 < tab.njobs && tile >= tab.j[jb + 1].tile0) ++jb;
+  const GemmJobDev J = tab.j[jb];
+  int local = tile - J.tile0;
+  const int per_p = J.mt * J.nt;
+  const int p = local / per_p;
+  local -= p * per_p;
+  const int mtile = local / J.nt;
+  const int ntile = local - mtile * J.nt;
+  const long long K = 3LL * V3;
+  const long long k_begin = blockIdx.y * kchunk, k_end = min(K, k_begin + kchunk);
+  G += blockIdx.y * part_stride;
+  const int M = Ne, N = J.nright * Ne;
+  const cplx<double>* Lc = chains + (long long)J.left * Ne * K;
+  const cplx<double>* Rc = chains + (long long)J.right0 * Ne * K;
+  const cplx<double>* ph = phases + (long long)p * V3;
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int lk = tid & 7, lr = tid >> 3;
+  DF are[TM][TN], aim[TM][TN];
+#pragma unroll
+  for (int a = 0; a < TM; ++a)
+#pragma unroll
+    for (int b = 0; b < TN; ++b) are[a][b] = aim[a][b] = DF{0.f, 0.f};
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  for (long long k0 = k_begin; k0 < k_end; k0 += F64_BK) {
+    const long long k = k0 + lk;
+    float4 phk = zero;
+    if (k < k_end) {
+      const cplx<double> pv = ld(ph + (k % V3));
+      phk = split_c128_bits(make_double2(pv.re, pv.im));
+    }
+#pragma unroll
+    for (int pass = 0; pass < BM / 32; ++pass) {
+      const int r = lr + 32 * pass;
+      const int gi = mtile * BM + r;
+      float4 a = zero;
+      if (gi < M && k < k_end) {
+        const cplx<double> xv = ld(Lc + (long long)gi * K + k);
+        a = df_cmul_conj(split_c128_bits(make_double2(xv.re, xv.im)), phk);
+      }
+      As[lk][r] = a;
+    }
+#pragma unroll
+    for (int pass = 0; pass < BN / 32; ++pass) {
+      const int r = lr + 32 * pass;
+      const int gj = ntile * BN + r;
+      float4 b = zero;
+      if (gj < N && k < k_end) {
+        const cplx<double> yv = ld(Rc + (long long)gj * K + k);
+        b = split_c128_bits(make_double2(yv.re, yv.im));
+      }
+      Bs[lk][r] = b;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < F64_BK; ++kk) {
+      float4 av[TM], bv[TN];
+#pragma unroll
+      for (int a = 0; a < TM; ++a) av[a] = As[kk][ty + 16 * a];
+#pragma unroll
+      for (int b = 0; b < TN; ++b) bv[b] = Bs[kk][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < TM; ++a)
+#pragma unroll
+        for (int b = 0; b < TN; ++b) {  // (ar + i ai)(br + i bi)
+          df_acc(are[a][b], av[a].x, av[a].z, bv[b].x, bv[b].z);
+          df_sub(are[a][b], av[a].y, av[a].w, bv[b].y, bv[b].w);
+          df_acc(aim[a][b], av[a].x, av[a].z, bv[b].y, bv[b].w);
+          df_acc(aim[a][b], av[a].y, av[a].w, bv[b].x, bv[b].z);
+        }
+    }
+    // K runs to 3 V3 (98304 at 32^3): renormalise the sums once per stage of F64_BK terms
+#pragma unroll
+    for (int a = 0; a < TM; ++a)
+#pragma unroll
+      for (int b = 0; b < TN; ++b) {
+        df_renorm(are[a][b]);
+        df_renorm(aim[a][b]);
+      }
+    __syncthreads();
+  }
+  cplx<double>* Gp = G + J.g_off + (long long)p * M * N;
+#pragma unroll
+  for (int a = 0; a < TM; ++a) {
+    const int gi = mtile * BM + ty + 16 * a;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int b = 0; b < TN; ++b) {
+      const int gj = ntile * BN + tx + 16 * b;
+      if (gj < N) Gp[(long long)gi * N + gj] = mk(df_value(are[a][b]), df_value(aim[a][b]));
+    }
+  }
+}
+
 // ------------------------------------------------------------ combine
 
 struct CombineTable {
@@ -388,10 +510,14 @@ int launch_pair_gemm_f64(const ed_elemental_plan* P, const cplx<double>* chains,
     d.tile0 = tiles;
     tiles += d.mt * d.nt * P->nmom;
   }
-  auto kern = shape == 0   ? pair_gemm_f64_kernel<4, 4>
-              : shape == 1 ? pair_gemm_f64_kernel<2, 4>
-              : shape == 2 ? pair_gemm_f64_kernel<4, 2>
-                           : pair_gemm_f64_kernel<2, 2>;
+  auto kern = P->f64_df ? (shape == 0   ? pair_gemm_df_kernel<4, 4>
+                           : shape == 1 ? pair_gemm_df_kernel<2, 4>
+                           : shape == 2 ? pair_gemm_df_kernel<4, 2>
+                                        : pair_gemm_df_kernel<2, 2>)
+                        : (shape == 0   ? pair_gemm_f64_kernel<4, 4>
+                           : shape == 1 ? pair_gemm_f64_kernel<2, 4>
+                           : shape == 2 ? pair_gemm_f64_kernel<4, 2>
+                                        : pair_gemm_f64_kernel<2, 2>);
   // Few output tiles (few momenta, small Ne) leave most SMs idle over a long K: split K into partials, summed in
   // a fixed order afterwards, up to the plan's partial buffers and at least F64_MIN_KCHUNK k per part.
   const long long K = 3LL * P->V3;
@@ -694,6 +820,10 @@ extern "C" int ed_elemental_set_tuning(ed_elemental_plan* plan, int key, int val
       ED_CHECK_ARG(value >= 0 && value <= 2, "ed_elemental_set_tuning: operand form %d (0, 1 or 2)", value);
       plan->tc_stack = value;
       return ED_OK;
+    case ED_TUNE_F64_DF:
+      ED_CHECK_ARG(value == 0 || value == 1, "ed_elemental_set_tuning: double-float switch %d (0 or 1)", value);
+      plan->f64_df = value;
+      return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_set_tuning: unknown key %d", key);
   }
@@ -723,6 +853,9 @@ extern "C" int ed_elemental_get_tuning(const ed_elemental_plan* plan, int key, i
       return ED_OK;
     case ED_TUNE_TC_STACK:
       *value = plan->tc_stack;
+      return ED_OK;
+    case ED_TUNE_F64_DF:
+      *value = plan->f64_df;
       return ED_OK;
     default:
       ED_CHECK_ARG(false, "ed_elemental_get_tuning: unknown key %d", key);

@@ -69,6 +69,7 @@ struct ed_elemental_plan {
   bool gauss = false;  // factorised split GEMM in the Gauss three-multiplication form (ED_MODE_FLAG_GAUSS)
   int tc_stack = 0;    // factorised GEMM on single SMs: 0/1 = stacked [re | im] B operand (N = 256), 2 = four products
   int f64_ksplit = 1;  // K-split partial buffers the FP64 pair GEMM may use (sized at plan build)
+  int f64_df = 0;      // FP64 pair GEMM in double-float arithmetic on the FP32 pipe (ED_TUNE_F64_DF)
 };
 
 namespace ed {

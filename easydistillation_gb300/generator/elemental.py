@@ -12,7 +12,9 @@ of it instead (the reference's numpy backend).
 Extra keyword-only arguments: ``precision``, ``device``, ``factorise`` and
 ``autotune``.
 ``"fp64"`` is plain FP64 arithmetic with V rounded to complex64, as the
-reference.  The tensor-core modes ``"f16x3"``, ``"tf32x3"`` (relative error
+reference; ``"df64"`` computes the same pair contractions in double-float
+arithmetic on the FP32 pipe (each complex128 operand as two complex64 parts,
+~1e-14 relative), several times faster than this part's FP64 pipe.  The tensor-core modes ``"f16x3"``, ``"tf32x3"`` (relative error
 ~1e-7) and ``"bf16x3"`` (~1e-5) store the derivative chains in complex64 and
 run the pair contractions as split-precision tcgen05 GEMMs with FP32
 accumulation; they need ``Lx*Ly*Lz`` divisible by 32.  When the momentum list

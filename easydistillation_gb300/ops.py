@@ -418,7 +418,7 @@ _FLAG_NO_FACTOR, _FLAG_FORCE_FACTOR, _FLAG_LEFT_FACTOR = 0x100, 0x200, 0x800
 _FLAG_GAUSS = 0x400  # ED_MODE_FLAG_GAUSS
 #: plan launch settings (ED_TUNE_* keys)
 TUNING_KEYS = {"f64_tile": 1, "tc_slab_kb": 2, "tc_grid": 3, "tc_stages": 4, "tc_pair": 5, "tc_kpb": 6,
-               "tc_stack": 7}
+               "tc_stack": 7, "f64_df": 8}
 #: FP64 pair GEMM tile shapes (rows, cols) by ED_TUNE_F64_TILE value
 F64_TILES = {0: (64, 64), 1: (32, 64), 2: (64, 32), 3: (32, 32)}
 
@@ -438,12 +438,16 @@ class ElementalPlan:
         unused combinations, for any list of at most 127 distinct momenta).
         ``gauss=True`` runs the factorised split
         GEMM in the Gauss three-multiplication form (ED_MODE_FLAG_GAUSS).
-        ``tuning``: launch settings (``TUNING_KEYS``, see ``set_tuning``)."""
-        if mode not in MODES:
-            raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES)}")
+        ``tuning``: launch settings (``TUNING_KEYS``, see ``set_tuning``).
+        ``mode="df64"``: the FP64 mode with its pair GEMM in double-float
+        arithmetic on the FP32 pipe (``ED_TUNE_F64_DF``; FP64-class results)."""
+        if mode == "df64":
+            tuning = {**(tuning or {}), "f64_df": 1}
+        elif mode not in MODES:
+            raise ValueError(f"unknown elemental mode {mode!r}; available: {sorted(MODES) + ['df64']}")
         if factorise not in (True, False, "force", "left"):
             raise ValueError(f"factorise must be True, False, 'force' or 'left', not {factorise!r}")
-        cmode = MODES[mode] | {True: 0, False: _FLAG_NO_FACTOR, "force": _FLAG_FORCE_FACTOR,
+        cmode = MODES["fp64" if mode == "df64" else mode] | {True: 0, False: _FLAG_NO_FACTOR, "force": _FLAG_FORCE_FACTOR,
                                "left": _FLAG_LEFT_FACTOR}[factorise]
         if gauss:
             cmode |= _FLAG_GAUSS

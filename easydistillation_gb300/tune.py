@@ -43,8 +43,11 @@ from . import _lib
 from .insertion import num_derivative
 from .ops import F64_TILES, MODES, ElementalPlan
 
+# the FP64 mode and its double-float form: the same plans, tiles and tolerance
+F64_MODES = ("fp64", "df64")
+
 #: relative Frobenius tolerance of a candidate against the default settings, per mode
-TOLERANCE = {"fp64": 1e-12, "f16x3": 1e-6, "tf32x3": 1e-6, "bf16x3": 1e-5, "ozaki_i8": 1e-6}
+TOLERANCE = {"fp64": 1e-12, "df64": 1e-12, "f16x3": 1e-6, "tf32x3": 1e-6, "bf16x3": 1e-5, "ozaki_i8": 1e-6}
 #: lock-step slab lengths (k-blocks) of the factorised GEMM: the default first, then the candidates
 SLABS = (256, 128, 64)
 
@@ -144,7 +147,7 @@ def factorise_options(latt_size, Ne, num_nabla, momentum_list, mode) -> List[obj
     to a product set and have at most ``LEFT_FACTOR_MAX_MOM`` momenta (its
     left operand grows with the momentum count), and ``False`` (on chip) when
     ``True`` factorises.  Host-side plans only."""
-    if mode == "fp64":
+    if mode in F64_MODES:
         return [True]
     if mode == "ozaki_i8":
         return [True]  # runs on factorised operands only
@@ -230,7 +233,7 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
     ``forms`` restricts the GEMM forms tried (``factorise`` values, e.g.
     ``[True]``: the library's default form for the momentum list).
     The FP64 mode is timed on a proxy lattice (``FP64_PROXY_EXTENT``)."""
-    if mode not in MODES:
+    if mode not in MODES and mode not in F64_MODES:
         raise ValueError(f"unknown elemental mode {mode!r}")
     device = torch.device(device or "cuda")
     cache = cache or TuningCache()
@@ -246,7 +249,7 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
     moms = [tuple(int(v) for v in p) for p in momentum_list]
     nd, nm = num_derivative(num_nabla), len(moms)
     meas_latt = list(latt_size[:3]) + list(latt_size[3:])
-    if mode == "fp64":
+    if mode in F64_MODES:
         meas_latt[:3] = [min(FP64_PROXY_EXTENT, int(L)) for L in latt_size[:3]]
         reps = min(reps, 2)  # the tile shapes differ by tens of percent
     links, vecs = _synthetic_inputs(meas_latt, Ne, device, evec_dtype)
@@ -259,7 +262,7 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
         try:
             run = lambda: plan.run_batch([links] * batch, V3 * 9, 9, [vecs] * batch, outs)
             run()  # warm-up: first-use setup, function attributes
-            if mode != "fp64":
+            if mode not in F64_MODES:
                 plan.check_status()
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
             torch.cuda.synchronize(device)
@@ -268,7 +271,7 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
                 run()
                 b.record()
             torch.cuda.synchronize(device)
-            if mode != "fp64":
+            if mode not in F64_MODES:
                 plan.check_status()
             times = sorted(a.elapsed_time(b) for a, b in ev)
             return times[len(times) // 2], outs[0].clone()
@@ -277,7 +280,7 @@ def tune_elemental(latt_size, Ne: int, num_nabla: int, momentum_list, mode: str 
             torch.cuda.empty_cache()
 
     stages: List[Callable[[Candidate], List[Candidate]]] = []
-    if mode == "fp64":
+    if mode in F64_MODES:
         stages.append(lambda best: [Candidate(True, {"f64_tile": t}) for t in sorted(F64_TILES)])
     else:
         tried = list(forms) if forms is not None else factorise_options(latt_size, Ne, num_nabla, moms, mode)

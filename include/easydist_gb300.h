@@ -119,6 +119,11 @@ extern "C" {
                               * 2.0e-7 with 1, 5.1e-7 with 2; stacked form 2.6e-7 with 2,
                               * 5.8e-7 with 4).  4 is meant for the stacked and Gauss forms: the
                               * four-product form with 4 exceeded 1e-6 at K = 9216. */
+#define ED_TUNE_F64_DF 8     /* FP64 mode's pair GEMM arithmetic: 0 (default) FP64 on the FP64 pipe, 1 =
+                              * double-float on the FP32 pipe (each complex128 operand as two complex64
+                              * parts, exact FP32 product splits with two-sum accumulation: ~2^-47 relative
+                              * per product instead of 2^-53, FP64-class results at several times the
+                              * FP64 pipe's speed).  The autotuner never changes it. */
 #define ED_TUNE_TC_STACK 7   /* single-SM factorised GEMM operand form: 0 (default) or 1 = stacked:
                               * B = [Br; Bi] in shared memory, two M = 128, N = 256 MMAs
                               * A_re [Br | Bi] and A_im [Br | Bi] per split product into single

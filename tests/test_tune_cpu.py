@@ -24,15 +24,15 @@ def test_tuning_settings_round_trip_and_validation():
 
     p = _plan()
     assert p.tuning() == {"f64_tile": 0, "tc_slab_kb": 0, "tc_grid": 0, "tc_stages": 0, "tc_pair": 0, "tc_kpb": 0,
-                          "tc_stack": 0}
-    p.set_tuning(f64_tile=3, tc_slab_kb=64, tc_grid=100, tc_stages=3, tc_pair=2, tc_kpb=4, tc_stack=1)
+                          "tc_stack": 0, "f64_df": 0}
+    p.set_tuning(f64_tile=3, tc_slab_kb=64, tc_grid=100, tc_stages=3, tc_pair=2, tc_kpb=4, tc_stack=1, f64_df=1)
     assert p.tuning() == {"f64_tile": 3, "tc_slab_kb": 64, "tc_grid": 100, "tc_stages": 3, "tc_pair": 2,
-                          "tc_kpb": 4, "tc_stack": 1}
+                          "tc_kpb": 4, "tc_stack": 1, "f64_df": 1}
     p.set_tuning(tc_slab_kb=0)
     assert p.tuning()["tc_slab_kb"] == 0
     for bad in ({"f64_tile": 4}, {"f64_tile": -1}, {"tc_slab_kb": 96}, {"tc_slab_kb": 512}, {"tc_grid": -2},
                 {"tc_stages": 1}, {"tc_stages": 5}, {"tc_pair": 4}, {"tc_pair": -1}, {"tc_kpb": 3},
-                {"tc_kpb": 8}, {"tc_stack": 3}, {"tc_stack": -1}):
+                {"tc_kpb": 8}, {"tc_stack": 3}, {"tc_stack": -1}, {"f64_df": 2}, {"f64_df": -1}):
         with pytest.raises(ValueError):
             p.set_tuning(**bad)
     with pytest.raises(ValueError):
