@@ -670,6 +670,8 @@ def run_ours(args, rank, world):
             torch.cuda.empty_cache()
             line["eigensolve_32cube"] = bench_eigen_32(dev)
             torch.cuda.empty_cache()
+            line["elementals_24cube"] = bench_elemental_24(dev)
+            torch.cuda.empty_cache()
             line["mixed_volumes"] = measure_mixed(args, dev)
             torch.cuda.empty_cache()
             line["gradient"] = measure_grad(args, dev)
@@ -804,6 +806,46 @@ def bench_eigen_default(dev, batch=8):
                                                 "FP64-class stencil on the FP32 pipe in double-float arithmetic "
                                                 "(~2^-47 products); recurrence, projected eigenproblem, "
                                                 "convergence test and final Rayleigh quotients FP64"}
+    return out
+
+
+def bench_elemental_24(dev):
+    """The plain-FP64 configuration's elementals: 24^3, Ne = 100, 13 operators
+    x 27 momenta, one timeslice per run (CUDA events, after a warm-up run):
+    FP64, its double-float form (df64) and f16x3, each with its relative
+    Frobenius error against the FP64 result."""
+    import torch
+
+    from easydistillation_gb300.generator.elemental import links_to_device
+    from easydistillation_gb300.insertion import mom_dict_to_list
+    from easydistillation_gb300.ops import ElementalPlan
+
+    latt, Ne = [24, 24, 24, 2], 100
+    V3 = 24 ** 3
+    moms = mom_dict_to_list(3)
+    gauge, evecs = make_inputs(latt, Ne, distinct_t=2)
+    U = links_to_device(gauge, latt, dev)
+    V = torch.from_numpy(evecs[0].reshape(Ne, -1)).to(dev)
+    out = {"workload": "24^3, Ne=100, 13 ops x 27 momenta, one timeslice per run"}
+    ref = None
+    for mode in ("fp64", "df64", "f16x3"):
+        plan = ElementalPlan(latt, Ne, NUM_NABLA, moms, mode, dev,
+                             tuning={"f64_tile": 3} if mode in ("fp64", "df64") else None)
+        o = torch.empty((13, 27, Ne, Ne), dtype=torch.complex128, device=dev)
+        plan.run(U[:, 0], 2 * V3 * 9, 9, V, o)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        plan.run(U[:, 0], 2 * V3 * 9, 9, V, o)
+        b.record()
+        torch.cuda.synchronize()
+        if mode != "fp64":
+            plan.check_status()
+        if ref is None:
+            ref = o
+        out[mode] = {"value": 1e3 / a.elapsed_time(b), "unit": "timeslices/s",
+                     "rel_err_vs_fp64": float(torch.linalg.vector_norm(o - ref) / torch.linalg.vector_norm(ref))}
+        del plan
     return out
 
 
