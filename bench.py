@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="f16x3",
-                    help="elemental mode: f16x3 (headline), tf32x3, bf16x3, ozaki_i8, fp64")
+                    help="elemental mode: f16x3 (headline), tf32x3, bf16x3, ozaki_i8, fp64, df64")
     ap.add_argument("--lattice", default=None, help="Lx,Ly,Lz,Lt override (parity runs only)")
     ap.add_argument("--ne", type=int, default=NE)
     ap.add_argument("--batch", type=int, default=4, help="timeslices per step (one pair-contraction launch)")
@@ -111,7 +111,7 @@ def launches_per_step(mode, B=1, factorised=False):
     (absmax, scale, 2 factor phases, 2 scalings, 2 splits, conversion)."""
     if mode == "ozaki_i8":  # 2 factor phases, 2 scalings, 2 row maxima, 2 digit splits; no absmax/conversion
         return B * (1 + 1 + 12 + 1) + 1 + 1 + 8
-    extra = 0 if mode == "fp64" else (9 if factorised else 5)
+    extra = 0 if mode in ("fp64", "df64") else (9 if factorised else 5)
     return B * (1 + 1 + 12 + 1) + 1 + 1 + extra
 
 
@@ -495,9 +495,11 @@ def run_ours(args, rank, world):
                     "note": "achieved in the 43-subset flop count; the kernel issues 40 int8 products per complex "
                             "multiply-add (10 slice pairs x 4); mma.sync int8 measured at 158 TOPS on this part "
                             "by a register-only probe (tcgen05 has no kind::i8 on sm_103a)"}
-    elif args.mode == "fp64":
-        roofline = {"bound": "fp64", "achieved": alg_flop / kms / 1e9, "peak": None, "unit": "TFLOP/s",
-                    "frac": None, "traffic": None, "kernel": "pair_gemm_f64_kernel", "kernel_ms": kms}
+    elif args.mode in ("fp64", "df64"):
+        roofline = {"bound": "fp64" if args.mode == "fp64" else "fp32 (double-float)",
+                    "achieved": alg_flop / kms / 1e9, "peak": None, "unit": "TFLOP/s", "frac": None,
+                    "traffic": None, "kernel": "pair_gemm_f64_kernel" if args.mode == "fp64" else "pair_gemm_df_kernel",
+                    "kernel_ms": kms}
     else:
         pk, pk_src = peaks.get("bf16_tflops_sustained"), "measured bf16 sustained"
         if pk is None:
@@ -537,7 +539,7 @@ def run_ours(args, rank, world):
     # the plain FP64 GPU path on the same timeslice: speed and the split-precision error against it
     fp64 = None
     split_modes = None
-    if args.mode != "fp64" and not args.no_fp64:
+    if args.mode not in ("fp64", "df64") and not args.no_fp64:
         t_tune = None
         if args.autotune:
             from easydistillation_gb300.tune import tuned_plan
@@ -645,7 +647,7 @@ def run_ours(args, rank, world):
         line = {
             "metric": METRIC, "value": value, "unit": "timeslices/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c128" if args.mode == "fp64" else args.mode, "data": "synthetic",
+            "vs_baseline": None, "dtype": "c128" if args.mode in ("fp64", "df64") else args.mode, "data": "synthetic",
             "config": {"workload": f"elemental {Lx}^3x{Lt}, Ne={Ne}, 13 ops x {NMOM} momenta, mode={args.mode}, "
                                    f"{B} timeslices per step",
                        "timeslices_per_step": B,
