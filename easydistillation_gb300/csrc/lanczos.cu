@@ -435,6 +435,15 @@ __global__ void __launch_bounds__(ROT_THREADS) lz_rotate_kernel(int m, int nkeep
           }
         }
     }
+    if constexpr (DFM) {  // one renormalisation per stage of ROT_R basis rows
+#pragma unroll
+      for (int p = 0; p < 2; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          df_renorm(are[p][q]);
+          df_renorm(aim[p][q]);
+        }
+    }
     __syncthreads();
   }
 #pragma unroll
