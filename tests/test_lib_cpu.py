@@ -80,6 +80,20 @@ def test_argument_validation_is_host_side():
     assert L.ed_decode_links(_lib.ED_C128 | BE, 0, 256, 4096, None) == _lib.ED_ERR_ARG
     assert L.ed_decode_links(_lib.ED_C128 | BE, 2, 256, 1000, None) == _lib.ED_ERR_ARG  # overlap (2 sites: 1152 B)
     assert L.ed_decode_links(_lib.ED_C64 | BE, 2, 256, 4104, None) == _lib.ED_ERR_ARG  # dst % 16
+    # double-float Laplacian and split: precision code accepted (then rejected on the null pointers), bad sizes
+    assert L.ed_laplacian(_lib.ED_DF, 3, 4, 4, 1, 1, None, None, 0, None, 0, None) == _lib.ED_ERR_ARG
+    assert "null" in _lib.last_error()  # an odd Lx is fine for ED_DF: the check that failed is the pointers'
+    assert L.ed_split_c128(-1, 256, 512, None) == _lib.ED_ERR_ARG
+    assert L.ed_split_c128(4, 264, 512, None) == _lib.ED_ERR_ARG  # misaligned source
+    assert L.ed_split_c128(0, None, None, None) == _lib.ED_OK  # nothing to split
+    # two-point profile: sizes, source timeslice, null pointers
+    assert L.ed_twopoint_profile(0, 10, 8, 0, 1, *([256] * 9), None, None) == _lib.ED_ERR_ARG
+    assert L.ed_twopoint_profile(4, 10, 8, 8, 1, *([256] * 9), None, None) == _lib.ED_ERR_ARG  # t_src >= Lt
+    assert L.ed_twopoint_profile(4, 10, 8, 0, 1, *([256] * 8), None, 256, None) == _lib.ED_ERR_ARG  # null work
+    assert L.ed_twopoint_profile_diag(4, 10, 8, 0, 1, -1, *([256] * 7), None) == _lib.ED_ERR_ARG  # nterm < 0
+    # the tensor-core wait settings (process-wide; restored)
+    assert L.ed_elemental_wait_limit(-1) == _lib.ED_ERR_ARG
+    assert L.ed_elemental_wait_limit(0) == _lib.ED_OK and L.ed_elemental_wait_probe(0) == _lib.ED_OK
 
 
 @pytest.mark.parametrize(
