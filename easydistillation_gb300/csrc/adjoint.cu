@@ -159,6 +159,7 @@ extern "C" int ed_chain_adjoint(int Lx, int Ly, int Lz, int Ne, int nchain, int 
                                 void* out, void* stream) {
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nchain > 0 && nmom > 0 && R >= 0,
                "ed_chain_adjoint: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_chain_adjoint: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(M && cx && ir && pr && chains && phases && out, "ed_chain_adjoint: null pointer");
   ED_CHECK_ARG(((uintptr_t)M % 16) == 0 && ((uintptr_t)chains % 16) == 0 && ((uintptr_t)phases % 16) == 0 &&
                    ((uintptr_t)out % 16) == 0,
@@ -177,6 +178,7 @@ extern "C" int ed_chain_adjoint(int Lx, int Ly, int Lz, int Ne, int nchain, int 
 extern "C" int ed_link_grad(int Lx, int Ly, int Lz, int dir, int nvec, double alpha, double beta, const void* wbar,
                             const void* f, void* grad_links, void* stream) {
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nvec > 0, "ed_link_grad: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_link_grad: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(dir >= 0 && dir < 3, "ed_link_grad: dir must be 0, 1 or 2");
   ED_CHECK_ARG(wbar && f && grad_links, "ed_link_grad: null pointer");
   const int V3 = Lx * Ly * Lz;

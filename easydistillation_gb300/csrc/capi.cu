@@ -184,6 +184,7 @@ extern "C" int ed_links_to_soa(int out_prec, int Lx, int Ly, int Lz, int nt, con
                                long long dir_stride, long long site_stride, void* out, void* stream) {
   ED_CHECK_ARG(valid_prec(out_prec), "ed_links_to_soa: bad precision");
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0, "ed_links_to_soa: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_links_to_soa: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(in && out, "ed_links_to_soa: null pointer");
   ED_CHECK_ARG(t_stride >= 0 && dir_stride >= 0 && site_stride >= 0, "ed_links_to_soa: negative stride");
   return ed::launch_links_to_soa(out_prec, ed::Latt{Lx, Ly, Lz}, nt, in, t_stride, dir_stride, site_stride, out,
@@ -208,6 +209,7 @@ extern "C" int ed_vectors_from_planes(int in_prec, int out_prec, long long nvec,
 
 extern "C" int ed_momentum_phases(int Lx, int Ly, int Lz, const int* moms, int nmom, void* out, void* stream) {
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nmom > 0, "ed_momentum_phases: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_momentum_phases: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(moms && out, "ed_momentum_phases: null pointer");
   ED_CHECK_ARG((long long)Lx * Ly * Lz * 2 * 64 < (1LL << 52), "ed_momentum_phases: lattice too large");
   for (int i = 0; i < 3 * nmom; ++i)

@@ -109,6 +109,13 @@ struct Latt {
   __host__ __device__ int V3() const { return Lx * Ly * Lz; }
 };
 
+// Largest spatial volume the entry points accept: kernels number sites and
+// colour-plane entries (3 * V3) with 32-bit integers.
+constexpr long long MAX_V3 = 1LL << 28;
+inline bool lattice_ok(int Lx, int Ly, int Lz) {
+  return Lx > 0 && Ly > 0 && Lz > 0 && (long long)Lx * Ly * Lz <= MAX_V3;
+}
+
 __host__ __device__ __forceinline__ int wrap_inc(int v, int L) { return v + 1 == L ? 0 : v + 1; }
 __host__ __device__ __forceinline__ int wrap_dec(int v, int L) { return v == 0 ? L - 1 : v - 1; }
 

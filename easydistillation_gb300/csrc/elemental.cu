@@ -904,6 +904,7 @@ extern "C" int ed_pair_plan_create(ed_elemental_plan** plan, int Lx, int Ly, int
   *plan = nullptr;
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && Ne > 0 && nmom > 0 && nchain > 0 && nright > 0,
                "ed_pair_plan_create: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_pair_plan_create: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(left >= 0 && left < nchain && right0 >= 0 && right0 + nright <= nchain,
                "ed_pair_plan_create: chain indices out of range");
   ED_CHECK_ARG(moms, "ed_pair_plan_create: null momentum list");

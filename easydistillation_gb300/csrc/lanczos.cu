@@ -478,6 +478,7 @@ int lz_rotate(cudaStream_t st, int B, long long n, int m, int nkeep, const doubl
 extern "C" int ed_lanczos_workspace(int Lx, int Ly, int Lz, int nt, int Ne, int ncv, size_t* bytes) {
   ED_CHECK_ARG(bytes, "ed_lanczos_workspace: null pointer");
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_workspace: bad sizes");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_lanczos_workspace: Lx*Ly*Lz above 2^28");
   const long long n = 3LL * Lx * Ly * Lz;
   ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_workspace: need Ne < ncv <= 3*Lx*Ly*Lz");
   const int nblk = (int)((n + ed::LZ_THREADS - 1) / ed::LZ_THREADS);
@@ -768,6 +769,7 @@ extern "C" int ed_lanczos_tr(int Lx, int Ly, int Lz, int nt, const void* links, 
                              void* workspace, size_t workspace_bytes, void* stream) {
   using namespace ed;
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr: bad sizes");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_lanczos_tr: Lx*Ly*Lz above 2^28");
   const long long n = 3LL * Lx * Ly * Lz;
   ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr: need Ne < ncv <= 3*Lx*Ly*Lz");
   ED_CHECK_ARG(tol > 0.0 && max_restarts > 0, "ed_lanczos_tr: need tol > 0 and max_restarts > 0");
@@ -802,6 +804,7 @@ extern "C" int ed_lanczos_workspace_ex(int Lx, int Ly, int Lz, int nt, int Ne, i
   const int sp = stencil_prec & ~ED_LANCZOS_GS_DF;
   ED_CHECK_ARG(sp == ED_C128 || sp == ED_C64, "ed_lanczos_workspace_ex: bad stencil precision");
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_workspace_ex: bad sizes");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_lanczos_workspace_ex: Lx*Ly*Lz above 2^28");
   const long long n = 3LL * Lx * Ly * Lz;
   ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_workspace_ex: need Ne < ncv <= 3*Lx*Ly*Lz");
   const int nblk = (int)((n + ed::LZ_THREADS - 1) / ed::LZ_THREADS);
@@ -833,6 +836,7 @@ extern "C" int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* link
   }
   if (sp == ED_C128) {  // FP64 stencil, double-float Gram-Schmidt
     ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr_ex: bad sizes");
+    ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_lanczos_tr_ex: Lx*Ly*Lz above 2^28");
     const long long n = 3LL * Lx * Ly * Lz;
     ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr_ex: need Ne < ncv <= 3*Lx*Ly*Lz");
     ED_CHECK_ARG(tol > 0.0 && max_restarts > 0, "ed_lanczos_tr_ex: need tol > 0 and max_restarts > 0");
@@ -855,6 +859,7 @@ extern "C" int ed_lanczos_tr_ex(int Lx, int Ly, int Lz, int nt, const void* link
     return rc;
   }
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nt <= 65535 && Ne > 0, "ed_lanczos_tr_ex: bad sizes");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_lanczos_tr_ex: Lx*Ly*Lz above 2^28");
   const long long n = 3LL * Lx * Ly * Lz;
   ED_CHECK_ARG(Ne < ncv && ncv <= n, "ed_lanczos_tr_ex: need Ne < ncv <= 3*Lx*Ly*Lz");
   ED_CHECK_ARG(tol > 0.0 && max_restarts > 0 && poly_deg >= 0, "ed_lanczos_tr_ex: need tol > 0, max_restarts > 0");

@@ -906,6 +906,7 @@ extern "C" int ed_laplacian(int prec, int Lx, int Ly, int Lz, int nt, int nvec, 
                             long long in_tstride, void* out, long long out_tstride, void* stream) {
   ED_CHECK_ARG(prec == ED_C128 || prec == ED_C64 || prec == ED_DF, "ed_laplacian: prec must be ED_C128, ED_C64 or ED_DF");
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0 && nvec > 0, "ed_laplacian: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_laplacian: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(prec != ED_C64 || Lx % 2 == 0, "ed_laplacian: c64 path needs an even Lx");
   ED_CHECK_ARG(nvec <= 65535 && nt <= 65535, "ed_laplacian: nvec and nt must be <= 65535");
   ED_CHECK_ARG(links && in && out, "ed_laplacian: null pointer");
@@ -972,6 +973,7 @@ extern "C" int ed_covariant_derivative(int in_prec, int out_prec, int Lx, int Ly
   ED_CHECK_ARG((in_prec == ED_C128 || in_prec == ED_C64) && (out_prec == ED_C128 || out_prec == ED_C64),
                "ed_covariant_derivative: bad precision");
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nvec > 0, "ed_covariant_derivative: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_covariant_derivative: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(dir >= 0 && dir < 3, "ed_covariant_derivative: dir must be 0, 1 or 2");
   ED_CHECK_ARG(links_c128 && in && out, "ed_covariant_derivative: null pointer");
   ED_CHECK_ARG(in != out, "ed_covariant_derivative: in and out must not alias");
@@ -1027,6 +1029,7 @@ __global__ void __launch_bounds__(128) transport_kernel(Latt L, int d, int sign,
 extern "C" int ed_parallel_transport(int Lx, int Ly, int Lz, int dir, int sign, int nvec, const void* links_c128,
                                      const void* in, void* out, void* stream) {
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nvec > 0, "ed_parallel_transport: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_parallel_transport: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(dir >= 0 && dir < 3 && (sign == 1 || sign == -1), "ed_parallel_transport: bad direction or sign");
   ED_CHECK_ARG(links_c128 && in && out && in != out, "ed_parallel_transport: null or aliasing pointers");
   constexpr int VB = 8;

@@ -255,6 +255,7 @@ extern "C" int ed_project_su3(long long nlinks, void* U, double tol, int max_ite
 extern "C" int ed_stout_smear_step(int Lx, int Ly, int Lz, int nt, double rho, const void* U_in, void* U_out,
                                    void* stream) {
   ED_CHECK_ARG(Lx > 0 && Ly > 0 && Lz > 0 && nt > 0, "ed_stout_smear_step: sizes must be positive");
+  ED_CHECK_ARG(ed::lattice_ok(Lx, Ly, Lz), "ed_stout_smear_step: Lx*Ly*Lz above 2^28");
   ED_CHECK_ARG(U_in && U_out && U_in != U_out, "ed_stout_smear_step: null or aliasing pointers");
   const long long n = 3LL * nt * Lx * Ly * Lz;
   ed::stout_step_kernel<<<ed::ceil_div(n, 128), 128, 0, (cudaStream_t)stream>>>(

@@ -15,6 +15,10 @@
  * There is no CPU fallback: without a usable sm_103a device the calls return
  * ED_ERR_CUDA.
  *
+ * Lattice sizes are positive with V3 = Lx*Ly*Lz <= 2^28 (sites and colour
+ * entries are numbered with 32-bit integers; elemental plans take V3 <= 2^26);
+ * larger lattices are rejected with ED_ERR_ARG.
+ *
  * Data layouts (V3 = Lx*Ly*Lz, site = x + Lx*(y + Ly*z), x fastest):
  *   reference links   : complex128, element (mu, site, a, b) at
  *                       mu*dir_stride + site*site_stride + 3*a + b

@@ -118,6 +118,33 @@ def test_elemental_plan_pairs(num_nabla, moms, herm_pairs, plain_pairs):
     assert plan.workspace_bytes >= (3 ** (num_nabla + 1) - 1) // 2 * 6 * 3 * V3 * 16
 
 
+def test_lattice_volume_bound():
+    """Every entry point that takes Lx, Ly, Lz rejects V3 above 2^28 on the
+    host (kernels number sites with 32-bit integers); 2^27 still plans."""
+    from easydistillation_gb300 import _lib
+
+    L = _lib.lib()
+    big = (1024, 1024, 1024)  # V3 = 2^30
+    p = 1 << 20  # a non-null, 16-byte aligned stand-in address: nothing is dereferenced
+    calls = {
+        "ed_laplacian": lambda: L.ed_laplacian(_lib.ED_C128, *big, 1, 1, p, p, 0, p + 4096, 0, None),
+        "ed_covariant_derivative": lambda: L.ed_covariant_derivative(0, 0, *big, 0, 1, p, p, p + 4096, None),
+        "ed_parallel_transport": lambda: L.ed_parallel_transport(*big, 0, 1, 1, p, p + 4096, p + 8192, None),
+        "ed_stout_smear_step": lambda: L.ed_stout_smear_step(*big, 1, ctypes.c_double(0.1), p, p + 4096, None),
+        "ed_link_grad": lambda: L.ed_link_grad(*big, 0, 1, ctypes.c_double(1.0), ctypes.c_double(0.0), p, p, p,
+                                               None),
+        "ed_links_to_soa": lambda: L.ed_links_to_soa(_lib.ED_C128, *big, 1, p, 0, 9, 36, p + 4096, None),
+    }
+    for name, call in calls.items():
+        assert call() == _lib.ED_ERR_ARG, name
+        assert "2^28" in _lib.last_error(), (name, _lib.last_error())
+    nb = ctypes.c_size_t()
+    assert L.ed_lanczos_workspace(*big, 1, 16, 40, ctypes.byref(nb)) == _lib.ED_ERR_ARG
+    assert "2^28" in _lib.last_error()
+    assert L.ed_lanczos_workspace(512, 512, 512, 1, 16, 40, ctypes.byref(nb)) == _lib.ED_OK
+    assert nb.value >= 41 * 3 * (1 << 27) * 16
+
+
 def test_plan_rejects_bad_arguments():
     from easydistillation_gb300.ops import ElementalPlan
 
