@@ -4,7 +4,6 @@ launch: one timeslice each of 16^3 (Ne = 64), 24^3 (Ne = 128) and 32^3
 f16x3, against the plain FP64 GPU path of each volume: relative Frobenius
 error <= 1e-6."""
 
-import numpy as np
 import pytest
 import torch
 
