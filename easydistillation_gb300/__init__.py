@@ -14,7 +14,7 @@ The arithmetic runs in ``libeasydist_gb300.so`` (C ABI:
 ``python -m easydistillation_gb300.build``.  There is no CPU fallback.
 """
 
-from .backend import get_backend, set_backend
+from .backend import check_QUDA, get_backend, set_backend
 from .generator import DisplacementElementalGenerator, EigenvectorGenerator, ElementalGenerator
 from .insertion import MomentumPhase, derivative, mom_dict_to_list, num_derivative
 from .preset import (
@@ -31,6 +31,7 @@ from .preset import (
 )
 
 NC, NS, ND = 3, 4, 4
+Nc, Ns, Nd = NC, NS, ND  # the reference's names (lattice/constant.py)
 
 __all__ = [
     "DisplacementElementalGenerator",
@@ -41,6 +42,7 @@ __all__ = [
     "mom_dict_to_list",
     "get_backend",
     "set_backend",
+    "check_QUDA",
     "num_derivative",
     "GaugeFieldIldg",
     "GaugeFieldBinary",
@@ -55,4 +57,7 @@ __all__ = [
     "NC",
     "NS",
     "ND",
+    "Nc",
+    "Ns",
+    "Nd",
 ]

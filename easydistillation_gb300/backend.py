@@ -67,3 +67,13 @@ def to_backend(x):
     import cupy
 
     return cupy.from_dlpack(x.detach())
+
+
+def check_QUDA(grid_size=None, backend="cupy", resource_path=None) -> bool:
+    """Counterpart of ``lattice/backend.py:36`` (``check_QUDA``), which
+    initialises PyQUDA when it is importable and reports whether it is.  The
+    paths the reference sends to QUDA (the Laplacian eigensolve, stout
+    smearing) run in this library's own kernels, so there is no QUDA to
+    initialise: always False, and driver code written against the reference
+    takes its non-QUDA branches."""
+    return False

@@ -1,7 +1,7 @@
 """GB300 drop-in for ``lattice.generator.DisplacementElementalGenerator``.
 
-Same constructor, ``load`` and ``calc`` as
-``lattice/generator/displacement_elemental.py:11-96``:
+Same constructor, ``load``, ``calc``, ``project_SU3`` and ``stout_smear`` as
+``lattice/generator/displacement_elemental.py:11-214``:
 ``E[dist, p, i, j] = sum_x phase_p(x) conj(V_i(x)) . R^dist_j(x)`` where
 ``R^0 = V`` and ``R^dist`` is the mean of the six straight-line parallel
 transports of ``V`` over ``dist`` links (``_D`` at ``:53-71``; V rounded to
@@ -51,6 +51,30 @@ class DisplacementElementalGenerator:
         self._U = gauge_to_device(self.gauge_field.load(key), self.latt_size, self.device)
         self._links = links_to_soa(self._U, self.latt_size)
         self._eigenvector_data = self.eigenvector.load(key)
+
+    def project_SU3(self):
+        """Iterative projection of the loaded spatial links back onto SU(3)
+        (``displacement_elemental.py:98-108``); later ``calc`` calls transport
+        with the projected links."""
+        from .eigenvector import project_su3_
+
+        self._require_links()
+        project_su3_(self._U)
+        self._links = links_to_soa(self._U, self.latt_size)
+
+    def stout_smear(self, nstep: int, rho: float):
+        """``nstep`` 3D stout steps of weight ``rho`` on the loaded spatial
+        links (``displacement_elemental.py:202-214``); later ``calc`` calls
+        transport with the smeared links."""
+        from .eigenvector import stout_smear_links_
+
+        self._require_links()
+        stout_smear_links_(self._U, self.latt_size, nstep, rho)
+        self._links = links_to_soa(self._U, self.latt_size)
+
+    def _require_links(self):
+        if self._U is None:
+            raise RuntimeError("call load(key) before smearing or projecting the links")
 
     def calc(self, t: int):
         if self._U is None:

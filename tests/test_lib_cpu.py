@@ -202,6 +202,9 @@ def test_backend_switch():
     finally:
         ed.set_backend("torch")
     assert ed.get_backend() is torch
+    # the reference's top-level constants and QUDA probe (lattice/constant.py, lattice/backend.py:36)
+    assert (ed.Nc, ed.Ns, ed.Nd) == (3, 4, 4)
+    assert ed.check_QUDA() is False and ed.check_QUDA([1, 1, 1, 2], "torch") is False
 
 
 def test_operator_parts_match_reference():
