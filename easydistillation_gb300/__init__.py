@@ -26,6 +26,7 @@ from .preset import (
     GaugeFieldBinary,
     GaugeFieldIldg,
     GaugeFieldTimeSlice,
+    Jpsi2gammaNpy,
     PerambulatorBinary,
     PerambulatorNpy,
 )
@@ -47,6 +48,7 @@ __all__ = [
     "GaugeFieldIldg",
     "GaugeFieldBinary",
     "GaugeFieldTimeSlice",
+    "Jpsi2gammaNpy",
     "EigenvectorNpy",
     "EigenvectorTimeSlice",
     "EigenvectorHostmem",

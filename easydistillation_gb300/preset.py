@@ -23,7 +23,8 @@ Formats:
   big-endian 8-byte length, a 128-byte type string and the 8-byte padded
   payload; ``ildg-format`` holds the XML (lx, ly, lz, lt, precision) and
   ``ildg-binary-data`` the big-endian field.
-* ``.npy`` (``ndarray.py:17-47``): numpy header, C order.
+* ``.npy`` (``ndarray.py:17-47``): numpy header, C order; per-source files
+  (``ndarray.py:54-90``) for ``PerambulatorTimeslicesNpy``.
 * raw binary (``binary.py:23-66``).
 * QDP LazyDiskMapObjFile (``timeslice.py:102-129``): magic string, version,
   XML, a trailer with key tuples and offsets.
@@ -36,6 +37,7 @@ import os
 import re
 import struct
 import xml.etree.ElementTree as ET
+from copy import deepcopy
 from time import time
 from typing import Dict, List, Tuple
 
@@ -177,6 +179,31 @@ class BinaryFileData(_Data):
         return np.memmap(self.file, dtype=self.dtype, mode="r", shape=tuple(self.shape))
 
 
+class NdarrayTimeslicesFileData(_Data):
+    """One ``.npy`` file per source timeslice (``ndarray.py:54-90``): the file
+    name holds ``.t???.``, which the first index of every key replaces with
+    ``.t{t:03d}.``; the remaining indices select within that file."""
+
+    def __init__(self, file: str, elem: FileMetaData):
+        self.file = file
+        self.shape = elem.shape if elem else None
+        self.dtype = elem.dtype if elem else None
+        self.time_in_sec = self.timeInSec = 0.0
+        self.size_in_byte = self.sizeInByte = 0
+
+    def source_file(self, t: int) -> str:
+        return re.sub(r"\.t\?\?\?\.", f".t{int(t):03d}.", self.file)
+
+    def _view(self, key):
+        head, rest = (key[0], tuple(key[1:])) if isinstance(key, tuple) else (key, ())
+        if not isinstance(head, (int, np.integer)):
+            raise TypeError("the first index selects the per-source file and must be an integer")
+        return np.load(self.source_file(head), mmap_mode="r")[rest]
+
+    def links_to_device(self, latt_size, device=None):
+        return None  # per-source perambulator files, not a gauge field
+
+
 def read_lime_records(path: str) -> Dict[str, Tuple[int, int]]:
     """type -> (payload offset, padded length) of every LIME record."""
     out = {}
@@ -268,6 +295,51 @@ class QDPLazyDiskMapObjFileData(_Data):
         return arr[tuple(key[self.extra :])]
 
 
+class GaugeField:
+    """Base of the gauge-field presets (``lattice/preset.py:11-13``)."""
+
+    def __init__(self, elem: FileMetaData) -> None:
+        self.elem = deepcopy(elem)
+
+
+class Eigenvector:
+    """Base of the eigenvector presets (``lattice/preset.py:16-19``)."""
+
+    def __init__(self, elem: FileMetaData, eigenNum: int) -> None:
+        self.elem = deepcopy(elem)
+        self.Ne = eigenNum
+
+
+class Elemental:
+    """Base of the elemental presets (``lattice/preset.py:22-25``)."""
+
+    def __init__(self, elem: FileMetaData, eigenNum: int) -> None:
+        self.elem = deepcopy(elem)
+        self.Ne = eigenNum
+
+
+class Perambulator:
+    """Base of the perambulator presets (``lattice/preset.py:28-31``)."""
+
+    def __init__(self, elem: FileMetaData, eigenNum: int) -> None:
+        self.elem = deepcopy(elem)
+        self.Ne = eigenNum
+
+
+class OnePoint:
+    """Base of the one-point data presets (``lattice/preset.py:34-36``)."""
+
+    def __init__(self, elem: FileMetaData) -> None:
+        self.elem = deepcopy(elem)
+
+
+class TwoPoint:
+    """Base of the two-point data presets (``lattice/preset.py:39-41``)."""
+
+    def __init__(self, elem: FileMetaData) -> None:
+        self.elem = deepcopy(elem)
+
+
 class _Preset:
     _data_cls = None
 
@@ -283,28 +355,28 @@ class _Preset:
         return self.data
 
 
-class GaugeFieldIldg(_Preset):
+class GaugeFieldIldg(_Preset, GaugeField):
     _data_cls = IldgFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[128, 16**3, 4, 3, 3]):
         super().__init__(prefix, ".lime" if suffix is None else suffix, FileMetaData(shape, ">c16", 0))
 
 
-class GaugeFieldBinary(_Preset):
+class GaugeFieldBinary(_Preset, GaugeField):
     _data_cls = BinaryFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[128, 16**3, 4, 3, 3], dtype: str = "<f8"):
         super().__init__(prefix, ".dat" if suffix is None else suffix, FileMetaData(shape, dtype, 0))
 
 
-class GaugeFieldTimeSlice(_Preset):
+class GaugeFieldTimeSlice(_Preset, GaugeField):
     _data_cls = QDPLazyDiskMapObjFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[128, 4, 16**3, 3, 3]):
         super().__init__(prefix, ".stout.n20.f0.12.mod" if suffix is None else suffix, FileMetaData(shape, ">c16", 2))
 
 
-class EigenvectorNpy(_Preset):
+class EigenvectorNpy(_Preset, Eigenvector):
     _data_cls = NdarrayFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[70, 128, 16**3, 3], totNe: int = 70):
@@ -312,7 +384,7 @@ class EigenvectorNpy(_Preset):
         self.Ne = totNe
 
 
-class EigenvectorTimeSlice(_Preset):
+class EigenvectorTimeSlice(_Preset, Eigenvector):
     _data_cls = QDPLazyDiskMapObjFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[128, 70, 16**3, 3], totNe: int = 70):
@@ -321,7 +393,7 @@ class EigenvectorTimeSlice(_Preset):
         self.Ne = totNe
 
 
-class EigenvectorHostmem:
+class EigenvectorHostmem(Eigenvector):
     """Eigenvectors already in host memory (``lattice/preset.py:77-89``)."""
 
     def __init__(self, host_ndarray, shape=[70, 128, 16**3, 3], totNe: int = 70):
@@ -337,7 +409,7 @@ class EigenvectorHostmem:
         return self.data
 
 
-class ElementalNpy(_Preset):
+class ElementalNpy(_Preset, Elemental):
     _data_cls = NdarrayFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[4, 123, 128, 70, 70], totNe: int = 70):
@@ -346,7 +418,7 @@ class ElementalNpy(_Preset):
         self.Ne = totNe
 
 
-class ElementalBinary(_Preset):
+class ElementalBinary(_Preset, Elemental):
     _data_cls = BinaryFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[40, 27, 128, 70, 70], totNe: int = 70):
@@ -355,7 +427,7 @@ class ElementalBinary(_Preset):
         self.Ne = totNe
 
 
-class PerambulatorNpy(_Preset):
+class PerambulatorNpy(_Preset, Perambulator):
     _data_cls = NdarrayFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[128, 128, 4, 4, 70, 70], totNe: int = 70):
@@ -364,13 +436,58 @@ class PerambulatorNpy(_Preset):
         self.Ne = totNe
 
 
-class PerambulatorBinary(_Preset):
+class PerambulatorBinary(_Preset, Perambulator):
     _data_cls = BinaryFileData
 
     def __init__(self, prefix: str, suffix: str, shape=[128, 128, 4, 4, 70, 70], totNe: int = 70):
         super().__init__(prefix, ".stout.n20.f0.12.nev70.peram" if suffix is None else suffix,
                          FileMetaData(shape, "<c16", 0))
         self.Ne = totNe
+
+
+class PerambulatorTimeslicesNpy(_Preset, Perambulator):
+    """Perambulators saved one source timeslice per ``.npy`` file
+    (``lattice/preset.py:114-126``): ``prefix + key + suffix`` names the files
+    with ``.t???.`` in place of the source index; ``[t_src, ...]`` reads
+    ``.t{t_src:03d}.``."""
+
+    _data_cls = NdarrayTimeslicesFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 128, 4, 4, 70, 70], totNe: int = 70):
+        super().__init__(prefix, ".stout.n20.f0.12.nev70.peram" if suffix is None else suffix,
+                         FileMetaData(shape, "<c8", 0))
+        self.Ne = totNe
+
+
+class Jpsi2gammaBinary(_Preset, TwoPoint):
+    """Raw float64 two-point data (``lattice/preset.py:140-148``)."""
+
+    _data_cls = BinaryFileData
+
+    def __init__(self, prefix: str, suffix: str, shape=[128, 2, 3, 4, 27, 128]):
+        super().__init__(prefix, ".mesonspec.2pt.bin" if suffix is None else suffix, FileMetaData(shape, "<f8", 0))
+
+
+class Jpsi2gammaNpy(_Preset, TwoPoint):
+    """Two-point data in ``.npy`` files (``lattice/preset.py:184-192``).  The
+    reference's class passes no metadata, and its ``.npy`` reader then fails
+    on ``load`` (``ndarray.py:12`` reads ``elem.shape``); here the file's own
+    header gives shape and dtype."""
+
+    _data_cls = NdarrayFileData
+
+    def __init__(self, prefix: str, suffix: str):
+        super().__init__(prefix, ".2pt.npy" if suffix is None else suffix, None)
+
+
+class OnePointNpy(_Preset, OnePoint):
+    """One-point data in ``.npy`` files (``lattice/preset.py:195-204``); as
+    for :class:`Jpsi2gammaNpy`, shape and dtype come from the file header."""
+
+    _data_cls = NdarrayFileData
+
+    def __init__(self, prefix: str, suffix: str):
+        super().__init__(prefix, ".1pt.npy" if suffix is None else suffix, None)
 
 
 def write_ildg(path: str, gauge: np.ndarray, latt_size: List[int]):

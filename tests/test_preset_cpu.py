@@ -145,3 +145,45 @@ def test_pinned_bytes_split_copy(monkeypatch):
 
     with pytest.raises(ValueError):
         preset.pinned_bytes(a, torch.zeros(a.nbytes - 1, dtype=torch.uint8))
+
+
+def test_per_source_perambulator_and_correlator_data(tmp_path):
+    """PerambulatorTimeslicesNpy (lattice/preset.py:114-126): one .npy per
+    source timeslice, ``.t???.`` in the name replaced by the first index;
+    the two-point / one-point data presets; every preset is an instance of the
+    reference's base class for its kind."""
+    import pytest
+
+    from easydistillation_gb300 import preset as P
+
+    rng = np.random.default_rng(3)
+    Lt, Ne = 3, 4
+    full = (rng.standard_normal((Lt, Lt, 4, 4, Ne, Ne)) + 1j * rng.standard_normal((Lt, Lt, 4, 4, Ne, Ne)))
+    full = full.astype(np.complex64)
+    for t in range(Lt):
+        np.save(tmp_path / f"cfgE.t{t:03d}.peram.npy", full[t])
+    pre = P.PerambulatorTimeslicesNpy(str(tmp_path) + "/", ".t???.peram.npy", list(full.shape), Ne)
+    d = pre.load("cfgE")
+    assert isinstance(pre, P.Perambulator) and pre.Ne == Ne
+    assert d.source_file(2).endswith("cfgE.t002.peram.npy")
+    np.testing.assert_array_equal(d[1], full[1])
+    key = (2, slice(None), slice(None), slice(None), slice(None, 3), slice(None, 3))  # the correlators' key
+    np.testing.assert_array_equal(d[key], full[2, :, :, :, :3, :3])
+    np.testing.assert_array_equal(d[0, [2, 0]], full[0, [2, 0]])
+    with pytest.raises(TypeError):
+        d[0:2]
+    assert d.size_in_byte > 0
+
+    two = rng.standard_normal((2, 2, 3, 4, 5, 6))
+    two.astype("<f8").tofile(tmp_path / "cfgF.2pt.bin")
+    jb = P.Jpsi2gammaBinary(str(tmp_path) + "/", ".2pt.bin", list(two.shape))
+    np.testing.assert_array_equal(jb.load("cfgF")[1, :, 2], two[1, :, 2])
+    np.save(tmp_path / "cfgG.2pt.npy", two)
+    np.testing.assert_array_equal(P.Jpsi2gammaNpy(str(tmp_path) + "/", None).load("cfgG")[:], two)
+    one = rng.standard_normal((2, 7, 5))
+    np.save(tmp_path / "cfgH.1pt.npy", one)
+    np.testing.assert_array_equal(P.OnePointNpy(str(tmp_path) + "/", None).load("cfgH")[1], one[1])
+    for obj, base in [(jb, P.TwoPoint), (P.OnePointNpy("a", None), P.OnePoint), (P.GaugeFieldIldg("a", None), P.GaugeField),
+                      (P.EigenvectorNpy("a", None), P.Eigenvector), (P.ElementalNpy("a", None), P.Elemental),
+                      (P.PerambulatorBinary("a", None), P.Perambulator)]:
+        assert isinstance(obj, base), (obj, base)
