@@ -32,6 +32,15 @@ def test_library_exports_every_declared_symbol():
     assert L.ed_version() >= 100
 
 
+def test_integration_notes_name_every_entry_point():
+    """The binding notes list each declared entry point with the reference
+    interface it replaces (or 'no counterpart')."""
+    notes = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    named = set(re.findall(r"\bed_\w+", notes))
+    missing = sorted(_declared() - named)
+    assert not missing, f"entry points without a line in the binding notes: {missing}"
+
+
 def test_argument_validation_is_host_side():
     from easydistillation_gb300 import _lib
 
