@@ -192,3 +192,18 @@ class EigenvectorGenerator:
     def calc(self, t: int, apply_renorm_phase: bool = True, polynomial_degree: int = 0, lambda_cut: float = 0.0):
         evecs, evals = self.calc_batch([t], apply_renorm_phase, polynomial_degree, lambda_cut)
         return to_backend(evecs[0]), to_backend(evals[0])
+
+    # The reference's per-backend solvers (scipy/cupyx eigsh on its numpy
+    # stencil, ``eigenvector.py:234-257``; QUDA's eigensolver with Chebyshev
+    # acceleration, ``:259-312``; eigsh on QUDA's stencil, ``:314-354``) return
+    # the same eigenpairs on the same scale as ``calc``; here each runs this
+    # library's eigensolve, with the Chebyshev acceleration where the QUDA
+    # solver takes a degree and a cut.
+    def laplacian_cupy_numpy(self, t: int, apply_renorm_phase: bool):
+        return self.calc(t, apply_renorm_phase)
+
+    def laplacian_quda(self, t: int, apply_renorm_phase: bool, polynomial_degree: int, lambda_cut: float):
+        return self.calc(t, apply_renorm_phase, polynomial_degree, lambda_cut)
+
+    def laplacian_quda_scipy(self, t: int, apply_renorm_phase: bool):
+        return self.calc(t, apply_renorm_phase)

@@ -266,3 +266,18 @@ def test_ozaki_plan_limits():
     assert p.factorised == (5, 3)
     with pytest.raises(Exception):
         ElementalPlan([40, 40, 36, 2], 10, 1, [(0, 0, 0)], "ozaki_i8", device="cpu")
+
+
+def test_eigenvector_backend_solver_names_route_to_calc():
+    """EigenvectorGenerator.laplacian_cupy_numpy / laplacian_quda /
+    laplacian_quda_scipy (lattice/generator/eigenvector.py:234-354) keep the
+    reference's signatures and run calc with the same arguments."""
+    from easydistillation_gb300 import EigenvectorGenerator
+
+    gen = EigenvectorGenerator.__new__(EigenvectorGenerator)
+    seen = []
+    gen.calc = lambda *a: seen.append(a) or ("evecs", "evals")
+    assert gen.laplacian_cupy_numpy(3, False) == ("evecs", "evals")
+    gen.laplacian_quda(4, True, 16, 0.5)
+    gen.laplacian_quda_scipy(5, True)
+    assert seen == [(3, False), (4, True, 16, 0.5), (5, True)]
