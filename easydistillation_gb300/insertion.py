@@ -65,6 +65,17 @@ def mom_dict_to_list(mom: int = 9) -> List[Tuple[int, int, int]]:
     raise ValueError(f"Unknown mom max = {mom}")
 
 
+def _mom_dict(mom: int):
+    return {i: f"{x} {y} {z}" for i, (x, y, z) in enumerate(mom_dict_to_list(mom))}
+
+
+# The reference's index -> "px py pz" tables (``mom_dict.py:1-159``), the
+# ``momentum_dict`` its insertion rows look momenta up in.
+momDict_mom1 = _mom_dict(1)
+momDict_mom3 = _mom_dict(3)
+momDict_mom9 = _mom_dict(9)
+
+
 class MomentumPhase:
     """Per-site phases ``exp(+2*pi*i*(px*x/Lx + py*y/Ly + pz*z/Lz))`` as FP64
     device tensors ``[Lz, Ly, Lx]``, cached per momentum."""

@@ -188,6 +188,13 @@ def test_momentum_lists_match_reference_tables():
     assert mom_dict_to_list(3)[:7] == [p for p in mom_dict_to_list(3) if sum(v * v for v in p) <= 1]
     with pytest.raises(ValueError):
         mom_dict_to_list(5)
+    # the index -> "px py pz" dictionaries insertion rows look momenta up in
+    from easydistillation_gb300.insertion import momDict_mom1, momDict_mom3, momDict_mom9
+
+    assert momDict_mom1 == {0: "0 0 0"}
+    assert momDict_mom3[1] == "0 0 1" and momDict_mom3[26] == "-1 -1 -1" and len(momDict_mom3) == 27
+    assert momDict_mom9[0] == "0 0 -3" and momDict_mom9[122] == "0 0 3"
+    assert [tuple(int(v) for v in s.split(" ")) for s in momDict_mom9.values()] == mom_dict_to_list(9)
 
 
 def test_backend_switch():
