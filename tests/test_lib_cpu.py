@@ -288,3 +288,13 @@ def test_eigenvector_backend_solver_names_route_to_calc():
     gen.laplacian_quda(4, True, 16, 0.5)
     gen.laplacian_quda_scipy(5, True)
     assert seen == [(3, False), (4, True, 16, 0.5), (5, True)]
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """Without the built library every call raises (there is no CPU path)."""
+    from easydistillation_gb300 import _lib
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libeasydist_gb300.so"))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.lib()
